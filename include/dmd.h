@@ -1,0 +1,200 @@
+/*
+ * dmd.h -- C ABI of the GB300 PRIME20 discontinuous-MD event engine.
+ *
+ * The engine replaces the event engine of the reference Fortran program
+ * (parallel-dmd-PRIME20/code): the subroutines events(), partial_events(),
+ * eventredo_up/down(), core(), bond(), sqwel(), nc_sqwel(), sqshlder(),
+ * eventdyn(), bumpoff(), repuls_*(), check_sigma(), nbor_setup(),
+ * cell_link(), cell_add(), nbor(), displ(), add_tbin()/del_tbin() and the
+ * master loop of program dmd (code/main.F90:484-1258) with the worker block
+ * (code/main.F90:1420-1960) folded in.  Those subroutines share the module
+ * GLOBAL (code/header.f:2-65) and have no API of their own; the functions
+ * below are the calls a host (a Fortran program through ISO_C_BINDING, C++,
+ * or Python ctypes) makes instead of running that loop.
+ *
+ * Conventions
+ *   - Plain C types only.  All floating point is IEEE double.
+ *   - Bead indices crossing the ABI are 1-based, as in the reference
+ *     (0 means "none").  Bead order inside every chain is
+ *     C-alpha(1..L), NH(1..L), CO(1..L), side chains R of the non-glycine
+ *     residues in sequence order (code/inputinfo.f:218-228).
+ *   - Every function returns 0 on success or a negative DMD_E_* status and
+ *     never calls exit(); dmd_last_error() gives the text.
+ *   - The library copies host inputs; the caller keeps ownership.
+ *   - A handle is single threaded.  Different handles may be used from
+ *     different threads.
+ */
+#ifndef DMD_H
+#define DMD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DMD_OK                 0
+#define DMD_E_INPUT          (-1)  /* malformed or inconsistent input */
+#define DMD_E_OVERLAP        (-2)  /* overlapping / broken-bond initial state */
+#define DMD_E_NEG_TIME       (-3)  /* negative predicted time beyond 1e-10 (reference debug check) */
+#define DMD_E_DEVICE_TIMEOUT (-4)  /* a bounded device wait gave up */
+#define DMD_E_OOM            (-5)  /* device or host memory exhausted / does not fit */
+#define DMD_E_CUDA           (-6)  /* a CUDA runtime call failed */
+#define DMD_E_CAPACITY       (-7)  /* a fixed-capacity structure (neighbour list, override table) overflowed */
+#define DMD_E_STATE          (-8)  /* call not valid in the handle's current state */
+
+/* Raw PRIME20 parameter tables in angstrom, exactly as the reference reads
+ * them from parameters/ and parametersep/ (code/inputinfo.f:152-420).
+ * Residue identities 9..28 map to row/column index 0..19 (order g r n d q e
+ * h k p s t a c i l m f w y v).  The engine scales by the box inside
+ * (code/scale_down.f:1-87). */
+typedef struct dmd_tables {
+    double sigma[4];      /* protein.data lines 1-4: NH, CA, generic side chain, CO bead diameters */
+    double welldia[4];    /* protein.data lines 5-8 */
+    double epsilon[4];    /* protein.data lines 9-12 (epsilon[0] is the H-bond depth) */
+    double mass[29];      /* mass.data, indexed by identity 1..28 ([0], [3] unused: mass(3)=mass(20)) */
+    double bds[20][20];   /* beadwell_*.data column 5: side-chain pair diameters */
+    double wel[20][20];   /* beadwell_*.data column 6: side-chain pair well diameters */
+    double ep[20][20];    /* parametersep table raw value; the well depth is -value */
+    double rca[20], rnh[20], rco[20];              /* rcarnrco.data columns 1-3 */
+    double del_rca[20], del_rnh[20], del_rco[20];  /* rcarnrco.data columns 4-6 (raised to del) */
+    double sqz[20][5];    /* sqz6to10.data in file column order: sz8, sz6, sz7, sz9, sz10 */
+} dmd_tables;
+
+/* Run settings: the temp_* file (T*, ncoll), the hard-coded constants of
+ * code/main.F90:144-174 and code/def.h, and the -D flags of qfile/script.sh. */
+typedef struct dmd_run_cfg {
+    double   tstar;       /* reduced temperature; setemp = 12 T* (code/main.F90:126-127) */
+    uint64_t seed;        /* key of the counter-based random streams */
+    int32_t  canon;       /* 1: Andersen ghost collisions (-Dcanon) */
+    int32_t  hbonds;      /* 1: backbone H-bonds on (0 = -Dno_hbs) */
+    int32_t  numbin;      /* calendar bins (reference: 2000); kept for reporting */
+    int32_t  n_wrap;      /* cells per neighbour-list radius (reference: 2) */
+    double   rl_const;    /* neighbour-list radius / largest interaction (1.2) */
+    double   t_fact;      /* interval = t_fact / sqrt(setemp) (5e-5) */
+    double   n_forced;    /* list horizon in intervals (150) */
+    int32_t  list_cap;    /* per-bead capacity of each neighbour list (0: default 128) */
+    int32_t  flags;       /* DMD_FLAG_* */
+} dmd_run_cfg;
+
+#define DMD_FLAG_STOP_AT_OUTPUT 1  /* dmd_run returns after every output (N+3) event */
+#define DMD_FLAG_COUNT_PHYSICAL 2  /* dmd_run counts pair + ghost events only (else the reference's coll) */
+#define DMD_FLAG_SERIAL         4  /* one event per step (no conflict-free batching) */
+
+/* One system: chains, sequences, initial state (code/inputinfo.f:5-101,
+ * code/main.F90:240-321). */
+typedef struct dmd_system {
+    int32_t n_beads;
+    int32_t n_chains;
+    const int32_t *chain_len;  /* residues per chain, [n_chains] */
+    const int32_t *residues;   /* residue identity 9..28 per residue, chains concatenated */
+    const int32_t *hp;         /* per-bead hydrophobic flag (hp*.inp), or NULL: 1 for side chains */
+    double boxl;               /* box side in angstrom */
+    const double *x, *y, *z;   /* positions in box units */
+    const double *vx, *vy, *vz;/* velocities */
+    const int32_t *bptnr;      /* H-bond partners, 1-based, or NULL; restored as with -Drunr */
+    double  t0;                /* starting time */
+    int64_t coll0;             /* starting collision count */
+} dmd_system;
+
+/* One committed event of the log (dmd_run's optional ring buffer). */
+typedef struct dmd_event {
+    int64_t coll;      /* reference collision counter after this event */
+    double  t;         /* time of the last interval commit */
+    double  tfalse;    /* event time relative to t */
+    int32_t i, j;      /* beads (1-based); j = 0 for pseudo events */
+    int32_t type;      /* final coltype 1..27, or DMD_EV_* for pseudo events */
+    int32_t evcode;    /* pair type ev_code(i,j) at the event */
+} dmd_event;
+
+#define DMD_EV_GHOST    100
+#define DMD_EV_INTERVAL 101
+#define DMD_EV_REBUILD  102   /* interval event that rebuilt the lists */
+#define DMD_EV_OUTPUT   103
+
+typedef struct dmd_event_log {
+    dmd_event *events;   /* caller-owned ring of capacity entries */
+    int64_t    capacity;
+    int64_t    count;    /* out: events written (may exceed capacity: ring wrapped) */
+} dmd_event_log;
+
+/* Diagnostics of code/energy.f, code/radgyr.f, code/end2end.f plus counters. */
+typedef struct dmd_diag {
+    double  e_total, temperature, rg, e2e, ehh_ii, ehh_ij, e_kin;
+    int32_t hb_alpha, hb_ii, hb_ij, pad;
+    int64_t nevents[32];      /* per final coltype */
+    int64_t coll, n_pair, n_ghost, n_interval, n_output, n_updates, n_forced_updates;
+    double  t, tfalse;
+} dmd_diag;
+
+typedef struct dmd_handle dmd_handle;
+
+/* Replaces the set-up of program dmd (code/main.F90:117-424: inputinfo,
+ * scale_down, make_code, runr restore, nbor_setup, cell_link, nbor, events). */
+int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables,
+               const dmd_system *sys, dmd_handle **out);
+
+/* Replaces the main event loop (code/main.F90:484-1258): commits n_events
+ * events (the reference's coll counting unless DMD_FLAG_COUNT_PHYSICAL).
+ * log may be NULL. */
+int dmd_run(dmd_handle *h, int64_t n_events, dmd_event_log *log);
+
+/* Full prediction pass of code/events.f:11-127 on the current state:
+ * tim/nptnr/coltype per bead (1-based partners, times relative to t). */
+int dmd_predict_all(dmd_handle *h, double *tim, int32_t *nptnr, int32_t *coltype);
+
+/* State read-back: positions advanced to the current time (box units),
+ * velocities, H-bond partners, identities, extra_repuls (4 per bead). */
+int dmd_get_state(dmd_handle *h, double *x, double *y, double *z,
+                  double *vx, double *vy, double *vz, int32_t *bptnr,
+                  int32_t *identity, int32_t *extra_repuls,
+                  double *t, double *tfalse, int64_t *coll);
+
+/* Replaces code/energy.f, code/radgyr.f, code/end2end.f at the current time. */
+int dmd_diagnostics(dmd_handle *h, dmd_diag *out);
+
+/* Dense pair-type table ev_code (n_beads x n_beads, row-major, 1-based
+ * rows/cols mapped to 0-based), reconstructed from the rule function and
+ * the shoulder overrides (code/make_code.f:6-573, code/repuls_add.f). */
+int dmd_get_evcode(dmd_handle *h, int8_t *out);
+
+void dmd_destroy(dmd_handle *h);
+
+const char *dmd_last_error(dmd_handle *h);
+const char *dmd_version(void);
+
+/* ---- batched replicas: many independent systems in one persistent launch
+ * (no reference counterpart: the reference runs one system per MPI job). */
+typedef struct dmd_batch dmd_batch;
+int dmd_batch_create(int32_t n, const dmd_run_cfg *cfgs, const dmd_tables *tables,
+                     const dmd_system *systems, dmd_batch **out);
+/* Advances every replica by n_events (per replica); per-replica logs optional. */
+int dmd_batch_run(dmd_batch *b, int64_t n_events, dmd_event_log *logs);
+int dmd_batch_get_state(dmd_batch *b, int32_t r, double *x, double *y, double *z,
+                        double *vx, double *vy, double *vz, int32_t *bptnr,
+                        int32_t *identity, int32_t *extra_repuls,
+                        double *t, double *tfalse, int64_t *coll);
+int dmd_batch_diagnostics(dmd_batch *b, int32_t r, dmd_diag *out);
+void dmd_batch_destroy(dmd_batch *b);
+const char *dmd_batch_last_error(dmd_batch *b);
+
+/* ---- synthetic systems (restates the insertion and velocity steps of
+ * genconfig/gen_config_random-SQZ.f90:665-891 on an extended template). */
+typedef struct dmd_gen_spec {
+    int32_t n_chains;
+    const int32_t *chain_len;  /* residues per chain */
+    const int32_t *residues;   /* residue identities 9..28, concatenated */
+    double  boxl;              /* angstrom */
+    double  tstar;
+    uint64_t seed;
+    double  min_sep;           /* inter-chain rejection distance, angstrom (5) */
+} dmd_gen_spec;
+/* Fills positions (box units) and velocities of n_beads beads. */
+int dmd_generate(const dmd_gen_spec *spec, const dmd_tables *tables, int32_t n_beads,
+                 double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                 char *err, int32_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMD_H */

@@ -1,0 +1,142 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes binding of the CPU restatement of the
+reference engine (dmd_oracle.cpp).  It is the checker of the GB300 engine
+and the timed CPU baseline; the product never imports it."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(REPO, "parallel-dmd-for-biomolecules_gb300"))
+from dmdgb import abi  # noqa: E402
+from dmdgb.params import default_tables  # noqa: E402
+
+LIB_PATH = os.path.join(HERE, "_build", "libdmd_oracle.so")
+_lib = None
+
+
+def build() -> str:
+    r = subprocess.run(["make", "-C", HERE], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.ora_create.restype = C.c_void_p
+        L.ora_create.argtypes = [C.POINTER(abi.RunCfg), C.POINTER(abi.Tables), C.POINTER(abi.System), C.c_char_p, C.c_int]
+        L.ora_run.restype = C.c_int64
+        L.ora_run.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+        L.ora_predict_all.argtypes = [C.c_void_p, abi.dbl_p, abi.i32_p, abi.i32_p]
+        L.ora_get_state.argtypes = [C.c_void_p] + [abi.dbl_p] * 6 + [abi.i32_p] * 3 + [abi.dbl_p, abi.dbl_p, abi.i64_p]
+        L.ora_diagnostics.argtypes = [C.c_void_p, C.POINTER(abi.Diag)]
+        L.ora_get_evcode.argtypes = [C.c_void_p, abi.i8_p]
+        L.ora_get_lists.argtypes = [C.c_void_p, abi.i32_p, abi.i32_p, abi.i32_p, abi.i32_p, C.c_int32]
+        L.ora_get_scalars.argtypes = [C.c_void_p, abi.dbl_p, C.c_int]
+        L.ora_n_outputs.argtypes = [C.c_void_p]
+        L.ora_get_output.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.Diag)]
+        L.ora_destroy.argtypes = [C.c_void_p]
+        L.ora_destroy.restype = None
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    def __init__(self, spec, tables=None, flags: int = 0, list_cap: int = 0):
+        self.L = lib()
+        self.spec = spec
+        self.n = spec.n_beads
+        self._tables = abi.tables_struct(tables or default_tables())
+        self._cfg = spec.run_cfg(flags, list_cap)
+        self._sys = spec.c_system()
+        err = C.create_string_buffer(512)
+        self.h = self.L.ora_create(C.byref(self._cfg), C.byref(self._tables), C.byref(self._sys), err, 512)
+        if not self.h:
+            raise RuntimeError("oracle create failed: " + err.value.decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ora_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, n_events: int, log_capacity: int = 0):
+        if log_capacity > 0:
+            buf = np.zeros(log_capacity, abi.EVENT_DTYPE)
+            n = self.L.ora_run(self.h, int(n_events), buf.ctypes.data, log_capacity)
+            if n < 0:
+                raise RuntimeError("oracle run failed")
+            return buf[:min(n, log_capacity)]
+        n = self.L.ora_run(self.h, int(n_events), None, 1)
+        if n < 0:
+            raise RuntimeError("oracle run failed")
+        return n
+
+    def predictions(self):
+        tim = np.zeros(self.n)
+        np_ = np.zeros(self.n, np.int32)
+        ct = np.zeros(self.n, np.int32)
+        self.L.ora_predict_all(self.h, abi.ptr(tim, abi.dbl_p), abi.ptr(np_, abi.i32_p), abi.ptr(ct, abi.i32_p))
+        return tim, np_, ct
+
+    def state(self) -> dict:
+        n = self.n
+        a = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        bp = np.zeros(n, np.int32)
+        ident = np.zeros(n, np.int32)
+        er = np.zeros(4 * n, np.int32)
+        t = C.c_double()
+        tf = C.c_double()
+        coll = C.c_int64()
+        self.L.ora_get_state(self.h, *[abi.ptr(a[k], abi.dbl_p) for k in ("x", "y", "z", "vx", "vy", "vz")],
+                             abi.ptr(bp, abi.i32_p), abi.ptr(ident, abi.i32_p), abi.ptr(er, abi.i32_p),
+                             C.byref(t), C.byref(tf), C.byref(coll))
+        a.update(bptnr=bp, identity=ident, extra_repuls=er.reshape(n, 4), t=t.value, tfalse=tf.value, coll=coll.value)
+        return a
+
+    def diagnostics(self) -> dict:
+        d = abi.Diag()
+        self.L.ora_diagnostics(self.h, C.byref(d))
+        return d.as_dict()
+
+    def evcode(self) -> np.ndarray:
+        out = np.zeros((self.n, self.n), np.int8)
+        self.L.ora_get_evcode(self.h, out.ctypes.data_as(abi.i8_p))
+        return out
+
+    def lists(self, cap: int = 256):
+        n = self.n
+        uc = np.zeros(n, np.int32)
+        dc = np.zeros(n, np.int32)
+        up = np.zeros(n * cap, np.int32)
+        dn = np.zeros(n * cap, np.int32)
+        self.L.ora_get_lists(self.h, abi.ptr(uc, abi.i32_p), abi.ptr(up, abi.i32_p), abi.ptr(dc, abi.i32_p),
+                             abi.ptr(dn, abi.i32_p), cap)
+        return uc, up.reshape(n, cap), dc, dn.reshape(n, cap)
+
+    def scalars(self) -> dict:
+        out = np.zeros(16)
+        self.L.ora_get_scalars(self.h, abi.ptr(out, abi.dbl_p), 16)
+        keys = ["interval", "interval_max", "sig_max_all", "hdelr", "num_cell", "width", "rlsq1", "rlsq15",
+                "rlsq16", "rlsq40", "n_forced", "t_fact", "evp1_15", "tim_ghost", "tim_interval", "tim_output"]
+        return dict(zip(keys, out.tolist()))
+
+    def outputs(self):
+        out = []
+        for k in range(self.L.ora_n_outputs(self.h)):
+            d = abi.Diag()
+            self.L.ora_get_output(self.h, k, C.byref(d))
+            out.append(d.as_dict())
+        return out

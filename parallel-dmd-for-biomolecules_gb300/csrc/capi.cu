@@ -1,0 +1,721 @@
+/*
+ * capi.cu -- host side of the C ABI (include/dmd.h).
+ *
+ * Turns the reference's input surface (raw parameter tables, chains,
+ * positions, velocities, H-bond partners) into the device layout of
+ * engine.cuh, then drives the kernels of engine.cu.  The set-up restates
+ * code/inputinfo.f:5-669, code/scale_down.f:1-87, code/make_code.f:15-60,
+ * code/nbor_setup.f:1-132 and the runr restore of code/main.F90:240-321.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "dmd.h"
+#include "engine.cuh"
+#include "engine_api.h"
+
+namespace {
+
+const double DEL = 0.02375;
+const double DNC = 1.46, DCC = 1.51, DCN = 1.33, DCACA = 3.8, DTIE = 2.41, DTIE2 = 2.45;
+const double SQZ[6] = {0, 1.1436, 0.88, 0.87829, 0.8, 0.7713};
+const double MAX_BOND_ANGSTROM = 6.5;  /* longest bonded pair (R-CO of arginine with its window) */
+
+struct HostSys {
+    dmd_run_cfg cfg;
+    int N = 0, nchains = 0, cap = 128, ncell = 0, nl1 = 0, nl2 = 0;
+    std::vector<int> chain_start, chain_len;
+    std::vector<BeadInfo> info;
+    std::vector<double> bm, blmin, blmax;
+    std::vector<double> x, y, z, vx, vy, vz;
+    std::vector<int8_t> ident;
+    std::vector<int> bptnr, er, ovp;
+    std::vector<int8_t> ovc;
+    DTab tab;
+    DScal sc;
+    double sigma_raw[29] = {}, welldia_raw[29] = {};
+    double sig_max[DMD_NC] = {}, sig_max_all = 0;
+};
+
+bool fail(std::string &err, const std::string &m) { err = m; return false; }
+
+/* code/inputinfo.f + scale_down.f + make_code.f:15-60 */
+void build_tables(HostSys &H, const dmd_tables *T, double boxl) {
+    DTab &D = H.tab;
+    std::memset(&D, 0, sizeof D);
+    double sigma[29] = {}, welldia[29] = {}, eps[29] = {}, bds[29][29] = {}, wel[29][29] = {}, ep[29][29] = {};
+    for (int k = 1; k <= 4; ++k) {
+        sigma[k] = T->sigma[k - 1]; welldia[k] = T->welldia[k - 1]; eps[k] = T->epsilon[k - 1];
+        sigma[k + 4] = sigma[k]; welldia[k + 4] = welldia[k]; eps[k + 4] = eps[k];
+    }
+    for (int a = 9; a <= 28; ++a)
+        for (int b = 9; b <= 28; ++b) { bds[a][b] = T->bds[a - 9][b - 9]; wel[a][b] = T->wel[a - 9][b - 9]; ep[a][b] = -T->ep[a - 9][b - 9]; }
+    for (int i = 9; i <= 28; ++i) { sigma[i] = 1.00 * bds[i][i]; welldia[i] = 1.5 * sigma[i]; }
+    sigma[9] = 1.00 * bds[9][9] - 1.2;
+    for (int i = 1; i <= 20; ++i) {
+        double sz8 = T->sqz[i - 1][0], sz6 = T->sqz[i - 1][1], sz7 = T->sqz[i - 1][2], sz9 = T->sqz[i - 1][3], sz10 = T->sqz[i - 1][4];
+        D.sqz610[1][i + 8] = sz6 * 2 / (sigma[i + 8] + sigma[4]);
+        D.sqz610[2][i + 8] = sz7 * 2 / (sigma[i + 8] + sigma[1]);
+        D.sqz610[3][i + 8] = sz8 * 2 / (sigma[i + 8] + sigma[2]);
+        D.sqz610[4][i + 8] = sz9 * 2 / (sigma[i + 8] + sigma[2]);
+        D.sqz610[5][i + 8] = sz10 * 2 / (sigma[i + 8] + sigma[4]);
+    }
+    const double B = boxl;
+    for (int k = 1; k <= 28; ++k) { sigma[k] = sigma[k] / B; welldia[k] = welldia[k] / B; }
+    D.shd1 = 5.00 / B; D.shd2 = 4.74 / B; D.shd3 = 4.86 / B; D.shd4 = 4.83 / B;
+    for (int k = 1; k <= 28; ++k)
+        for (int kk = 1; kk <= 28; ++kk) {
+            double s = sigma[k] + sigma[kk];
+            D.sigma_sq[k][kk] = 0.25 * (s * s);
+            double w = welldia[k] + welldia[kk];
+            D.welldia_sq[k][kk] = 0.25 * (w * w);
+            D.ep_sqrt[k][kk] = std::sqrt(eps[k] * eps[kk]);
+            D.shlddia_sq[k][kk] = D.shd4 * D.shd4;
+        }
+    for (int k = 9; k <= 28; ++k)
+        for (int kk = 9; kk <= 28; ++kk) {
+            D.ep_sqrt[k][kk] = eps[1] * ep[k][kk];
+            D.sigma_sq[k][kk] = (bds[k][kk] * bds[k][kk]) / (B * B);
+            D.welldia_sq[k][kk] = (wel[k][kk] * wel[k][kk]) / (B * B);
+        }
+    double d1 = D.shd1 * D.shd1, d2 = D.shd2 * D.shd2, d3 = D.shd3 * D.shd3;
+    D.shlddia_sq[1][2] = d1; D.shlddia_sq[2][1] = d1; D.shlddia_sq[5][2] = d1; D.shlddia_sq[2][5] = d1;
+    D.shlddia_sq[1][1] = d2; D.shlddia_sq[5][5] = d2; D.shlddia_sq[1][5] = d2; D.shlddia_sq[5][1] = d2;
+    D.shlddia_sq[2][4] = d3; D.shlddia_sq[4][2] = d3; D.shlddia_sq[2][8] = d3; D.shlddia_sq[8][2] = d3;
+    for (int l = 0; l < DMD_NC; ++l) { D.evp1[l] = 1; D.evp2[l] = 1; D.evp3[l] = 1; }
+    D.evp1[15] = 1.05 * ((2.24 / B) / ((sigma[1] + sigma[4]) / 2.0));
+    for (int k = 1; k <= 5; ++k) D.evp1[16 + k] = SQZ[k];
+    D.evp1[27] = 1.0;
+    const double bl[10] = {0, 0, 0, 0, DNC, DCC, DCN, DTIE, DTIE2, DCACA};
+    for (int c = 4; c <= 6; ++c) { D.evp2[c] = bl[c] * (1.0 - DEL) / B; D.evp3[c] = bl[c] * (1.0 + DEL) / B; }
+    for (int c = 7; c <= 9; ++c) { D.evp2[c] = bl[c] * (1.0 - DEL) / B; D.evp3[c] = (1.0 + DEL) * bl[c] / B; }
+    for (int c = 10; c <= 12; ++c) { D.evp2[c] = (1.0 - DEL); D.evp3[c] = (1.0 + DEL); }
+    D.eps1 = eps[1];
+    D.eps_hb = D.ep_sqrt[5][8];
+    D.boxl_orig = B;
+    /* kept for nbor_setup: scaled bead diameters and the side-chain wells */
+    for (int k = 1; k <= 28; ++k) { H.sigma_raw[k] = sigma[k]; H.welldia_raw[k] = welldia[k]; }
+    (void)wel;
+}
+
+double sig_of(const HostSys &H, const dmd_tables *T, int code, int a, int b) {  /* code/nbor_setup.f:22-38 */
+    if (code <= 3) {
+        if (a >= 9 && b >= 9) return T->bds[a - 9][b - 9] / H.tab.boxl_orig;
+        return 0.50 * (H.sigma_raw[a] + H.sigma_raw[b]);
+    }
+    if (code == 15) return 0.5 * (H.welldia_raw[a] + H.welldia_raw[b]);
+    if (code == 16) return T->wel[a - 9][b - 9] / H.tab.boxl_orig;
+    return 0.0;
+}
+
+/* code/nbor_setup.f:1-132: cutoffs from the maximum over every pair type
+ * present in the system (intra-chain pairs of each distinct chain, and the
+ * identity combinations that meet across two different chains) */
+void nbor_setup(HostSys &H, const dmd_tables *T, int hbonds) {
+    for (int c = 0; c < DMD_NC; ++c) H.sig_max[c] = 0.0;
+    H.sig_max_all = 0.0;
+    auto visit = [&](int code, int a, int b) {
+        if (code > 26) return;
+        double s = sig_of(H, T, code, a, b);
+        if (s > H.sig_max[code]) { H.sig_max[code] = s; if (s > H.sig_max_all) H.sig_max_all = s; }
+    };
+    std::set<std::vector<int>> seen;
+    for (int c = 0; c < H.nchains; ++c) {
+        int s = H.chain_start[c], nb = (c + 1 < H.nchains ? H.chain_start[c + 1] : H.N) - s;
+        std::vector<int> key;
+        key.push_back(H.chain_len[c]);
+        for (int q = 0; q < nb; ++q) { key.push_back(H.ident[s + q]); key.push_back(H.info[s + q].hp); }
+        if (!seen.insert(key).second) continue;
+        for (int a = s; a < s + nb; ++a)
+            for (int b = a + 1; b < s + nb; ++b) visit(static_code(H.info[b], H.info[a], hbonds), H.ident[a], H.ident[b]);
+    }
+    /* inter-chain: (identity, hp, kind, pro) signatures and the chains holding them */
+    std::map<std::vector<int>, std::set<int>> sig_chains;
+    for (int b = 0; b < H.N; ++b) {
+        const BeadInfo &I = H.info[b];
+        std::vector<int> k = {H.ident[b], I.hp, I.kind, I.pro_nh};
+        auto &st = sig_chains[k];
+        if (st.size() < 2) st.insert(I.chain);
+    }
+    for (auto &p : sig_chains)
+        for (auto &q : sig_chains) {
+            bool meet = false;
+            for (int c1 : p.second) for (int c2 : q.second) if (c1 != c2) meet = true;
+            if (!meet) continue;
+            BeadInfo A{}, Bq{};
+            A.kind = (int8_t)p.first[2]; A.hp = (int8_t)p.first[1]; A.pro_nh = (int8_t)p.first[3];
+            Bq.kind = (int8_t)q.first[2]; Bq.hp = (int8_t)q.first[1]; Bq.pro_nh = (int8_t)q.first[3];
+            for (int order = 0; order < 2; ++order) {
+                A.chain = order; Bq.chain = 1 - order;
+                visit(static_code(Bq, A, hbonds), p.first[0], q.first[0]);
+            }
+        }
+    double sigij = 0.0, sg = 0.0;
+    for (int i = 1; i <= 4; ++i)
+        for (int j = 1; j <= 4; ++j) {
+            if ((i != 3) || (j != 3)) sg = H.sigma_raw[i] + H.sigma_raw[j];
+            if (sg > sigij) sigij = sg;
+        }
+    for (int i = 40; i <= 50; ++i) {
+        H.sig_max[i] = 0.5 * sigij * 1.0;
+        if (H.sig_max[i] > H.sig_max_all) H.sig_max_all = H.sig_max[i];
+    }
+    const double rl_const = H.cfg.rl_const;
+    for (int i = 1; i <= 50; ++i) {
+        H.tab.rlsq[i] = 0.0;
+        if (H.sig_max[i] != 0.0) { double r = (rl_const - 1) * H.sig_max_all + H.sig_max[i]; H.tab.rlsq[i] = r * r; }
+    }
+    double rl = rl_const * H.sig_max_all;
+    double h = 0.4 * (rl - H.sig_max_all);
+    H.tab.hdelr = h * h;
+    H.tab.rl = rl;
+    double wmin = std::max(rl, MAX_BOND_ANGSTROM / H.tab.boxl_orig);
+    H.ncell = (int)std::floor(1.0 / wmin);
+    if (H.ncell < 3) H.ncell = 1;  /* small box: all-pairs list build */
+}
+
+void repuls_add_host(HostSys &H, int i, int j, int hbonds, std::string &err) {
+    auto set = [&](int a, int b, int code) {
+        int st = static_code(H.info[a], H.info[b], hbonds);
+        for (int s = 0; s < 4; ++s)
+            if (H.ovp[4 * a + s] == b) { if (code == st) H.ovp[4 * a + s] = -1; else H.ovc[4 * a + s] = (int8_t)code; return; }
+        if (code == st) return;
+        for (int s = 0; s < 4; ++s)
+            if (H.ovp[4 * a + s] < 0) { H.ovp[4 * a + s] = b; H.ovc[4 * a + s] = (int8_t)code; return; }
+        err = "shoulder override table full";
+    };
+    int Li = H.info[i].L, Lj = H.info[j].L;
+    int ncim1 = i + Li - 1, ncai = i - Li, ncaj = j - 2 * Lj, nnjp1 = j - Lj + 1;
+    set(ncaj, i, 50); set(i, ncaj, 40); set(i, nnjp1, 40); set(nnjp1, i, 50);
+    set(ncai, j, 50); set(j, ncai, 40); set(j, ncim1, 40); set(ncim1, j, 50);
+    int *er = H.er.data();
+    er[4 * i + 0] = ncaj; er[4 * i + 1] = nnjp1; er[4 * ncaj + 2] = i; er[4 * nnjp1 + 2] = i;
+    er[4 * j + 0] = ncai; er[4 * j + 1] = ncim1; er[4 * ncai + 2] = j; er[4 * ncim1 + 2] = j;
+    er[4 * i + 3] = j; er[4 * j + 3] = i;
+}
+
+bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const dmd_system *S, std::string &err) {
+    H.cfg = *cfg;
+    if (H.cfg.rl_const <= 0) H.cfg.rl_const = 1.2;
+    if (H.cfg.t_fact <= 0) H.cfg.t_fact = 0.00005;
+    if (H.cfg.n_forced <= 0) H.cfg.n_forced = 150.0;
+    if (H.cfg.n_wrap <= 0) H.cfg.n_wrap = 2;
+    if (H.cfg.numbin <= 0) H.cfg.numbin = 2000;
+    H.cap = cfg->list_cap > 0 ? cfg->list_cap : 128;
+    if (!(cfg->tstar > 0)) return fail(err, "tstar must be positive");
+    if (!S || S->n_beads <= 0 || S->n_chains <= 0 || !S->chain_len || !S->residues) return fail(err, "empty system");
+    if (!S->x || !S->y || !S->z || !S->vx || !S->vy || !S->vz) return fail(err, "positions and velocities are required");
+    if (!(S->boxl > 0)) return fail(err, "boxl must be positive");
+    const int hbonds = cfg->hbonds != 0;
+    H.N = S->n_beads;
+    H.nchains = S->n_chains;
+    H.info.assign(H.N, BeadInfo{});
+    H.ident.assign(H.N, 0);
+    H.chain_start.assign(H.nchains, 0);
+    H.chain_len.assign(H.nchains, 0);
+    H.blmin.assign(H.N, 0.0);
+    H.blmax.assign(H.N, 0.0);
+    double bmass[29];
+    for (int k = 0; k < 29; ++k) bmass[k] = T->mass[k];
+    bmass[3] = bmass[20];
+    for (int k = 1; k <= 4; ++k) bmass[k + 4] = bmass[k];
+    int pos = 0, rpos = 0;
+    for (int c = 0; c < H.nchains; ++c) {
+        int L = S->chain_len[c];
+        if (L < 3 || L > 30000) return fail(err, "chain length out of range");
+        int nr = 0;
+        for (int k = 0; k < L; ++k) {
+            int r = S->residues[rpos + k];
+            if (r < 9 || r > 28) return fail(err, "residue identity out of 9..28");
+            nr += r != 9;
+        }
+        int nb = 3 * L + nr;
+        if (pos + nb > H.N) return fail(err, "n_beads smaller than the chains need");
+        H.chain_start[c] = pos;
+        H.chain_len[c] = L;
+        for (int k = 1; k <= L; ++k) {
+            int idx[3] = {pos + k - 1, pos + L + k - 1, pos + 2 * L + k - 1};
+            int kinds[3] = {BK_CA, BK_NH, BK_CO};
+            int ids[3] = {2, 1, 4};
+            for (int m = 0; m < 3; ++m) {
+                BeadInfo &I = H.info[idx[m]];
+                I.chain = c; I.cstart = pos; I.L = (int16_t)L; I.res = (int16_t)k; I.kind = (int8_t)kinds[m];
+                I.hp = 0; I.pro_nh = 0; I.is_end = 0;
+                H.ident[idx[m]] = (int8_t)ids[m];
+            }
+            if (k == 1) H.info[pos + L].is_end = 1;           /* NH of residue 1 (local L+1) */
+            if (k == L) H.info[pos + 2 * L + L - 1].is_end = 1; /* CO of residue L (local 3L) */
+        }
+        int q = 0;
+        for (int k = 1; k <= L; ++k) {
+            int r = S->residues[rpos + k - 1];
+            int iii = r != 9 ? r - 8 : 1;  /* code/inputinfo.f:300-318: glycine takes row 1 */
+            double dra = std::max(T->del_rca[iii - 1], DEL), drn = std::max(T->del_rnh[iii - 1], DEL),
+                   drc = std::max(T->del_rco[iii - 1], DEL);
+            double lca = T->rca[iii - 1] / S->boxl, lnh = T->rnh[iii - 1] / S->boxl, lco = T->rco[iii - 1] / S->boxl;
+            H.blmin[pos + k - 1] = (1.0 - dra) * lca; H.blmax[pos + k - 1] = (1.0 + dra) * lca;
+            H.blmin[pos + L + k - 1] = (1.0 - drn) * lnh; H.blmax[pos + L + k - 1] = (1.0 + drn) * lnh;
+            H.blmin[pos + 2 * L + k - 1] = (1.0 - drc) * lco; H.blmax[pos + 2 * L + k - 1] = (1.0 + drc) * lco;
+            if (r == 9) continue;
+            ++q;
+            int b = pos + 3 * L + q - 1;
+            BeadInfo &I = H.info[b];
+            I.chain = c; I.cstart = pos; I.L = (int16_t)L; I.res = (int16_t)k; I.kind = BK_R;
+            I.hp = 1; I.pro_nh = 0; I.is_end = 0;
+            H.ident[b] = (int8_t)r;
+            if (r == 17) H.info[pos + L + q - 1].pro_nh = 1;  /* code/make_code.f:145-169 */
+        }
+        if (S->hp)
+            for (int m = 0; m < nb; ++m) H.info[pos + m].hp = (int8_t)(S->hp[pos + m] != 0);
+        pos += nb;
+        rpos += L;
+    }
+    if (pos != H.N) return fail(err, "n_beads larger than the chains need");
+    H.bm.assign(H.N, 0.0);
+    for (int b = 0; b < H.N; ++b) H.bm[b] = bmass[H.ident[b]];
+
+    build_tables(H, T, S->boxl);
+    H.tab.setemp = cfg->tstar * 12.0;
+    H.tab.avegtime = 0.00005 / std::sqrt(H.tab.setemp);
+
+    H.x.assign(S->x, S->x + H.N); H.y.assign(S->y, S->y + H.N); H.z.assign(S->z, S->z + H.N);
+    H.vx.assign(S->vx, S->vx + H.N); H.vy.assign(S->vy, S->vy + H.N); H.vz.assign(S->vz, S->vz + H.N);
+    for (int k = 0; k < H.N; ++k) {
+        if (!std::isfinite(H.x[k]) || !std::isfinite(H.y[k]) || !std::isfinite(H.z[k]) ||
+            !std::isfinite(H.vx[k]) || !std::isfinite(H.vy[k]) || !std::isfinite(H.vz[k]))
+            return fail(err, "non-finite position or velocity");
+        H.x[k] = H.x[k] - std::round(H.x[k]); H.y[k] = H.y[k] - std::round(H.y[k]); H.z[k] = H.z[k] - std::round(H.z[k]);
+    }
+    H.bptnr.assign(H.N, -1);
+    H.er.assign((size_t)4 * H.N, -1);
+    H.ovp.assign((size_t)4 * H.N, -1);
+    H.ovc.assign((size_t)4 * H.N, 0);
+    nbor_setup(H, T, hbonds);
+    if (S->bptnr) {  /* code/main.F90:240-321 */
+        for (int k = 0; k < H.N; ++k) {
+            int p = S->bptnr[k];
+            if (p < 0 || p > H.N) return fail(err, "bptnr out of range");
+            H.bptnr[k] = p - 1;
+        }
+        for (int k = 0; k < H.N - 1; ++k)
+            for (int kj = k + 1; kj < H.N; ++kj) {
+                if (H.ident[k] + H.ident[kj] == 5 && static_code(H.info[k], H.info[kj], hbonds) == 15) {
+                    bool over = false;
+                    for (int s = 0; s < 4; ++s) if (H.ovp[4 * k + s] == kj) over = true;
+                    if (!over) {
+                        double rx = H.x[k] - H.x[kj], ry = H.y[k] - H.y[kj], rz = H.z[k] - H.z[kj];
+                        rx = rx - std::round(rx); ry = ry - std::round(ry); rz = rz - std::round(rz);
+                        double r2 = rx * rx + ry * ry + rz * rz;
+                        double diff = r2 - H.tab.welldia_sq[H.ident[k]][H.ident[kj]];
+                        if (diff < 0.0 && !H.info[k].is_end && !H.info[kj].is_end) {
+                            if (H.ident[k] == 1) repuls_add_host(H, k, kj, hbonds, err); else repuls_add_host(H, kj, k, hbonds, err);
+                            if (!err.empty()) return false;
+                        }
+                    }
+                }
+                if (kj == H.bptnr[k]) {
+                    if (H.ident[k] == 1) { H.ident[k] = 5; H.ident[kj] = 8; } else { H.ident[k] = 8; H.ident[kj] = 5; }
+                }
+            }
+    }
+    /* scalars (code/main.F90:144-156, 198-234, 408-423) */
+    std::memset(&H.sc, 0, sizeof H.sc);
+    H.sc.t = S->t0;
+    H.sc.coll = S->coll0;
+    H.sc.t_fact = H.cfg.t_fact;
+    H.sc.n_forced = H.cfg.n_forced;
+    H.sc.interval = H.sc.t_fact / std::sqrt(H.tab.setemp);
+    H.sc.interval_max = H.sc.n_forced * H.sc.interval;
+    H.nl1 = (H.N + 3 + 31) / 32;
+    H.nl2 = (H.nl1 + 31) / 32;
+    return true;
+}
+
+/* ------------------------------------------------------------------ */
+/* device memory of a set of systems                                   */
+/* ------------------------------------------------------------------ */
+struct DevSys {
+    DSys d;          /* device pointers */
+    void *pool = nullptr;
+    size_t bytes = 0;
+};
+
+struct Pool {
+    char *base;
+    size_t off;
+    template <class T> T *take(size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T *p = (T *)(base + off);
+        off += n * sizeof(T);
+        return p;
+    }
+};
+
+size_t layout(const HostSys &H, DSys &d, char *base) {
+    Pool P{base, 0};
+    size_t N = H.N, NE = H.N + 3, cap = H.cap;
+    size_t nc3 = (size_t)H.ncell * H.ncell * H.ncell;
+    d.tab = P.take<DTab>(1);
+    d.sc = P.take<DScal>(1);
+    d.info = P.take<BeadInfo>(N);
+    d.bm = P.take<double>(N); d.blmin = P.take<double>(N); d.blmax = P.take<double>(N);
+    d.x = P.take<double>(N); d.y = P.take<double>(N); d.z = P.take<double>(N);
+    d.vx = P.take<double>(N); d.vy = P.take<double>(N); d.vz = P.take<double>(N);
+    d.ox = P.take<double>(N); d.oy = P.take<double>(N); d.oz = P.take<double>(N);
+    d.ident = P.take<int8_t>(N);
+    d.bptnr = P.take<int>(N);
+    d.er = P.take<int>(4 * N);
+    d.ovp = P.take<int>(4 * N);
+    d.ovc = P.take<int8_t>(4 * N);
+    d.tim = P.take<double>(NE); d.nptnr = P.take<int>(NE); d.colt = P.take<int8_t>(NE); d.queued = P.take<uint8_t>(NE);
+    d.up = P.take<int>(N * cap); d.dn = P.take<int>(N * cap); d.upc = P.take<int8_t>(N * cap);
+    d.upn = P.take<int>(N); d.dnn = P.take<int>(N);
+    d.cell_count = P.take<int>(nc3 + 1); d.cell_start = P.take<int>(nc3 + 1); d.cell_beads = P.take<int>(N);
+    d.l1i = P.take<int>(H.nl1); d.l2i = P.take<int>(H.nl2);
+    return P.off + 256;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) { err = std::string(#call) + ": " + cudaGetErrorString(e_); return DMD_E_CUDA; } \
+    } while (0)
+
+}  // namespace
+
+/* ---------------------------------------------------------------------- */
+struct dmd_batch {
+    std::vector<HostSys> hs;
+    std::vector<DevSys> ds;
+    DSys *d_sys = nullptr;
+    int *d_cstart = nullptr, *d_clen = nullptr, *d_coff = nullptr;
+    dmd_diag *d_diag = nullptr;
+    dmd_event *d_log = nullptr;
+    long long log_cap = 0;
+    int hbonds = 1;
+    cudaStream_t st = nullptr;
+    std::string err;
+    int ready = 0;
+};
+struct dmd_handle { dmd_batch b; };
+
+namespace {
+
+int upload(dmd_batch &B) {
+    std::string &err = B.err;
+    int n = (int)B.hs.size();
+    B.ds.resize(n);
+    CK(cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking));
+    std::vector<DSys> hd(n);
+    std::vector<int> cstart, clen, coff;
+    for (int r = 0; r < n; ++r) {
+        HostSys &H = B.hs[r];
+        DevSys &D = B.ds[r];
+        DSys tmp{};
+        size_t bytes = layout(H, tmp, nullptr);
+        CK(cudaMalloc(&D.pool, bytes));
+        D.bytes = bytes;
+        DSys &d = D.d;
+        layout(H, d, (char *)D.pool);
+        d.N = H.N; d.nchains = H.nchains; d.cap = H.cap; d.ncell = H.ncell;
+        d.seed = H.cfg.seed; d.canon = H.cfg.canon; d.flags = H.cfg.flags;
+        d.nl1 = H.nl1; d.nl2 = H.nl2;
+        d.log = nullptr; d.log_cap = 0;
+        size_t N = H.N;
+        CK(cudaMemcpy((void *)d.tab, &H.tab, sizeof(DTab), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.sc, &H.sc, sizeof(DScal), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((void *)d.info, H.info.data(), N * sizeof(BeadInfo), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((void *)d.bm, H.bm.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((void *)d.blmin, H.blmin.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((void *)d.blmax, H.blmax.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.x, H.x.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.y, H.y.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.z, H.z.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.vx, H.vx.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.vy, H.vy.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.vz, H.vz.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.ident, H.ident.data(), N, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.bptnr, H.bptnr.data(), N * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.er, H.er.data(), 4 * N * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.ovp, H.ovp.data(), 4 * N * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.ovc, H.ovc.data(), 4 * N, cudaMemcpyHostToDevice));
+        /* pseudo events (code/main.F90:408-423) and bead placeholders */
+        std::vector<double> tim(N + 3, H.sc.interval_max + DMD_LTSTEP);
+        std::vector<int> np(N + 3, -1);
+        std::vector<int8_t> ct(N + 3, -1);
+        std::vector<uint8_t> q(N + 3, 0);
+        if (H.cfg.canon) {
+            double tgho = 0.0;
+            uint32_t k = 0;
+            while ((tgho < 1e-18) || (tgho == 1.0)) tgho = dmd_uniform(H.cfg.seed, DMD_STREAM_GHOST0, 0, k++);
+            tim[N] = -1.0 * dmd_log(tgho) * H.tab.avegtime * .0000001;
+        } else {
+            tim[N] = 1000000000.0;
+        }
+        tim[N + 1] = H.sc.interval;
+        tim[N + 2] = 3.3 / (std::sqrt(H.tab.setemp)) + 5;
+        np[N] = np[N + 1] = np[N + 2] = -2;
+        ct[N] = ct[N + 1] = ct[N + 2] = -2;
+        CK(cudaMemcpy(d.tim, tim.data(), (N + 3) * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.nptnr, np.data(), (N + 3) * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.colt, ct.data(), N + 3, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d.queued, q.data(), N + 3, cudaMemcpyHostToDevice));
+        hd[r] = d;
+        coff.push_back((int)cstart.size());
+        for (int c = 0; c < H.nchains; ++c) { cstart.push_back(H.chain_start[c]); clen.push_back(H.chain_len[c]); }
+    }
+    CK(cudaMalloc(&B.d_sys, n * sizeof(DSys)));
+    CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&B.d_cstart, cstart.size() * 4));
+    CK(cudaMalloc(&B.d_clen, clen.size() * 4));
+    CK(cudaMalloc(&B.d_coff, coff.size() * 4));
+    CK(cudaMemcpy(B.d_cstart, cstart.data(), cstart.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_clen, clen.data(), clen.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_coff, coff.data(), coff.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&B.d_diag, n * sizeof(dmd_diag)));
+    CK(dmd_launch_init(B.d_sys, n, B.hbonds, B.st));
+    CK(cudaStreamSynchronize(B.st));
+    for (int r = 0; r < n; ++r) {
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        if (sc.err) { err = "device error during list build (code " + std::to_string(sc.err) + ")"; return sc.err; }
+    }
+    B.ready = 1;
+    return DMD_OK;
+}
+
+int batch_create(dmd_batch &B, int n, const dmd_run_cfg *cfgs, const dmd_tables *tables, const dmd_system *systems) {
+    if (n <= 0 || !cfgs || !tables || !systems) { B.err = "null or empty argument"; return DMD_E_INPUT; }
+    B.hs.resize(n);
+    B.hbonds = cfgs[0].hbonds != 0;
+    for (int r = 0; r < n; ++r) {
+        if ((cfgs[r].hbonds != 0) != (B.hbonds != 0)) { B.err = "all replicas of a batch share the hbonds flag"; return DMD_E_INPUT; }
+        if (!setup_host(B.hs[r], &cfgs[r], tables, &systems[r], B.err)) return DMD_E_INPUT;
+    }
+    return upload(B);
+}
+
+int sync_check(dmd_batch &B) {
+    std::string &err = B.err;
+    CK(cudaStreamSynchronize(B.st));
+    for (size_t r = 0; r < B.ds.size(); ++r) {
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        B.hs[r].sc = sc;
+        if (sc.err) {
+            err = "device error " + std::to_string(sc.err) + " in system " + std::to_string(r) + " (info " + std::to_string(sc.err_info) + ")";
+            return sc.err;
+        }
+    }
+    return DMD_OK;
+}
+
+int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
+    std::string &err = B.err;
+    if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    int n = (int)B.hs.size();
+    /* event logs: one device ring per system for this call */
+    std::vector<DSys> hd(n);
+    long long cap = 0;
+    if (logs) for (int r = 0; r < n; ++r) cap = std::max<long long>(cap, logs[r].capacity);
+    if (cap > B.log_cap) {
+        if (B.d_log) cudaFree(B.d_log);
+        B.d_log = nullptr;
+        CK(cudaMalloc(&B.d_log, (size_t)cap * n * sizeof(dmd_event)));
+        B.log_cap = cap;
+    }
+    std::vector<long long> count0(n, 0);
+    for (int r = 0; r < n; ++r) {
+        hd[r] = B.ds[r].d;
+        if (logs && logs[r].capacity > 0) { hd[r].log = B.d_log + (size_t)r * cap; hd[r].log_cap = logs[r].capacity; }
+        else { hd[r].log = nullptr; hd[r].log_cap = 0; }
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        sc.log_count = 0;
+        CK(cudaMemcpy(B.ds[r].d.sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
+    CK(dmd_launch_run(B.d_sys, n, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr, B.st));
+    int rc = sync_check(B);
+    if (logs) {
+        for (int r = 0; r < n; ++r) {
+            long long cnt = B.hs[r].sc.log_count;
+            logs[r].count = cnt;
+            long long c = logs[r].capacity;
+            if (c <= 0 || !logs[r].events) continue;
+            long long m = std::min(cnt, c);
+            std::vector<dmd_event> tmp((size_t)m);
+            cudaError_t e = cudaMemcpy(tmp.data(), B.d_log + (size_t)r * cap, (size_t)m * sizeof(dmd_event), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) { err = cudaGetErrorString(e); return DMD_E_CUDA; }
+            /* ring positions are taken modulo the capacity */
+            for (long long k = 0; k < m; ++k) logs[r].events[k] = tmp[(size_t)k];
+        }
+    }
+    return rc;
+}
+
+int get_state(dmd_batch &B, int r, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+              int32_t *bptnr, int32_t *identity, int32_t *er_out, double *t, double *tfalse, int64_t *coll) {
+    std::string &err = B.err;
+    if (r < 0 || r >= (int)B.hs.size()) { err = "replica index out of range"; return DMD_E_INPUT; }
+    const DSys &d = B.ds[r].d;
+    size_t N = d.N;
+    CK(cudaStreamSynchronize(B.st));
+    if (x) { CK(cudaMemcpy(x, d.x, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(y, d.y, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(z, d.z, N * 8, cudaMemcpyDeviceToHost)); }
+    if (vx) { CK(cudaMemcpy(vx, d.vx, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(vy, d.vy, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(vz, d.vz, N * 8, cudaMemcpyDeviceToHost)); }
+    if (bptnr) {
+        std::vector<int> b(N);
+        CK(cudaMemcpy(b.data(), d.bptnr, N * 4, cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < N; ++k) bptnr[k] = b[k] + 1;
+    }
+    if (identity) {
+        std::vector<int8_t> b(N);
+        CK(cudaMemcpy(b.data(), d.ident, N, cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < N; ++k) identity[k] = b[k];
+    }
+    if (er_out) {
+        std::vector<int> b(4 * N);
+        CK(cudaMemcpy(b.data(), d.er, 4 * N * 4, cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < 4 * N; ++k) er_out[k] = b[k] + 1;
+    }
+    DScal sc;
+    CK(cudaMemcpy(&sc, d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+    if (t) *t = sc.t;
+    if (tfalse) *tfalse = sc.tfalse;
+    if (coll) *coll = sc.coll;
+    return DMD_OK;
+}
+
+int diagnostics(dmd_batch &B, int r, dmd_diag *out) {
+    std::string &err = B.err;
+    if (r < 0 || r >= (int)B.hs.size() || !out) { err = "bad argument"; return DMD_E_INPUT; }
+    CK(dmd_launch_diag(B.d_sys, (int)B.hs.size(), B.d_cstart, B.d_clen, B.d_coff, B.d_diag, B.st));
+    CK(cudaStreamSynchronize(B.st));
+    CK(cudaMemcpy(out, B.d_diag + r, sizeof(dmd_diag), cudaMemcpyDeviceToHost));
+    return DMD_OK;
+}
+
+void batch_free(dmd_batch &B) {
+    for (auto &D : B.ds) if (D.pool) cudaFree(D.pool);
+    if (B.d_sys) cudaFree(B.d_sys);
+    if (B.d_cstart) cudaFree(B.d_cstart);
+    if (B.d_clen) cudaFree(B.d_clen);
+    if (B.d_coff) cudaFree(B.d_coff);
+    if (B.d_diag) cudaFree(B.d_diag);
+    if (B.d_log) cudaFree(B.d_log);
+    if (B.st) cudaStreamDestroy(B.st);
+    B.ds.clear();
+}
+
+}  // namespace
+
+/* ---------------------------------------------------------------------- */
+/* C ABI                                                                   */
+/* ---------------------------------------------------------------------- */
+extern "C" {
+
+const char *dmd_version(void) { return "dmd-gb300 0.1 (sm_103a)"; }
+
+int dmd_batch_create(int32_t n, const dmd_run_cfg *cfgs, const dmd_tables *tables, const dmd_system *systems,
+                     dmd_batch **out) {
+    if (!out) return DMD_E_INPUT;
+    dmd_batch *B = new dmd_batch();
+    int rc = batch_create(*B, n, cfgs, tables, systems);
+    *out = B;  /* returned even on failure so that dmd_batch_last_error works; free with destroy */
+    return rc;
+}
+int dmd_batch_run(dmd_batch *b, int64_t n_events, dmd_event_log *logs) {
+    if (!b) return DMD_E_INPUT;
+    if (n_events < 0) { b->err = "negative event count"; return DMD_E_INPUT; }
+    return batch_run(*b, n_events, logs);
+}
+int dmd_batch_get_state(dmd_batch *b, int32_t r, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                        int32_t *bptnr, int32_t *identity, int32_t *er, double *t, double *tfalse, int64_t *coll) {
+    if (!b) return DMD_E_INPUT;
+    return get_state(*b, r, x, y, z, vx, vy, vz, bptnr, identity, er, t, tfalse, coll);
+}
+int dmd_batch_diagnostics(dmd_batch *b, int32_t r, dmd_diag *out) {
+    if (!b) return DMD_E_INPUT;
+    return diagnostics(*b, r, out);
+}
+void dmd_batch_destroy(dmd_batch *b) {
+    if (!b) return;
+    batch_free(*b);
+    delete b;
+}
+const char *dmd_batch_last_error(dmd_batch *b) { return b ? b->err.c_str() : "null handle"; }
+
+int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, dmd_handle **out) {
+    if (!out) return DMD_E_INPUT;
+    dmd_handle *h = new dmd_handle();
+    int rc = batch_create(h->b, 1, cfg, tables, sys);
+    *out = h;
+    return rc;
+}
+int dmd_run(dmd_handle *h, int64_t n_events, dmd_event_log *log) {
+    if (!h) return DMD_E_INPUT;
+    if (n_events < 0) { h->b.err = "negative event count"; return DMD_E_INPUT; }
+    return batch_run(h->b, n_events, log);
+}
+int dmd_predict_all(dmd_handle *h, double *tim, int32_t *nptnr, int32_t *coltype) {
+    if (!h || !h->b.ready) return DMD_E_STATE;
+    dmd_batch &B = h->b;
+    std::string &err = B.err;
+    const DSys &d = B.ds[0].d;
+    size_t N = d.N;
+    std::vector<int> np(N);
+    std::vector<int8_t> ct(N);
+    CK(cudaStreamSynchronize(B.st));
+    if (tim) CK(cudaMemcpy(tim, d.tim, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(np.data(), d.nptnr, N * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ct.data(), d.colt, N, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < N; ++k) {
+        if (nptnr) nptnr[k] = np[k] >= 0 ? np[k] + 1 : np[k];
+        if (coltype) coltype[k] = ct[k];
+    }
+    return DMD_OK;
+}
+int dmd_get_state(dmd_handle *h, double *x, double *y, double *z, double *vx, double *vy, double *vz, int32_t *bptnr,
+                  int32_t *identity, int32_t *er, double *t, double *tfalse, int64_t *coll) {
+    if (!h) return DMD_E_INPUT;
+    return get_state(h->b, 0, x, y, z, vx, vy, vz, bptnr, identity, er, t, tfalse, coll);
+}
+int dmd_diagnostics(dmd_handle *h, dmd_diag *out) {
+    if (!h) return DMD_E_INPUT;
+    return diagnostics(h->b, 0, out);
+}
+int dmd_get_evcode(dmd_handle *h, int8_t *out) {
+    if (!h || !out || !h->b.ready) return DMD_E_INPUT;
+    dmd_batch &B = h->b;
+    std::string &err = B.err;
+    const DSys &d = B.ds[0].d;
+    const HostSys &H = B.hs[0];
+    size_t N = d.N;
+    std::vector<int> ovp(4 * N);
+    std::vector<int8_t> ovc(4 * N);
+    CK(cudaStreamSynchronize(B.st));
+    CK(cudaMemcpy(ovp.data(), d.ovp, 4 * N * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ovc.data(), d.ovc, 4 * N, cudaMemcpyDeviceToHost));
+    for (size_t a = 0; a < N; ++a)
+        for (size_t b = 0; b < N; ++b) out[a * N + b] = a == b ? 1 : (int8_t)static_code(H.info[a], H.info[b], B.hbonds);
+    for (size_t a = 0; a < N; ++a)
+        for (int s = 0; s < 4; ++s)
+            if (ovp[4 * a + s] >= 0) out[a * N + ovp[4 * a + s]] = ovc[4 * a + s];
+    return DMD_OK;
+}
+void dmd_destroy(dmd_handle *h) {
+    if (!h) return;
+    batch_free(h->b);
+    delete h;
+}
+const char *dmd_last_error(dmd_handle *h) { return h ? h->b.err.c_str() : "null handle"; }
+
+}  // extern "C"

@@ -1,0 +1,282 @@
+/*
+ * engine.cuh -- device data layout and per-pair physics of the GB300 DMD
+ * event engine.
+ *
+ * Every expression below keeps the operation order of the reference Fortran
+ * (cited per function) and the build uses --fmad=false, so a prediction or
+ * an impulse computed here is bit-identical to the same arithmetic on the
+ * host.  Bead indices are 0-based on the device; -1 means "none".
+ */
+#ifndef DMD_ENGINE_CUH
+#define DMD_ENGINE_CUH
+
+#include <stdint.h>
+#include "dmd_rng.h"
+
+#define DMD_NT 29     /* identities 1..28 */
+#define DMD_NC 51     /* pair codes 1..50 */
+#define DMD_LTSTEP 1e-10
+#define DMD_SMDIST 5e-12
+#define DMD_BIG 1000000000.0
+
+/* bead kind inside a chain */
+#define BK_CA 0
+#define BK_NH 1
+#define BK_CO 2
+#define BK_R 3
+
+/* per-bead static description (make_code inputs, code/make_code.f) */
+struct BeadInfo {
+    int32_t chain;     /* chain index */
+    int32_t cstart;    /* index of the chain's first bead */
+    int16_t L;         /* residues in the chain */
+    int16_t res;       /* residue number 1..L this bead belongs to */
+    int8_t kind;       /* BK_* */
+    int8_t hp;         /* hydrophobic flag */
+    int8_t pro_nh;     /* NH whose index equals a proline side chain minus 2L */
+    int8_t is_end;     /* NH of residue 1 or CO of residue L */
+};
+
+/* box-scaled tables (code/scale_down.f, code/make_code.f:15-60, code/nbor_setup.f) */
+struct DTab {
+    double sigma_sq[DMD_NT][DMD_NT];
+    double welldia_sq[DMD_NT][DMD_NT];
+    double ep_sqrt[DMD_NT][DMD_NT];
+    double shlddia_sq[DMD_NT][DMD_NT];
+    double sqz610[6][DMD_NT];
+    double evp1[DMD_NC], evp2[DMD_NC], evp3[DMD_NC];
+    double rlsq[DMD_NC];
+    double shd1, shd2, shd3, shd4;
+    double eps1;       /* epsilon(1): H-bond depth */
+    double setemp, avegtime, hdelr, rl;
+    double eps_hb;     /* ep_sqrt(5,8) */
+    double boxl_orig;
+};
+
+/* per-system scalars kept between launches */
+struct DScal {
+    double t, tfalse, old_tfalse, interval, interval_max, t_fact, n_forced;
+    long long coll, n_pair, n_ghost, n_interval, n_output, n_updates, n_forced_updates, ghost_index;
+    long long nevents[32];
+    long long log_count;
+    long long done;       /* events counted toward the current run target */
+    int err;              /* DMD_E_* of the first device error, 0 if none */
+    int err_info;
+    int stop;             /* 1: stopped at an output event */
+    int pad;
+};
+
+/* device view of one system; all arrays in global memory */
+struct DSys {
+    int N, nchains, cap, ncell;   /* ncell: cells per side of the rebuild grid */
+    uint64_t seed;
+    int canon, flags;
+    const DTab *tab;
+    DScal *sc;
+    const BeadInfo *info;
+    const double *bm;
+    const double *blmin, *blmax;  /* side-chain bond window of a backbone bead (codes 10/11/12) */
+    double *x, *y, *z, *vx, *vy, *vz;
+    double *ox, *oy, *oz;          /* positions at the last list rebuild */
+    int8_t *ident;                 /* identity 1..28 (5..8: bonded backbone) */
+    int *bptnr;                    /* H-bond partner or -1 */
+    int *er;                       /* extra_repuls(b,1..4) at er[4b+0..3], -1 = none */
+    int *ovp;                      /* shoulder overrides: partner at ovp[4b+s], -1 free */
+    int8_t *ovc;                   /* ev_code(b, partner) of the override */
+    double *tim;                   /* N + 3 entries: beads, ghost, interval, output */
+    int *nptnr;
+    int8_t *colt;
+    uint8_t *queued;
+    int *up, *dn;                  /* neighbour lists [N*cap] */
+    int8_t *upc;                   /* static pair code of each up entry */
+    int *upn, *dnn;
+    int *cell_count, *cell_start, *cell_beads;  /* rebuild grid */
+    int *l1i;                      /* tournament level 1: argmin of 32 entries */
+    int *l2i;                      /* level 2: argmin of 32 level-1 groups */
+    int nl1, nl2;
+    void *log;                     /* dmd_event ring or NULL */
+    long long log_cap;
+};
+
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ double d_nint(double x) { return round(x); }
+
+/* lexicographic (time, partner) order used for every minimum */
+__device__ __forceinline__ bool lex_less(double ta, int pa, double tb, int pb) {
+    return ta < tb || (ta == tb && pa < pb);
+}
+
+/* static pair code: code/make_code.f:6-573 applied per chain, as a rule */
+__host__ __device__ __forceinline__ int bond_code_dir(int ka, int kb, int ra, int rb) {
+    int d = rb - ra;
+    switch (ka * 4 + kb) {
+        case BK_CA * 4 + BK_NH: return d == 0 ? 4 : d == 1 ? 7 : d == -1 ? 18 : 0;
+        case BK_CA * 4 + BK_CO: return d == 0 ? 5 : d == -1 ? 8 : d == 1 ? 17 : 0;
+        case BK_NH * 4 + BK_CO: return d == -1 ? 6 : d == 0 ? 8 : d == -2 ? 19 : 0;
+        case BK_CA * 4 + BK_CA: return d == 1 ? 9 : 0;
+        case BK_CA * 4 + BK_R: return d == 0 ? 10 : d == 1 ? 24 : d == -1 ? 25 : 0;
+        case BK_NH * 4 + BK_R: return d == 0 ? 11 : d == -1 ? 23 : 0;
+        case BK_CO * 4 + BK_R: return d == 0 ? 12 : d == 1 ? 22 : d == 2 ? 26 : 0;
+        case BK_NH * 4 + BK_NH: return d == 1 ? 20 : 0;
+        case BK_CO * 4 + BK_CO: return d == 1 ? 21 : 0;
+        default: return 0;
+    }
+}
+
+__host__ __device__ __forceinline__ int static_code(const BeadInfo &A, const BeadInfo &B, int hbonds) {
+    if (A.chain == B.chain) {
+        int c = bond_code_dir(A.kind, B.kind, A.res, B.res);
+        if (!c) c = bond_code_dir(B.kind, A.kind, B.res, A.res);
+        if (c) return c;
+        int dr = A.res - B.res;
+        if (dr < 0) dr = -dr;
+        if (A.kind == BK_R && B.kind == BK_R) return (dr >= 4 && A.hp == 1 && B.hp == 1) ? 16 : 1;
+        if (hbonds && ((A.kind == BK_NH && B.kind == BK_CO) || (A.kind == BK_CO && B.kind == BK_NH)))
+            return dr >= 4 ? 15 : 1;
+        return 1;
+    }
+    if (A.kind == BK_R && B.kind == BK_R) return (A.hp == 1 && B.hp == 1) ? 16 : 1;
+    if (hbonds) {
+        if (A.kind == BK_NH && B.kind == BK_CO) return (A.pro_nh && B.chain > A.chain) ? 1 : 15;
+        if (A.kind == BK_CO && B.kind == BK_NH) return (B.pro_nh && A.chain > B.chain) ? 1 : 15;
+    }
+    return 1;
+}
+
+/* ev_code(a,b): the rule plus the H-bond shoulder overrides of repuls_add */
+__device__ __forceinline__ int pair_code(const DSys &S, int a, int b, int hbonds) {
+    const int *op = S.ovp + 4 * a;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        if (op[s] == b) return S.ovc[4 * a + s];
+    return static_code(S.info[a], S.info[b], hbonds);
+}
+
+/* ------------------------------------------------------------------ */
+struct Rel { double rx, ry, rz, vx, vy, vz, bij, rijsq, vijsq; };
+
+/* relative coordinates advanced to tfalse with the minimum image
+ * (code/core.f:14-24 and the copies in every predictor) */
+__device__ __forceinline__ Rel d_rel(const DSys &S, int i, int j, double tfalse) {
+    Rel r;
+    r.vx = S.vx[i] - S.vx[j]; r.vy = S.vy[i] - S.vy[j]; r.vz = S.vz[i] - S.vz[j];
+    r.rx = S.x[i] - S.x[j] + r.vx * tfalse;
+    r.ry = S.y[i] - S.y[j] + r.vy * tfalse;
+    r.rz = S.z[i] - S.z[j] + r.vz * tfalse;
+    r.rx = r.rx - d_nint(r.rx); r.ry = r.ry - d_nint(r.ry); r.rz = r.rz - d_nint(r.rz);
+    r.bij = r.rx * r.vx + r.ry * r.vy + r.rz * r.vz;
+    r.rijsq = r.rx * r.rx + r.ry * r.ry + r.rz * r.rz;
+    r.vijsq = r.vx * r.vx + r.vy * r.vy + r.vz * r.vz;
+    return r;
+}
+
+/* code/bond.f:19-33 */
+__device__ __forceinline__ void bond_limits(const DSys &S, int i, int evcode, double &blmin, double &blmax) {
+    if (evcode >= 10 && evcode <= 12) { blmin = S.blmin[i]; blmax = S.blmax[i]; }
+    else { blmin = S.tab->evp2[evcode]; blmax = S.tab->evp3[evcode]; }
+}
+
+/* pair prediction, dispatch of code/eventredo_up.f:28-46 into
+ * code/core.f, bond.f, nc_sqwel.f, sqwel.f, sqshlder.f.  Returns false on an
+ * invalid code (reference: "error in ev_code matrix"). */
+static __device__ __noinline__ bool d_predict(const DSys &S, int i, int j, int evcode, double tfalse,
+                                       double &tij, int &type) {
+    const DTab &T = *S.tab;
+    tij = DMD_BIG; type = 0;
+    Rel r = d_rel(S, i, j, tfalse);
+    int a = S.ident[i], b = S.ident[j];
+    if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {            /* core.f:3-44 */
+        if (r.bij < 0.0) {
+            double p = T.evp1[evcode];
+            double sigsq = T.sigma_sq[a][b] * (p * p);
+            if (evcode >= 22 && evcode <= 26) {
+                int k = a > b ? a : b;
+                double s = T.sqz610[evcode - 21][k];
+                sigsq = sigsq * (s * s);
+            }
+            double discr = r.bij * r.bij - r.vijsq * (r.rijsq - sigsq);
+            if (discr > 0.0) { tij = (-r.bij - sqrt(discr)) / r.vijsq; type = 1; }
+        }
+    } else if (evcode >= 4 && evcode <= 12) {                      /* bond.f:4-121 */
+        double blmin, blmax;
+        bond_limits(S, i, evcode, blmin, blmax);
+        if (r.bij < 0.0) {
+            double discr1 = r.bij * r.bij - r.vijsq * (r.rijsq - blmin * blmin);
+            if (discr1 > 0.0) {
+                tij = (-r.bij - sqrt(discr1)) / r.vijsq; type = 2;
+            } else {
+                double discr2 = r.bij * r.bij - r.vijsq * (r.rijsq - blmax * blmax);
+                if (discr2 > 0.0) { tij = (-r.bij + sqrt(discr2)) / r.vijsq; type = 3; }
+            }
+        } else {
+            double discr2 = r.bij * r.bij - r.vijsq * (r.rijsq - blmax * blmax);
+            if (discr2 > 0.0) { tij = -(r.rijsq - blmax * blmax) / (sqrt(discr2) + r.bij); type = 3; }
+        }
+    } else if (evcode == 15) {                                      /* nc_sqwel.f:7-126 */
+        double diff = r.rijsq - T.welldia_sq[a][b];
+        if (a + b == 5) {
+            if (r.bij < 0.0) {
+                if (diff < 0.0) {
+                    double corediscr = r.bij * r.bij - r.vijsq * (r.rijsq - T.sigma_sq[a][b]);
+                    if (corediscr > 0.0) { tij = (-r.bij - sqrt(corediscr)) / r.vijsq; type = 1; }
+                    else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 16; }
+                } else {
+                    double w = r.bij * r.bij - r.vijsq * diff;
+                    if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 7; }
+                }
+            } else if (diff < 0.0) {
+                double w = r.bij * r.bij - r.vijsq * diff;
+                tij = (-r.bij + sqrt(w)) / r.vijsq; type = 16;
+            }
+        } else if (S.bptnr[i] == j) {
+            if (r.bij < 0.0) {
+                double p = T.evp1[15];
+                double fac_sigsq = T.sigma_sq[a][b] * p * p;
+                double fac_cored = r.bij * r.bij - r.vijsq * (r.rijsq - fac_sigsq);
+                if (fac_cored > 0.0) { tij = (-r.bij - sqrt(fac_cored)) / r.vijsq; type = 1; }
+                else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8; }
+            } else {
+                double w = r.bij * r.bij - r.vijsq * diff;
+                tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8;
+            }
+        } else if (r.bij < 0.0) {
+            double w = r.bij * r.bij - r.vijsq * diff;
+            if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 9; }
+        }
+    } else if (evcode == 16) {                                      /* sqwel.f:5-67 */
+        double diff = r.rijsq - T.welldia_sq[a][b];
+        if (r.bij < 0.0) {
+            if (diff < 0.0) {
+                double corediscr = r.bij * r.bij - r.vijsq * (r.rijsq - T.sigma_sq[a][b]);
+                if (corediscr > 0.0) { tij = (-r.bij - sqrt(corediscr)) / r.vijsq; type = 1; }
+                else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8; }
+            } else {
+                double w = r.bij * r.bij - r.vijsq * diff;
+                if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 4; }
+            }
+        } else if (diff < 0.0) {
+            double w = r.bij * r.bij - r.vijsq * diff;
+            tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8;
+        }
+    } else if (evcode >= 40) {                                      /* sqshlder.f:5-66 */
+        double diff = r.rijsq - T.shlddia_sq[a][b];
+        if (r.bij < 0.0) {
+            if (diff < 0.0) {
+                double corediscr = r.bij * r.bij - r.vijsq * (r.rijsq - T.sigma_sq[a][b]);
+                if (corediscr > 0.0) { tij = (-r.bij - sqrt(corediscr)) / r.vijsq; type = 1; }
+                else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 10; }
+            } else {
+                double w = r.bij * r.bij - r.vijsq * diff;
+                if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 12; }
+            }
+        } else if (diff < 0.0) {
+            double w = r.bij * r.bij - r.vijsq * diff;
+            tij = (-r.bij + sqrt(w)) / r.vijsq; type = 10;
+        }
+    } else {
+        return false;
+    }
+    return true;
+}
+
+#endif /* DMD_ENGINE_CUH */

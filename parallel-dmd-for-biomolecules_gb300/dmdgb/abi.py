@@ -1,0 +1,167 @@
+"""ctypes mirror of include/dmd.h and loaders for the in-tree shared objects.
+
+The engine library (libdmd_gb300.so, built by build.py from csrc/) is the
+product.  ``load_engine`` fails loudly when it is missing; there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPO_DIR = os.path.dirname(PKG_DIR)
+ENGINE_SO = os.path.join(PKG_DIR, "_build", "libdmd_gb300.so")
+
+DMD_OK = 0
+ERRORS = {
+    -1: "DMD_E_INPUT", -2: "DMD_E_OVERLAP", -3: "DMD_E_NEG_TIME", -4: "DMD_E_DEVICE_TIMEOUT",
+    -5: "DMD_E_OOM", -6: "DMD_E_CUDA", -7: "DMD_E_CAPACITY", -8: "DMD_E_STATE",
+}
+FLAG_STOP_AT_OUTPUT = 1
+FLAG_COUNT_PHYSICAL = 2
+FLAG_SERIAL = 4
+EV_GHOST, EV_INTERVAL, EV_REBUILD, EV_OUTPUT = 100, 101, 102, 103
+
+dbl_p = C.POINTER(C.c_double)
+i32_p = C.POINTER(C.c_int32)
+i64_p = C.POINTER(C.c_int64)
+i8_p = C.POINTER(C.c_int8)
+
+
+class Tables(C.Structure):
+    _fields_ = [
+        ("sigma", C.c_double * 4), ("welldia", C.c_double * 4), ("epsilon", C.c_double * 4),
+        ("mass", C.c_double * 29),
+        ("bds", (C.c_double * 20) * 20), ("wel", (C.c_double * 20) * 20), ("ep", (C.c_double * 20) * 20),
+        ("rca", C.c_double * 20), ("rnh", C.c_double * 20), ("rco", C.c_double * 20),
+        ("del_rca", C.c_double * 20), ("del_rnh", C.c_double * 20), ("del_rco", C.c_double * 20),
+        ("sqz", (C.c_double * 5) * 20),
+    ]
+
+
+class RunCfg(C.Structure):
+    _fields_ = [
+        ("tstar", C.c_double), ("seed", C.c_uint64), ("canon", C.c_int32), ("hbonds", C.c_int32),
+        ("numbin", C.c_int32), ("n_wrap", C.c_int32), ("rl_const", C.c_double), ("t_fact", C.c_double),
+        ("n_forced", C.c_double), ("list_cap", C.c_int32), ("flags", C.c_int32),
+    ]
+
+
+class System(C.Structure):
+    _fields_ = [
+        ("n_beads", C.c_int32), ("n_chains", C.c_int32), ("chain_len", i32_p), ("residues", i32_p),
+        ("hp", i32_p), ("boxl", C.c_double),
+        ("x", dbl_p), ("y", dbl_p), ("z", dbl_p), ("vx", dbl_p), ("vy", dbl_p), ("vz", dbl_p),
+        ("bptnr", i32_p), ("t0", C.c_double), ("coll0", C.c_int64),
+    ]
+
+
+class Event(C.Structure):
+    _fields_ = [("coll", C.c_int64), ("t", C.c_double), ("tfalse", C.c_double), ("i", C.c_int32),
+                ("j", C.c_int32), ("type", C.c_int32), ("evcode", C.c_int32)]
+
+
+EVENT_DTYPE = np.dtype([("coll", "<i8"), ("t", "<f8"), ("tfalse", "<f8"), ("i", "<i4"), ("j", "<i4"),
+                        ("type", "<i4"), ("evcode", "<i4")])
+assert EVENT_DTYPE.itemsize == C.sizeof(Event)
+
+
+class EventLog(C.Structure):
+    _fields_ = [("events", C.POINTER(Event)), ("capacity", C.c_int64), ("count", C.c_int64)]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("e_total", C.c_double), ("temperature", C.c_double), ("rg", C.c_double), ("e2e", C.c_double),
+        ("ehh_ii", C.c_double), ("ehh_ij", C.c_double), ("e_kin", C.c_double),
+        ("hb_alpha", C.c_int32), ("hb_ii", C.c_int32), ("hb_ij", C.c_int32), ("pad", C.c_int32),
+        ("nevents", C.c_int64 * 32),
+        ("coll", C.c_int64), ("n_pair", C.c_int64), ("n_ghost", C.c_int64), ("n_interval", C.c_int64),
+        ("n_output", C.c_int64), ("n_updates", C.c_int64), ("n_forced_updates", C.c_int64),
+        ("t", C.c_double), ("tfalse", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("nevents", "pad")}
+        d["nevents"] = list(self.nevents)
+        return d
+
+
+class GenSpec(C.Structure):
+    _fields_ = [("n_chains", C.c_int32), ("chain_len", i32_p), ("residues", i32_p), ("boxl", C.c_double),
+                ("tstar", C.c_double), ("seed", C.c_uint64), ("min_sep", C.c_double)]
+
+
+# the symbols include/dmd.h declares
+ENGINE_SYMBOLS = [
+    "dmd_create", "dmd_run", "dmd_predict_all", "dmd_get_state", "dmd_diagnostics", "dmd_get_evcode",
+    "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
+    "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
+    "dmd_generate",
+]
+
+
+def tables_struct(t) -> Tables:
+    s = Tables()
+    for name, _ in Tables._fields_:
+        arr = np.ascontiguousarray(np.asarray(getattr(t, name), dtype=np.float64))
+        C.memmove(C.addressof(getattr(s, name)), arr.ctypes.data, arr.nbytes)
+    return s
+
+
+def ptr(a, typ):
+    return a.ctypes.data_as(typ) if a is not None else None
+
+
+def _declare(lib) -> None:
+    lib.dmd_create.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), C.POINTER(C.c_void_p)]
+    lib.dmd_create.restype = C.c_int
+    lib.dmd_run.argtypes = [C.c_void_p, C.c_int64, C.POINTER(EventLog)]
+    lib.dmd_run.restype = C.c_int
+    lib.dmd_predict_all.argtypes = [C.c_void_p, dbl_p, i32_p, i32_p]
+    lib.dmd_predict_all.restype = C.c_int
+    lib.dmd_get_state.argtypes = [C.c_void_p] + [dbl_p] * 6 + [i32_p] * 3 + [dbl_p, dbl_p, i64_p]
+    lib.dmd_get_state.restype = C.c_int
+    lib.dmd_diagnostics.argtypes = [C.c_void_p, C.POINTER(Diag)]
+    lib.dmd_diagnostics.restype = C.c_int
+    lib.dmd_get_evcode.argtypes = [C.c_void_p, i8_p]
+    lib.dmd_get_evcode.restype = C.c_int
+    lib.dmd_destroy.argtypes = [C.c_void_p]
+    lib.dmd_destroy.restype = None
+    lib.dmd_last_error.argtypes = [C.c_void_p]
+    lib.dmd_last_error.restype = C.c_char_p
+    lib.dmd_version.argtypes = []
+    lib.dmd_version.restype = C.c_char_p
+    lib.dmd_batch_create.argtypes = [C.c_int32, C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System),
+                                     C.POINTER(C.c_void_p)]
+    lib.dmd_batch_create.restype = C.c_int
+    lib.dmd_batch_run.argtypes = [C.c_void_p, C.c_int64, C.POINTER(EventLog)]
+    lib.dmd_batch_run.restype = C.c_int
+    lib.dmd_batch_get_state.argtypes = [C.c_void_p, C.c_int32] + [dbl_p] * 6 + [i32_p] * 3 + [dbl_p, dbl_p, i64_p]
+    lib.dmd_batch_get_state.restype = C.c_int
+    lib.dmd_batch_diagnostics.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Diag)]
+    lib.dmd_batch_diagnostics.restype = C.c_int
+    lib.dmd_batch_destroy.argtypes = [C.c_void_p]
+    lib.dmd_batch_destroy.restype = None
+    lib.dmd_batch_last_error.argtypes = [C.c_void_p]
+    lib.dmd_batch_last_error.restype = C.c_char_p
+    lib.dmd_generate.argtypes = [C.POINTER(GenSpec), C.POINTER(Tables), C.c_int32] + [dbl_p] * 6 + [C.c_char_p, C.c_int32]
+    lib.dmd_generate.restype = C.c_int
+
+
+_engine = None
+
+
+def load_engine(path: str = ENGINE_SO):
+    """The GB300 engine library.  Raises if it has not been built."""
+    global _engine
+    if _engine is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"GB300 engine library missing: {path} (run __graft_entry__.build())")
+        lib = C.CDLL(path)
+        _declare(lib)
+        _engine = lib
+    return _engine

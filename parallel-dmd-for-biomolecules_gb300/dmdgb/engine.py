@@ -1,0 +1,171 @@
+"""Python host of the GB300 engine: the calls a driver makes in place of the
+reference's program dmd main loop (code/main.F90:117-1258), through the C
+ABI of include/dmd.h.  There is no CPU path: every method runs the CUDA
+engine and raises if the library or the GPU is unavailable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from .params import Tables, default_tables
+from .systems import SystemSpec
+
+
+class DMDError(RuntimeError):
+    def __init__(self, rc: int, msg: str):
+        super().__init__(f"{abi.ERRORS.get(rc, rc)}: {msg}")
+        self.rc = rc
+
+
+def _check(rc: int, lib, handle, fn="dmd_last_error"):
+    if rc != 0:
+        msg = getattr(lib, fn)(handle)
+        raise DMDError(rc, msg.decode() if msg else "")
+
+
+class Engine:
+    """One system on the GPU (the plain one-system-per-launch path)."""
+
+    def __init__(self, spec: SystemSpec, tables: Optional[Tables] = None, flags: int = 0, list_cap: int = 0):
+        self.lib = abi.load_engine()
+        self.spec = spec
+        self.n = spec.n_beads
+        self._tables = abi.tables_struct(tables or default_tables())
+        self._cfg = spec.run_cfg(flags, list_cap)
+        self._sys = spec.c_system()
+        h = C.c_void_p()
+        rc = self.lib.dmd_create(C.byref(self._cfg), C.byref(self._tables), C.byref(self._sys), C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.lib.dmd_last_error(h)
+            self.lib.dmd_destroy(h)
+            self.h = None
+            raise DMDError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dmd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, n_events: int, log_capacity: int = 0) -> Optional[np.ndarray]:
+        """Commit n_events events; returns the event log (structured array) if
+        log_capacity > 0."""
+        log = None
+        if log_capacity > 0:
+            buf = np.zeros(log_capacity, abi.EVENT_DTYPE)
+            log = abi.EventLog(buf.ctypes.data_as(C.POINTER(abi.Event)), log_capacity, 0)
+            rc = self.lib.dmd_run(self.h, int(n_events), C.byref(log))
+            _check(rc, self.lib, self.h)
+            return buf[:min(log.count, log_capacity)]
+        rc = self.lib.dmd_run(self.h, int(n_events), None)
+        _check(rc, self.lib, self.h)
+        return None
+
+    def predictions(self):
+        tim = np.zeros(self.n)
+        np_ = np.zeros(self.n, np.int32)
+        ct = np.zeros(self.n, np.int32)
+        _check(self.lib.dmd_predict_all(self.h, abi.ptr(tim, abi.dbl_p), abi.ptr(np_, abi.i32_p),
+                                        abi.ptr(ct, abi.i32_p)), self.lib, self.h)
+        return tim, np_, ct
+
+    def state(self) -> dict:
+        n = self.n
+        a = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        bp = np.zeros(n, np.int32)
+        ident = np.zeros(n, np.int32)
+        er = np.zeros(4 * n, np.int32)
+        t = C.c_double()
+        tf = C.c_double()
+        coll = C.c_int64()
+        rc = self.lib.dmd_get_state(self.h, *[abi.ptr(a[k], abi.dbl_p) for k in ("x", "y", "z", "vx", "vy", "vz")],
+                                    abi.ptr(bp, abi.i32_p), abi.ptr(ident, abi.i32_p), abi.ptr(er, abi.i32_p),
+                                    C.byref(t), C.byref(tf), C.byref(coll))
+        _check(rc, self.lib, self.h)
+        a.update(bptnr=bp, identity=ident, extra_repuls=er.reshape(n, 4), t=t.value, tfalse=tf.value, coll=coll.value)
+        return a
+
+    def diagnostics(self) -> dict:
+        d = abi.Diag()
+        _check(self.lib.dmd_diagnostics(self.h, C.byref(d)), self.lib, self.h)
+        return d.as_dict()
+
+    def evcode(self) -> np.ndarray:
+        out = np.zeros((self.n, self.n), np.int8)
+        _check(self.lib.dmd_get_evcode(self.h, out.ctypes.data_as(abi.i8_p)), self.lib, self.h)
+        return out
+
+
+class Batch:
+    """Many independent systems advanced by one persistent launch."""
+
+    def __init__(self, specs: Sequence[SystemSpec], tables: Optional[Tables] = None, flags: int = 0, list_cap: int = 0):
+        self.lib = abi.load_engine()
+        self.specs = list(specs)
+        n = len(self.specs)
+        self._tables = abi.tables_struct(tables or default_tables())
+        self._cfgs = (abi.RunCfg * n)(*[s.run_cfg(flags, list_cap) for s in self.specs])
+        self._syss = (abi.System * n)(*[s.c_system() for s in self.specs])
+        h = C.c_void_p()
+        rc = self.lib.dmd_batch_create(n, self._cfgs, C.byref(self._tables), self._syss, C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.lib.dmd_batch_last_error(h)
+            self.lib.dmd_batch_destroy(h)
+            self.h = None
+            raise DMDError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dmd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, n_events: int, log_capacity: int = 0) -> Optional[List[np.ndarray]]:
+        n = len(self.specs)
+        if log_capacity > 0:
+            bufs = [np.zeros(log_capacity, abi.EVENT_DTYPE) for _ in range(n)]
+            logs = (abi.EventLog * n)(*[abi.EventLog(b.ctypes.data_as(C.POINTER(abi.Event)), log_capacity, 0)
+                                        for b in bufs])
+            rc = self.lib.dmd_batch_run(self.h, int(n_events), logs)
+            _check(rc, self.lib, self.h, "dmd_batch_last_error")
+            return [b[:min(logs[r].count, log_capacity)] for r, b in enumerate(bufs)]
+        rc = self.lib.dmd_batch_run(self.h, int(n_events), None)
+        _check(rc, self.lib, self.h, "dmd_batch_last_error")
+        return None
+
+    def state(self, r: int) -> dict:
+        n = self.specs[r].n_beads
+        a = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        bp = np.zeros(n, np.int32)
+        ident = np.zeros(n, np.int32)
+        er = np.zeros(4 * n, np.int32)
+        t = C.c_double()
+        tf = C.c_double()
+        coll = C.c_int64()
+        rc = self.lib.dmd_batch_get_state(self.h, r, *[abi.ptr(a[k], abi.dbl_p) for k in ("x", "y", "z", "vx", "vy", "vz")],
+                                          abi.ptr(bp, abi.i32_p), abi.ptr(ident, abi.i32_p), abi.ptr(er, abi.i32_p),
+                                          C.byref(t), C.byref(tf), C.byref(coll))
+        _check(rc, self.lib, self.h, "dmd_batch_last_error")
+        a.update(bptnr=bp, identity=ident, extra_repuls=er.reshape(n, 4), t=t.value, tfalse=tf.value, coll=coll.value)
+        return a
+
+    def diagnostics(self, r: int) -> dict:
+        d = abi.Diag()
+        _check(self.lib.dmd_batch_diagnostics(self.h, r, C.byref(d)), self.lib, self.h, "dmd_batch_last_error")
+        return d.as_dict()

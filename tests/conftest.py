@@ -1,0 +1,28 @@
+import os
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(REPO, "parallel-dmd-for-biomolecules_gb300")
+for p in (REPO, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+REFERENCE = "/root/reference/parallel-dmd-PRIME20"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and runs the engine")
+
+
+@pytest.fixture(scope="session")
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    return True
+
+
+def has_reference() -> bool:
+    return os.path.isdir(REFERENCE)

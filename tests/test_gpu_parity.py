@@ -1,0 +1,89 @@
+"""GPU engine against the CPU restatement of the reference: the committed
+event sequence (bead pair, final collision type, pair code, time) and the
+final state must be identical bit for bit, on the same seeded inputs."""
+import numpy as np
+import pytest
+
+from dmdgb import abi, systems
+from dmdgb.engine import Batch, Engine
+from helpers import dense_system, describe, first_mismatch
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare_run(spec, n_events, flags=0):
+    with Engine(spec, flags=flags) as eng:
+        glog = eng.run(n_events, log_capacity=n_events + 64)
+        gst = eng.state()
+    ora = Oracle(spec, flags=flags)
+    olog = ora.run(n_events, log_capacity=n_events + 64)
+    ost = ora.state()
+    k = first_mismatch(glog, olog)
+    assert k < 0, f"event logs diverge at {k} of {len(olog)}:\n{describe(glog, olog, k)}"
+    for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity", "extra_repuls"):
+        assert np.array_equal(gst[key], ost[key]), f"final {key} differs"
+    assert gst["t"] == ost["t"] and gst["tfalse"] == ost["tfalse"] and gst["coll"] == ost["coll"]
+    return glog
+
+
+def test_predict_all_initial(built):
+    spec = systems.generate(systems.config_c1())
+    with Engine(spec) as eng:
+        gt, gp, gc = eng.predictions()
+    ot, op, oc = Oracle(spec).predictions()
+    assert np.array_equal(gp, op)
+    assert np.array_equal(gc, oc)
+    assert np.array_equal(gt, ot)
+
+
+def test_c1_event_sequence(built):
+    spec = systems.generate(systems.config_c1())
+    log = _compare_run(spec, 20000)
+    assert (log["type"] == abi.EV_GHOST).any() and (log["type"] == abi.EV_REBUILD).any()
+
+
+def test_dense_all_event_kinds(built):
+    spec = dense_system()
+    log = _compare_run(spec, 40000)
+    kinds = set(np.unique(log["type"]).tolist())
+    assert {1, 2, 3}.issubset(kinds)
+
+
+def test_no_thermostat(built):
+    spec = dense_system(seed=5)
+    spec.canon = False
+    _compare_run(spec, 20000)
+
+
+def test_evcode_after_run(built):
+    spec = dense_system(n_chains=4, L=10, box=45.0, seed=9)
+    with Engine(spec) as eng:
+        eng.run(30000)
+        g = eng.evcode()
+    ora = Oracle(spec)
+    ora.run(30000)
+    assert np.array_equal(g, ora.evcode())
+
+
+def test_batch_equals_single(built):
+    specs = [systems.generate(systems.klvffae_system(4, 5.0, 0.2 + 0.05 * r, seed=r + 1)) for r in range(3)]
+    b = Batch(specs)
+    logs = b.run(5000, log_capacity=5100)
+    for r, spec in enumerate(specs):
+        olog = Oracle(spec).run(5000, log_capacity=5100)
+        assert first_mismatch(logs[r], olog) < 0
+
+
+def test_diagnostics_match(built):
+    spec = dense_system(seed=4)
+    with Engine(spec) as eng:
+        eng.run(20000)
+        gd = eng.diagnostics()
+    ora = Oracle(spec)
+    ora.run(20000)
+    od = ora.diagnostics()
+    for k in ("e_total", "temperature", "rg", "e2e", "ehh_ii", "ehh_ij"):
+        assert gd[k] == pytest.approx(od[k], rel=1e-12, abs=1e-12), k
+    for k in ("hb_alpha", "hb_ii", "hb_ij", "coll", "n_pair", "n_ghost", "n_interval", "n_updates"):
+        assert gd[k] == od[k], k
