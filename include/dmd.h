@@ -125,6 +125,7 @@ typedef struct dmd_diag {
     int64_t nevents[32];      /* per final coltype */
     int64_t coll, n_pair, n_ghost, n_interval, n_output, n_updates, n_forced_updates;
     double  t, tfalse;
+    double  nbr_mean;         /* mean neighbour-list entries per bead (up + down) */
 } dmd_diag;
 
 typedef struct dmd_handle dmd_handle;
@@ -143,7 +144,8 @@ int dmd_run(dmd_handle *h, int64_t n_events, dmd_event_log *log);
  * tim/nptnr/coltype per bead (1-based partners, times relative to t). */
 int dmd_predict_all(dmd_handle *h, double *tim, int32_t *nptnr, int32_t *coltype);
 
-/* State read-back: positions advanced to the current time (box units),
+/* State read-back: the stored positions (box units; the position at the
+ * current time is x + vx * tfalse, as in code/config.f:15-24),
  * velocities, H-bond partners, identities, extra_repuls (4 per bead). */
 int dmd_get_state(dmd_handle *h, double *x, double *y, double *z,
                   double *vx, double *vy, double *vz, int32_t *bptnr,
@@ -158,10 +160,26 @@ int dmd_diagnostics(dmd_handle *h, dmd_diag *out);
  * the shoulder overrides (code/make_code.f:6-573, code/repuls_add.f). */
 int dmd_get_evcode(dmd_handle *h, int8_t *out);
 
+/* Device time in ms of the kernel of the last dmd_run, measured with CUDA
+ * events on the stream it was launched on (no reference counterpart). */
+double dmd_last_run_ms(dmd_handle *h);
+
 void dmd_destroy(dmd_handle *h);
 
 const char *dmd_last_error(dmd_handle *h);
 const char *dmd_version(void);
+
+/* Host-only (no GPU): the static pair-type table ev_code of code/make_code.f
+ * as the engine's rule computes it, before any H-bond shoulder (dense,
+ * row-major n_beads x n_beads). */
+int dmd_static_evcode(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,
+                      int8_t *out, char *err, int32_t errlen);
+/* Host-only: set-up values of code/main.F90:144-156 and code/nbor_setup.f:
+ * interval, interval_max, sig_max_all, hdelr, cells per side, rl, rlsq(1),
+ * rlsq(15), rlsq(16), rlsq(40), n_forced, t_fact, ev_param(1,15).
+ * Returns the number of values available. */
+int dmd_inspect(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,
+                double *out, int32_t n, char *err, int32_t errlen);
 
 /* ---- batched replicas: many independent systems in one persistent launch
  * (no reference counterpart: the reference runs one system per MPI job). */
@@ -175,6 +193,7 @@ int dmd_batch_get_state(dmd_batch *b, int32_t r, double *x, double *y, double *z
                         int32_t *identity, int32_t *extra_repuls,
                         double *t, double *tfalse, int64_t *coll);
 int dmd_batch_diagnostics(dmd_batch *b, int32_t r, dmd_diag *out);
+double dmd_batch_last_run_ms(dmd_batch *b);
 void dmd_batch_destroy(dmd_batch *b);
 const char *dmd_batch_last_error(dmd_batch *b);
 

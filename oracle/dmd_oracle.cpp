@@ -1257,12 +1257,12 @@ struct Oracle {
             if (rec) { rec->coll = coll; rec->t = t; rec->tfalse = tfalse; rec->i = last_ghost_bead; rec->j = 0; rec->type = type; rec->evcode = 0; }
             return type;
         } else if (i == N + 2) {
-            double tf = tfalse;
+            double tf = tfalse, t_before = t;
             bool rb = interval_event();
             type = rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL;
             n_interval += 1;
             old_tfalse = tfalse;
-            if (rec) { rec->coll = coll; rec->t = t - tf; rec->tfalse = tf; rec->i = i; rec->j = 0; rec->type = type; rec->evcode = 0; }
+            if (rec) { rec->coll = coll; rec->t = t_before; rec->tfalse = tf; rec->i = i; rec->j = 0; rec->type = type; rec->evcode = 0; }
             return type;
         } else {
             output_event();
@@ -1343,6 +1343,9 @@ struct Oracle {
         d->coll = coll; d->n_pair = n_pair; d->n_ghost = numghosts; d->n_interval = n_interval;
         d->n_output = n_output; d->n_updates = nupdates; d->n_forced_updates = nforcedupdate;
         d->t = t; d->tfalse = tfalse;
+        double nbr = 0.0;
+        for (int i = 1; i <= N; ++i) nbr += (double)(na_npt[i] + nnabdn[i]);
+        d->nbr_mean = nbr / (double)N;
     }
 };
 

@@ -402,6 +402,8 @@ struct dmd_batch {
     long long log_cap = 0;
     int hbonds = 1;
     cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
     std::string err;
     int ready = 0;
 };
@@ -414,6 +416,8 @@ int upload(dmd_batch &B) {
     int n = (int)B.hs.size();
     B.ds.resize(n);
     CK(cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&B.ev0));
+    CK(cudaEventCreate(&B.ev1));
     std::vector<DSys> hd(n);
     std::vector<int> cstart, clen, coff;
     for (int r = 0; r < n; ++r) {
@@ -543,8 +547,12 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
         CK(cudaMemcpy(B.ds[r].d.sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
     }
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
+    CK(cudaEventRecord(B.ev0, B.st));
     CK(dmd_launch_run(B.d_sys, n, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr, B.st));
+    CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) B.last_ms = ms;
     if (logs) {
         for (int r = 0; r < n; ++r) {
             long long cnt = B.hs[r].sc.log_count;
@@ -611,6 +619,8 @@ void batch_free(dmd_batch &B) {
     if (B.d_coff) cudaFree(B.d_coff);
     if (B.d_diag) cudaFree(B.d_diag);
     if (B.d_log) cudaFree(B.d_log);
+    if (B.ev0) cudaEventDestroy(B.ev0);
+    if (B.ev1) cudaEventDestroy(B.ev1);
     if (B.st) cudaStreamDestroy(B.st);
     B.ds.clear();
 }
@@ -652,6 +662,8 @@ void dmd_batch_destroy(dmd_batch *b) {
     delete b;
 }
 const char *dmd_batch_last_error(dmd_batch *b) { return b ? b->err.c_str() : "null handle"; }
+double dmd_batch_last_run_ms(dmd_batch *b) { return b ? b->last_ms : 0.0; }
+double dmd_last_run_ms(dmd_handle *h) { return h ? h->b.last_ms : 0.0; }
 
 int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, dmd_handle **out) {
     if (!out) return DMD_E_INPUT;
@@ -717,5 +729,38 @@ void dmd_destroy(dmd_handle *h) {
     delete h;
 }
 const char *dmd_last_error(dmd_handle *h) { return h ? h->b.err.c_str() : "null handle"; }
+
+int dmd_static_evcode(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, int8_t *out,
+                      char *err, int32_t errlen) {
+    HostSys H;
+    std::string e;
+    if (!cfg || !tables || !sys || !out) return DMD_E_INPUT;
+    if (!setup_host(H, cfg, tables, sys, e)) {
+        if (err && errlen > 0) std::snprintf(err, errlen, "%s", e.c_str());
+        return DMD_E_INPUT;
+    }
+    size_t N = H.N;
+    int hb = cfg->hbonds != 0;
+    for (size_t a = 0; a < N; ++a)
+        for (size_t b = 0; b < N; ++b) out[a * N + b] = a == b ? 1 : (int8_t)static_code(H.info[a], H.info[b], hb);
+    return DMD_OK;
+}
+
+int dmd_inspect(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, double *out, int32_t n,
+                char *err, int32_t errlen) {
+    HostSys H;
+    std::string e;
+    if (!cfg || !tables || !sys || !out) return DMD_E_INPUT;
+    if (!setup_host(H, cfg, tables, sys, e)) {
+        if (err && errlen > 0) std::snprintf(err, errlen, "%s", e.c_str());
+        return DMD_E_INPUT;
+    }
+    double v[] = {H.sc.interval, H.sc.interval_max, H.sig_max_all, H.tab.hdelr, (double)H.ncell, H.tab.rl,
+                  H.tab.rlsq[1], H.tab.rlsq[15], H.tab.rlsq[16], H.tab.rlsq[40], H.sc.n_forced, H.sc.t_fact,
+                  H.tab.evp1[15]};
+    int m = (int)(sizeof v / sizeof v[0]);
+    for (int k = 0; k < n && k < m; ++k) out[k] = v[k];
+    return m;
+}
 
 }  // extern "C"

@@ -484,6 +484,8 @@ __device__ int lane_pair_event(const DSys &S, SharedState &sh, int i, int j, lon
         }
     } else if (ct == 10) {
         double rating;
+        int hbchk = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
+        if (hbchk < 0) { set_err(sh, DMD_E_STATE, i); return ct; }
         if (evcode < 45) {
             int hb = er[4 * i + 3];
             rating = id[i] < id[hb] ? repuls_check_3(S, i, hb, j, tfalse) : repuls_check_3(S, hb, i, j, tfalse);
@@ -493,6 +495,8 @@ __device__ int lane_pair_event(const DSys &S, SharedState &sh, int i, int j, lon
         }
         ct = rating <= 10.0 ? 5 : 15;
     } else if (ct == 12) {
+        int hbchk = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
+        if (hbchk < 0) { set_err(sh, DMD_E_STATE, i); return ct; }
         if (evcode < 45) {
             int hb = er[4 * i + 3];
             if (S.bptnr[i] == hb) ct = check_sigma(S, i, hb, tfalse) > 10.0 ? 6 : 13; else ct = 15;
@@ -502,6 +506,10 @@ __device__ int lane_pair_event(const DSys &S, SharedState &sh, int i, int j, lon
         }
     }
     if (ct < 14) ct = eventdyn(S, i, j, evcode, ct, tfalse);
+    if (ct == 24 || ct == 25) {
+        int hbchk = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
+        if (hbchk < 0) { set_err(sh, DMD_E_STATE, i); return ct; }
+    }
     if (ct == 20) {
         if (id[i] + id[j] == 5) {
             S.bptnr[i] = j; S.bptnr[j] = i;
@@ -559,7 +567,8 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
     uint32_t k = 0;
     int N = S.N;
     int i;
-    do { i = (int)(dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) * N) + 1; } while (i == N + 1);
+    do { i = (int)(dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) * N) + 1; } while (i == N + 1 && k < 64);
+    if (i > N) i = N;
     i -= 1;
     sh.sc.n_ghost += 1;
     S.x[i] = S.x[i] + S.vx[i] * tfalse; S.y[i] = S.y[i] + S.vy[i] * tfalse; S.z[i] = S.z[i] + S.vz[i] * tfalse;
@@ -569,7 +578,7 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
         v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         r = v1 * v1 + v2 * v2;
-    } while ((r == 0.0) || (r >= 1.0));
+    } while (((r == 0.0) || (r >= 1.0)) && k < 4096);
     double fact = sqrt(-2.0 * T.setemp * bmi * dmd_log(r) / r);
     S.vx[i] = v1 * fact / bmi;
     S.vy[i] = v2 * fact / bmi;
@@ -577,12 +586,13 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
         v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         r = v1 * v1 + v2 * v2;
-    } while ((r == 0.0) || (r >= 1.0));
+    } while (((r == 0.0) || (r >= 1.0)) && k < 8192);
     fact = sqrt(-2.0 * T.setemp * bmi * dmd_log(r) / r);
     S.vz[i] = v1 * fact / bmi;
     S.x[i] = S.x[i] - S.vx[i] * tfalse; S.y[i] = S.y[i] - S.vy[i] * tfalse; S.z[i] = S.z[i] - S.vz[i] * tfalse;
     double tgho = 0.0;
-    while ((tgho < 1e-18) || (tgho == 1.0)) tgho = dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++);
+    while (((tgho < 1e-18) || (tgho == 1.0)) && k < 12288) tgho = dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++);
+    if (i > N || r == 0.0 || r >= 1.0 || tgho < 1e-18) set_err(sh, DMD_E_STATE, -1);
     double tn = -1.0 * dmd_log(tgho) * T.avegtime + tfalse;
     S.tim[N] = tn;
     S.queued[N] = tn < sh.sc.interval_max;
@@ -629,6 +639,12 @@ __device__ int cta_sum_i(SharedState &sh, int v) {
 
 /* ------------------------------------------------------------------ */
 /* CTA-wide: list rebuild and full prediction (code/nbor.f, code/events.f) */
+__device__ __forceinline__ int cell_coord(double p, int nc) {
+    double c = (p + 0.5) * nc;
+    if (!(c >= 0.0)) return 0;   /* also catches NaN */
+    int k = (int)c;
+    return k < nc ? k : nc - 1;
+}
 /* ------------------------------------------------------------------ */
 __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
     const int N = S.N, nc = S.ncell;
@@ -638,8 +654,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
         for (int c = threadIdx.x; c < ncell3; c += blockDim.x) S.cell_count[c] = 0;
         __syncthreads();
         for (int b = threadIdx.x; b < N; b += blockDim.x) {
-            int cx = min((int)((S.x[b] + 0.5) * nc), nc - 1), cy = min((int)((S.y[b] + 0.5) * nc), nc - 1),
-                cz = min((int)((S.z[b] + 0.5) * nc), nc - 1);
+            int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc);
             atomicAdd(&S.cell_count[(cz * nc + cy) * nc + cx], 1);
         }
         __syncthreads();
@@ -665,8 +680,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             __syncthreads();
         }
         for (int b = threadIdx.x; b < N; b += blockDim.x) {
-            int cx = min((int)((S.x[b] + 0.5) * nc), nc - 1), cy = min((int)((S.y[b] + 0.5) * nc), nc - 1),
-                cz = min((int)((S.z[b] + 0.5) * nc), nc - 1);
+            int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc);
             int c = (cz * nc + cy) * nc + cx;
             int slot = atomicAdd(&S.cell_count[c], 1);
             S.cell_beads[S.cell_start[c] + slot] = b;
@@ -700,8 +714,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             }
         };
         if (nc >= 3) {
-            int cx = min((int)((xb + 0.5) * nc), nc - 1), cy = min((int)((yb + 0.5) * nc), nc - 1),
-                cz = min((int)((zb + 0.5) * nc), nc - 1);
+            int cx = cell_coord(xb, nc), cy = cell_coord(yb, nc), cz = cell_coord(zb, nc);
             for (int dz = -1; dz <= 1; ++dz)
                 for (int dy = -1; dy <= 1; ++dy)
                     for (int dx = -1; dx <= 1; ++dx) {
@@ -824,9 +837,10 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
     const int N = S.N;
     const DTab &T = *S.tab;
     double tf = sh.sc.tfalse;
-    double sumvel = 0.0, ehh_ii = 0.0, ehh_ij = 0.0;
+    double sumvel = 0.0, ehh_ii = 0.0, ehh_ij = 0.0, nbr = 0.0;
     int hb_ii = 0, hb_ij = 0;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        nbr += (double)(S.upn[i] + S.dnn[i]);
         sumvel += S.bm[i] * (S.vx[i] * S.vx[i] + S.vy[i] * S.vy[i] + S.vz[i] * S.vz[i]);
         int p = S.bptnr[i];
         if (p > i) { if (S.info[p].chain == S.info[i].chain) ++hb_ii; else ++hb_ij; }
@@ -844,6 +858,7 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
         }
     }
     sumvel = cta_sum(sh, sumvel);
+    nbr = cta_sum(sh, nbr);
     ehh_ii = cta_sum(sh, ehh_ii);
     ehh_ij = cta_sum(sh, ehh_ij);
     hb_ii = cta_sum_i(sh, hb_ii);
@@ -908,6 +923,7 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
         out->coll = sh.sc.coll; out->n_pair = sh.sc.n_pair; out->n_ghost = sh.sc.n_ghost;
         out->n_interval = sh.sc.n_interval; out->n_output = sh.sc.n_output; out->n_updates = sh.sc.n_updates;
         out->n_forced_updates = sh.sc.n_forced_updates; out->t = sh.sc.t; out->tfalse = sh.sc.tfalse;
+        out->nbr_mean = nbr / (double)N;
     }
     __syncthreads();
 }
@@ -956,8 +972,17 @@ __global__ void __launch_bounds__(NTHREADS) k_run(DSys *systems, int nsys, long 
     if (threadIdx.x == 0) { sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0; }
     __syncthreads();
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
+    /* every committed pair or ghost event advances done; interval and output
+     * events are bounded by this cap so that a launch always ends */
+    const long long max_iter = 16 * target + 1000000;
+    long long iter = 0;
     while (true) {
         if (sh.sc.done >= target || sh.sc.err || sh.sc.stop) break;
+        if (++iter > max_iter) {
+            if (threadIdx.x == 0) set_err(sh, DMD_E_DEVICE_TIMEOUT, 0);
+            __syncthreads();
+            break;
+        }
         if (warp == 0) {
             int e = warp_tree_root(S);
             if (lane == 0) {

@@ -81,7 +81,7 @@ class Diag(C.Structure):
         ("nevents", C.c_int64 * 32),
         ("coll", C.c_int64), ("n_pair", C.c_int64), ("n_ghost", C.c_int64), ("n_interval", C.c_int64),
         ("n_output", C.c_int64), ("n_updates", C.c_int64), ("n_forced_updates", C.c_int64),
-        ("t", C.c_double), ("tfalse", C.c_double),
+        ("t", C.c_double), ("tfalse", C.c_double), ("nbr_mean", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -100,7 +100,7 @@ ENGINE_SYMBOLS = [
     "dmd_create", "dmd_run", "dmd_predict_all", "dmd_get_state", "dmd_diagnostics", "dmd_get_evcode",
     "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
-    "dmd_generate",
+    "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms",
 ]
 
 
@@ -150,6 +150,14 @@ def _declare(lib) -> None:
     lib.dmd_batch_last_error.restype = C.c_char_p
     lib.dmd_generate.argtypes = [C.POINTER(GenSpec), C.POINTER(Tables), C.c_int32] + [dbl_p] * 6 + [C.c_char_p, C.c_int32]
     lib.dmd_generate.restype = C.c_int
+    lib.dmd_last_run_ms.argtypes = [C.c_void_p]
+    lib.dmd_last_run_ms.restype = C.c_double
+    lib.dmd_batch_last_run_ms.argtypes = [C.c_void_p]
+    lib.dmd_batch_last_run_ms.restype = C.c_double
+    lib.dmd_static_evcode.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), i8_p, C.c_char_p, C.c_int32]
+    lib.dmd_static_evcode.restype = C.c_int
+    lib.dmd_inspect.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), dbl_p, C.c_int32, C.c_char_p, C.c_int32]
+    lib.dmd_inspect.restype = C.c_int
 
 
 _engine = None

@@ -247,6 +247,8 @@ def read_records(path: str) -> List[bytes]:
     pos = 0
     while pos + 4 <= len(data):
         (n,) = struct.unpack_from("<i", data, pos)
+        if n < 0 or pos + 8 + n > len(data):
+            raise ValueError(f"{path}: corrupt record framing at byte {pos}")
         body = data[pos + 4:pos + 4 + n]
         (n2,) = struct.unpack_from("<i", data, pos + 4 + n)
         if n2 != n or len(body) != n:
