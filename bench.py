@@ -1,0 +1,338 @@
+"""Benchmark of the GB300 PRIME20 DMD event engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c3|c2|c1|c4] [--events E]
+
+Workload (default c3): 32 independent replicas (seeded 8-96 chains of
+random 16-residue sequences at 5 mM, T* evenly spaced over 0.18-0.50),
+advanced together by one persistent launch.  A step commits E events in
+every replica (the reference's collision count).  ``value`` is committed
+events/s of the whole job with the state resident in HBM, timed with CUDA
+events on the launching stream; ``e2e`` is the same metric through the
+public C ABI with host buffers (create from host arrays, run, read the
+state back).  The plain one-system-per-launch path on the same replicas
+and the CPU restatement on the host cores are reported beside it.
+
+``--impl reference`` times the CPU restatement of the reference engine (the
+reference itself is Fortran + MPI and cannot be built here) on all host
+cores for the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "parallel-dmd-for-biomolecules_gb300")
+for p in (REPO, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "DMD events/s on 1 GB300: batched vs plain GPU vs host CPU; p50/p99 latency"
+UNIT = "events/s"
+
+
+# --------------------------------------------------------------- workloads
+def make_workload(name: str, rank: int = 0):
+    from dmdgb import systems
+
+    if name == "c3":
+        specs = systems.config_c3(32, seed=1 + 1000 * rank)
+        desc = "C3: 32 replicas, 8-96 chains x 16-mer random sequences, 5 mM, T* 0.18-0.50"
+    elif name == "c2":
+        specs = [systems.config_c2(seed=1 + rank)]
+        desc = "C2: 48 x KLVFFAE (1,344 beads), 5 mM, T* 0.18"
+    elif name == "c1":
+        specs = [systems.config_c1(seed=1 + rank)]
+        desc = "C1: 8 x KLVFFAE (224 beads), 5 mM, T* 0.20"
+    elif name == "c4":
+        specs = [systems.config_c4(seed=1 + rank)]
+        desc = "C4: 1000 x random 10-mer (~40,000 beads), 10 mM, T* 0.22"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    for s in specs:
+        systems.generate(s)
+    return specs, desc
+
+
+def algorithmic_bytes_per_event(nbr_mean: float) -> float:
+    """Minimal unique bytes one committed pair event touches: i and j
+    read+written (2 x 96), their per-bead constants (2 x 33), and for every
+    neighbour of i and j its position/velocity, identity, pair type, list
+    index and prediction read+write (86 bytes)."""
+    return 289.0 + 86.0 * 2.0 * nbr_mean
+
+
+def rebuild_bytes(n: int, nbr_mean: float) -> float:
+    return n * (24 + 4) + n * nbr_mean * (4 + 54)
+
+
+# ------------------------------------------------------------ clock sampler
+class ClockSampler:
+    def __init__(self, index: int = 0):
+        self.samples = []
+        self.index = index
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self):
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 3 + k and s[3 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def _cpu_worker(args):
+    spec, n_events = args
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, PKG)
+    from oracle.oracle import Oracle
+
+    o = Oracle(spec)
+    t0 = time.perf_counter()
+    o.run(n_events)
+    return n_events, time.perf_counter() - t0
+
+
+def cpu_rate(specs, events_per_replica: int, cores: int):
+    """Aggregate events/s of the CPU restatement, one replica per core."""
+    work = [(specs[k % len(specs)], events_per_replica) for k in range(cores)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, work)
+    wall = time.perf_counter() - t0
+    total = sum(r[0] for r in res)
+    slowest = max(r[1] for r in res)
+    return total / slowest, total, wall
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_event():
+    """DRAM bytes per committed event of the persistent kernel, from the
+    committed ncu capture summary (profiles/), or None."""
+    p = os.path.join(REPO, "profiles", "k_run_traffic.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["dram_bytes"]) / float(d["events"])
+    except Exception:
+        return None
+
+
+# ----------------------------------------------------------------- arms
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    specs, desc = make_workload(args.workload)
+    cores = max(1, min(os.cpu_count() or 1, 64))
+    n_ev = args.cpu_events
+    for _ in range(args.warmup):
+        cpu_rate(specs, max(1000, n_ev // 10), cores)
+    rates, times = [], []
+    total_ev = 0
+    for _ in range(args.steps):
+        r, tot, wall = cpu_rate(specs, n_ev, cores)
+        rates.append(r)
+        times.append(tot / r)
+        total_ev += tot
+    value = total_ev / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "events_per_replica_per_step": n_ev},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes, one C3 replica each, {n_ev} events per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    import __graft_entry__ as g
+
+    g.build()
+    from dmdgb import abi
+    from dmdgb.engine import Batch, Engine
+
+    specs, desc = make_workload(args.workload, rank)
+    E = args.events
+    batch = Batch(specs)
+    lib = batch.lib
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        batch.run(E)
+        flush.fill_(1.0)
+    barrier()
+    d0 = [batch.diagnostics(r) for r in range(len(specs))]
+    ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(2.0)          # evict the state from L2 between steps
+            torch.cuda.synchronize()
+            batch.run(E)
+            ms.append(lib.dmd_batch_last_run_ms(batch.h))
+    barrier()
+    d1 = [batch.diagnostics(r) for r in range(len(specs))]
+    step_s = sum(ms) / 1000.0
+    events = E * len(specs) * args.steps
+    if world > 1:
+        t = torch.tensor([step_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_s = float(t.item())
+    value = events * world / step_s
+    pair_events = sum(b["n_pair"] - a["n_pair"] for a, b in zip(d0, d1))
+    nbr = float(np.mean([d["nbr_mean"] for d in d1]))
+    rebuilds = sum(b["n_updates"] - a["n_updates"] for a, b in zip(d0, d1))
+    nbeads = int(np.mean([s.n_beads for s in specs]))
+    alg_bytes = pair_events * algorithmic_bytes_per_event(nbr) + rebuilds * rebuild_bytes(nbeads, nbr)
+    per_launch_bytes = alg_bytes / args.steps
+    launch_s = step_s / args.steps
+    hbm, peak_kind = peaks()
+    achieved = per_launch_bytes / launch_s / 1e9
+    tpe = traffic_per_event()
+    traffic = tpe * E * len(specs) if tpe else None
+
+    # the plain one-system-per-launch path on the same replicas
+    plain_events, plain_s = 0, 0.0
+    n_plain = min(len(specs), args.plain_replicas)
+    for s in specs[:n_plain]:
+        with Engine(s) as eng:
+            eng.run(E)          # warm-up of this system
+            eng.run(E)
+            plain_s += eng.lib.dmd_last_run_ms(eng.h) / 1000.0
+            plain_events += E
+    plain_value = plain_events / plain_s if plain_s > 0 else None
+
+    # end to end through the public API with host buffers
+    e2e_times, h2d, d2h = [], 0, 0
+    for s in specs:
+        n = s.n_beads
+        h2d += 6 * 8 * n + 4 * len(s.chain_len) + 4 * len(s.residues) + abi.C.sizeof(abi.Tables) + abi.C.sizeof(abi.RunCfg)
+        d2h += 6 * 8 * n + 3 * 4 * n + 4 * 4 * n + 24
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b2 = Batch(specs)
+        b2.run(E)
+        states = [b2.state(r) for r in range(len(specs))]
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        b2.close()
+        del states
+    e2e_value = E * len(specs) * world / statistics.median(e2e_times)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = max(1, min(os.cpu_count() or 1, 64))
+        r, tot, wall = cpu_rate(specs, args.cpu_events, cores)
+        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"CPU restatement, {cores} processes, one replica each, {args.cpu_events} events, {wall:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * step_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "replicas": len(specs), "events_per_replica_per_step": E,
+                       "beads_total": int(sum(s.n_beads for s in specs)), "l2": "flushed (256 MB write) between steps",
+                       "parallelism": f"replicas: one CTA per system, {world} GPU(s)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "plain_gpu": {"value": plain_value, "unit": UNIT, "replicas_timed": n_plain,
+                          "note": "same replicas, one system per launch, one after another"},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
+                         "bytes_per_event": algorithmic_bytes_per_event(nbr), "nbr_mean": nbr},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c3")
+    ap.add_argument("--events", type=int, default=20000, help="events per replica per step")
+    ap.add_argument("--cpu-events", type=int, default=200000)
+    ap.add_argument("--plain-replicas", type=int, default=32)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()
