@@ -174,6 +174,29 @@ const char *dmd_version(void);
  * row-major n_beads x n_beads). */
 int dmd_static_evcode(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,
                       int8_t *out, char *err, int32_t errlen);
+/* Allocation-free variant of dmd_create + dmd_predict_all (no counterpart in
+ * the reference, which has no device code).  For callers that cannot allocate
+ * device memory themselves: a host whose device memory is owned by another
+ * runtime or pool (a Fortran program under OpenACC/CUDA Fortran data regions,
+ * a serving process that reserves a fixed budget up front), where a
+ * cudaMalloc would synchronise the device, fail, or break that accounting.
+ * The caller passes the same host inputs as dmd_create and three device
+ * buffers of n_beads entries that receive the full prediction pass
+ * (code/events.f): times, 1-based partners, event types.  All intermediate
+ * data lives in one static device array of 8 MiB inside the library, which
+ * every GPU that loads the library holds until the process exits; systems of
+ * at most 8192 beads, neighbour lists of at most 64 entries (list_cap) and a
+ * rebuild grid of at most 48 cells per side fit, and larger inputs are
+ * rejected with DMD_E_CAPACITY and a message.  The first call on a device
+ * looks up the array's address (with that device current); make that first
+ * call before any stream capture.  Every call reuses the array: calls whose
+ * work overlaps on the GPU (different streams or host threads) race on it.
+ * stream: a cudaStream_t, or NULL for the default stream; the call returns
+ * after the stream has finished the pass. */
+int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,
+                            double *d_tim, int32_t *d_nptnr, int32_t *d_coltype, void *stream,
+                            char *err, int32_t errlen);
+
 /* Host-only: set-up values of code/main.F90:144-156 and code/nbor_setup.f:
  * interval, interval_max, sig_max_all, hdelr, cells per side, rl, rlsq(1),
  * rlsq(15), rlsq(16), rlsq(40), n_forced, t_fact, ev_param(1,15).

@@ -746,6 +746,86 @@ int dmd_static_evcode(const dmd_run_cfg *cfg, const dmd_tables *tables, const dm
     return DMD_OK;
 }
 
+/* The prediction pass of dmd_create + dmd_predict_all for callers that cannot
+ * allocate device memory: every intermediate array lives in the library's
+ * static scratch (engine.cu g_noalloc_scratch), the outputs go to the
+ * caller's device buffers, and no device memory is allocated or freed. */
+int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,
+                            double *d_tim, int32_t *d_nptnr, int32_t *d_coltype, void *stream,
+                            char *err, int32_t errlen) {
+    auto fail_msg = [&](int rc, const std::string &m) {
+        if (err && errlen > 0) std::snprintf(err, errlen, "%s", m.c_str());
+        return rc;
+    };
+    if (!cfg || !tables || !sys || !d_tim || !d_nptnr || !d_coltype) return fail_msg(DMD_E_INPUT, "null argument");
+    if (sys->n_beads > DMD_NOALLOC_MAX_BEADS)
+        return fail_msg(DMD_E_CAPACITY, "dmd_predict_all_noalloc: at most " + std::to_string(DMD_NOALLOC_MAX_BEADS) +
+                                            " beads (got " + std::to_string(sys->n_beads) + ")");
+    if (cfg->list_cap > DMD_NOALLOC_MAX_CAP)
+        return fail_msg(DMD_E_CAPACITY, "dmd_predict_all_noalloc: list_cap at most " + std::to_string(DMD_NOALLOC_MAX_CAP));
+    dmd_run_cfg c = *cfg;
+    if (c.list_cap <= 0) c.list_cap = DMD_NOALLOC_MAX_CAP;
+    HostSys H;
+    std::string e;
+    if (!setup_host(H, &c, tables, sys, e)) return fail_msg(DMD_E_INPUT, e);
+    if (H.ncell > DMD_NOALLOC_MAX_CELLS)
+        return fail_msg(DMD_E_CAPACITY, "dmd_predict_all_noalloc: the box needs " + std::to_string(H.ncell) +
+                                            " cells per side, at most " + std::to_string(DMD_NOALLOC_MAX_CELLS));
+    void *base = nullptr;
+    cudaError_t ce = dmd_noalloc_scratch(&base);
+    if (ce != cudaSuccess) return fail_msg(DMD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce));
+    DSys d{};
+    size_t bytes = layout(H, d, (char *)base);
+    if (bytes > DMD_NOALLOC_SCRATCH_BYTES)
+        return fail_msg(DMD_E_CAPACITY, "dmd_predict_all_noalloc: system needs " + std::to_string(bytes) +
+                                            " scratch bytes, the array holds " + std::to_string(DMD_NOALLOC_SCRATCH_BYTES));
+    d.N = H.N; d.nchains = H.nchains; d.cap = H.cap; d.ncell = H.ncell;
+    d.seed = H.cfg.seed; d.canon = H.cfg.canon; d.flags = H.cfg.flags;
+    d.nl1 = H.nl1; d.nl2 = H.nl2; d.log = nullptr; d.log_cap = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t N = H.N;
+    std::vector<double> tim(N + 3, H.sc.interval_max + DMD_LTSTEP);
+    std::vector<int> np(N + 3, -1);
+    std::vector<int8_t> ct(N + 3, -1);
+    std::vector<uint8_t> q(N + 3, 0);
+    if (H.cfg.canon) {
+        double tgho = 0.0;
+        uint32_t k = 0;
+        while ((tgho < 1e-18) || (tgho == 1.0)) tgho = dmd_uniform(H.cfg.seed, DMD_STREAM_GHOST0, 0, k++);
+        tim[N] = -1.0 * dmd_log(tgho) * H.tab.avegtime * .0000001;
+    } else {
+        tim[N] = 1000000000.0;
+    }
+    tim[N + 1] = H.sc.interval;
+    tim[N + 2] = 3.3 / (std::sqrt(H.tab.setemp)) + 5;
+    np[N] = np[N + 1] = np[N + 2] = -2;
+    ct[N] = ct[N + 1] = ct[N + 2] = -2;
+    struct Cp { void *dst; const void *src; size_t n; };
+    const Cp cps[] = {
+        {(void *)d.tab, &H.tab, sizeof(DTab)}, {d.sc, &H.sc, sizeof(DScal)},
+        {(void *)d.info, H.info.data(), N * sizeof(BeadInfo)}, {(void *)d.bm, H.bm.data(), N * 8},
+        {(void *)d.blmin, H.blmin.data(), N * 8}, {(void *)d.blmax, H.blmax.data(), N * 8},
+        {d.x, H.x.data(), N * 8}, {d.y, H.y.data(), N * 8}, {d.z, H.z.data(), N * 8},
+        {d.vx, H.vx.data(), N * 8}, {d.vy, H.vy.data(), N * 8}, {d.vz, H.vz.data(), N * 8},
+        {d.ident, H.ident.data(), N}, {d.bptnr, H.bptnr.data(), N * 4}, {d.er, H.er.data(), 4 * N * 4},
+        {d.ovp, H.ovp.data(), 4 * N * 4}, {d.ovc, H.ovc.data(), 4 * N},
+        {d.tim, tim.data(), (N + 3) * 8}, {d.nptnr, np.data(), (N + 3) * 4}, {d.colt, ct.data(), N + 3},
+        {d.queued, q.data(), N + 3},
+    };
+    for (const Cp &cp : cps) {
+        ce = cudaMemcpyAsync(cp.dst, cp.src, cp.n, cudaMemcpyHostToDevice, st);
+        if (ce != cudaSuccess) return fail_msg(DMD_E_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(ce));
+    }
+    ce = dmd_launch_predict_noalloc(d, H.cfg.hbonds != 0, d_tim, (int *)d_nptnr, (int *)d_coltype, st);
+    if (ce != cudaSuccess) return fail_msg(DMD_E_CUDA, std::string("launch: ") + cudaGetErrorString(ce));
+    DScal sc;
+    ce = cudaMemcpyAsync(&sc, d.sc, sizeof sc, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return fail_msg(DMD_E_CUDA, std::string("sync: ") + cudaGetErrorString(ce));
+    if (sc.err) return fail_msg(sc.err, "device error " + std::to_string(sc.err) + " (info " + std::to_string(sc.err_info) + ")");
+    return DMD_OK;
+}
+
 int dmd_inspect(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, double *out, int32_t n,
                 char *err, int32_t errlen) {
     HostSys H;

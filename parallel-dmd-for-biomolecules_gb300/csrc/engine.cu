@@ -21,6 +21,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "dmd.h"
 #include "engine.cuh"
 #include "engine_api.h"
@@ -1104,5 +1106,63 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, long long target, int hbon
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st) {
     k_diag<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, chain_start, chain_len, chain_off, out);
+    return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------ */
+/* allocation-free prediction pass                                     */
+/* ------------------------------------------------------------------ */
+/* Device memory of dmd_predict_all_noalloc: one file-scope array that every
+ * GPU loading this library holds until the process exits.  It carries a
+ * whole system (tables, bead state, neighbour lists, cell grid) for at most
+ * DMD_NOALLOC_MAX_BEADS beads with lists of DMD_NOALLOC_MAX_CAP entries.
+ * Every call reuses it and overwrites what the previous call left; calls
+ * whose work overlaps on the GPU (several streams, or several host threads)
+ * race on it. */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[DMD_NOALLOC_SCRATCH_BYTES];
+
+__global__ void __launch_bounds__(NTHREADS) k_predict_noalloc(DSys S_in, int hbonds, double *tim_out,
+                                                              int *nptnr_out, int *colt_out) {
+    __shared__ SharedState sh;
+    __shared__ DSys S_sh;
+    if (threadIdx.x == 0) { S_sh = S_in; sh.sc = *S_in.sc; }
+    __syncthreads();
+    const DSys &S = S_sh;
+    cta_rebuild(S, sh, hbonds);
+    for (int b = threadIdx.x; b < S.N; b += blockDim.x) {
+        tim_out[b] = S.tim[b];
+        int p = S.nptnr[b];
+        nptnr_out[b] = p >= 0 ? p + 1 : p;
+        colt_out[b] = S.colt[b];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *S.sc = sh.sc;
+}
+
+/* Address of the scratch array on the current device, looked up once per
+ * device (with that device current) and cached. */
+cudaError_t dmd_noalloc_scratch(void **ptr) {
+    static void *cached[256];
+    static bool have[256];
+    static std::mutex mu;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!have[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        cached[dev] = p;
+        have[dev] = true;
+    }
+    *ptr = cached[dev];
+    return cudaSuccess;
+}
+
+cudaError_t dmd_launch_predict_noalloc(const DSys &S, int hbonds, double *tim_out, int *nptnr_out, int *colt_out,
+                                       cudaStream_t st) {
+    k_predict_noalloc<<<1, NTHREADS, 0, st>>>(S, hbonds, tim_out, nptnr_out, colt_out);
     return cudaGetLastError();
 }

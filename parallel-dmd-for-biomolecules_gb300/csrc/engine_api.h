@@ -13,4 +13,14 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, long long target, int hbon
                            const int *chain_len, const int *chain_off, dmd_diag *outputs, cudaStream_t st);
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st);
+
+/* allocation-free prediction pass (engine.cu): the scratch array's size and
+ * limits, its per-device address, and the launch */
+#define DMD_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define DMD_NOALLOC_MAX_BEADS 8192
+#define DMD_NOALLOC_MAX_CAP 64
+#define DMD_NOALLOC_MAX_CELLS 48
+cudaError_t dmd_noalloc_scratch(void **ptr);
+cudaError_t dmd_launch_predict_noalloc(const DSys &S, int hbonds, double *tim_out, int *nptnr_out, int *colt_out,
+                                       cudaStream_t st);
 #endif

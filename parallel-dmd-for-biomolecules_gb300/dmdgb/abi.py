@@ -100,7 +100,7 @@ ENGINE_SYMBOLS = [
     "dmd_create", "dmd_run", "dmd_predict_all", "dmd_get_state", "dmd_diagnostics", "dmd_get_evcode",
     "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
-    "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms",
+    "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
 ]
 
 
@@ -154,6 +154,9 @@ def _declare(lib) -> None:
     lib.dmd_last_run_ms.restype = C.c_double
     lib.dmd_batch_last_run_ms.argtypes = [C.c_void_p]
     lib.dmd_batch_last_run_ms.restype = C.c_double
+    lib.dmd_predict_all_noalloc.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System),
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int32]
+    lib.dmd_predict_all_noalloc.restype = C.c_int
     lib.dmd_static_evcode.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), i8_p, C.c_char_p, C.c_int32]
     lib.dmd_static_evcode.restype = C.c_int
     lib.dmd_inspect.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), dbl_p, C.c_int32, C.c_char_p, C.c_int32]
