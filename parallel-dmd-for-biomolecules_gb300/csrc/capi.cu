@@ -210,6 +210,7 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
     if (H.cfg.n_wrap <= 0) H.cfg.n_wrap = 2;
     if (H.cfg.numbin <= 0) H.cfg.numbin = 2000;
     H.cap = cfg->list_cap > 0 ? cfg->list_cap : 128;
+    if (H.cap > 128) return fail(err, "list_cap at most 128");
     if (!(cfg->tstar > 0)) return fail(err, "tstar must be positive");
     if (!S || S->n_beads <= 0 || S->n_chains <= 0 || !S->chain_len || !S->residues) return fail(err, "empty system");
     if (!S->x || !S->y || !S->z || !S->vx || !S->vy || !S->vz) return fail(err, "positions and velocities are required");
@@ -380,6 +381,7 @@ size_t layout(const HostSys &H, DSys &d, char *base) {
     d.upn = P.take<int>(N); d.dnn = P.take<int>(N);
     d.cell_count = P.take<int>(nc3 + 1); d.cell_start = P.take<int>(nc3 + 1); d.cell_beads = P.take<int>(N);
     d.l1i = P.take<int>(H.nl1); d.l2i = P.take<int>(H.nl2);
+    d.key = P.take<long long>(NE); d.owner = P.take<int>(N);
     return P.off + 256;
 }
 

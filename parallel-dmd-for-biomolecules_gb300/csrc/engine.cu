@@ -2,24 +2,37 @@
  * engine.cu -- kernels of the GB300 PRIME20 DMD event engine.
  *
  * One CTA owns one system (a replica or a served request) for the whole
- * launch and runs the reference's main loop (code/main.F90:484-1258) on it:
- * select the earliest queued event, commit it, re-predict what it touched.
+ * launch and runs the reference's main loop (code/main.F90:484-1258) on it.
  * A launch with many CTAs advances many independent systems at once (the
- * batched-replica path); a launch with one CTA is the plain path.
+ * batched-replica and serving paths); a launch with one CTA is the plain path.
  *
- * Per-event work inside the CTA:
- *   - event selection: a two-level tournament (argmin of 32 entries, then of
- *     32 groups) over the keys (queued ? tim : inf) in (time, index) order,
- *     which replaces the calendar queue of code/add_tbin.f / del_tbin.f;
- *   - the collision itself on one lane (it is O(1) and branch heavy);
- *   - re-prediction (code/partial_events.f) warp-parallel over neighbour
- *     lists, keeping the reference's per-bead order of down-list operations;
- *   - interval events (code/main.F90:1126-1187) and list rebuilds
- *     (code/nbor.f, code/events.f) spread over all threads of the CTA.
+ * Inside a CTA, pair events are committed in conflict-free batches:
+ *   1. candidates: the earliest queued bead events below a time cut (and
+ *      below every pseudo event), sorted in (time, index) order;
+ *   2. footprints: each candidate claims the beads its commit reads or
+ *      writes (its two beads, both neighbour lists, H-bond helpers, and the
+ *      lists of beads it may fully re-predict); the batch is the longest
+ *      prefix whose footprints are disjoint;
+ *   3. one warp per event: collision (written, with a snapshot), then the
+ *      re-prediction of code/partial_events.f into a warp-private buffer;
+ *   4. validation: event k stands only if no earlier event of the batch
+ *      produced a new prediction before it, so the committed events are
+ *      exactly the next events of the serial (time, index) order;
+ *   5. commit the buffers of the standing events; roll the others back.
+ * Because the footprints are disjoint, each event reads exactly what it
+ * would read in the serial order and the results are bit-identical to
+ * one-at-a-time processing.  Ghost, interval and output events are batch
+ * barriers and run alone.
+ *
+ * GB300 executes an FP64 warp instruction in about 64 cycles per SM
+ * sub-partition whatever the number of active lanes (DDIV ~500, DSQRT ~690),
+ * so: times are compared as integer keys, the collision's independent
+ * components run on separate lanes, and several events share the SM.
  */
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <limits.h>
 
 #include <mutex>
 
@@ -29,66 +42,115 @@
 
 #define NTHREADS 256
 #define NWARPS (NTHREADS / 32)
-#define OPS_MAX 1024
+#define OPS_MAX 264        /* 2 * list capacity (128) + 6 extras + slack */
+#define CAND_MAX 64
+#define META_MAX 16
+#define REDO_MAX OPS_MAX
+#define CASC_MAX 64
+#define FULL 0xffffffffu
 
-struct SharedState {
-    DScal sc;            /* this system's scalars while the CTA runs */
-    int ev;              /* selected event entry */
-    int ops_l[OPS_MAX];  /* down-list operations (bead, source) in reference order */
-    int ops_s[OPS_MAX];
-    int nops;
-    int touched[OPS_MAX + 8];
-    int ntouched;
-    int redo_flag[32];   /* leaders whose op walk stopped at a full redo */
-    double red_d[NWARPS];
-    long long red_l[NWARPS * 4];
-    int red_i[NWARPS * 4];
-    int xpulse, ev_i, ev_j, ev_ct;
-    int rebuild;
+/* per-warp working area of one event (dynamic shared memory) */
+struct WarpArea {
+    int nops, nlead, npred, nredo, nmeta, ncasc;
+    int ops_l[OPS_MAX], ops_s[OPS_MAX];
+    int lead_l[OPS_MAX], lead_q[OPS_MAX];
+    /* buffered predictions: bead, time, partner, type, queued */
+    int pb[OPS_MAX + 2];
+    double pt[OPS_MAX + 2];
+    int pn[OPS_MAX + 2];
+    int8_t pc[OPS_MAX + 2];
+    uint8_t pq[OPS_MAX + 2];
+    int redo_l[REDO_MAX], redo_p[REDO_MAX], redo_slot[REDO_MAX];
+    /* snapshot of what the collision may write */
+    int mb[META_MAX];
+    int8_t mident[META_MAX];
+    int mbp[META_MAX];
+    int mer[META_MAX][4];
+    int movp[META_MAX][4];
+    int8_t movc[META_MAX][4];
+    double sij[12];
+    int8_t colt_i;
+    int casc[CASC_MAX];
+    /* the event */
+    int i, j, ct, evcode, xpulse, conflict, casc_over;
+    int err, err_info;
+    long long coll;
+    double tf;
+    long long tnew_key;
+    int tnew_idx;
 };
 
-__device__ __forceinline__ void set_err(SharedState &sh, int code, int info) {
-    if (sh.sc.err == 0) { sh.sc.err = code; sh.sc.err_info = info; }
+struct SharedState {
+    DScal sc;
+    int ev;
+    long long cand_key[CAND_MAX];
+    int cand_idx[CAND_MAX];
+    long long sort_key[CAND_MAX];
+    int sort_idx[CAND_MAX];
+    int ncand, m, nbatch, nvalid, overflow;
+    long long kcut;
+    double delta;        /* time window of the candidate cut */
+    int groups[256];
+    int ngroups;
+    double red_d[NWARPS];
+    int red_i[NWARPS * 4];
+    int rebuild;
+    int touched[8];
+};
+
+/* where an error goes: the system's status, or the status of one
+ * speculative event (raised only if that event is committed) */
+struct Err { int *code; int *info; };
+__device__ __forceinline__ void set_err(Err e, int code, int info) {
+    if (atomicCAS(e.code, 0, code) == 0) *e.info = info;
 }
+__device__ __forceinline__ Err cta_err(SharedState &sh) { return Err{&sh.sc.err, &sh.sc.err_info}; }
+__device__ __forceinline__ void set_err(SharedState &sh, int code, int info) { set_err(cta_err(sh), code, info); }
 
 /* ------------------------------------------------------------------ */
-/* warp helpers                                                        */
+/* keys and minima                                                     */
 /* ------------------------------------------------------------------ */
-__device__ __forceinline__ void warp_lexmin(double &t, int &p, int &ty) {
+/* lexicographic (key, partner) minimum across the warp, carrying time and type */
+__device__ __forceinline__ void warp_keymin(long long &k, int &p, double &t, int &ty) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        double t2 = __shfl_xor_sync(0xffffffffu, t, o);
-        int p2 = __shfl_xor_sync(0xffffffffu, p, o);
-        int y2 = __shfl_xor_sync(0xffffffffu, ty, o);
-        if (lex_less(t2, p2, t, p)) { t = t2; p = p2; ty = y2; }
+        long long k2 = __shfl_xor_sync(FULL, k, o);
+        int p2 = __shfl_xor_sync(FULL, p, o);
+        double t2 = __shfl_xor_sync(FULL, t, o);
+        int y2 = __shfl_xor_sync(FULL, ty, o);
+        if (key_less(k2, p2, k, p)) { k = k2; p = p2; t = t2; ty = y2; }
     }
 }
 
-__device__ __forceinline__ double entry_key(const DSys &S, int e) {
-    return S.queued[e] ? S.tim[e] : HUGE_VAL;
+__device__ __forceinline__ void set_pred(const DSys &S, int b, double t, int p, int ty, bool q) {
+    S.tim[b] = t;
+    S.nptnr[b] = p;
+    S.colt[b] = (int8_t)ty;
+    S.queued[b] = q ? 1 : 0;
+    S.key[b] = q ? okey(t) : DMD_KEY_INF;
 }
 
 /* ------------------------------------------------------------------ */
-/* tournament                                                          */
+/* tournament over the integer keys                                    */
 /* ------------------------------------------------------------------ */
-__device__ void l1_update(const DSys &S, int g, int NE) {  /* one thread, group g */
-    int best = -1;
-    double bk = HUGE_VAL;
+__device__ void l1_update(const DSys &S, int g, int NE) {
     int lo = g * 32, hi = min(lo + 32, NE);
-    for (int e = lo; e < hi; ++e) {
-        double k = entry_key(S, e);
-        if (best < 0 || k < bk) { bk = k; best = e; }   /* ascending e: ties keep the lower index */
+    int best = lo;
+    long long bk = S.key[lo];
+    for (int e = lo + 1; e < hi; ++e) {
+        long long k = S.key[e];
+        if (k < bk) { bk = k; best = e; }
     }
     S.l1i[g] = best;
 }
-__device__ void l2_update(const DSys &S, int h) {  /* one thread, group h */
-    int best = -1;
-    double bk = HUGE_VAL;
+__device__ void l2_update(const DSys &S, int h) {
     int lo = h * 32, hi = min(lo + 32, S.nl1);
-    for (int g = lo; g < hi; ++g) {
+    int best = S.l1i[lo];
+    long long bk = S.key[best];
+    for (int g = lo + 1; g < hi; ++g) {
         int e = S.l1i[g];
-        double k = entry_key(S, e);
-        if (best < 0 || lex_less(k, e, bk, best)) { bk = k; best = e; }
+        long long k = S.key[e];
+        if (key_less(k, e, bk, best)) { bk = k; best = e; }
     }
     S.l2i[h] = best;
 }
@@ -99,174 +161,38 @@ __device__ void cta_tree_rebuild(const DSys &S) {
     for (int h = threadIdx.x; h < S.nl2; h += blockDim.x) l2_update(S, h);
     __syncthreads();
 }
-/* warp: root of the tournament */
-__device__ int warp_tree_root(const DSys &S) {
+__device__ int warp_tree_root(const DSys &S, long long &kroot) {
     int lane = threadIdx.x & 31;
-    double bk = HUGE_VAL;
-    int best = 0x7fffffff, dummy = 0;
+    long long bk = DMD_KEY_INF;
+    int best = INT_MAX;
     for (int h = lane; h < S.nl2; h += 32) {
         int e = S.l2i[h];
-        double k = entry_key(S, e);
-        if (lex_less(k, e, bk, best)) { bk = k; best = e; }
+        long long k = S.key[e];
+        if (key_less(k, e, bk, best)) { bk = k; best = e; }
     }
-    warp_lexmin(bk, best, dummy);
-    return bk == HUGE_VAL ? -1 : best;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long k2 = __shfl_xor_sync(FULL, bk, o);
+        int b2 = __shfl_xor_sync(FULL, best, o);
+        if (key_less(k2, b2, bk, best)) { bk = k2; best = b2; }
+    }
+    kroot = bk;
+    return bk == DMD_KEY_INF ? -1 : best;
 }
-/* warp: refresh the groups holding the touched entries */
-__device__ void warp_tree_update(const DSys &S, const int *touched, int nt) {
+/* warp: refresh the level-1 groups of the given entries (level 2 after a sync) */
+__device__ void warp_l1_refresh(const DSys &S, const int *entries, int n) {
     int lane = threadIdx.x & 31;
-    int NE = S.N + 3;
-    for (int q = lane; q < nt; q += 32) l1_update(S, touched[q] >> 5, NE);
-    __syncwarp();
-    __threadfence_block();
-    for (int q = lane; q < nt; q += 32) l2_update(S, touched[q] >> 10);
-    __syncwarp();
-    __threadfence_block();
+    for (int q = lane; q < n; q += 32) { int e = entries[q]; if (e >= 0) l1_update(S, e >> 5, S.N + 3); }
 }
-
-/* ------------------------------------------------------------------ */
-/* re-prediction (code/partial_events.f, eventredo_up.f, eventredo_down.f) */
-/* ------------------------------------------------------------------ */
-__device__ __forceinline__ bool check_tij(SharedState &sh, double tij, int i, int j) {
-    /* reference debug check: negative time beyond 1e-10 (code/eventredo_up.f:58-74) */
-    if (tij < 0.0 && fabs(tij) > 1.0e-10) { set_err(sh, DMD_E_NEG_TIME, i); return false; }
-    return true;
-}
-
-/* warp: full re-prediction of bead l at time tfalse */
-__device__ void warp_redo_full(const DSys &S, SharedState &sh, int l, double tfalse, double interval_max, int hbonds) {
+__device__ void warp_l2_refresh(const DSys &S, const int *entries, int n) {
     int lane = threadIdx.x & 31;
-    double H = interval_max + DMD_LTSTEP - tfalse;
-    double bt = H;
-    int bp = -1, by = -1;
-    int n = S.upn[l];
-    const int *up = S.up + (size_t)l * S.cap;
-    for (int k = lane; k < n + 3; k += 32) {
-        int m;
-        int code;
-        if (k < n) {
-            m = up[k];
-            code = pair_code(S, m, l, hbonds);
-        } else {
-            m = S.er[4 * l + (k - n)];
-            if (m <= l) continue;
-            code = pair_code(S, m, l, hbonds);
-        }
-        double tij; int ty;
-        if (!d_predict(S, l, m, code, tfalse, tij, ty)) { set_err(sh, DMD_E_INPUT, code); continue; }
-        check_tij(sh, tij, l, m);
-        if (lex_less(tij, m, bt, bp)) { bt = tij; bp = m; by = ty; }
-    }
-    warp_lexmin(bt, bp, by);
-    if (lane == 0) {
-        double tn = bt + tfalse;
-        S.tim[l] = tn;
-        S.nptnr[l] = bp;
-        S.colt[l] = (int8_t)by;
-        S.queued[l] = tn < interval_max;
-    }
-    __syncwarp();
-}
-
-/* one lane: eventredo_down(l, src) */
-__device__ void lane_redo_down(const DSys &S, SharedState &sh, int l, int src, double tfalse, double interval_max, int hbonds) {
-    int code = pair_code(S, l, src, hbonds);
-    double tij; int ty;
-    if (!d_predict(S, l, src, code, tfalse, tij, ty)) { set_err(sh, DMD_E_INPUT, code); return; }
-    check_tij(sh, tij, l, src);
-    tij = tij + tfalse;
-    if (lex_less(tij, src, S.tim[l], S.nptnr[l])) {
-        S.tim[l] = tij;
-        S.nptnr[l] = src;
-        S.colt[l] = (int8_t)ty;
-        S.queued[l] = tij < interval_max;
-    }
-}
-
-/* warp: partial_events(i, j) after the pair (or ghost, j = -1) event */
-__device__ void warp_partial_events(const DSys &S, SharedState &sh, int i, int j, double tfalse, double interval_max, int hbonds) {
-    int lane = threadIdx.x & 31;
-    warp_redo_full(S, sh, i, tfalse, interval_max, hbonds);
-    if (j >= 0) warp_redo_full(S, sh, j, tfalse, interval_max, hbonds);
-    /* the down-list operations in reference order */
-    if (lane == 0) {
-        int n = 0;
-        const int *dn = S.dn + (size_t)i * S.cap;
-        for (int k = 0; k < S.dnn[i] && n < OPS_MAX; ++k) { sh.ops_l[n] = dn[k]; sh.ops_s[n] = i; ++n; }
-        for (int k = 0; k < 3 && n < OPS_MAX; ++k) {
-            int l = S.er[4 * i + k];
-            if (l >= 0 && l < i) { sh.ops_l[n] = l; sh.ops_s[n] = i; ++n; }
-        }
-        if (j >= 0) {
-            const int *dj = S.dn + (size_t)j * S.cap;
-            for (int k = 0; k < S.dnn[j] && n < OPS_MAX; ++k) {
-                int l = dj[k];
-                if (l != i) { sh.ops_l[n] = l; sh.ops_s[n] = j; ++n; }
-            }
-            for (int k = 0; k < 3 && n < OPS_MAX; ++k) {
-                int l = S.er[4 * j + k];
-                if (l >= 0 && l < j) { sh.ops_l[n] = l; sh.ops_s[n] = j; ++n; }
-            }
-        }
-        sh.nops = n;
-        sh.ntouched = 0;
-    }
-    __syncwarp();
-    int nops = sh.nops;
-    /* lanes walk the operations of distinct beads; a bead whose walk reaches
-     * a full redo hands it to the whole warp */
-    for (int base = 0; base < nops; base += 32) {
-        int q = base + lane;
-        bool leader = false;
-        int l = -1, stop_at = -1;
-        if (q < nops) {
-            l = sh.ops_l[q];
-            leader = true;
-            for (int p = 0; p < q; ++p) if (sh.ops_l[p] == l) { leader = false; break; }
-        }
-        if (leader) {
-            for (int p = q; p < nops; ++p) {
-                if (sh.ops_l[p] != l) continue;
-                int src = sh.ops_s[p];
-                if (S.nptnr[l] != src) lane_redo_down(S, sh, l, src, tfalse, interval_max, hbonds);
-                else { stop_at = p; break; }
-            }
-            int slot = atomicAdd(&sh.ntouched, 1);
-            if (slot < OPS_MAX) sh.touched[slot] = l;
-        }
-        __syncwarp();
-        unsigned pend = __ballot_sync(0xffffffffu, stop_at >= 0);
-        while (pend) {
-            int src_lane = __ffs(pend) - 1;
-            pend &= pend - 1;
-            int lb = __shfl_sync(0xffffffffu, l, src_lane);
-            int p0 = __shfl_sync(0xffffffffu, stop_at, src_lane);
-            /* operation p0 needs a full redo; continue this bead's walk */
-            for (int p = p0; p < nops; ++p) {
-                if (sh.ops_l[p] != lb) continue;
-                int src = sh.ops_s[p];
-                bool full = S.nptnr[lb] == src;
-                __syncwarp();
-                if (full) warp_redo_full(S, sh, lb, tfalse, interval_max, hbonds);
-                else if (lane == 0) lane_redo_down(S, sh, lb, src, tfalse, interval_max, hbonds);
-                __syncwarp();
-            }
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        int nt = sh.ntouched < OPS_MAX ? sh.ntouched : OPS_MAX;
-        sh.touched[nt++] = i;
-        if (j >= 0) sh.touched[nt++] = j;
-        sh.ntouched = nt;
-    }
-    __syncwarp();
+    for (int q = lane; q < n; q += 32) { int e = entries[q]; if (e >= 0) l2_update(S, e >> 10); }
 }
 
 /* ------------------------------------------------------------------ */
 /* H-bond bookkeeping (code/repuls_add.f, repuls_del_b.f, main.F90:825-868) */
 /* ------------------------------------------------------------------ */
-__device__ void ovr_set(const DSys &S, SharedState &sh, int a, int b, int code, int hbonds) {
+__device__ void ovr_set(const DSys &S, Err E, int a, int b, int code, int hbonds) {
     int *op = S.ovp + 4 * a;
     int8_t *oc = S.ovc + 4 * a;
     int st = static_code(S.info[a], S.info[b], hbonds);
@@ -278,30 +204,38 @@ __device__ void ovr_set(const DSys &S, SharedState &sh, int a, int b, int code, 
     if (code == st) return;
     for (int s = 0; s < 4; ++s)
         if (op[s] < 0) { op[s] = b; oc[s] = (int8_t)code; return; }
-    set_err(sh, DMD_E_CAPACITY, a);
+    set_err(E, DMD_E_CAPACITY, a);
 }
-__device__ void helpers_of(const DSys &S, int i, int j, int &ncim1, int &ncai, int &ncaj, int &nnjp1) {
+__device__ __forceinline__ void helpers_of(const DSys &S, int i, int j, int &ncim1, int &ncai, int &ncaj, int &nnjp1) {
     int Li = S.info[i].L, Lj = S.info[j].L;
     ncim1 = i + Li - 1; ncai = i - Li; ncaj = j - 2 * Lj; nnjp1 = j - Lj + 1;
 }
-__device__ void repuls_add(const DSys &S, SharedState &sh, int i, int j, int hbonds) {  /* i = NH, j = CO */
+/* the two index-derived helpers of an NH or CO bead, else -1 */
+__device__ __forceinline__ void own_helpers(const DSys &S, int x, int &h1, int &h2) {
+    h1 = h2 = -1;
+    if (x < 0) return;
+    BeadInfo I = S.info[x];
+    if (I.kind == BK_NH) { h1 = x + I.L - 1; h2 = x - I.L; }
+    else if (I.kind == BK_CO) { h1 = x - 2 * I.L; h2 = x - I.L + 1; }
+}
+__device__ void repuls_add(const DSys &S, Err E, int i, int j, int hbonds) {  /* i = NH, j = CO */
     int ncim1, ncai, ncaj, nnjp1;
     helpers_of(S, i, j, ncim1, ncai, ncaj, nnjp1);
-    ovr_set(S, sh, ncaj, i, 50, hbonds); ovr_set(S, sh, i, ncaj, 40, hbonds);
-    ovr_set(S, sh, i, nnjp1, 40, hbonds); ovr_set(S, sh, nnjp1, i, 50, hbonds);
-    ovr_set(S, sh, ncai, j, 50, hbonds); ovr_set(S, sh, j, ncai, 40, hbonds);
-    ovr_set(S, sh, j, ncim1, 40, hbonds); ovr_set(S, sh, ncim1, j, 50, hbonds);
+    ovr_set(S, E, ncaj, i, 50, hbonds); ovr_set(S, E, i, ncaj, 40, hbonds);
+    ovr_set(S, E, i, nnjp1, 40, hbonds); ovr_set(S, E, nnjp1, i, 50, hbonds);
+    ovr_set(S, E, ncai, j, 50, hbonds); ovr_set(S, E, j, ncai, 40, hbonds);
+    ovr_set(S, E, j, ncim1, 40, hbonds); ovr_set(S, E, ncim1, j, 50, hbonds);
     int *er = S.er;
     er[4 * i + 0] = ncaj; er[4 * i + 1] = nnjp1; er[4 * ncaj + 2] = i; er[4 * nnjp1 + 2] = i;
     er[4 * j + 0] = ncai; er[4 * j + 1] = ncim1; er[4 * ncai + 2] = j; er[4 * ncim1 + 2] = j;
     er[4 * i + 3] = j; er[4 * j + 3] = i;
 }
-__device__ void shoulders_off(const DSys &S, SharedState &sh, int n, int c, int hbonds) {
+__device__ void shoulders_off(const DSys &S, Err E, int n, int c, int hbonds) {
     int ncaj = S.er[4 * n + 0], nnjp1 = S.er[4 * n + 1], ncai = S.er[4 * c + 0], ncim1 = S.er[4 * c + 1];
-    if (ncaj >= 0) { ovr_set(S, sh, ncaj, n, 1, hbonds); ovr_set(S, sh, n, ncaj, 1, hbonds); }
-    if (nnjp1 >= 0) { ovr_set(S, sh, n, nnjp1, 1, hbonds); ovr_set(S, sh, nnjp1, n, 1, hbonds); }
-    if (ncai >= 0) { ovr_set(S, sh, ncai, c, 1, hbonds); ovr_set(S, sh, c, ncai, 1, hbonds); }
-    if (ncim1 >= 0) { ovr_set(S, sh, c, ncim1, 1, hbonds); ovr_set(S, sh, ncim1, c, 1, hbonds); }
+    if (ncaj >= 0) { ovr_set(S, E, ncaj, n, 1, hbonds); ovr_set(S, E, n, ncaj, 1, hbonds); }
+    if (nnjp1 >= 0) { ovr_set(S, E, n, nnjp1, 1, hbonds); ovr_set(S, E, nnjp1, n, 1, hbonds); }
+    if (ncai >= 0) { ovr_set(S, E, ncai, c, 1, hbonds); ovr_set(S, E, c, ncai, 1, hbonds); }
+    if (ncim1 >= 0) { ovr_set(S, E, c, ncim1, 1, hbonds); ovr_set(S, E, ncim1, c, 1, hbonds); }
 }
 __device__ void repuls_del_b(const DSys &S, int i, int j) {
     int ncim1, ncai, ncaj, nnjp1;
@@ -313,170 +247,271 @@ __device__ void repuls_del_b(const DSys &S, int i, int j) {
 }
 
 /* ------------------------------------------------------------------ */
-/* collision dynamics (code/eventdyn.f, bumped.f, repuls_check*.f, check_sigma.f) */
+/* warp-collective pair geometry: components on lanes 0..2             */
 /* ------------------------------------------------------------------ */
-__device__ double dist_now(const DSys &S, int a, int b, double tfalse) {
-    double vxa = S.vx[a] - S.vx[b], vya = S.vy[a] - S.vy[b], vza = S.vz[a] - S.vz[b];
-    double rx = S.x[a] - S.x[b] + vxa * tfalse, ry = S.y[a] - S.y[b] + vya * tfalse, rz = S.z[a] - S.z[b] + vza * tfalse;
-    rx = rx - d_nint(rx); ry = ry - d_nint(ry); rz = rz - d_nint(rz);
-    double d = rx * rx + ry * ry + rz * rz;
-    return sqrt(d);
-}
-__device__ double repuls_check(const DSys &S, int i, int j, double tfalse) {
-    int ncim1, ncai, ncaj, nnjp1;
-    helpers_of(S, i, j, ncim1, ncai, ncaj, nnjp1);
-    const DTab &T = *S.tab;
-    double d1 = dist_now(S, i, ncaj, tfalse), d2 = dist_now(S, i, nnjp1, tfalse);
-    double d3 = dist_now(S, j, ncai, tfalse), d4 = dist_now(S, j, ncim1, tfalse);
-    if ((d1 > T.shd1) && (d2 > T.shd2) && (d3 > T.shd3) && (d4 > T.shd4)) return 10.0;
-    return 11.0;
-}
-__device__ double repuls_check_3(const DSys &S, int i, int j, int k, double tfalse) {
-    int ncim1, ncai, ncaj, nnjp1;
-    helpers_of(S, i, j, ncim1, ncai, ncaj, nnjp1);
-    const DTab &T = *S.tab;
-    int m = 0;
-    double d1 = dist_now(S, i, ncaj, tfalse);
-    if ((ncaj != k) && (d1 > T.shd1)) m = m + 1;
-    double d2 = dist_now(S, i, nnjp1, tfalse);
-    if ((nnjp1 != k) && (d2 > T.shd2)) m = m + 1;
-    double d3 = dist_now(S, j, ncai, tfalse);
-    if ((ncai != k) && (d3 > T.shd3)) m = m + 1;
-    double d4 = dist_now(S, j, ncim1, tfalse);
-    if ((ncim1 != k) && (d4 > T.shd4)) m = m + 1;
-    return m == 3 ? 10.0 : 11.0;
-}
-__device__ double check_sigma(const DSys &S, int i, int j, double tfalse) {
-    double vxa = S.vx[i] - S.vx[j], vya = S.vy[i] - S.vy[j], vza = S.vz[i] - S.vz[j];
-    double rx = S.x[i] - S.x[j] + vxa * tfalse, ry = S.y[i] - S.y[j] + vya * tfalse, rz = S.z[i] - S.z[j] + vza * tfalse;
-    rx = rx - d_nint(rx); ry = ry - d_nint(ry); rz = rz - d_nint(rz);
-    double rijsq = rx * rx + ry * ry + rz * rz;
-    double diff = rijsq - S.tab->sigma_sq[S.ident[i]][S.ident[j]];
-    return diff < 0.0 ? 10.0 : 11.0;
-}
-__device__ void bump_in(const DSys &S, int i, int j, const Rel &r, double bd) {
-    S.x[i] = S.x[i] - bd * r.rx; S.y[i] = S.y[i] - bd * r.ry; S.z[i] = S.z[i] - bd * r.rz;
-    S.x[j] = S.x[j] + bd * r.rx; S.y[j] = S.y[j] + bd * r.ry; S.z[j] = S.z[j] + bd * r.rz;
-}
-__device__ void bump_out(const DSys &S, int i, int j, const Rel &r, double bd) {
-    S.x[i] = S.x[i] + bd * r.rx; S.y[i] = S.y[i] + bd * r.ry; S.z[i] = S.z[i] + bd * r.rz;
-    S.x[j] = S.x[j] - bd * r.rx; S.y[j] = S.y[j] - bd * r.ry; S.z[j] = S.z[j] - bd * r.rz;
-}
-__device__ int eventdyn(const DSys &S, int i, int j, int evcode, int ct, double tfalse) {
-    const DTab &T = *S.tab;
-    Rel r = d_rel(S, i, j, tfalse);
-    double bij = r.bij;
-    double bmi = S.bm[i], bmj = S.bm[j];
-    double rmass = 2 * bmi * bmj / (bmi + bmj);
-    int a = S.ident[i], b = S.ident[j];
-    double ratio = 0.0;
-    if (ct == 2) {
-        double blmin, blmax; bond_limits(S, i, evcode, blmin, blmax);
-        ratio = rmass * bij / (blmin * blmin);
-    } else if (ct == 3) {
-        double blmin, blmax; bond_limits(S, i, evcode, blmin, blmax);
-        ratio = rmass * bij / (blmax * blmax);
-    } else if (ct == 1) {
-        double sigsq;
-        if (evcode == 15) {
-            if (S.bptnr[i] == j) { double p = T.evp1[evcode]; sigsq = T.sigma_sq[a][b] * (p * p); }
-            else sigsq = T.sigma_sq[a][b];
-        } else {
-            double p = T.evp1[evcode];
-            sigsq = T.sigma_sq[a][b] * (p * p);
-            if (evcode >= 22 && evcode <= 26) {
-                int k = a > b ? a : b;
-                double s = T.sqz610[evcode - 21][k];
-                sigsq = sigsq * (s * s);
-            }
-        }
-        ratio = rmass * bij / sigsq;
-    } else if (ct == 4) {
-        double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
-        double del_pe = 4.0 * wellsq * epsave / rmass;
-        double bd = DMD_SMDIST * sqrt(wellsq);
-        if (bij * bij + del_pe > 0.0) {
-            ratio = rmass * (sqrt((4.0 * wellsq * epsave / rmass) + bij * bij) + bij) / (2.0 * wellsq);
-            ct = 20; bump_in(S, i, j, r, bd);
-        } else {
-            ratio = rmass * bij / wellsq;
-            ct = 22; bump_out(S, i, j, r, bd);
-        }
-    } else if (ct == 8) {
-        double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
-        double del_pe = 4.0 * wellsq * epsave / rmass;
-        double bd = DMD_SMDIST * sqrt(wellsq);
-        if (bij * bij > del_pe) {
-            ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
-            ct = 21; bump_out(S, i, j, r, bd);
-        } else {
-            ratio = rmass * bij / wellsq;
-            ct = 22; bump_in(S, i, j, r, bd);
-        }
-    } else if (ct == 9) {
-        double wellsq = T.welldia_sq[a][b];
-        ratio = rmass * bij / wellsq;
-        ct = 23; bump_out(S, i, j, r, DMD_SMDIST * sqrt(wellsq));
-    } else if (ct == 5) {
-        double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
-        double del_pe = 4.0 * wellsq * epsave / rmass;
-        double bd = DMD_SMDIST * sqrt(wellsq);
-        ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
-        ct = 24; bump_out(S, i, j, r, bd);
-    } else if (ct == 6) {
-        double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
-        double del_pe = 4.0 * wellsq * epsave / rmass;
-        double bd = DMD_SMDIST * sqrt(wellsq);
-        if (bij * bij > -del_pe) {
-            ratio = rmass * (sqrt(del_pe + bij * bij) + bij) / (2.0 * wellsq);
-            ct = 25; bump_in(S, i, j, r, bd);
-        } else {
-            ratio = rmass * bij / wellsq;
-            ct = 26; bump_out(S, i, j, r, bd);
-        }
-    } else if (ct == 13) {
-        double wellsq = T.shlddia_sq[a][b];
-        ratio = rmass * bij / wellsq;
-        ct = 27; bump_out(S, i, j, r, DMD_SMDIST * sqrt(wellsq));
-    }
-    double delvx = ratio * r.rx, delvy = ratio * r.ry, delvz = ratio * r.rz;
-    S.vx[i] = S.vx[i] - delvx / bmi; S.vx[j] = S.vx[j] + delvx / bmj;
-    S.vy[i] = S.vy[i] - delvy / bmi; S.vy[j] = S.vy[j] + delvy / bmj;
-    S.vz[i] = S.vz[i] - delvz / bmi; S.vz[j] = S.vz[j] + delvz / bmj;
-    S.x[i] = S.x[i] + delvx * tfalse / bmi;
-    S.y[i] = S.y[i] + delvy * tfalse / bmi;
-    S.z[i] = S.z[i] + delvz * tfalse / bmi;
-    S.x[j] = S.x[j] - delvx * tfalse / bmj;
-    S.y[j] = S.y[j] - delvy * tfalse / bmj;
-    S.z[j] = S.z[j] - delvz * tfalse / bmj;
-    return ct;
-}
-__device__ void bumpoff(const DSys &S, int i, int j, int evcode, double tfalse) {
-    Rel r = d_rel(S, i, j, tfalse);
-    const DTab &T = *S.tab;
-    double bd = (evcode >= 40) ? DMD_SMDIST * sqrt(T.shlddia_sq[S.ident[i]][S.ident[j]])
-                               : DMD_SMDIST * sqrt(T.welldia_sq[S.ident[i]][S.ident[j]]);
-    if (r.bij < 0.0) bump_in(S, i, j, r, bd); else bump_out(S, i, j, r, bd);
+struct WRel { double rx, ry, rz, bij, rijsq, vijsq; };
+
+/* relative position at tfalse with the minimum image, and the products of
+ * code/core.f:14-26 (sums kept in the reference's left-to-right order) */
+__device__ WRel warp_rel(const DSys &S, int i, int j, double tf) {
+    int lane = threadIdx.x & 31;
+    int d = lane % 3;
+    const double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+    const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+    double v = V[i] - V[j];
+    double r = P[i] - P[j] + v * tf;
+    r = r - d_nint(r);
+    double pb = r * v, pr = r * r, pv = v * v;
+    WRel w;
+    w.rx = __shfl_sync(FULL, r, 0); w.ry = __shfl_sync(FULL, r, 1); w.rz = __shfl_sync(FULL, r, 2);
+    double b0 = __shfl_sync(FULL, pb, 0), b1 = __shfl_sync(FULL, pb, 1), b2 = __shfl_sync(FULL, pb, 2);
+    double r0 = __shfl_sync(FULL, pr, 0), r1 = __shfl_sync(FULL, pr, 1), r2 = __shfl_sync(FULL, pr, 2);
+    double v0 = __shfl_sync(FULL, pv, 0), v1 = __shfl_sync(FULL, pv, 1), v2 = __shfl_sync(FULL, pv, 2);
+    /* three independent sums on three lanes, then broadcast */
+    double s = lane == 0 ? b0 + b1 + b2 : (lane == 1 ? r0 + r1 + r2 : v0 + v1 + v2);
+    w.bij = __shfl_sync(FULL, s, 0);
+    w.rijsq = __shfl_sync(FULL, s, 1);
+    w.vijsq = __shfl_sync(FULL, s, 2);
+    return w;
 }
 
-/* one lane: worker block (code/main.F90:1432-1956) and master application
- * (code/main.F90:646-943) of the pair event (i, j); returns the final
- * coltype and whether the shoulder links must be cleared afterwards */
-__device__ int lane_pair_event(const DSys &S, SharedState &sh, int i, int j, long long coll, double tfalse,
-                               int hbonds, int &xpulse_del, int &evcode_out) {
+/* four distances at tfalse (code/repuls_check.f), pair q on lanes 3q..3q+2 */
+__device__ void warp_dist4(const DSys &S, const int *a, const int *b, double tf, double *dout) {
+    int lane = threadIdx.x & 31;
+    int q = lane / 3 < 4 ? lane / 3 : 3, d = lane % 3;
+    int ia = a[q], ib = b[q];
+    const double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+    const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+    double v = V[ia] - V[ib];
+    double r = P[ia] - P[ib] + v * tf;
+    r = r - d_nint(r);
+    double p = r * r;
+    double c0 = __shfl_sync(FULL, p, 3 * (lane & 3));
+    double c1 = __shfl_sync(FULL, p, 3 * (lane & 3) + 1);
+    double c2 = __shfl_sync(FULL, p, 3 * (lane & 3) + 2);
+    double dd = c0 + c1 + c2;
+    double dist = sqrt(dd);
+    for (int k = 0; k < 4; ++k) dout[k] = __shfl_sync(FULL, dist, k);
+}
+
+/* the per-component tail of code/eventdyn.f:357-381 after the bumpdist push:
+ * lanes 0..5 = (bead i/j) x (x,y,z) */
+__device__ void warp_impulse(const DSys &S, int i, int j, const WRel &w, double ratio, double bd, int bump,
+                             double tf) {
+    int lane = threadIdx.x & 31;
+    if (lane < 6) {
+        int d = lane % 3;
+        bool isj = lane >= 3;
+        int b = isj ? j : i;
+        double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+        double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+        double r = d == 0 ? w.rx : (d == 1 ? w.ry : w.rz);
+        double p = P[b];
+        /* bump = -1: pair pushed together (i - bd*r, j + bd*r); +1: apart; 0: none */
+        if (bump != 0) {
+            bool minus = (bump < 0) != isj;
+            p = minus ? p - bd * r : p + bd * r;
+        }
+        double bmb = S.bm[b];
+        double delv = ratio * r;
+        V[b] = isj ? V[b] + delv / bmb : V[b] - delv / bmb;
+        p = isj ? p - delv * tf / bmb : p + delv * tf / bmb;
+        P[b] = p;
+    }
+    __syncwarp();
+}
+__device__ void warp_bump_only(const DSys &S, int i, int j, const WRel &w, double bd, int bump) {
+    int lane = threadIdx.x & 31;
+    if (lane < 6) {
+        int d = lane % 3;
+        bool isj = lane >= 3;
+        int b = isj ? j : i;
+        double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+        double r = d == 0 ? w.rx : (d == 1 ? w.ry : w.rz);
+        bool minus = (bump < 0) != isj;
+        double p = P[b];
+        P[b] = minus ? p - bd * r : p + bd * r;
+    }
+    __syncwarp();
+}
+
+/* code/eventdyn.f:4-385: ratio on lane 0, the six component updates on lanes 0..5 */
+__device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, double tf) {
+    int lane = threadIdx.x & 31;
+    const DTab &T = *S.tab;
+    WRel w = warp_rel(S, i, j, tf);
+    double ratio = 0.0, bd = 0.0;
+    int bump = 0;
+    if (lane == 0) {
+        double bij = w.bij;
+        double bmi = S.bm[i], bmj = S.bm[j];
+        double rmass = 2 * bmi * bmj / (bmi + bmj);
+        int a = S.ident[i], b = S.ident[j];
+        if (ct == 2) {
+            double blmin, blmax; bond_limits(S, i, evcode, blmin, blmax);
+            ratio = rmass * bij / (blmin * blmin);
+        } else if (ct == 3) {
+            double blmin, blmax; bond_limits(S, i, evcode, blmin, blmax);
+            ratio = rmass * bij / (blmax * blmax);
+        } else if (ct == 1) {
+            double sigsq;
+            if (evcode == 15) {
+                if (S.bptnr[i] == j) { double p = T.evp1[evcode]; sigsq = T.sigma_sq[a][b] * (p * p); }
+                else sigsq = T.sigma_sq[a][b];
+            } else {
+                double p = T.evp1[evcode];
+                sigsq = T.sigma_sq[a][b] * (p * p);
+                if (evcode >= 22 && evcode <= 26) {
+                    int k = a > b ? a : b;
+                    double s = T.sqz610[evcode - 21][k];
+                    sigsq = sigsq * (s * s);
+                }
+            }
+            ratio = rmass * bij / sigsq;
+        } else if (ct == 4) {
+            double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
+            double del_pe = 4.0 * wellsq * epsave / rmass;
+            bd = DMD_SMDIST * sqrt(wellsq);
+            if (bij * bij + del_pe > 0.0) {
+                ratio = rmass * (sqrt((4.0 * wellsq * epsave / rmass) + bij * bij) + bij) / (2.0 * wellsq);
+                ct = 20; bump = -1;
+            } else {
+                ratio = rmass * bij / wellsq;
+                ct = 22; bump = 1;
+            }
+        } else if (ct == 8) {
+            double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
+            double del_pe = 4.0 * wellsq * epsave / rmass;
+            bd = DMD_SMDIST * sqrt(wellsq);
+            if (bij * bij > del_pe) {
+                ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
+                ct = 21; bump = 1;
+            } else {
+                ratio = rmass * bij / wellsq;
+                ct = 22; bump = -1;
+            }
+        } else if (ct == 9) {
+            double wellsq = T.welldia_sq[a][b];
+            ratio = rmass * bij / wellsq;
+            ct = 23; bump = 1; bd = DMD_SMDIST * sqrt(wellsq);
+        } else if (ct == 5) {
+            double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
+            double del_pe = 4.0 * wellsq * epsave / rmass;
+            bd = DMD_SMDIST * sqrt(wellsq);
+            ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
+            ct = 24; bump = 1;
+        } else if (ct == 6) {
+            double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
+            double del_pe = 4.0 * wellsq * epsave / rmass;
+            bd = DMD_SMDIST * sqrt(wellsq);
+            if (bij * bij > -del_pe) {
+                ratio = rmass * (sqrt(del_pe + bij * bij) + bij) / (2.0 * wellsq);
+                ct = 25; bump = -1;
+            } else {
+                ratio = rmass * bij / wellsq;
+                ct = 26; bump = 1;
+            }
+        } else if (ct == 13) {
+            double wellsq = T.shlddia_sq[a][b];
+            ratio = rmass * bij / wellsq;
+            ct = 27; bump = 1; bd = DMD_SMDIST * sqrt(wellsq);
+        }
+    }
+    ratio = __shfl_sync(FULL, ratio, 0);
+    bd = __shfl_sync(FULL, bd, 0);
+    bump = __shfl_sync(FULL, bump, 0);
+    ct = __shfl_sync(FULL, ct, 0);
+    warp_impulse(S, i, j, w, ratio, bd, bump, tf);
+    return ct;
+}
+/* code/bumped.f:1-47 */
+__device__ void warp_bumpoff(const DSys &S, int i, int j, int evcode, double tf) {
+    WRel w = warp_rel(S, i, j, tf);
+    const DTab &T = *S.tab;
+    int a = S.ident[i], b = S.ident[j];
+    double bd = (evcode >= 40) ? DMD_SMDIST * sqrt(T.shlddia_sq[a][b]) : DMD_SMDIST * sqrt(T.welldia_sq[a][b]);
+    warp_bump_only(S, i, j, w, bd, w.bij < 0.0 ? -1 : 1);
+}
+__device__ double warp_check_sigma(const DSys &S, int i, int j, double tf) {  /* code/check_sigma.f */
+    WRel w = warp_rel(S, i, j, tf);
+    double diff = w.rijsq - S.tab->sigma_sq[S.ident[i]][S.ident[j]];
+    return diff < 0.0 ? 10.0 : 11.0;
+}
+
+/* ------------------------------------------------------------------ */
+/* one event on one warp                                               */
+/* ------------------------------------------------------------------ */
+/* snapshot of everything the collision of (i, j) may write */
+__device__ void warp_snapshot(const DSys &S, WarpArea &W, int i, int j) {
+    int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        int n = 0;
+        auto add = [&](int b) { if (b >= 0 && n < META_MAX) W.mb[n++] = b; };
+        add(i); add(j);
+        for (int k = 0; k < 4; ++k) { add(S.er[4 * i + k]); add(S.er[4 * j + k]); }
+        int h1, h2;
+        own_helpers(S, i, h1, h2); add(h1); add(h2);
+        own_helpers(S, j, h1, h2); add(h1); add(h2);
+        W.nmeta = n;
+        W.colt_i = S.colt[i];
+    }
+    __syncwarp();
+    for (int q = lane; q < W.nmeta; q += 32) {
+        int b = W.mb[q];
+        W.mident[q] = S.ident[b];
+        W.mbp[q] = S.bptnr[b];
+        for (int k = 0; k < 4; ++k) { W.mer[q][k] = S.er[4 * b + k]; W.movp[q][k] = S.ovp[4 * b + k]; W.movc[q][k] = S.ovc[4 * b + k]; }
+    }
+    if (lane < 12) {
+        int b = lane < 6 ? i : j, f = lane % 6;
+        const double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
+        W.sij[lane] = A[b];
+    }
+    __syncwarp();
+}
+__device__ void warp_restore(const DSys &S, WarpArea &W) {
+    int lane = threadIdx.x & 31;
+    /* entries naming the same bead hold the same values, so order does not matter */
+    for (int q = lane; q < W.nmeta; q += 32) {
+        int b = W.mb[q];
+        S.ident[b] = W.mident[q];
+        S.bptnr[b] = W.mbp[q];
+        for (int k = 0; k < 4; ++k) { S.er[4 * b + k] = W.mer[q][k]; S.ovp[4 * b + k] = W.movp[q][k]; S.ovc[4 * b + k] = W.movc[q][k]; }
+    }
+    if (lane < 12) {
+        int b = lane < 6 ? W.i : W.j, f = lane % 6;
+        double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
+        A[b] = W.sij[lane];
+    }
+    if (lane == 0) S.colt[W.i] = W.colt_i;
+    __syncwarp();
+}
+
+/* worker block (code/main.F90:1432-1956) and master application
+ * (code/main.F90:646-943) of the pair event (i, j), warp-wide */
+__device__ void warp_collision(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, long long coll,
+                               int hbonds) {
+    int lane = threadIdx.x & 31;
     int8_t *id = S.ident;
     int *er = S.er;
     int ct = S.colt[i];
     int evcode = pair_code(S, i, j, hbonds);
-    evcode_out = evcode;
     bool nonend = !S.info[i].is_end && !S.info[j].is_end;
-    xpulse_del = 0;
+    int xpulse = 0;
     int nb = id[i] < id[j] ? i : j;
     int cb = id[i] < id[j] ? j : i;
+    int err = 0;
     if (ct == 7) {
         if (er[4 * i + 3] < 0 && er[4 * j + 3] < 0) {
             if (nonend) {
-                ct = repuls_check(S, nb, cb, tfalse) <= 10.0 ? 4 : 14;
+                int ncim1, ncai, ncaj, nnjp1;
+                helpers_of(S, nb, cb, ncim1, ncai, ncaj, nnjp1);
+                int a[4] = {nb, nb, cb, cb}, b[4] = {ncaj, nnjp1, ncai, ncim1};
+                double d[4];
+                warp_dist4(S, a, b, tf, d);
+                const DTab &T = *S.tab;
+                double rating = ((d[0] > T.shd1) && (d[1] > T.shd2) && (d[2] > T.shd3) && (d[3] > T.shd4)) ? 10.0 : 11.0;
+                ct = rating <= 10.0 ? 4 : 14;
             } else {
                 double ran_non = dmd_uniform(S.seed, DMD_STREAM_CAPTURE, (uint64_t)coll, 0);
                 ct = ran_non <= 0.2 ? 4 : 9;
@@ -484,85 +519,83 @@ __device__ int lane_pair_event(const DSys &S, SharedState &sh, int i, int j, lon
         } else {
             ct = 9;
         }
-    } else if (ct == 10) {
-        double rating;
-        int hbchk = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
-        if (hbchk < 0) { set_err(sh, DMD_E_STATE, i); return ct; }
-        if (evcode < 45) {
-            int hb = er[4 * i + 3];
-            rating = id[i] < id[hb] ? repuls_check_3(S, i, hb, j, tfalse) : repuls_check_3(S, hb, i, j, tfalse);
+    } else if (ct == 10 || ct == 12) {
+        int hb = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
+        if (hb < 0) err = 1;
+        else if (ct == 10) {
+            /* code/repuls_check_3.f with (n, c, k) */
+            int x = evcode < 45 ? i : j, k = evcode < 45 ? j : i;
+            int n = id[x] < id[hb] ? x : hb, c = id[x] < id[hb] ? hb : x;
+            int ncim1, ncai, ncaj, nnjp1;
+            helpers_of(S, n, c, ncim1, ncai, ncaj, nnjp1);
+            int a[4] = {n, n, c, c}, b[4] = {ncaj, nnjp1, ncai, ncim1};
+            double d[4];
+            warp_dist4(S, a, b, tf, d);
+            const DTab &T = *S.tab;
+            int m = 0;
+            if ((ncaj != k) && (d[0] > T.shd1)) m = m + 1;
+            if ((nnjp1 != k) && (d[1] > T.shd2)) m = m + 1;
+            if ((ncai != k) && (d[2] > T.shd3)) m = m + 1;
+            if ((ncim1 != k) && (d[3] > T.shd4)) m = m + 1;
+            ct = (m == 3 ? 10.0 : 11.0) <= 10.0 ? 5 : 15;
         } else {
-            int hb = er[4 * j + 3];
-            rating = id[j] < id[hb] ? repuls_check_3(S, j, hb, i, tfalse) : repuls_check_3(S, hb, j, i, tfalse);
-        }
-        ct = rating <= 10.0 ? 5 : 15;
-    } else if (ct == 12) {
-        int hbchk = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
-        if (hbchk < 0) { set_err(sh, DMD_E_STATE, i); return ct; }
-        if (evcode < 45) {
-            int hb = er[4 * i + 3];
-            if (S.bptnr[i] == hb) ct = check_sigma(S, i, hb, tfalse) > 10.0 ? 6 : 13; else ct = 15;
-        } else {
-            int hb = er[4 * j + 3];
-            if (S.bptnr[j] == hb) ct = check_sigma(S, j, hb, tfalse) > 10.0 ? 6 : 13; else ct = 15;
+            int x = evcode < 45 ? i : j;
+            if (S.bptnr[x] == hb) ct = warp_check_sigma(S, x, hb, tf) > 10.0 ? 6 : 13;
+            else ct = 15;
         }
     }
-    if (ct < 14) ct = eventdyn(S, i, j, evcode, ct, tfalse);
-    if (ct == 24 || ct == 25) {
-        int hbchk = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
-        if (hbchk < 0) { set_err(sh, DMD_E_STATE, i); return ct; }
+    if (err) {
+        if (lane == 0) { set_err(E, DMD_E_STATE, i); W.ct = ct; W.evcode = evcode; W.xpulse = 0; }
+        __syncwarp();
+        return;
     }
-    if (ct == 20) {
-        if (id[i] + id[j] == 5) {
-            S.bptnr[i] = j; S.bptnr[j] = i;
-            id[i] = id[i] + 4; id[j] = id[j] + 4;
-            if (nonend) { if (id[i] < id[j]) repuls_add(S, sh, i, j, hbonds); else repuls_add(S, sh, j, i, hbonds); }
-        }
-    } else if (ct == 21) {
-        if (id[i] <= 8) {
+    if (ct < 14) ct = warp_eventdyn(S, i, j, evcode, ct, tf);
+    if ((ct == 24 || ct == 25) && (evcode < 45 ? er[4 * i + 3] : er[4 * j + 3]) < 0) {
+        if (lane == 0) { set_err(E, DMD_E_STATE, i); W.ct = ct; W.evcode = evcode; W.xpulse = 0; }
+        __syncwarp();
+        return;
+    }
+    if (ct == 14 || ct == 15 || ct == 16) warp_bumpoff(S, i, j, evcode, tf);
+    if (lane == 0) {
+        if (ct == 20) {
+            if (id[i] + id[j] == 5) {
+                S.bptnr[i] = j; S.bptnr[j] = i;
+                id[i] = id[i] + 4; id[j] = id[j] + 4;
+                if (nonend) { if (id[i] < id[j]) repuls_add(S, E, i, j, hbonds); else repuls_add(S, E, j, i, hbonds); }
+            }
+        } else if (ct == 21) {
+            if (id[i] <= 8) {
+                if (nonend) {
+                    xpulse = 1;
+                    if (id[i] < id[j]) shoulders_off(S, E, i, j, hbonds); else shoulders_off(S, E, j, i, hbonds);
+                }
+                if (S.bptnr[i] == j) {
+                    S.bptnr[i] = -1; S.bptnr[j] = -1;
+                    id[i] = id[i] - 4; id[j] = id[j] - 4;
+                }
+            }
+        } else if (ct == 24) {
+            int x = evcode < 45 ? i : j, hb = er[4 * x + 3];
+            if (id[x] + id[hb] == 5) { S.bptnr[x] = hb; S.bptnr[hb] = x; id[x] += 4; id[hb] += 4; }
+        } else if (ct == 25) {
+            int x = evcode < 45 ? i : j, hb = er[4 * x + 3];
+            if (id[x] >= 5) { S.bptnr[x] = -1; S.bptnr[hb] = -1; id[x] -= 4; id[hb] -= 4; }
+        } else if (ct == 14) {
+            if (nonend) { if (id[i] < id[j]) repuls_add(S, E, i, j, hbonds); else repuls_add(S, E, j, i, hbonds); }
+        } else if (ct == 16) {
             if (nonend) {
-                xpulse_del = 1;
-                if (id[i] < id[j]) shoulders_off(S, sh, i, j, hbonds); else shoulders_off(S, sh, j, i, hbonds);
-            }
-            if (S.bptnr[i] == j) {
-                S.bptnr[i] = -1; S.bptnr[j] = -1;
-                id[i] = id[i] - 4; id[j] = id[j] - 4;
+                xpulse = 1;
+                if (id[i] < id[j]) shoulders_off(S, E, i, j, hbonds); else shoulders_off(S, E, j, i, hbonds);
             }
         }
-    } else if (ct == 24) {
-        if (evcode < 45) {
-            int hb = er[4 * i + 3];
-            if (id[i] + id[hb] == 5) { S.bptnr[i] = hb; S.bptnr[hb] = i; id[i] += 4; id[hb] += 4; }
-        } else {
-            int hb = er[4 * j + 3];
-            if (id[j] + id[hb] == 5) { S.bptnr[j] = hb; S.bptnr[hb] = j; id[j] += 4; id[hb] += 4; }
-        }
-    } else if (ct == 25) {
-        if (evcode < 45) {
-            int hb = er[4 * i + 3];
-            if (id[i] >= 5) { S.bptnr[i] = -1; S.bptnr[hb] = -1; id[i] -= 4; id[hb] -= 4; }
-        } else {
-            int hb = er[4 * j + 3];
-            if (id[j] >= 5) { S.bptnr[j] = -1; S.bptnr[hb] = -1; id[j] -= 4; id[hb] -= 4; }
-        }
-    } else if (ct == 14) {
-        bumpoff(S, i, j, evcode, tfalse);
-        if (nonend) { if (id[i] < id[j]) repuls_add(S, sh, i, j, hbonds); else repuls_add(S, sh, j, i, hbonds); }
-    } else if (ct == 15) {
-        bumpoff(S, i, j, evcode, tfalse);
-    } else if (ct == 16) {
-        bumpoff(S, i, j, evcode, tfalse);
-        if (nonend) {
-            xpulse_del = 1;
-            if (id[i] < id[j]) shoulders_off(S, sh, i, j, hbonds); else shoulders_off(S, sh, j, i, hbonds);
-        }
+        S.colt[i] = (int8_t)ct;
+        W.ct = ct; W.evcode = evcode; W.xpulse = xpulse;
     }
-    S.colt[i] = (int8_t)ct;
-    return ct;
+    __syncwarp();
 }
 
-/* one lane: Andersen ghost collision (code/main.F90:997-1121) up to the
- * re-prediction; returns the bead */
+/* Andersen ghost collision (code/main.F90:997-1121) up to the re-prediction;
+ * lane 0, returns the bead and the (possibly clamped) event time */
 __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
     const DTab &T = *S.tab;
     long long g = sh.sc.ghost_index++;
@@ -594,19 +627,316 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
     S.x[i] = S.x[i] - S.vx[i] * tfalse; S.y[i] = S.y[i] - S.vy[i] * tfalse; S.z[i] = S.z[i] - S.vz[i] * tfalse;
     double tgho = 0.0;
     while (((tgho < 1e-18) || (tgho == 1.0)) && k < 12288) tgho = dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++);
-    if (i > N || r == 0.0 || r >= 1.0 || tgho < 1e-18) set_err(sh, DMD_E_STATE, -1);
+    if (r == 0.0 || r >= 1.0 || tgho < 1e-18) set_err(sh, DMD_E_STATE, -1);
     double tn = -1.0 * dmd_log(tgho) * T.avegtime + tfalse;
-    S.tim[N] = tn;
-    S.queued[N] = tn < sh.sc.interval_max;
+    set_pred(S, N, tn, -2, -2, tn < sh.sc.interval_max);
     if (tfalse < sh.sc.old_tfalse) tfalse = sh.sc.old_tfalse;
     return i;
 }
 
 /* ------------------------------------------------------------------ */
-/* CTA-wide: block reductions                                          */
+/* re-prediction into the warp's buffer (code/partial_events.f)         */
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ bool check_tij(Err E, double tij, int i) {
+    /* reference debug check: negative time beyond 1e-10 (code/eventredo_up.f:58-74) */
+    if (tij < 0.0 && fabs(tij) > 1.0e-10) { set_err(E, DMD_E_NEG_TIME, i); return false; }
+    return true;
+}
+
+/* warp: full re-prediction of bead l (the pass of partial_events.f:16-35) */
+__device__ void warp_redo_full(const DSys &S, Err E, int l, double tf, double imax, int hbonds,
+                               double &t_out, int &p_out, int &y_out, bool &q_out) {
+    int lane = threadIdx.x & 31;
+    double H = imax + DMD_LTSTEP - tf;
+    long long bk = okey(H);
+    double bt = H;
+    int bp = -1, by = -1;
+    int n = S.upn[l];
+    const int *up = S.up + (size_t)l * S.cap;
+    for (int k = lane; k < n + 3; k += 32) {
+        int m = k < n ? up[k] : S.er[4 * l + (k - n)];
+        if (m <= l) continue;
+        double tij; int ty;
+        if (!d_predict(S, l, m, pair_code(S, m, l, hbonds), tf, tij, ty)) { set_err(E, DMD_E_INPUT, l); continue; }
+        check_tij(E, tij, l);
+        long long kk = okey(tij);
+        if (key_less(kk, m, bk, bp)) { bk = kk; bp = m; bt = tij; by = ty; }
+    }
+    warp_keymin(bk, bp, bt, by);
+    double tn = bt + tf;
+    t_out = tn; p_out = bp; y_out = by; q_out = tn < imax;
+}
+
+/* eventredo_down(l, src) on one lane against the running (t, p, y, q) of l */
+__device__ __forceinline__ void lane_redo_down(const DSys &S, Err E, int l, int src, double tf, double imax,
+                                               int hbonds, double &t, int &p, int &y, bool &q) {
+    double tij; int ty;
+    if (!d_predict(S, l, src, pair_code(S, l, src, hbonds), tf, tij, ty)) { set_err(E, DMD_E_INPUT, l); return; }
+    check_tij(E, tij, l);
+    tij = tij + tf;
+    if (key_less(okey(tij), src, okey(t), p)) { t = tij; p = src; y = ty; q = tij < imax; }
+}
+
+/* warp: partial_events(i, j) (j = -1 after a ghost) into W's buffer */
+__device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, double imax,
+                               int hbonds) {
+    int lane = threadIdx.x & 31;
+    /* 1. the down-list operations in the reference's order */
+    int n = 0;
+    {
+        int cnt = S.dnn[i];
+        const int *dn = S.dn + (size_t)i * S.cap;
+        for (int q = lane; q < cnt; q += 32) { W.ops_l[q] = dn[q]; W.ops_s[q] = i; }
+        n = cnt;
+        if (lane == 0)
+            for (int k = 0; k < 3; ++k) {
+                int l = S.er[4 * i + k];
+                if (l >= 0 && l < i) { W.ops_l[n] = l; W.ops_s[n] = i; ++n; }
+            }
+        n = __shfl_sync(FULL, n, 0);
+        if (j >= 0) {
+            int cj = S.dnn[j];
+            const int *dj = S.dn + (size_t)j * S.cap;
+            for (int base = 0; base < cj; base += 32) {
+                int q = base + lane;
+                int l = q < cj ? dj[q] : -1;
+                bool keep = q < cj && l != i;
+                unsigned m = __ballot_sync(FULL, keep);
+                int pos = n + __popc(m & ((1u << lane) - 1));
+                if (keep) { W.ops_l[pos] = l; W.ops_s[pos] = j; }
+                n += __popc(m);
+            }
+            if (lane == 0)
+                for (int k = 0; k < 3; ++k) {
+                    int l = S.er[4 * j + k];
+                    if (l >= 0 && l < j) { W.ops_l[n] = l; W.ops_s[n] = j; ++n; }
+                }
+            n = __shfl_sync(FULL, n, 0);
+        }
+    }
+    __syncwarp();
+    /* 2. distinct beads (leaders) with their first operation */
+    int nl = 0;
+    for (int base = 0; base < n; base += 32) {
+        int q = base + lane;
+        bool lead = false;
+        if (q < n) {
+            int l = W.ops_l[q];
+            lead = true;
+            for (int p = 0; p < q; ++p) if (W.ops_l[p] == l) { lead = false; break; }
+        }
+        unsigned m = __ballot_sync(FULL, lead);
+        int pos = nl + __popc(m & ((1u << lane) - 1));
+        if (lead) { W.lead_l[pos] = W.ops_l[q]; W.lead_q[pos] = q; }
+        nl += __popc(m);
+    }
+    if (lane == 0) { W.nredo = 0; W.nlead = nl; }
+    __syncwarp();
+    /* 3. one pass over: i's partners, j's partners, the leaders' operations */
+    int ni = S.upn[i] + 3, nj = j >= 0 ? S.upn[j] + 3 : 0;
+    double Hd = imax + DMD_LTSTEP - tf;
+    long long Hk = okey(Hd);
+    long long ki = Hk, kj = Hk;
+    double ti = Hd, tj = Hd;
+    int pi = -1, pj = -1, yi = -1, yj = -1;
+    const int *upi = S.up + (size_t)i * S.cap;
+    const int *upj = j >= 0 ? S.up + (size_t)j * S.cap : nullptr;
+    for (int q = lane; q < ni + nj + nl; q += 32) {
+        if (q < ni + nj) {
+            bool isj = q >= ni;
+            int x = isj ? j : i, k = isj ? q - ni : q, nx = isj ? nj - 3 : ni - 3;
+            int m = k < nx ? (isj ? upj[k] : upi[k]) : S.er[4 * x + (k - nx)];
+            if (m <= x) continue;
+            double tij; int ty;
+            if (!d_predict(S, x, m, pair_code(S, m, x, hbonds), tf, tij, ty)) { set_err(E, DMD_E_INPUT, x); continue; }
+            check_tij(E, tij, x);
+            long long kk = okey(tij);
+            if (isj) { if (key_less(kk, m, kj, pj)) { kj = kk; pj = m; tj = tij; yj = ty; } }
+            else { if (key_less(kk, m, ki, pi)) { ki = kk; pi = m; ti = tij; yi = ty; } }
+        } else {
+            int ld = q - ni - nj;
+            int l = W.lead_l[ld], q0 = W.lead_q[ld];
+            int slot = 2 + ld;
+            W.pb[slot] = l;
+            if (l == i) {   /* a j-extras operation on i waits for i's new prediction */
+                int r = atomicAdd(&W.nredo, 1);
+                if (r < REDO_MAX) { W.redo_l[r] = l; W.redo_p[r] = q0; W.redo_slot[r] = slot; }
+                else set_err(E, DMD_E_CAPACITY, l);
+                continue;
+            }
+            double t = S.tim[l];
+            int p = S.nptnr[l], y = S.colt[l];
+            bool qq = S.queued[l] != 0;
+            int stop = -1;
+            for (int pp = q0; pp < n; ++pp) {
+                if (W.ops_l[pp] != l) continue;
+                int src = W.ops_s[pp];
+                if (p == src) { stop = pp; break; }
+                lane_redo_down(S, E, l, src, tf, imax, hbonds, t, p, y, qq);
+            }
+            W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
+            if (stop >= 0) {
+                int r = atomicAdd(&W.nredo, 1);
+                if (r < REDO_MAX) { W.redo_l[r] = l; W.redo_p[r] = stop; W.redo_slot[r] = slot; }
+                else set_err(E, DMD_E_CAPACITY, l);
+            }
+        }
+    }
+    warp_keymin(ki, pi, ti, yi);
+    if (j >= 0) warp_keymin(kj, pj, tj, yj);
+    if (lane == 0) {
+        double tn = ti + tf;
+        W.pb[0] = i; W.pt[0] = tn; W.pn[0] = pi; W.pc[0] = (int8_t)yi; W.pq[0] = tn < imax;
+        if (j >= 0) {
+            double tn2 = tj + tf;
+            W.pb[1] = j; W.pt[1] = tn2; W.pn[1] = pj; W.pc[1] = (int8_t)yj; W.pq[1] = tn2 < imax;
+        } else {
+            W.pb[1] = -1;
+        }
+        W.npred = 2 + nl;
+    }
+    __syncwarp();
+    /* 4. operations that need a full re-prediction, in operation order per bead */
+    int nr = min(W.nredo, REDO_MAX);
+    for (int r = 0; r < nr; ++r) {
+        int l = W.redo_l[r], p0 = W.redo_p[r], slot = W.redo_slot[r];
+        double t; int p, y; bool qq;
+        if (l == i) { t = W.pt[0]; p = W.pn[0]; y = W.pc[0]; qq = W.pq[0] != 0; }
+        else { t = W.pt[slot]; p = W.pn[slot]; y = W.pc[slot]; qq = W.pq[slot] != 0; }
+        for (int pp = p0; pp < n; ++pp) {
+            if (W.ops_l[pp] != l) continue;
+            int src = W.ops_s[pp];
+            if (p == src) {
+                warp_redo_full(S, E, l, tf, imax, hbonds, t, p, y, qq);
+            } else {
+                double t2 = t; int p2 = p, y2 = y; bool q2 = qq;
+                if (lane == 0) lane_redo_down(S, E, l, src, tf, imax, hbonds, t2, p2, y2, q2);
+                t = __shfl_sync(FULL, t2, 0); p = __shfl_sync(FULL, p2, 0);
+                y = __shfl_sync(FULL, y2, 0); qq = __shfl_sync(FULL, (int)q2, 0) != 0;
+            }
+        }
+        if (lane == 0) {
+            if (l == i) { W.pb[slot] = -1; W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq; }
+            else { W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq; }
+        }
+        __syncwarp();
+    }
+    /* 5. the earliest new queued entry of this event */
+    long long bk = DMD_KEY_INF;
+    int bb = INT_MAX;
+    for (int q = lane; q < W.npred; q += 32) {
+        int b = W.pb[q];
+        if (b < 0 || !W.pq[q]) continue;
+        long long kk = okey(W.pt[q]);
+        if (key_less(kk, b, bk, bb)) { bk = kk; bb = b; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long k2 = __shfl_xor_sync(FULL, bk, o);
+        int b2 = __shfl_xor_sync(FULL, bb, o);
+        if (key_less(k2, b2, bk, bb)) { bk = k2; bb = b2; }
+    }
+    if (lane == 0) { W.tnew_key = bk; W.tnew_idx = bb; }
+    __syncwarp();
+}
+
+__device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
+    int lane = threadIdx.x & 31;
+    for (int q = lane; q < W.npred; q += 32) {
+        int b = W.pb[q];
+        if (b < 0) continue;
+        set_pred(S, b, W.pt[q], W.pn[q], W.pc[q], W.pq[q] != 0);
+    }
+    __syncwarp();
+}
+
+/* ------------------------------------------------------------------ */
+/* footprints of a batch candidate                                     */
+/* ------------------------------------------------------------------ */
+/* act 0: claim (atomicMin of the candidate index), 1: test for an earlier
+ * claim, 2: release.  The set covers every bead the event reads or writes
+ * in the serial order: i, j, their extra_repuls, their H-bond helpers and
+ * those of their H-bond partners, both neighbour lists of i and j, and for
+ * every bead that may need a full re-prediction its up list and extras. */
+__device__ bool warp_footprint(const DSys &S, WarpArea &W, int k, int i, int j, int act) {
+    int lane = threadIdx.x & 31;
+    bool conflict = false;
+    auto visit = [&](int b) {
+        if (b < 0) return;
+        if (act == 0) atomicMin(&S.owner[b], k);
+        else if (act == 1) { if (S.owner[b] < k) conflict = true; }
+        else S.owner[b] = INT_MAX;
+    };
+    /* fixed part: 18 entries on lanes 0..17 */
+    if (lane < 18) {
+        int b = -1;
+        if (lane == 0) b = i;
+        else if (lane == 1) b = j;
+        else if (lane < 6) b = S.er[4 * i + lane - 2];
+        else if (lane < 10) b = S.er[4 * j + lane - 6];
+        else {
+            int which = (lane - 10) >> 1;
+            int x = which == 0 ? i : which == 1 ? j : which == 2 ? S.er[4 * i + 3] : S.er[4 * j + 3];
+            int h1, h2;
+            own_helpers(S, x, h1, h2);
+            b = (lane & 1) ? h2 : h1;
+        }
+        visit(b);
+    }
+    /* neighbour lists of i and j */
+    int ui = S.upn[i], di = S.dnn[i], uj = S.upn[j], dj = S.dnn[j];
+    const int *UI = S.up + (size_t)i * S.cap, *DI = S.dn + (size_t)i * S.cap;
+    const int *UJ = S.up + (size_t)j * S.cap, *DJ = S.dn + (size_t)j * S.cap;
+    for (int q = lane; q < ui; q += 32) visit(UI[q]);
+    for (int q = lane; q < di; q += 32) visit(DI[q]);
+    for (int q = lane; q < uj; q += 32) visit(UJ[q]);
+    for (int q = lane; q < dj; q += 32) visit(DJ[q]);
+    /* beads that may be fully re-predicted (listed once, at the claim) */
+    if (act == 0) {
+        int nc = 0;
+        for (int base = 0; base < di + dj; base += 32) {
+            int q = base + lane;
+            int l = -1;
+            if (q < di) { l = DI[q]; if (S.nptnr[l] != i) l = -1; }
+            else if (q < di + dj) { l = DJ[q - di]; if (S.nptnr[l] != j) l = -1; }
+            unsigned m = __ballot_sync(FULL, l >= 0);
+            int pos = nc + __popc(m & ((1u << lane) - 1));
+            if (l >= 0 && pos < CASC_MAX - 14) W.casc[pos] = l;
+            nc += __popc(m);
+        }
+        if (lane == 0) W.casc_over = nc > CASC_MAX - 14;
+        nc = min(nc, CASC_MAX - 14);
+        if (lane < 14) {
+            int b = -1;
+            if (lane < 3) b = S.er[4 * i + lane];
+            else if (lane < 6) b = S.er[4 * j + lane - 3];
+            else if (lane < 10) {
+                int x = lane < 8 ? i : j, h1, h2;
+                own_helpers(S, x, h1, h2);
+                b = (lane & 1) ? h2 : h1;
+            }
+            W.casc[nc + lane] = b;
+        }
+        if (lane == 0) W.ncasc = nc + 14;
+        __syncwarp();
+    }
+    int nc = W.ncasc;
+    for (int c = 0; c < nc; ++c) {
+        int l = W.casc[c];
+        if (l < 0) continue;
+        int ul = S.upn[l];
+        const int *UL = S.up + (size_t)l * S.cap;
+        for (int q = lane; q < ul; q += 32) visit(UL[q]);
+        if (lane < 3) visit(S.er[4 * l + lane]);
+    }
+    return __any_sync(FULL, conflict);
+}
+
+/* ------------------------------------------------------------------ */
+/* CTA-wide reductions                                                 */
 /* ------------------------------------------------------------------ */
 __device__ double cta_max(SharedState &sh, double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
     int w = threadIdx.x >> 5;
     __syncthreads();
     if ((threadIdx.x & 31) == 0) sh.red_d[w] = v;
@@ -617,7 +947,7 @@ __device__ double cta_max(SharedState &sh, double v) {
     return r;
 }
 __device__ double cta_sum(SharedState &sh, double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
     int w = threadIdx.x >> 5;
     __syncthreads();
     if ((threadIdx.x & 31) == 0) sh.red_d[w] = v;
@@ -628,7 +958,7 @@ __device__ double cta_sum(SharedState &sh, double v) {
     return r;
 }
 __device__ int cta_sum_i(SharedState &sh, int v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
     int w = threadIdx.x >> 5;
     __syncthreads();
     if ((threadIdx.x & 31) == 0) sh.red_i[w] = v;
@@ -641,13 +971,14 @@ __device__ int cta_sum_i(SharedState &sh, int v) {
 
 /* ------------------------------------------------------------------ */
 /* CTA-wide: list rebuild and full prediction (code/nbor.f, code/events.f) */
+/* ------------------------------------------------------------------ */
 __device__ __forceinline__ int cell_coord(double p, int nc) {
     double c = (p + 0.5) * nc;
     if (!(c >= 0.0)) return 0;   /* also catches NaN */
     int k = (int)c;
     return k < nc ? k : nc - 1;
 }
-/* ------------------------------------------------------------------ */
+
 __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
     const int N = S.N, nc = S.ncell;
     const int ncell3 = nc * nc * nc;
@@ -660,7 +991,6 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             atomicAdd(&S.cell_count[(cz * nc + cy) * nc + cx], 1);
         }
         __syncthreads();
-        /* exclusive scan of the counts: each thread a contiguous chunk */
         {
             int per = (ncell3 + blockDim.x - 1) / blockDim.x;
             int lo = threadIdx.x * per, hi = min(lo + per, ncell3);
@@ -668,7 +998,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             for (int c = lo; c < hi; ++c) s += S.cell_count[c];
             int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
             int incl = s;
-            for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(0xffffffffu, incl, o); if (lane >= o) incl += v; }
+            for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
             __syncthreads();
             if (lane == 31) sh.red_i[w] = incl;
             __syncthreads();
@@ -739,30 +1069,27 @@ __device__ void cta_predict_all(const DSys &S, SharedState &sh, double interval_
     const int N = S.N;
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
         double bt = interval_max + DMD_LTSTEP;
+        long long bk = okey(bt);
         int bp = -1, by = -1;
         const int *up = S.up + (size_t)b * S.cap;
-        for (int k = 0; k < S.upn[b]; ++k) {
-            int m = up[k];
+        int nu = S.upn[b];
+        for (int k = 0; k < nu + 3; ++k) {
+            int m = k < nu ? up[k] : S.er[4 * b + (k - nu)];
+            if (m <= b) continue;
             double tij; int ty;
-            int code = pair_code(S, m, b, hbonds);
-            if (!d_predict(S, b, m, code, 0.0, tij, ty)) { set_err(sh, DMD_E_INPUT, code); continue; }
-            check_tij(sh, tij, b, m);
-            if (lex_less(tij, m, bt, bp)) { bt = tij; bp = m; by = ty; }
+            if (!d_predict(S, b, m, pair_code(S, m, b, hbonds), 0.0, tij, ty)) { set_err(sh, DMD_E_INPUT, b); continue; }
+            check_tij(cta_err(sh), tij, b);
+            long long kk = okey(tij);
+            if (key_less(kk, m, bk, bp)) { bk = kk; bt = tij; bp = m; by = ty; }
         }
-        for (int k = 0; k < 3; ++k) {
-            int m = S.er[4 * b + k];
-            if (m > b) {
-                double tij; int ty;
-                int code = pair_code(S, m, b, hbonds);
-                if (!d_predict(S, b, m, code, 0.0, tij, ty)) { set_err(sh, DMD_E_INPUT, code); continue; }
-                check_tij(sh, tij, b, m);
-                if (lex_less(tij, m, bt, bp)) { bt = tij; bp = m; by = ty; }
-            }
-        }
-        S.tim[b] = bt; S.nptnr[b] = bp; S.colt[b] = (int8_t)by;
-        S.queued[b] = bt < interval_max;
+        set_pred(S, b, bt, bp, by, bt < interval_max);
     }
-    if (threadIdx.x < 3) S.queued[N + threadIdx.x] = S.tim[N + threadIdx.x] < interval_max;
+    if (threadIdx.x < 3) {
+        int e = N + threadIdx.x;
+        bool q = S.tim[e] < interval_max;
+        S.queued[e] = q;
+        S.key[e] = q ? okey(S.tim[e]) : DMD_KEY_INF;
+    }
     __syncthreads();
 }
 
@@ -785,18 +1112,26 @@ __device__ bool cta_interval(const DSys &S, SharedState &sh, int hbonds) {
     double tf = sh.sc.tfalse;
     const DTab &T = *S.tab;
     __syncthreads();
-    for (int k = threadIdx.x; k < N + 3; k += blockDim.x) S.tim[k] = S.tim[k] - tf;
-    double moved_far = 0.0;
+    for (int k = threadIdx.x; k < N + 3; k += blockDim.x) {
+        double tn = S.tim[k] - tf;
+        S.tim[k] = tn;
+        S.key[k] = S.queued[k] ? okey(tn) : DMD_KEY_INF;
+    }
+    /* displ.f: the largest squared displacement over hdelr; dividing after
+     * the maximum gives the same value, division being monotone */
+    double dmax = 0.0;
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
         double px = S.x[k] + S.vx[k] * tf, py = S.y[k] + S.vy[k] * tf, pz = S.z[k] + S.vz[k] * tf;
         S.x[k] = px; S.y[k] = py; S.z[k] = pz;
         double a = S.ox[k] - px, b = S.oy[k] - py, c = S.oz[k] - pz;
         double dis = a * a + b * b + c * c;
-        double moved = dis / T.hdelr;
-        if (moved > moved_far) moved_far = moved;
+        if (dis > dmax) dmax = dis;
     }
-    moved_far = cta_max(sh, moved_far);
+    dmax = cta_max(sh, dmax);
     if (threadIdx.x == 0) {
+        double moved_far = 0.0;
+        double moved = dmax / T.hdelr;
+        if (moved > moved_far) moved_far = moved;
         sh.sc.t = sh.sc.t + tf;
         sh.sc.interval_max = sh.sc.interval_max - tf;
         sh.sc.tfalse = 0.0;
@@ -819,14 +1154,11 @@ __device__ bool cta_interval(const DSys &S, SharedState &sh, int hbonds) {
     __syncthreads();
     bool rb = sh.rebuild != 0;
     if (rb) {
-        for (int k = threadIdx.x; k < N; k += blockDim.x) { S.tim[k] = sh.sc.interval_max + DMD_LTSTEP; S.colt[k] = -1; S.nptnr[k] = -1; }
+        for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
         __syncthreads();
         cta_rebuild(S, sh, hbonds);
     }
-    if (threadIdx.x == 0) {
-        S.tim[N + 1] = sh.sc.interval * 0.999;
-        S.queued[N + 1] = 1;
-    }
+    if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
     __syncthreads();
     cta_tree_rebuild(S);
     return rb;
@@ -834,6 +1166,13 @@ __device__ bool cta_interval(const DSys &S, SharedState &sh, int hbonds) {
 
 /* diagnostics (code/energy.f:1-105, radgyr.f:1-139, end2end.f:1-48) over the
  * neighbour lists; done by the whole CTA */
+__device__ double dist_now(const DSys &S, int a, int b, double tfalse) {
+    double vxa = S.vx[a] - S.vx[b], vya = S.vy[a] - S.vy[b], vza = S.vz[a] - S.vz[b];
+    double rx = S.x[a] - S.x[b] + vxa * tfalse, ry = S.y[a] - S.y[b] + vya * tfalse, rz = S.z[a] - S.z[b] + vza * tfalse;
+    rx = rx - d_nint(rx); ry = ry - d_nint(ry); rz = rz - d_nint(rz);
+    double d = rx * rx + ry * ry + rz * rz;
+    return sqrt(d);
+}
 __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start, const int *chain_len,
                          dmd_diag *out) {
     const int N = S.N;
@@ -931,13 +1270,88 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
 }
 
 /* ------------------------------------------------------------------ */
+/* batch selection                                                     */
+/* ------------------------------------------------------------------ */
+/* The bead events below the cut, sorted in (key, index) order into
+ * sh.sort_*; returns how many there are (1 when the window could not be
+ * made small enough: the root alone). */
+__device__ int cta_candidates(const DSys &S, SharedState &sh, int root, long long kroot) {
+    const int N = S.N;
+    long long kp = min(min(S.key[N], S.key[N + 1]), S.key[N + 2]);
+    bool ok = false;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        if (threadIdx.x == 0) {
+            double tr = S.tim[root];
+            long long kc = okey(tr + sh.delta);
+            if (kc <= kroot) kc = kroot + 1;
+            if (kc > kp) kc = kp;
+            sh.kcut = kc;
+            sh.ncand = 0;
+            sh.ngroups = 0;
+        }
+        __syncthreads();
+        long long kc = sh.kcut;
+        /* groups whose minimum lies below the cut */
+        for (int g = threadIdx.x; g < S.nl1; g += blockDim.x) {
+            if (S.key[S.l1i[g]] < kc) {
+                int s = atomicAdd(&sh.ngroups, 1);
+                if (s < 256) sh.groups[s] = g;
+            }
+        }
+        __syncthreads();
+        int ng = sh.ngroups;
+        if (ng <= 256) {
+            int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            for (int gi = warp; gi < ng; gi += NWARPS) {
+                int e = sh.groups[gi] * 32 + lane;
+                long long k = (e < N) ? S.key[e] : DMD_KEY_INF;
+                if (k < kc) {
+                    int s = atomicAdd(&sh.ncand, 1);
+                    if (s < CAND_MAX) { sh.cand_key[s] = k; sh.cand_idx[s] = e; }
+                }
+            }
+        }
+        __syncthreads();
+        if (ng <= 256 && sh.ncand <= CAND_MAX) { ok = true; break; }
+        if (threadIdx.x == 0) {
+            sh.delta = sh.delta * 0.25;
+            if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
+        }
+        __syncthreads();
+    }
+    int nc = sh.ncand;
+    if (!ok || nc < 1) {
+        if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = root; }
+        __syncthreads();
+        return 1;
+    }
+    if ((int)threadIdx.x < nc) {
+        long long k = sh.cand_key[threadIdx.x];
+        int e = sh.cand_idx[threadIdx.x];
+        int rank = 0;
+        for (int u = 0; u < nc; ++u)
+            if (key_less(sh.cand_key[u], sh.cand_idx[u], k, e)) ++rank;
+        sh.sort_key[rank] = k;
+        sh.sort_idx[rank] = e;
+    }
+    if (threadIdx.x == 0) {
+        /* aim at about one to four candidates per warp */
+        if (nc < NWARPS) sh.delta = sh.delta * 2.0;
+        else if (nc > 4 * NWARPS) sh.delta = sh.delta * 0.5;
+        if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
+    }
+    __syncthreads();
+    return nc;
+}
+
+/* ------------------------------------------------------------------ */
 /* kernels                                                             */
 /* ------------------------------------------------------------------ */
-__device__ void log_event(const DSys &S, SharedState &sh, double t, double tfalse, int i, int j, int type, int evcode) {
+__device__ void log_event(const DSys &S, long long slot, long long coll, double t, double tfalse, int i, int j,
+                          int type, int evcode) {
     if (!S.log || S.log_cap <= 0) return;
-    long long k = sh.sc.log_count++;
-    dmd_event *L = (dmd_event *)S.log + (k % S.log_cap);
-    L->coll = sh.sc.coll; L->t = t; L->tfalse = tfalse;
+    dmd_event *L = (dmd_event *)S.log + (slot % S.log_cap);
+    L->coll = coll; L->t = t; L->tfalse = tfalse;
     L->i = i + 1; L->j = j + 1; L->type = type; L->evcode = evcode;
 }
 
@@ -949,16 +1363,18 @@ __global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int 
     if (threadIdx.x == 0) S_sh = systems[r];
     __syncthreads();
     const DSys &S = S_sh;
-    int hbonds = (hbonds_mask >> 0) & 1;
+    int hbonds = hbonds_mask & 1;
     if (threadIdx.x == 0) { sh.sc = *S.sc; }
+    for (int b = threadIdx.x; b < S.N; b += blockDim.x) S.owner[b] = INT_MAX;
     __syncthreads();
     cta_rebuild(S, sh, hbonds);
     if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_run(DSys *systems, int nsys, long long target, int hbonds_mask,
-                                                  const int *chain_start, const int *chain_len,
-                                                  const int *chain_off, dmd_diag *outputs) {
+__global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target, int hbonds_mask,
+                                                     const int *chain_start, const int *chain_len,
+                                                     const int *chain_off, dmd_diag *outputs) {
+    extern __shared__ WarpArea warea[];
     __shared__ SharedState sh;
     __shared__ DSys S_sh;
     int r = blockIdx.x;
@@ -970,12 +1386,15 @@ __global__ void __launch_bounds__(NTHREADS) k_run(DSys *systems, int nsys, long 
     const int hbonds = hbonds_mask & 1;
     const bool phys = (S.flags & DMD_FLAG_COUNT_PHYSICAL) != 0;
     const bool stop_out = (S.flags & DMD_FLAG_STOP_AT_OUTPUT) != 0;
+    const bool serial = (S.flags & DMD_FLAG_SERIAL) != 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) { sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0; }
+    WarpArea &W = warea[warp];
+    if (threadIdx.x == 0) {
+        sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0;
+        sh.delta = sh.sc.interval * 0.05;
+    }
     __syncthreads();
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
-    /* every committed pair or ghost event advances done; interval and output
-     * events are bounded by this cap so that a launch always ends */
     const long long max_iter = 16 * target + 1000000;
     long long iter = 0;
     while (true) {
@@ -986,90 +1405,188 @@ __global__ void __launch_bounds__(NTHREADS) k_run(DSys *systems, int nsys, long 
             break;
         }
         if (warp == 0) {
-            int e = warp_tree_root(S);
+            long long kroot;
+            int e = warp_tree_root(S, kroot);
             if (lane == 0) {
                 sh.ev = e;
+                sh.kcut = kroot;
                 if (e < 0) set_err(sh, DMD_E_STATE, 0);
-                else {
-                    sh.sc.coll += 1;
-                    sh.sc.tfalse = S.tim[e];
-                }
             }
         }
         __syncthreads();
         int e = sh.ev;
         if (e < 0) break;
         if (e < N) {
-            if (warp == 0) {
-                double tf = sh.sc.tfalse;
-                int j = S.nptnr[e];
-                if (lane == 0) {
-                    int xp, evc;
-                    int ct = lane_pair_event(S, sh, e, j, sh.sc.coll, tf, hbonds, xp, evc);
-                    if (ct >= 1 && ct < 32) sh.sc.nevents[ct] += 1;
-                    sh.sc.n_pair += 1;
-                    sh.xpulse = xp;
-                    log_event(S, sh, sh.sc.t, tf, e, j, ct, evc);
-                }
-                __syncwarp();
-                warp_partial_events(S, sh, e, j, tf, sh.sc.interval_max, hbonds);
-                if (lane == 0 && sh.xpulse) {
-                    if (S.ident[e] < S.ident[j]) repuls_del_b(S, e, j); else repuls_del_b(S, j, e);
-                }
-                __syncwarp();
-                warp_tree_update(S, sh.touched, sh.ntouched);
-                if (lane == 0) { sh.sc.old_tfalse = tf; sh.sc.done += 1; }
+            /* ---- a batch of pair events ---- */
+            long long kroot = sh.kcut;
+            int m;
+            long long left = target - sh.sc.done;
+            __syncthreads();
+            if (serial || left <= 1) {
+                if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = e; }
+                __syncthreads();
+                m = 1;
+            } else {
+                m = cta_candidates(S, sh, e, kroot);
+                if (m > NWARPS) m = NWARPS;
+                if (m > left) m = (int)left;
             }
+            /* footprints: claim, test, release */
+            int P = m;
+            if (m > 1) {
+                if (warp < m) {
+                    int i = sh.sort_idx[warp];
+                    warp_footprint(S, W, warp, i, S.nptnr[i], 0);
+                }
+                __syncthreads();
+                if (warp < m) {
+                    int i = sh.sort_idx[warp];
+                    bool c = warp_footprint(S, W, warp, i, S.nptnr[i], 1);
+                    if (lane == 0) W.conflict = c;
+                }
+                __syncthreads();
+                if (warp < m) {
+                    int i = sh.sort_idx[warp];
+                    warp_footprint(S, W, warp, i, S.nptnr[i], 2);
+                }
+                if (threadIdx.x == 0) {
+                    /* the longest conflict-free prefix; an incomplete footprint
+                     * (cascade list overflow) ends the batch after its event */
+                    int p = m;
+                    for (int k = 0; k < m; ++k) {
+                        if (k > 0 && warea[k].conflict) { p = k; break; }
+                        if (warea[k].casc_over) { p = k > 0 ? k : 1; break; }
+                    }
+                    sh.nbatch = p;
+                }
+                __syncthreads();
+                P = sh.nbatch;
+            }
+            /* speculative commit of each event on its warp */
+            long long coll0 = sh.sc.coll;
+            double imax = sh.sc.interval_max;
+            if (warp < P) {
+                int i = sh.sort_idx[warp];
+                int j = S.nptnr[i];
+                double tf = S.tim[i];
+                if (lane == 0) { W.i = i; W.j = j; W.tf = tf; W.coll = coll0 + warp + 1; }
+                __syncwarp();
+                warp_snapshot(S, W, i, j);
+                if (lane == 0) { W.err = 0; W.err_info = 0; }
+                __syncwarp();
+                Err E{&W.err, &W.err_info};
+                warp_collision(S, E, W, i, j, tf, coll0 + warp + 1, hbonds);
+                warp_repredict(S, E, W, i, j, tf, imax, hbonds);
+                if (lane == 0 && W.xpulse) {
+                    if (S.ident[i] < S.ident[j]) repuls_del_b(S, i, j); else repuls_del_b(S, j, i);
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+            /* validation: event k stands if it precedes every new entry of events 0..k-1 */
+            if (threadIdx.x == 0) {
+                int v = P;
+                long long bk = DMD_KEY_INF;
+                int bb = INT_MAX;
+                for (int k = 0; k < P; ++k) {
+                    if (k > 0 && !key_less(sh.sort_key[k], sh.sort_idx[k], bk, bb)) { v = k; break; }
+                    if (warea[k].err) {   /* the run stops after the first event in error */
+                        set_err(sh, warea[k].err, warea[k].err_info);
+                        v = k + 1;
+                        break;
+                    }
+                    if (key_less(warea[k].tnew_key, warea[k].tnew_idx, bk, bb)) { bk = warea[k].tnew_key; bb = warea[k].tnew_idx; }
+                }
+                sh.nvalid = v;
+            }
+            __syncthreads();
+            int V = sh.nvalid;
+            if (warp < P) {
+                if (warp < V) {
+                    warp_commit_preds(S, W);
+                    if (lane == 0) log_event(S, sh.sc.log_count + warp, W.coll, sh.sc.t, W.tf, W.i, W.j, W.ct, W.evcode);
+                } else {
+                    warp_restore(S, W);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int k = 0; k < V; ++k) {
+                    int ct = warea[k].ct;
+                    if (ct >= 1 && ct < 32) sh.sc.nevents[ct] += 1;
+                }
+                sh.sc.coll = coll0 + V;
+                sh.sc.n_pair += V;
+                sh.sc.done += V;
+                sh.sc.tfalse = warea[V - 1].tf;
+                sh.sc.old_tfalse = warea[V - 1].tf;
+                if (S.log && S.log_cap > 0) sh.sc.log_count += V;
+            }
+            if (warp < V) warp_l1_refresh(S, W.pb, W.npred);
+            __syncthreads();
+            if (warp < V) warp_l2_refresh(S, W.pb, W.npred);
         } else if (e == N) {
+            /* ---- ghost collision: alone ---- */
             if (warp == 0) {
-                double tf = sh.sc.tfalse;
-                int i = 0;
+                double tf = S.tim[N];
                 if (lane == 0) {
-                    i = lane_ghost(S, sh, tf);
+                    sh.sc.coll += 1;
+                    int i = lane_ghost(S, sh, tf);
+                    W.i = i; W.tf = tf;
+                }
+                __syncwarp();
+                int i = W.i;
+                tf = W.tf;
+                warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds);
+                warp_commit_preds(S, W);
+                if (lane == 0) {
+                    W.pb[W.npred] = N;   /* the ghost entry itself */
+                    log_event(S, sh.sc.log_count, sh.sc.coll, sh.sc.t, tf, i, -1, DMD_EV_GHOST, 0);
+                    if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
                     sh.sc.tfalse = tf;
-                    sh.ev_i = i;
-                }
-                __syncwarp();
-                i = sh.ev_i;
-                tf = sh.sc.tfalse;
-                warp_partial_events(S, sh, i, -1, tf, sh.sc.interval_max, hbonds);
-                if (lane == 0) {
-                    int nt = sh.ntouched;
-                    sh.touched[nt++] = N;
-                    sh.ntouched = nt;
-                }
-                __syncwarp();
-                warp_tree_update(S, sh.touched, sh.ntouched);
-                if (lane == 0) {
-                    log_event(S, sh, sh.sc.t, tf, i, -1, DMD_EV_GHOST, 0);
                     sh.sc.old_tfalse = tf;
                     sh.sc.done += 1;
                 }
+                __syncwarp();
+                warp_l1_refresh(S, W.pb, W.npred + 1);
+                __syncwarp();
+                warp_l2_refresh(S, W.pb, W.npred + 1);
             }
         } else if (e == N + 1) {
+            /* ---- interval ---- */
+            if (threadIdx.x == 0) { sh.sc.coll += 1; sh.sc.tfalse = S.tim[N + 1]; }
+            __syncthreads();
             double t_before = sh.sc.t, tf = sh.sc.tfalse;
             bool rb = cta_interval(S, sh, hbonds);
             if (threadIdx.x == 0) {
                 sh.sc.n_interval += 1;
-                log_event(S, sh, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
+                log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
+                if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
                 sh.sc.old_tfalse = sh.sc.tfalse;
                 if (!phys) sh.sc.done += 1;
             }
         } else {
+            /* ---- output ---- */
+            if (threadIdx.x == 0) { sh.sc.coll += 1; sh.sc.tfalse = S.tim[N + 2]; }
+            __syncthreads();
             cta_diag(S, sh, cs, cl, outputs ? outputs + r : nullptr);
             if (threadIdx.x == 0) {
                 sh.sc.n_output += 1;
                 double tn = 3.3 / (sqrt(S.tab->setemp)) + 5 + sh.sc.tfalse;
-                S.tim[N + 2] = tn;
-                S.queued[N + 2] = tn < sh.sc.interval_max;
-                log_event(S, sh, sh.sc.t, sh.sc.tfalse, N + 2, -1, DMD_EV_OUTPUT, 0);
+                set_pred(S, N + 2, tn, -2, -2, tn < sh.sc.interval_max);
+                log_event(S, sh.sc.log_count, sh.sc.coll, sh.sc.t, sh.sc.tfalse, N + 2, -1, DMD_EV_OUTPUT, 0);
+                if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
                 sh.sc.old_tfalse = sh.sc.tfalse;
                 if (!phys) sh.sc.done += 1;
                 if (stop_out) sh.sc.stop = 1;
                 sh.touched[0] = N + 2;
             }
             __syncthreads();
-            if (warp == 0) warp_tree_update(S, sh.touched, 1);
+            if (warp == 0) {
+                warp_l1_refresh(S, sh.touched, 1);
+                __syncwarp();
+                warp_l2_refresh(S, sh.touched, 1);
+            }
         }
         __syncthreads();
     }
@@ -1094,13 +1611,28 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, cons
 /* ------------------------------------------------------------------ */
 /* launch wrappers                                                     */
 /* ------------------------------------------------------------------ */
+static size_t run_smem() { return sizeof(WarpArea) * NWARPS; }
+
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st) {
     k_init<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
     return cudaGetLastError();
 }
 cudaError_t dmd_launch_run(DSys *d_systems, int nsys, long long target, int hbonds, const int *chain_start,
                            const int *chain_len, const int *chain_off, dmd_diag *outputs, cudaStream_t st) {
-    k_run<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off, outputs);
+    static std::mutex mu;
+    static bool done[256];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (dev >= 0 && dev < 256 && !done[dev]) {
+            e = cudaFuncSetAttribute(k_run, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem());
+            if (e != cudaSuccess) return e;
+            done[dev] = true;
+        }
+    }
+    k_run<<<nsys, NTHREADS, run_smem(), st>>>(d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off, outputs);
     return cudaGetLastError();
 }
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,

@@ -87,6 +87,8 @@ struct DSys {
     int *nptnr;
     int8_t *colt;
     uint8_t *queued;
+    long long *key;                /* ordered integer key of (queued ? tim : +inf), N + 3 entries */
+    int *owner;                    /* footprint claims of a batch, N entries (INT_MAX = free) */
     int *up, *dn;                  /* neighbour lists [N*cap] */
     int8_t *upc;                   /* static pair code of each up entry */
     int *upn, *dnn;
@@ -104,6 +106,23 @@ __device__ __forceinline__ double d_nint(double x) { return round(x); }
 /* lexicographic (time, partner) order used for every minimum */
 __device__ __forceinline__ bool lex_less(double ta, int pa, double tb, int pb) {
     return ta < tb || (ta == tb && pa < pb);
+}
+
+/* Integer key with the order of the doubles (finite values; -0 and +0 equal):
+ * comparisons of event times run on the integer pipes, not the FP64 unit. */
+#define DMD_KEY_INF 0x7fffffffffffffffLL
+__host__ __device__ __forceinline__ long long okey(double t) {
+#ifdef __CUDA_ARCH__
+    long long b = __double_as_longlong(t);
+#else
+    long long b;
+    memcpy(&b, &t, sizeof b);
+#endif
+    if (b == (long long)0x8000000000000000ULL) b = 0;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool key_less(long long ka, int pa, long long kb, int pb) {
+    return ka < kb || (ka == kb && pa < pb);
 }
 
 /* static pair code: code/make_code.f:6-573 applied per chain, as a rule */
