@@ -126,6 +126,9 @@ typedef struct dmd_diag {
     int64_t coll, n_pair, n_ghost, n_interval, n_output, n_updates, n_forced_updates;
     double  t, tfalse;
     double  nbr_mean;         /* mean neighbour-list entries per bead (up + down) */
+    int64_t n_batches;        /* engine: pair-event batches committed (0 in a serial run) */
+    int64_t n_rolled_back;    /* engine: speculative pair events undone and redone later */
+    int64_t n_candidates;     /* engine: pair events that entered a batch (before validation) */
 } dmd_diag;
 
 typedef struct dmd_handle dmd_handle;

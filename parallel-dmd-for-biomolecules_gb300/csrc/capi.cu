@@ -381,7 +381,7 @@ size_t layout(const HostSys &H, DSys &d, char *base) {
     d.upn = P.take<int>(N); d.dnn = P.take<int>(N);
     d.cell_count = P.take<int>(nc3 + 1); d.cell_start = P.take<int>(nc3 + 1); d.cell_beads = P.take<int>(N);
     d.l1i = P.take<int>(H.nl1); d.l2i = P.take<int>(H.nl2);
-    d.key = P.take<long long>(NE); d.owner = P.take<int>(N);
+    d.key = P.take<long long>(NE); d.owner = P.take<unsigned long long>(N);
     return P.off + 256;
 }
 

@@ -49,6 +49,31 @@
 #define CASC_MAX 64
 #define FULL 0xffffffffu
 
+/* Optional phase timers of k_run (build with -DDMD_PHASE_TIMERS): thread 0
+ * of each CTA adds the clock cycles spent in each phase of the event loop;
+ * dmd_debug_phase_cycles() reads them back.  Off by default. */
+#ifdef DMD_PHASE_TIMERS
+#define DMD_PHASE_SLOTS 16
+#define DMD_PHASE_CTAS 1024
+__device__ long long g_phase_cycles[DMD_PHASE_CTAS][DMD_PHASE_SLOTS];
+#define DMD_PHASE_START() long long ph_t_ = clock64()
+#define DMD_PHASE(k)                                                                       \
+    do {                                                                                   \
+        if (threadIdx.x == 0 && blockIdx.x < DMD_PHASE_CTAS) {                             \
+            long long now_ = clock64();                                                    \
+            g_phase_cycles[blockIdx.x][(k)] += now_ - ph_t_;                               \
+            ph_t_ = now_;                                                                  \
+        }                                                                                  \
+    } while (0)
+extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
+    if (nctas > DMD_PHASE_CTAS) nctas = DMD_PHASE_CTAS;
+    return (int)cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(long long) * DMD_PHASE_SLOTS * nctas);
+}
+#else
+#define DMD_PHASE_START() do {} while (0)
+#define DMD_PHASE(k) do { (void)(k); } while (0)
+#endif
+
 /* per-warp working area of one event (dynamic shared memory) */
 struct WarpArea {
     int nops, nlead, npred, nredo, nmeta, ncasc;
@@ -853,19 +878,23 @@ __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
 /* ------------------------------------------------------------------ */
 /* footprints of a batch candidate                                     */
 /* ------------------------------------------------------------------ */
-/* act 0: claim (atomicMin of the candidate index), 1: test for an earlier
- * claim, 2: release.  The set covers every bead the event reads or writes
- * in the serial order: i, j, their extra_repuls, their H-bond helpers and
- * those of their H-bond partners, both neighbour lists of i and j, and for
- * every bead that may need a full re-prediction its up list and extras. */
-__device__ bool warp_footprint(const DSys &S, WarpArea &W, int k, int i, int j, int act) {
+/* Claim (claim = true) or test the footprint of one candidate.  A claim
+ * raises owner[b] to the candidate's ticket, (batch sequence) * 64 +
+ * (63 - position), so that after the claims every bead holds the ticket of
+ * the earliest candidate that touches it; the test reports whether an
+ * earlier candidate holds any bead of this one.  Tickets grow from batch to
+ * batch, so the array needs no reset.  The set covers every bead the event
+ * reads or writes in the serial order: i, j, their extra_repuls, their
+ * H-bond helpers and those of their H-bond partners, both neighbour lists of
+ * i and j, and for every bead that may need a full re-prediction its up
+ * list and extras. */
+__device__ bool warp_footprint(const DSys &S, WarpArea &W, unsigned long long ticket, int i, int j, bool claim) {
     int lane = threadIdx.x & 31;
     bool conflict = false;
     auto visit = [&](int b) {
         if (b < 0) return;
-        if (act == 0) atomicMin(&S.owner[b], k);
-        else if (act == 1) { if (S.owner[b] < k) conflict = true; }
-        else S.owner[b] = INT_MAX;
+        if (claim) atomicMax(&S.owner[b], ticket);
+        else if (S.owner[b] > ticket) conflict = true;
     };
     /* fixed part: 18 entries on lanes 0..17 */
     if (lane < 18) {
@@ -892,7 +921,7 @@ __device__ bool warp_footprint(const DSys &S, WarpArea &W, int k, int i, int j, 
     for (int q = lane; q < uj; q += 32) visit(UJ[q]);
     for (int q = lane; q < dj; q += 32) visit(DJ[q]);
     /* beads that may be fully re-predicted (listed once, at the claim) */
-    if (act == 0) {
+    if (claim) {
         int nc = 0;
         for (int base = 0; base < di + dj; base += 32) {
             int q = base + lane;
@@ -901,33 +930,34 @@ __device__ bool warp_footprint(const DSys &S, WarpArea &W, int k, int i, int j, 
             else if (q < di + dj) { l = DJ[q - di]; if (S.nptnr[l] != j) l = -1; }
             unsigned m = __ballot_sync(FULL, l >= 0);
             int pos = nc + __popc(m & ((1u << lane) - 1));
-            if (l >= 0 && pos < CASC_MAX - 14) W.casc[pos] = l;
+            if (l >= 0 && pos < CASC_MAX - 10) W.casc[pos] = l;
             nc += __popc(m);
         }
-        if (lane == 0) W.casc_over = nc > CASC_MAX - 14;
-        nc = min(nc, CASC_MAX - 14);
-        if (lane < 14) {
-            int b = -1;
+        if (lane == 0) W.casc_over = nc > CASC_MAX - 10;
+        nc = min(nc, CASC_MAX - 10);
+        if (lane < 10) {
+            int b;
             if (lane < 3) b = S.er[4 * i + lane];
             else if (lane < 6) b = S.er[4 * j + lane - 3];
-            else if (lane < 10) {
+            else {
                 int x = lane < 8 ? i : j, h1, h2;
                 own_helpers(S, x, h1, h2);
                 b = (lane & 1) ? h2 : h1;
             }
             W.casc[nc + lane] = b;
         }
-        if (lane == 0) W.ncasc = nc + 14;
+        if (lane == 0) W.ncasc = nc + 10;
         __syncwarp();
     }
+    /* their up lists and extras, one cascade bead per lane */
     int nc = W.ncasc;
-    for (int c = 0; c < nc; ++c) {
+    for (int c = lane; c < nc; c += 32) {
         int l = W.casc[c];
         if (l < 0) continue;
         int ul = S.upn[l];
         const int *UL = S.up + (size_t)l * S.cap;
-        for (int q = lane; q < ul; q += 32) visit(UL[q]);
-        if (lane < 3) visit(S.er[4 * l + lane]);
+        for (int q = 0; q < ul; ++q) visit(UL[q]);
+        visit(S.er[4 * l + 0]); visit(S.er[4 * l + 1]); visit(S.er[4 * l + 2]);
     }
     return __any_sync(FULL, conflict);
 }
@@ -1265,6 +1295,8 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
         out->n_interval = sh.sc.n_interval; out->n_output = sh.sc.n_output; out->n_updates = sh.sc.n_updates;
         out->n_forced_updates = sh.sc.n_forced_updates; out->t = sh.sc.t; out->tfalse = sh.sc.tfalse;
         out->nbr_mean = nbr / (double)N;
+        out->n_batches = sh.sc.n_batches; out->n_rolled_back = sh.sc.n_rolled_back;
+        out->n_candidates = sh.sc.n_candidates;
     }
     __syncthreads();
 }
@@ -1365,7 +1397,7 @@ __global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int 
     const DSys &S = S_sh;
     int hbonds = hbonds_mask & 1;
     if (threadIdx.x == 0) { sh.sc = *S.sc; }
-    for (int b = threadIdx.x; b < S.N; b += blockDim.x) S.owner[b] = INT_MAX;
+    for (int b = threadIdx.x; b < S.N; b += blockDim.x) S.owner[b] = 0ull;
     __syncthreads();
     cta_rebuild(S, sh, hbonds);
     if (threadIdx.x == 0) *S.sc = sh.sc;
@@ -1394,6 +1426,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
         sh.delta = sh.sc.interval * 0.05;
     }
     __syncthreads();
+    DMD_PHASE_START();
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
     const long long max_iter = 16 * target + 1000000;
     long long iter = 0;
@@ -1414,9 +1447,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             }
         }
         __syncthreads();
+        DMD_PHASE(0);
+        int ph_kind __attribute__((unused)) = 9;
         int e = sh.ev;
         if (e < 0) break;
         if (e < N) {
+            ph_kind = 5;
             /* ---- a batch of pair events ---- */
             long long kroot = sh.kcut;
             int m;
@@ -1428,28 +1464,27 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 m = 1;
             } else {
                 m = cta_candidates(S, sh, e, kroot);
+                DMD_PHASE(1);
                 if (m > NWARPS) m = NWARPS;
                 if (m > left) m = (int)left;
             }
             /* footprints: claim, test, release */
             int P = m;
             if (m > 1) {
+                unsigned long long ticket = (unsigned long long)(sh.sc.bseq + 1) * 64ull + (unsigned long long)(63 - warp);
                 if (warp < m) {
                     int i = sh.sort_idx[warp];
-                    warp_footprint(S, W, warp, i, S.nptnr[i], 0);
+                    warp_footprint(S, W, ticket, i, S.nptnr[i], true);
                 }
                 __syncthreads();
                 if (warp < m) {
                     int i = sh.sort_idx[warp];
-                    bool c = warp_footprint(S, W, warp, i, S.nptnr[i], 1);
+                    bool c = warp_footprint(S, W, ticket, i, S.nptnr[i], false);
                     if (lane == 0) W.conflict = c;
                 }
                 __syncthreads();
-                if (warp < m) {
-                    int i = sh.sort_idx[warp];
-                    warp_footprint(S, W, warp, i, S.nptnr[i], 2);
-                }
                 if (threadIdx.x == 0) {
+                    sh.sc.bseq += 1;
                     /* the longest conflict-free prefix; an incomplete footprint
                      * (cascade list overflow) ends the batch after its event */
                     int p = m;
@@ -1461,6 +1496,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 }
                 __syncthreads();
                 P = sh.nbatch;
+                DMD_PHASE(2);
             }
             /* speculative commit of each event on its warp */
             long long coll0 = sh.sc.coll;
@@ -1483,6 +1519,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 __syncwarp();
             }
             __syncthreads();
+            DMD_PHASE(3);
             /* validation: event k stands if it precedes every new entry of events 0..k-1 */
             if (threadIdx.x == 0) {
                 int v = P;
@@ -1500,6 +1537,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 sh.nvalid = v;
             }
             __syncthreads();
+            DMD_PHASE(4);
             int V = sh.nvalid;
             if (warp < P) {
                 if (warp < V) {
@@ -1517,6 +1555,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 }
                 sh.sc.coll = coll0 + V;
                 sh.sc.n_pair += V;
+                sh.sc.n_batches += 1;
+                sh.sc.n_rolled_back += P - V;
+                sh.sc.n_candidates += m;
                 sh.sc.done += V;
                 sh.sc.tfalse = warea[V - 1].tf;
                 sh.sc.old_tfalse = warea[V - 1].tf;
@@ -1526,6 +1567,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             __syncthreads();
             if (warp < V) warp_l2_refresh(S, W.pb, W.npred);
         } else if (e == N) {
+            ph_kind = 6;
             /* ---- ghost collision: alone ---- */
             if (warp == 0) {
                 double tf = S.tim[N];
@@ -1553,6 +1595,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 warp_l2_refresh(S, W.pb, W.npred + 1);
             }
         } else if (e == N + 1) {
+            ph_kind = 7;
             /* ---- interval ---- */
             if (threadIdx.x == 0) { sh.sc.coll += 1; sh.sc.tfalse = S.tim[N + 1]; }
             __syncthreads();
@@ -1566,6 +1609,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 if (!phys) sh.sc.done += 1;
             }
         } else {
+            ph_kind = 8;
             /* ---- output ---- */
             if (threadIdx.x == 0) { sh.sc.coll += 1; sh.sc.tfalse = S.tim[N + 2]; }
             __syncthreads();
@@ -1589,6 +1633,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             }
         }
         __syncthreads();
+        DMD_PHASE(ph_kind);
     }
     __syncthreads();
     if (threadIdx.x == 0) *S.sc = sh.sc;

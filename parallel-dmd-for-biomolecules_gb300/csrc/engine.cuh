@@ -64,6 +64,8 @@ struct DScal {
     int err_info;
     int stop;             /* 1: stopped at an output event */
     int pad;
+    long long n_batches, n_rolled_back, n_candidates;   /* batch statistics */
+    long long bseq;       /* footprint claims made so far (ticket base) */
 };
 
 /* device view of one system; all arrays in global memory */
@@ -88,7 +90,7 @@ struct DSys {
     int8_t *colt;
     uint8_t *queued;
     long long *key;                /* ordered integer key of (queued ? tim : +inf), N + 3 entries */
-    int *owner;                    /* footprint claims of a batch, N entries (INT_MAX = free) */
+    unsigned long long *owner;     /* footprint tickets, N entries (0 = never claimed) */
     int *up, *dn;                  /* neighbour lists [N*cap] */
     int8_t *upc;                   /* static pair code of each up entry */
     int *upn, *dnn;
