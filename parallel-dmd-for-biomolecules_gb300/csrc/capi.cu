@@ -34,7 +34,7 @@ struct HostSys {
     int N = 0, nchains = 0, cap = 128, ncell = 0, nl1 = 0, nl2 = 0;
     std::vector<int> chain_start, chain_len;
     std::vector<BeadInfo> info;
-    std::vector<double> bm, blmin, blmax;
+    std::vector<double> bm, blmin, blmax, blmin_sq, blmax_sq;
     std::vector<double> x, y, z, vx, vy, vz;
     std::vector<int8_t> ident;
     std::vector<int> bptnr, er, ovp;
@@ -101,6 +101,28 @@ void build_tables(HostSys &H, const dmd_tables *T, double boxl) {
     D.eps1 = eps[1];
     D.eps_hb = D.ep_sqrt[5][8];
     D.boxl_orig = B;
+    /* squared diameters in the operation order of code/core.f:27-33 and
+     * code/nc_sqwel.f:80-84 (the device looks them up) */
+    for (int code = 0; code <= 26; ++code) {
+        if (code > 3 && code < 17) continue;
+        for (int a = 0; a < DMD_NT; ++a)
+            for (int b = 0; b < DMD_NT; ++b) {
+                double p = D.evp1[code];
+                double sigsq = D.sigma_sq[a][b] * (p * p);
+                if (code >= 22 && code <= 26) {
+                    int k = a > b ? a : b;
+                    double s = D.sqz610[code - 21][k];
+                    sigsq = sigsq * (s * s);
+                }
+                D.core_sq[core_slot(code)][a][b] = sigsq;
+            }
+    }
+    for (int a = 0; a < DMD_NT; ++a)
+        for (int b = 0; b < DMD_NT; ++b) {
+            double p = D.evp1[15];
+            D.ncfac_sq[a][b] = D.sigma_sq[a][b] * p * p;
+        }
+    for (int l = 0; l < DMD_NC; ++l) { D.evp2_sq[l] = D.evp2[l] * D.evp2[l]; D.evp3_sq[l] = D.evp3[l] * D.evp3[l]; }
     /* kept for nbor_setup: scaled bead diameters and the side-chain wells */
     for (int k = 1; k <= 28; ++k) { H.sigma_raw[k] = sigma[k]; H.welldia_raw[k] = welldia[k]; }
     (void)wel;
@@ -282,6 +304,9 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
     if (pos != H.N) return fail(err, "n_beads larger than the chains need");
     H.bm.assign(H.N, 0.0);
     for (int b = 0; b < H.N; ++b) H.bm[b] = bmass[H.ident[b]];
+    H.blmin_sq.assign(H.N, 0.0);
+    H.blmax_sq.assign(H.N, 0.0);
+    for (int b = 0; b < H.N; ++b) { H.blmin_sq[b] = H.blmin[b] * H.blmin[b]; H.blmax_sq[b] = H.blmax[b] * H.blmax[b]; }
 
     build_tables(H, T, S->boxl);
     H.tab.setemp = cfg->tstar * 12.0;
@@ -368,6 +393,7 @@ size_t layout(const HostSys &H, DSys &d, char *base) {
     d.sc = P.take<DScal>(1);
     d.info = P.take<BeadInfo>(N);
     d.bm = P.take<double>(N); d.blmin = P.take<double>(N); d.blmax = P.take<double>(N);
+    d.blmin_sq = P.take<double>(N); d.blmax_sq = P.take<double>(N);
     d.x = P.take<double>(N); d.y = P.take<double>(N); d.z = P.take<double>(N);
     d.vx = P.take<double>(N); d.vy = P.take<double>(N); d.vz = P.take<double>(N);
     d.ox = P.take<double>(N); d.oy = P.take<double>(N); d.oz = P.take<double>(N);
@@ -442,6 +468,8 @@ int upload(dmd_batch &B) {
         CK(cudaMemcpy((void *)d.bm, H.bm.data(), N * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy((void *)d.blmin, H.blmin.data(), N * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy((void *)d.blmax, H.blmax.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((void *)d.blmin_sq, H.blmin_sq.data(), N * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((void *)d.blmax_sq, H.blmax_sq.data(), N * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d.x, H.x.data(), N * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d.y, H.y.data(), N * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d.z, H.z.data(), N * 8, cudaMemcpyHostToDevice));
@@ -807,6 +835,7 @@ int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, co
         {(void *)d.tab, &H.tab, sizeof(DTab)}, {d.sc, &H.sc, sizeof(DScal)},
         {(void *)d.info, H.info.data(), N * sizeof(BeadInfo)}, {(void *)d.bm, H.bm.data(), N * 8},
         {(void *)d.blmin, H.blmin.data(), N * 8}, {(void *)d.blmax, H.blmax.data(), N * 8},
+        {(void *)d.blmin_sq, H.blmin_sq.data(), N * 8}, {(void *)d.blmax_sq, H.blmax_sq.data(), N * 8},
         {d.x, H.x.data(), N * 8}, {d.y, H.y.data(), N * 8}, {d.z, H.z.data(), N * 8},
         {d.vx, H.vx.data(), N * 8}, {d.vy, H.vy.data(), N * 8}, {d.vz, H.vz.data(), N * 8},
         {d.ident, H.ident.data(), N}, {d.bptnr, H.bptnr.data(), N * 4}, {d.er, H.er.data(), 4 * N * 4},

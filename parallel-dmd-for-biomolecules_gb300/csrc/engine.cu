@@ -45,7 +45,7 @@
 #define OPS_MAX 264        /* 2 * list capacity (128) + 6 extras + slack */
 #define CAND_MAX 64
 #define META_MAX 16
-#define REDO_MAX OPS_MAX
+#define TG_MAX 64         /* full re-predictions per round (i, j, marked beads) */
 #define CASC_MAX 64
 #define FULL 0xffffffffu
 
@@ -76,16 +76,30 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
 
 /* per-warp working area of one event (dynamic shared memory) */
 struct WarpArea {
-    int nops, nlead, npred, nredo, nmeta, ncasc;
+    int nops, nlead, npred, nmeta, ncasc, ntg, nmarked;
+    /* down-list operations (bead, source) in the reference's order, and
+     * the prediction of each operation's pair (time + tfalse, type) */
     int ops_l[OPS_MAX], ops_s[OPS_MAX];
-    int lead_l[OPS_MAX], lead_q[OPS_MAX];
+    double op_t[OPS_MAX];
+    int8_t op_y[OPS_MAX];
+    /* distinct operation beads: bead, first operation, full-redo mark */
+    int lead_l[OPS_MAX];
+    int16_t lead_q[OPS_MAX];
+    int8_t lead_m[OPS_MAX];
+    int16_t mk[OPS_MAX];          /* marked leaders, in leader order */
+    /* full re-predictions of one round: bead, first task, running minimum */
+    int tg_b[TG_MAX];
+    int tg_base[TG_MAX + 1];
+    long long tg_k[TG_MAX];
+    int tg_p[TG_MAX];
+    double tg_raw[TG_MAX];
+    int8_t tg_y[TG_MAX];
     /* buffered predictions: bead, time, partner, type, queued */
     int pb[OPS_MAX + 2];
     double pt[OPS_MAX + 2];
     int pn[OPS_MAX + 2];
     int8_t pc[OPS_MAX + 2];
     uint8_t pq[OPS_MAX + 2];
-    int redo_l[REDO_MAX], redo_p[REDO_MAX], redo_slot[REDO_MAX];
     /* snapshot of what the collision may write */
     int mb[META_MAX];
     int8_t mident[META_MAX];
@@ -285,7 +299,7 @@ __device__ WRel warp_rel(const DSys &S, int i, int j, double tf) {
     const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
     double v = V[i] - V[j];
     double r = P[i] - P[j] + v * tf;
-    r = r - d_nint(r);
+    r = d_wrap(r);
     double pb = r * v, pr = r * r, pv = v * v;
     WRel w;
     w.rx = __shfl_sync(FULL, r, 0); w.ry = __shfl_sync(FULL, r, 1); w.rz = __shfl_sync(FULL, r, 2);
@@ -309,7 +323,7 @@ __device__ void warp_dist4(const DSys &S, const int *a, const int *b, double tf,
     const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
     double v = V[ia] - V[ib];
     double r = P[ia] - P[ib] + v * tf;
-    r = r - d_nint(r);
+    r = d_wrap(r);
     double p = r * r;
     double c0 = __shfl_sync(FULL, p, 3 * (lane & 3));
     double c1 = __shfl_sync(FULL, p, 3 * (lane & 3) + 1);
@@ -668,41 +682,22 @@ __device__ __forceinline__ bool check_tij(Err E, double tij, int i) {
     return true;
 }
 
-/* warp: full re-prediction of bead l (the pass of partial_events.f:16-35) */
-__device__ void warp_redo_full(const DSys &S, Err E, int l, double tf, double imax, int hbonds,
-                               double &t_out, int &p_out, int &y_out, bool &q_out) {
-    int lane = threadIdx.x & 31;
-    double H = imax + DMD_LTSTEP - tf;
-    long long bk = okey(H);
-    double bt = H;
-    int bp = -1, by = -1;
-    int n = S.upn[l];
-    const int *up = S.up + (size_t)l * S.cap;
-    for (int k = lane; k < n + 3; k += 32) {
-        int m = k < n ? up[k] : S.er[4 * l + (k - n)];
-        if (m <= l) continue;
-        double tij; int ty;
-        if (!d_predict(S, l, m, pair_code(S, m, l, hbonds), tf, tij, ty)) { set_err(E, DMD_E_INPUT, l); continue; }
-        check_tij(E, tij, l);
-        long long kk = okey(tij);
-        if (key_less(kk, m, bk, bp)) { bk = kk; bp = m; bt = tij; by = ty; }
-    }
-    warp_keymin(bk, bp, bt, by);
-    double tn = bt + tf;
-    t_out = tn; p_out = bp; y_out = by; q_out = tn < imax;
-}
-
-/* eventredo_down(l, src) on one lane against the running (t, p, y, q) of l */
-__device__ __forceinline__ void lane_redo_down(const DSys &S, Err E, int l, int src, double tf, double imax,
-                                               int hbonds, double &t, int &p, int &y, bool &q) {
-    double tij; int ty;
-    if (!d_predict(S, l, src, pair_code(S, l, src, hbonds), tf, tij, ty)) { set_err(E, DMD_E_INPUT, l); return; }
-    check_tij(E, tij, l);
-    tij = tij + tf;
-    if (key_less(okey(tij), src, okey(t), p)) { t = tij; p = src; y = ty; q = tij < imax; }
-}
-
-/* warp: partial_events(i, j) (j = -1 after a ghost) into W's buffer */
+/* warp: partial_events(i, j) (code/partial_events.f:5-205; j = -1 after a
+ * ghost) into W's buffer.
+ *
+ * The reference updates beads one operation at a time: the full
+ * re-prediction of i and of j (eventredo_up over the up list and the
+ * extras), then for every bead l of the down lists and the lower extras of
+ * i and then j, either a full re-prediction of l (when l's current partner
+ * is the source) or a comparison with the pair (l, source)
+ * (eventredo_down).  No prediction depends on another: all read the state
+ * after the collision.  So the pairs are predicted as one flat task list,
+ * 32 per pass with one call site, and the order-dependent part - which
+ * candidate wins, when a full re-prediction is due - is replayed per bead
+ * on integer keys.  A bead needs its full re-prediction only if its
+ * partner before the event is one of its sources or a source repeats;
+ * those beads ("marked") are fully re-predicted up front, in rounds of at
+ * most TG_MAX - 2. */
 __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, double imax,
                                int hbonds) {
     int lane = threadIdx.x & 31;
@@ -740,113 +735,179 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
         }
     }
     __syncwarp();
-    /* 2. distinct beads (leaders) with their first operation */
-    int nl = 0;
+    /* 2. distinct beads (leaders), their first operation and mark */
+    int nl = 0, nm = 0;
     for (int base = 0; base < n; base += 32) {
         int q = base + lane;
-        bool lead = false;
+        bool lead = false, mark = false;
+        int l = -1;
         if (q < n) {
-            int l = W.ops_l[q];
+            l = W.ops_l[q];
             lead = true;
             for (int p = 0; p < q; ++p) if (W.ops_l[p] == l) { lead = false; break; }
+            if (lead && l != i) {
+                int p0 = S.nptnr[l];
+                int s1 = -1, s2 = -1;   /* sources are i or j: two at most */
+                for (int pp = q; pp < n; ++pp) {
+                    if (W.ops_l[pp] != l) continue;
+                    int src = W.ops_s[pp];
+                    if (src == p0 || src == s1 || src == s2) mark = true;
+                    if (s1 < 0) s1 = src; else s2 = src;
+                }
+            }
         }
         unsigned m = __ballot_sync(FULL, lead);
         int pos = nl + __popc(m & ((1u << lane) - 1));
-        if (lead) { W.lead_l[pos] = W.ops_l[q]; W.lead_q[pos] = q; }
+        unsigned mm = __ballot_sync(FULL, lead && mark);
+        int mpos = nm + __popc(mm & ((1u << lane) - 1));
+        if (lead) { W.lead_l[pos] = l; W.lead_q[pos] = (int16_t)q; W.lead_m[pos] = mark; }
+        if (lead && mark) W.mk[mpos] = (int16_t)pos;
         nl += __popc(m);
+        nm += __popc(mm);
     }
-    if (lane == 0) { W.nredo = 0; W.nlead = nl; }
+    if (lane == 0) {
+        W.nlead = nl; W.nmarked = nm; W.npred = 2 + nl;
+        W.pb[0] = i; W.pb[1] = j;
+    }
     __syncwarp();
-    /* 3. one pass over: i's partners, j's partners, the leaders' operations */
-    int ni = S.upn[i] + 3, nj = j >= 0 ? S.upn[j] + 3 : 0;
-    double Hd = imax + DMD_LTSTEP - tf;
-    long long Hk = okey(Hd);
-    long long ki = Hk, kj = Hk;
-    double ti = Hd, tj = Hd;
-    int pi = -1, pj = -1, yi = -1, yj = -1;
-    const int *upi = S.up + (size_t)i * S.cap;
-    const int *upj = j >= 0 ? S.up + (size_t)j * S.cap : nullptr;
-    for (int q = lane; q < ni + nj + nl; q += 32) {
-        if (q < ni + nj) {
-            bool isj = q >= ni;
-            int x = isj ? j : i, k = isj ? q - ni : q, nx = isj ? nj - 3 : ni - 3;
-            int m = k < nx ? (isj ? upj[k] : upi[k]) : S.er[4 * x + (k - nx)];
-            if (m <= x) continue;
-            double tij; int ty;
-            if (!d_predict(S, x, m, pair_code(S, m, x, hbonds), tf, tij, ty)) { set_err(E, DMD_E_INPUT, x); continue; }
-            check_tij(E, tij, x);
-            long long kk = okey(tij);
-            if (isj) { if (key_less(kk, m, kj, pj)) { kj = kk; pj = m; tj = tij; yj = ty; } }
-            else { if (key_less(kk, m, ki, pi)) { ki = kk; pi = m; ti = tij; yi = ty; } }
-        } else {
-            int ld = q - ni - nj;
-            int l = W.lead_l[ld], q0 = W.lead_q[ld];
-            int slot = 2 + ld;
-            W.pb[slot] = l;
-            if (l == i) {   /* a j-extras operation on i waits for i's new prediction */
-                int r = atomicAdd(&W.nredo, 1);
-                if (r < REDO_MAX) { W.redo_l[r] = l; W.redo_p[r] = q0; W.redo_slot[r] = slot; }
-                else set_err(E, DMD_E_CAPACITY, l);
-                continue;
+    const double Hraw = imax + DMD_LTSTEP - tf;   /* eventredo_up's starting time */
+    const long long Hkey = okey(Hraw), imax_key = okey(imax);
+    const int per_round = TG_MAX - 2;
+    int rounds = nm > 0 ? (nm + per_round - 1) / per_round : 1;
+    for (int rd = 0; rd < rounds; ++rd) {
+        /* 3. this round's full re-predictions: i, j (round 0), marked beads */
+        int m0 = rd * per_round, m1 = min(nm, m0 + per_round);
+        int ntg = 2 + (m1 - m0);
+        for (int t = lane; t < ntg; t += 32) {
+            int b;
+            if (t == 0) b = rd == 0 ? i : -1;
+            else if (t == 1) b = rd == 0 ? j : -1;
+            else b = W.lead_l[W.mk[m0 + t - 2]];
+            W.tg_b[t] = b;
+            W.tg_k[t] = Hkey; W.tg_p[t] = -1; W.tg_raw[t] = Hraw; W.tg_y[t] = -1;
+        }
+        /* task offsets: an inclusive scan of (upn + 3) over the targets */
+        int run = 0;
+        for (int base = 0; base < ntg; base += 32) {
+            int t = base + lane;
+            int b = t < ntg ? W.tg_b[t] : -1;
+            int c = b >= 0 ? S.upn[b] + 3 : 0;
+            int incl = c;
+            for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
+            if (t < ntg) W.tg_base[t] = run + incl - c;
+            run += __shfl_sync(FULL, incl, 31);
+        }
+        if (lane == 0) W.tg_base[ntg] = run;
+        __syncwarp();
+        int nop = rd == 0 ? n : 0;
+        int ntask = nop + run;
+        /* 4. every task of the round, 32 per pass, one predictor call site */
+        for (int base = 0; base < ntask; base += 32) {
+            int q = base + lane;
+            int pa = -1, pbb = -1, code = 1, tgt = -1;
+            if (q < nop) {
+                pa = W.ops_l[q]; pbb = W.ops_s[q];
+                code = pair_code(S, pa, pbb, hbonds);
+            } else if (q < ntask) {
+                int rel = q - nop;
+                int lo = 0, hi = ntg - 1;        /* last target with tg_base <= rel */
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (W.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
+                }
+                tgt = lo;
+                int b = W.tg_b[lo];
+                int k = rel - W.tg_base[lo];
+                int nu = S.upn[b];
+                int m = k < nu ? S.up[(size_t)b * S.cap + k] : S.er[4 * b + (k - nu)];
+                if (m > b) { pa = b; pbb = m; code = pair_code(S, m, b, hbonds); }
             }
-            double t = S.tim[l];
-            int p = S.nptnr[l], y = S.colt[l];
-            bool qq = S.queued[l] != 0;
-            int stop = -1;
-            for (int pp = q0; pp < n; ++pp) {
+            double tij = 0.0;
+            int ty = 0;
+            bool ok = false;
+            if (pa >= 0) {
+                ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
+                if (!ok) set_err(E, DMD_E_INPUT, pa);
+                else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
+            }
+            /* a down operation's candidate time is tij + tfalse; a full
+             * re-prediction adds tfalse after its minimum (x + (-0.0) == x) */
+            double tt = tij + (q < nop ? tf : -0.0);
+            if (q < nop) { W.op_t[q] = tt; W.op_y[q] = ok ? (int8_t)ty : (int8_t)-128; }
+            /* segmented minimum of the full tasks, segment = target */
+            long long k = (tgt >= 0 && ok) ? okey(tt) : DMD_KEY_INF;
+            int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
+            double rt = tt;
+            int y = ty;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                long long k2 = __shfl_down_sync(FULL, k, o);
+                int p2 = __shfl_down_sync(FULL, p, o);
+                double r2 = __shfl_down_sync(FULL, rt, o);
+                int y2 = __shfl_down_sync(FULL, y, o);
+                int g2 = __shfl_down_sync(FULL, tgt, o);
+                if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
+            }
+            int gprev = __shfl_up_sync(FULL, tgt, 1);
+            bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
+            if (head && key_less(k, p, W.tg_k[tgt], W.tg_p[tgt])) {
+                W.tg_k[tgt] = k; W.tg_p[tgt] = p; W.tg_raw[tgt] = rt; W.tg_y[tgt] = (int8_t)y;
+            }
+            __syncwarp();
+        }
+        /* 5. the full results: time = minimum + tfalse */
+        for (int t = lane; t < ntg; t += 32) W.tg_raw[t] = W.tg_raw[t] + tf;
+        __syncwarp();
+        if (rd == 0 && lane < 2 && (lane == 0 || j >= 0)) {
+            double tn = W.tg_raw[lane];
+            W.pt[lane] = tn; W.pn[lane] = W.tg_p[lane]; W.pc[lane] = W.tg_y[lane];
+            W.pq[lane] = okey(tn) < imax_key;
+        }
+        __syncwarp();
+        /* 6. replay of the operations per bead: round 0 replays the
+         * unmarked beads and i, each round its marked beads */
+        int nrep = rd == 0 ? nl : 0;
+        int nrep_m = m1 - m0;
+        for (int q = lane; q < nrep + nrep_m; q += 32) {
+            int ld, ft;
+            if (q < nrep) {
+                ld = q;
+                if (W.lead_m[ld]) continue;          /* replayed in its round */
+                ft = W.lead_l[ld] == i ? 0 : -1;
+            } else {
+                ld = W.mk[m0 + q - nrep];
+                ft = 2 + (q - nrep);
+            }
+            int l = W.lead_l[ld];
+            double t;
+            int p, y;
+            bool qq;
+            if (l == i) { t = W.tg_raw[0]; p = W.tg_p[0]; y = W.tg_y[0]; qq = okey(t) < imax_key; }
+            else { t = S.tim[l]; p = S.nptnr[l]; y = S.colt[l]; qq = S.queued[l] != 0; }
+            for (int pp = W.lead_q[ld]; pp < n; ++pp) {
                 if (W.ops_l[pp] != l) continue;
                 int src = W.ops_s[pp];
-                if (p == src) { stop = pp; break; }
-                lane_redo_down(S, E, l, src, tf, imax, hbonds, t, p, y, qq);
+                if (p == src) {
+                    if (ft < 0) { set_err(E, DMD_E_STATE, l); break; }
+                    t = W.tg_raw[ft]; p = W.tg_p[ft]; y = W.tg_y[ft]; qq = okey(t) < imax_key;
+                } else if (W.op_y[pp] != -128) {
+                    double tn = W.op_t[pp];
+                    long long kn = okey(tn);
+                    if (key_less(kn, src, okey(t), p)) { t = tn; p = src; y = W.op_y[pp]; qq = kn < imax_key; }
+                }
             }
-            W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
-            if (stop >= 0) {
-                int r = atomicAdd(&W.nredo, 1);
-                if (r < REDO_MAX) { W.redo_l[r] = l; W.redo_p[r] = stop; W.redo_slot[r] = slot; }
-                else set_err(E, DMD_E_CAPACITY, l);
-            }
-        }
-    }
-    warp_keymin(ki, pi, ti, yi);
-    if (j >= 0) warp_keymin(kj, pj, tj, yj);
-    if (lane == 0) {
-        double tn = ti + tf;
-        W.pb[0] = i; W.pt[0] = tn; W.pn[0] = pi; W.pc[0] = (int8_t)yi; W.pq[0] = tn < imax;
-        if (j >= 0) {
-            double tn2 = tj + tf;
-            W.pb[1] = j; W.pt[1] = tn2; W.pn[1] = pj; W.pc[1] = (int8_t)yj; W.pq[1] = tn2 < imax;
-        } else {
-            W.pb[1] = -1;
-        }
-        W.npred = 2 + nl;
-    }
-    __syncwarp();
-    /* 4. operations that need a full re-prediction, in operation order per bead */
-    int nr = min(W.nredo, REDO_MAX);
-    for (int r = 0; r < nr; ++r) {
-        int l = W.redo_l[r], p0 = W.redo_p[r], slot = W.redo_slot[r];
-        double t; int p, y; bool qq;
-        if (l == i) { t = W.pt[0]; p = W.pn[0]; y = W.pc[0]; qq = W.pq[0] != 0; }
-        else { t = W.pt[slot]; p = W.pn[slot]; y = W.pc[slot]; qq = W.pq[slot] != 0; }
-        for (int pp = p0; pp < n; ++pp) {
-            if (W.ops_l[pp] != l) continue;
-            int src = W.ops_s[pp];
-            if (p == src) {
-                warp_redo_full(S, E, l, tf, imax, hbonds, t, p, y, qq);
+            int slot = 2 + ld;
+            if (l == i) {
+                W.pb[slot] = -1;
+                W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq;
             } else {
-                double t2 = t; int p2 = p, y2 = y; bool q2 = qq;
-                if (lane == 0) lane_redo_down(S, E, l, src, tf, imax, hbonds, t2, p2, y2, q2);
-                t = __shfl_sync(FULL, t2, 0); p = __shfl_sync(FULL, p2, 0);
-                y = __shfl_sync(FULL, y2, 0); qq = __shfl_sync(FULL, (int)q2, 0) != 0;
+                W.pb[slot] = l;
+                W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
             }
-        }
-        if (lane == 0) {
-            if (l == i) { W.pb[slot] = -1; W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq; }
-            else { W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq; }
         }
         __syncwarp();
     }
-    /* 5. the earliest new queued entry of this event */
+    /* 7. the earliest new queued entry of this event */
     long long bk = DMD_KEY_INF;
     int bb = INT_MAX;
     for (int q = lane; q < W.npred; q += 32) {
@@ -1107,7 +1168,7 @@ __device__ void cta_predict_all(const DSys &S, SharedState &sh, double interval_
             int m = k < nu ? up[k] : S.er[4 * b + (k - nu)];
             if (m <= b) continue;
             double tij; int ty;
-            if (!d_predict(S, b, m, pair_code(S, m, b, hbonds), 0.0, tij, ty)) { set_err(sh, DMD_E_INPUT, b); continue; }
+            if (!d_predict_c(S, b, m, pair_code(S, m, b, hbonds), 0.0, tij, ty)) { set_err(sh, DMD_E_INPUT, b); continue; }
             check_tij(cta_err(sh), tij, b);
             long long kk = okey(tij);
             if (key_less(kk, m, bk, bp)) { bk = kk; bt = tij; bp = m; by = ty; }

@@ -51,7 +51,15 @@ struct DTab {
     double setemp, avegtime, hdelr, rl;
     double eps_hb;     /* ep_sqrt(5,8) */
     double boxl_orig;
+    /* squared contact diameters, computed once in the predictors' own
+     * operation order (so a lookup gives the same bits as the inline
+     * product): core codes 1-3 and 17-26 (slot core_slot(code)), the
+     * bonded H-bond pair's inner core (code 15), the bond windows */
+    double core_sq[14][DMD_NT][DMD_NT];
+    double ncfac_sq[DMD_NT][DMD_NT];
+    double evp2_sq[DMD_NC], evp3_sq[DMD_NC];
 };
+__host__ __device__ __forceinline__ int core_slot(int code) { return code <= 3 ? code : code - 13; }
 
 /* per-system scalars kept between launches */
 struct DScal {
@@ -78,6 +86,7 @@ struct DSys {
     const BeadInfo *info;
     const double *bm;
     const double *blmin, *blmax;  /* side-chain bond window of a backbone bead (codes 10/11/12) */
+    const double *blmin_sq, *blmax_sq;   /* their squares */
     double *x, *y, *z, *vx, *vy, *vz;
     double *ox, *oy, *oz;          /* positions at the last list rebuild */
     int8_t *ident;                 /* identity 1..28 (5..8: bonded backbone) */
@@ -197,107 +206,132 @@ __device__ __forceinline__ void bond_limits(const DSys &S, int i, int evcode, do
     else { blmin = S.tab->evp2[evcode]; blmax = S.tab->evp3[evcode]; }
 }
 
-/* pair prediction, dispatch of code/eventredo_up.f:28-46 into
- * code/core.f, bond.f, nc_sqwel.f, sqwel.f, sqshlder.f.  Returns false on an
- * invalid code (reference: "error in ev_code matrix"). */
-static __device__ __noinline__ bool d_predict(const DSys &S, int i, int j, int evcode, double tfalse,
-                                       double &tij, int &type) {
+/* ------------------------------------------------------------------ */
+/* pair prediction with warp-convergent control flow                  */
+/* ------------------------------------------------------------------ */
+/* Pair prediction: the dispatch of code/eventredo_up.f:28-46 into
+ * code/core.f, bond.f, nc_sqwel.f, sqwel.f and sqshlder.f.  Returns false on
+ * an invalid code (reference: "error in ev_code matrix").
+ *
+ * On GB300 an FP64 warp instruction occupies the SM sub-partition's FP64
+ * unit for about 64 cycles whatever the number of active lanes, and lanes
+ * of one warp that take different branches pay for every branch.  So the
+ * predictors are not written branch by branch; they give the reference's
+ * (tij, type) bit for bit, because every branch of them is one of
+ *   tij = (-bij - sqrt(D)) / vijsq,  (-bij + sqrt(D)) / vijsq,
+ *   or  -(rijsq - R) / (sqrt(D) + bij)          (bond.f, outward, bij >= 0)
+ * with D = bij*bij - vijsq*(rijsq - R) for one or two squared diameters R
+ * chosen by integer tests, so all lanes run one or two discriminants, one
+ * square root and one division.  Sign and order tests read the bit
+ * patterns on the integer pipes, and the minimum image skips the rounding
+ * where |r| < 0.5 (there x - nint(x) == x exactly). */
+
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+/* x < 0.0 (false for -0.0) */
+__device__ __forceinline__ bool d_lt0(double x) { long long b = dbits(x); return b < 0 && b != (long long)0x8000000000000000ULL; }
+/* x > 0.0 */
+__device__ __forceinline__ bool d_gt0(double x) { return dbits(x) > 0; }
+/* a < b for a, b >= +0.0 (non-negative, not NaN) */
+__device__ __forceinline__ bool d_lt_nn(double a, double b) { return dbits(a) < dbits(b); }
+__device__ __forceinline__ double d_negate(double x) { return __longlong_as_double(dbits(x) ^ (long long)0x8000000000000000ULL); }
+/* x - nint(x); skips the rounding where |x| < 0.5 and x is not -0.0 */
+__device__ __forceinline__ double d_wrap(double x) {
+    long long b = dbits(x);
+    if ((b & 0x7fffffffffffffffLL) < 0x3fe0000000000000LL && b != (long long)0x8000000000000000ULL) return x;
+    return x - round(x);
+}
+__device__ __forceinline__ Rel d_rel_c(const DSys &S, int i, int j, double tfalse) {
+    Rel r;
+    r.vx = S.vx[i] - S.vx[j]; r.vy = S.vy[i] - S.vy[j]; r.vz = S.vz[i] - S.vz[j];
+    r.rx = S.x[i] - S.x[j] + r.vx * tfalse;
+    r.ry = S.y[i] - S.y[j] + r.vy * tfalse;
+    r.rz = S.z[i] - S.z[j] + r.vz * tfalse;
+    r.rx = d_wrap(r.rx); r.ry = d_wrap(r.ry); r.rz = d_wrap(r.rz);
+    r.bij = r.rx * r.vx + r.ry * r.vy + r.rz * r.vz;
+    r.rijsq = r.rx * r.rx + r.ry * r.ry + r.rz * r.rz;
+    r.vijsq = r.vx * r.vx + r.vy * r.vy + r.vz * r.vz;
+    return r;
+}
+
+#define PK_NONE 0
+#define PK_MINUS 1
+#define PK_PLUS 2
+#define PK_BOND 3   /* -(rijsq - R) / (sqrt(D) + bij) */
+#define PK_STAGE2 4
+
+__device__ __forceinline__ bool d_predict_c(const DSys &S, int i, int j, int evcode, double tfalse,
+                                            double &tij, int &type) {
     const DTab &T = *S.tab;
-    tij = DMD_BIG; type = 0;
-    Rel r = d_rel(S, i, j, tfalse);
+    Rel r = d_rel_c(S, i, j, tfalse);
     int a = S.ident[i], b = S.ident[j];
-    if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {            /* core.f:3-44 */
-        if (r.bij < 0.0) {
-            double p = T.evp1[evcode];
-            double sigsq = T.sigma_sq[a][b] * (p * p);
-            if (evcode >= 22 && evcode <= 26) {
-                int k = a > b ? a : b;
-                double s = T.sqz610[evcode - 21][k];
-                sigsq = sigsq * (s * s);
-            }
-            double discr = r.bij * r.bij - r.vijsq * (r.rijsq - sigsq);
-            if (discr > 0.0) { tij = (-r.bij - sqrt(discr)) / r.vijsq; type = 1; }
-        }
-    } else if (evcode >= 4 && evcode <= 12) {                      /* bond.f:4-121 */
-        double blmin, blmax;
-        bond_limits(S, i, evcode, blmin, blmax);
-        if (r.bij < 0.0) {
-            double discr1 = r.bij * r.bij - r.vijsq * (r.rijsq - blmin * blmin);
-            if (discr1 > 0.0) {
-                tij = (-r.bij - sqrt(discr1)) / r.vijsq; type = 2;
-            } else {
-                double discr2 = r.bij * r.bij - r.vijsq * (r.rijsq - blmax * blmax);
-                if (discr2 > 0.0) { tij = (-r.bij + sqrt(discr2)) / r.vijsq; type = 3; }
-            }
+    bool neg = d_lt0(r.bij);
+    bool valid = true;
+    /* stage 1: diameter R1; outcome if D1 > 0 (k1p, y1p) or not (k1n, y1n);
+     * stage 2 (k1n == PK_STAGE2): diameter R2, outcome (k2p, y2p) / (k2n, y2n) */
+    double R1 = 0.0, R2 = 0.0;
+    int k1p = PK_NONE, y1p = 0, k1n = PK_NONE, y1n = 0, k2p = PK_NONE, y2p = 0, k2n = PK_NONE, y2n = 0;
+    if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {                 /* core.f:3-44 */
+        if (neg) { R1 = T.core_sq[core_slot(evcode)][a][b]; k1p = PK_MINUS; y1p = 1; }
+    } else if (evcode >= 4 && evcode <= 12) {                           /* bond.f:4-121 */
+        bool side = evcode >= 10;
+        double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];
+        double hi = side ? S.blmax_sq[i] : T.evp3_sq[evcode];
+        if (neg) {
+            R1 = lo; k1p = PK_MINUS; y1p = 2; k1n = PK_STAGE2;
+            R2 = hi; k2p = PK_PLUS; y2p = 3;
         } else {
-            double discr2 = r.bij * r.bij - r.vijsq * (r.rijsq - blmax * blmax);
-            if (discr2 > 0.0) { tij = -(r.rijsq - blmax * blmax) / (sqrt(discr2) + r.bij); type = 3; }
+            R1 = hi; k1p = PK_BOND; y1p = 3;
         }
-    } else if (evcode == 15) {                                      /* nc_sqwel.f:7-126 */
-        double diff = r.rijsq - T.welldia_sq[a][b];
-        if (a + b == 5) {
-            if (r.bij < 0.0) {
-                if (diff < 0.0) {
-                    double corediscr = r.bij * r.bij - r.vijsq * (r.rijsq - T.sigma_sq[a][b]);
-                    if (corediscr > 0.0) { tij = (-r.bij - sqrt(corediscr)) / r.vijsq; type = 1; }
-                    else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 16; }
-                } else {
-                    double w = r.bij * r.bij - r.vijsq * diff;
-                    if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 7; }
-                }
-            } else if (diff < 0.0) {
-                double w = r.bij * r.bij - r.vijsq * diff;
-                tij = (-r.bij + sqrt(w)) / r.vijsq; type = 16;
-            }
-        } else if (S.bptnr[i] == j) {
-            if (r.bij < 0.0) {
-                double p = T.evp1[15];
-                double fac_sigsq = T.sigma_sq[a][b] * p * p;
-                double fac_cored = r.bij * r.bij - r.vijsq * (r.rijsq - fac_sigsq);
-                if (fac_cored > 0.0) { tij = (-r.bij - sqrt(fac_cored)) / r.vijsq; type = 1; }
-                else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8; }
+    } else if (evcode == 15 || evcode == 16 || evcode >= 40) {
+        /* nc_sqwel.f:7-126, sqwel.f:5-67, sqshlder.f:5-66 */
+        double well = evcode >= 40 ? T.shlddia_sq[a][b] : T.welldia_sq[a][b];
+        bool inside = d_lt_nn(r.rijsq, well);          /* diff < 0 */
+        int y_in, y_out;                                /* exit / entry types */
+        bool two_stage = true;                          /* core inside the well */
+        double core = T.sigma_sq[a][b];
+        if (evcode == 16) { y_in = 8; y_out = 4; }
+        else if (evcode >= 40) { y_in = 10; y_out = 12; }
+        else if (a + b == 5) { y_in = 16; y_out = 7; }
+        else if (S.bptnr[i] == j) {
+            /* bonded H-bond pair: always inside, core with the 1.05 factor */
+            y_in = 8; y_out = 8; inside = true; core = T.ncfac_sq[a][b];
+        } else { y_in = 0; y_out = 9; two_stage = false; inside = false; }
+        if (neg) {
+            if (inside && two_stage) {
+                R1 = core; k1p = PK_MINUS; y1p = 1; k1n = PK_STAGE2;
+                R2 = well; k2p = PK_PLUS; y2p = y_in; k2n = PK_PLUS; y2n = y_in;
             } else {
-                double w = r.bij * r.bij - r.vijsq * diff;
-                tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8;
+                R1 = well; k1p = PK_MINUS; y1p = y_out;
             }
-        } else if (r.bij < 0.0) {
-            double w = r.bij * r.bij - r.vijsq * diff;
-            if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 9; }
-        }
-    } else if (evcode == 16) {                                      /* sqwel.f:5-67 */
-        double diff = r.rijsq - T.welldia_sq[a][b];
-        if (r.bij < 0.0) {
-            if (diff < 0.0) {
-                double corediscr = r.bij * r.bij - r.vijsq * (r.rijsq - T.sigma_sq[a][b]);
-                if (corediscr > 0.0) { tij = (-r.bij - sqrt(corediscr)) / r.vijsq; type = 1; }
-                else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8; }
-            } else {
-                double w = r.bij * r.bij - r.vijsq * diff;
-                if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 4; }
-            }
-        } else if (diff < 0.0) {
-            double w = r.bij * r.bij - r.vijsq * diff;
-            tij = (-r.bij + sqrt(w)) / r.vijsq; type = 8;
-        }
-    } else if (evcode >= 40) {                                      /* sqshlder.f:5-66 */
-        double diff = r.rijsq - T.shlddia_sq[a][b];
-        if (r.bij < 0.0) {
-            if (diff < 0.0) {
-                double corediscr = r.bij * r.bij - r.vijsq * (r.rijsq - T.sigma_sq[a][b]);
-                if (corediscr > 0.0) { tij = (-r.bij - sqrt(corediscr)) / r.vijsq; type = 1; }
-                else { double w = r.bij * r.bij - r.vijsq * diff; tij = (-r.bij + sqrt(w)) / r.vijsq; type = 10; }
-            } else {
-                double w = r.bij * r.bij - r.vijsq * diff;
-                if (w > 0.0) { tij = (-r.bij - sqrt(w)) / r.vijsq; type = 12; }
-            }
-        } else if (diff < 0.0) {
-            double w = r.bij * r.bij - r.vijsq * diff;
-            tij = (-r.bij + sqrt(w)) / r.vijsq; type = 10;
+        } else if (inside) {
+            R1 = well; k1p = PK_PLUS; y1p = y_in; k1n = PK_PLUS; y1n = y_in;
         }
     } else {
-        return false;
+        valid = false;
     }
-    return true;
+    double b2 = r.bij * r.bij;
+    double c = r.rijsq - R1;
+    double D = b2 - r.vijsq * c;
+    int k, y;
+    if (d_gt0(D)) { k = k1p; y = y1p; } else { k = k1n; y = y1n; }
+    if (k == PK_STAGE2) {
+        c = r.rijsq - R2;
+        D = b2 - r.vijsq * c;
+        if (d_gt0(D)) { k = k2p; y = y2p; } else { k = k2n; y = y2n; }
+    }
+    tij = DMD_BIG; type = 0;
+    if (k != PK_NONE) {
+        double sq = sqrt(D);
+        bool bond = k == PK_BOND;
+        double X = bond ? sq : d_negate(r.bij);
+        double Y = bond ? r.bij : (k == PK_MINUS ? d_negate(sq) : sq);
+        double s1 = X + Y;
+        double num = bond ? d_negate(c) : s1;
+        double den = bond ? s1 : r.vijsq;
+        tij = num / den;
+        type = y;
+    }
+    return valid;
 }
 
 #endif /* DMD_ENGINE_CUH */

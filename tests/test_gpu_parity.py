@@ -87,3 +87,33 @@ def test_diagnostics_match(built):
         assert gd[k] == pytest.approx(od[k], rel=1e-12, abs=1e-12), k
     for k in ("hb_alpha", "hb_ii", "hb_ij", "coll", "n_pair", "n_ghost", "n_interval", "n_updates"):
         assert gd[k] == od[k], k
+
+
+def test_hbond_events(built):
+    """A crowded cold system in which H-bonds form and break: captures,
+    escapes, bounces and the shoulder events of repuls_add all occur."""
+    spec = dense_system(n_chains=10, L=10, box=38.0, tstar=0.12, seed=21, rng_seed=5)
+    log = _compare_run(spec, 400000)
+    kinds = set(np.unique(log["type"]).tolist())
+    assert {14, 16, 20, 21, 22, 26}.issubset(kinds), kinds
+
+
+def test_c3_replicas_batched(built):
+    """Replicas of the 32-replica workload, advanced together in one launch,
+    each against its own serial oracle run."""
+    specs = systems.config_c3(32, seed=1)
+    small = sorted(specs, key=lambda s: s.n_beads)[:4] + [specs[31]]
+    for s in small:
+        systems.generate(s)
+    n = 30000
+    b = Batch(small)
+    logs = b.run(n, log_capacity=n + 64)
+    for r, s in enumerate(small):
+        ora = Oracle(s)
+        olog = ora.run(n, log_capacity=n + 64)
+        k = first_mismatch(logs[r], olog)
+        assert k < 0, f"replica {r}: logs diverge at {k}:\n{describe(logs[r], olog, k)}"
+        st, ost = b.state(r), ora.state()
+        for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity"):
+            assert np.array_equal(st[key], ost[key]), (r, key)
+    b.close()
