@@ -121,6 +121,7 @@ void build_tables(HostSys &H, const dmd_tables *T, double boxl) {
         for (int b = 0; b < DMD_NT; ++b) {
             double p = D.evp1[15];
             D.ncfac_sq[a][b] = D.sigma_sq[a][b] * p * p;
+            D.core15_sq[a][b] = D.sigma_sq[a][b] * (p * p);
         }
     for (int l = 0; l < DMD_NC; ++l) { D.evp2_sq[l] = D.evp2[l] * D.evp2[l]; D.evp3_sq[l] = D.evp3[l] * D.evp3[l]; }
     /* kept for nbor_setup: scaled bead diameters and the side-chain wells */
@@ -309,6 +310,11 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
     for (int b = 0; b < H.N; ++b) { H.blmin_sq[b] = H.blmin[b] * H.blmin[b]; H.blmax_sq[b] = H.blmax[b] * H.blmax[b]; }
 
     build_tables(H, T, S->boxl);
+    for (int a = 0; a < DMD_NT; ++a)
+        for (int b = 0; b < DMD_NT; ++b) {
+            double bmi = bmass[a], bmj = bmass[b];
+            H.tab.rmass[a][b] = (bmi + bmj) != 0.0 ? 2 * bmi * bmj / (bmi + bmj) : 0.0;
+        }
     H.tab.setemp = cfg->tstar * 12.0;
     H.tab.avegtime = 0.00005 / std::sqrt(H.tab.setemp);
 
@@ -407,7 +413,8 @@ size_t layout(const HostSys &H, DSys &d, char *base) {
     d.upn = P.take<int>(N); d.dnn = P.take<int>(N);
     d.cell_count = P.take<int>(nc3 + 1); d.cell_start = P.take<int>(nc3 + 1); d.cell_beads = P.take<int>(N);
     d.l1i = P.take<int>(H.nl1); d.l2i = P.take<int>(H.nl2);
-    d.key = P.take<long long>(NE); d.owner = P.take<unsigned long long>(N);
+    d.l1k = P.take<long long>(H.nl1); d.l2k = P.take<long long>(H.nl2);
+    d.key = P.take<long long>(NE); d.owner = P.take<unsigned int>(N);
     return P.off + 256;
 }
 
@@ -578,7 +585,10 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     }
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
     CK(cudaEventRecord(B.ev0, B.st));
-    CK(dmd_launch_run(B.d_sys, n, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr, B.st));
+    int max_beads = 0;
+    for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
+    CK(dmd_launch_run(B.d_sys, n, max_beads, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr,
+                      B.st));
     CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
     float ms = 0.f;

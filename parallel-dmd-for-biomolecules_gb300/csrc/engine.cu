@@ -47,6 +47,9 @@
 #define META_MAX 16
 #define TG_MAX 64         /* full re-predictions per round (i, j, marked beads) */
 #define CASC_MAX 64
+#define RSET_MAX 384
+#define OWN_SMEM_MAX 16384   /* systems up to this size keep the claim table in shared memory */
+#define DMD_TICKET_SEQ_MAX ((1 << 27) - 2)
 #define FULL 0xffffffffu
 
 /* Optional phase timers of k_run (build with -DDMD_PHASE_TIMERS): thread 0
@@ -110,6 +113,8 @@ struct WarpArea {
     double sij[12];
     int8_t colt_i;
     int casc[CASC_MAX];
+    int rset[RSET_MAX];            /* beads of the footprint claim */
+    int nrset;
     /* the event */
     int i, j, ct, evcode, xpulse, conflict, casc_over;
     int err, err_info;
@@ -135,6 +140,7 @@ struct SharedState {
     int red_i[NWARPS * 4];
     int rebuild;
     int touched[8];
+    int bseq;            /* footprint claims of this launch (ticket base) */
 };
 
 /* where an error goes: the system's status, or the status of one
@@ -172,26 +178,37 @@ __device__ __forceinline__ void set_pred(const DSys &S, int b, double t, int p, 
 /* ------------------------------------------------------------------ */
 /* tournament over the integer keys                                    */
 /* ------------------------------------------------------------------ */
+/* level-1 group g: argmin over its 32 keys (lowest index on ties); the 32
+ * loads are issued before the first comparison */
 __device__ void l1_update(const DSys &S, int g, int NE) {
-    int lo = g * 32, hi = min(lo + 32, NE);
-    int best = lo;
-    long long bk = S.key[lo];
-    for (int e = lo + 1; e < hi; ++e) {
-        long long k = S.key[e];
-        if (k < bk) { bk = k; best = e; }
-    }
-    S.l1i[g] = best;
+    int lo = g * 32, n = min(32, NE - lo);
+    long long k[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) k[q] = q < n ? S.key[lo + q] : DMD_KEY_INF;
+    int best = 0;
+    long long bk = k[0];
+#pragma unroll
+    for (int q = 1; q < 32; ++q)
+        if (k[q] < bk) { bk = k[q]; best = q; }
+    S.l1i[g] = lo + best;
+    S.l1k[g] = bk;
 }
 __device__ void l2_update(const DSys &S, int h) {
-    int lo = h * 32, hi = min(lo + 32, S.nl1);
+    int lo = h * 32, n = min(32, S.nl1 - lo);
+    long long k[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) k[q] = q < n ? S.l1k[lo + q] : DMD_KEY_INF;
     int best = S.l1i[lo];
-    long long bk = S.key[best];
-    for (int g = lo + 1; g < hi; ++g) {
-        int e = S.l1i[g];
-        long long k = S.key[e];
-        if (key_less(k, e, bk, best)) { bk = k; best = e; }
+    long long bk = k[0];
+#pragma unroll
+    for (int q = 1; q < 32; ++q) {
+        if (q < n) {
+            int e = S.l1i[lo + q];
+            if (key_less(k[q], e, bk, best)) { bk = k[q]; best = e; }
+        }
     }
     S.l2i[h] = best;
+    S.l2k[h] = bk;
 }
 __device__ void cta_tree_rebuild(const DSys &S) {
     int NE = S.N + 3;
@@ -206,7 +223,7 @@ __device__ int warp_tree_root(const DSys &S, long long &kroot) {
     int best = INT_MAX;
     for (int h = lane; h < S.nl2; h += 32) {
         int e = S.l2i[h];
-        long long k = S.key[e];
+        long long k = S.l2k[h];
         if (key_less(k, e, bk, best)) { bk = k; best = e; }
     }
 #pragma unroll
@@ -383,29 +400,21 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
     int bump = 0;
     if (lane == 0) {
         double bij = w.bij;
-        double bmi = S.bm[i], bmj = S.bm[j];
-        double rmass = 2 * bmi * bmj / (bmi + bmj);
         int a = S.ident[i], b = S.ident[j];
+        /* the masses, squared diameters and bond windows come from tables
+         * computed in the same operation order (bm(i) = mass(identity(i))) */
+        double rmass = T.rmass[a][b];
+        bool side = evcode >= 10 && evcode <= 12;
         if (ct == 2) {
-            double blmin, blmax; bond_limits(S, i, evcode, blmin, blmax);
-            ratio = rmass * bij / (blmin * blmin);
+            double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];
+            ratio = rmass * bij / lo;
         } else if (ct == 3) {
-            double blmin, blmax; bond_limits(S, i, evcode, blmin, blmax);
-            ratio = rmass * bij / (blmax * blmax);
+            double hi = side ? S.blmax_sq[i] : T.evp3_sq[evcode];
+            ratio = rmass * bij / hi;
         } else if (ct == 1) {
             double sigsq;
-            if (evcode == 15) {
-                if (S.bptnr[i] == j) { double p = T.evp1[evcode]; sigsq = T.sigma_sq[a][b] * (p * p); }
-                else sigsq = T.sigma_sq[a][b];
-            } else {
-                double p = T.evp1[evcode];
-                sigsq = T.sigma_sq[a][b] * (p * p);
-                if (evcode >= 22 && evcode <= 26) {
-                    int k = a > b ? a : b;
-                    double s = T.sqz610[evcode - 21][k];
-                    sigsq = sigsq * (s * s);
-                }
-            }
+            if (evcode == 15) sigsq = S.bptnr[i] == j ? T.core15_sq[a][b] : T.sigma_sq[a][b];
+            else sigsq = T.core_sq[core_slot(evcode)][a][b];
             ratio = rmass * bij / sigsq;
         } else if (ct == 4) {
             double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
@@ -786,12 +795,17 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             W.tg_b[t] = b;
             W.tg_k[t] = Hkey; W.tg_p[t] = -1; W.tg_raw[t] = Hraw; W.tg_y[t] = -1;
         }
-        /* task offsets: an inclusive scan of (upn + 3) over the targets */
+        /* task offsets: an inclusive scan over the targets of the up-list
+         * length plus the extras above the bead */
         int run = 0;
         for (int base = 0; base < ntg; base += 32) {
             int t = base + lane;
             int b = t < ntg ? W.tg_b[t] : -1;
-            int c = b >= 0 ? S.upn[b] + 3 : 0;
+            int c = 0;
+            if (b >= 0) {
+                c = S.upn[b];
+                for (int k = 0; k < 3; ++k) c += S.er[4 * b + k] > b;
+            }
             int incl = c;
             for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
             if (t < ntg) W.tg_base[t] = run + incl - c;
@@ -819,7 +833,16 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
                 int b = W.tg_b[lo];
                 int k = rel - W.tg_base[lo];
                 int nu = S.upn[b];
-                int m = k < nu ? S.up[(size_t)b * S.cap + k] : S.er[4 * b + (k - nu)];
+                int m;
+                if (k < nu) m = S.up[(size_t)b * S.cap + k];
+                else {
+                    int want = k - nu;
+                    m = -1;
+                    for (int k2 = 0; k2 < 3; ++k2) {
+                        int e = S.er[4 * b + k2];
+                        if (e > b) { if (want == 0) { m = e; break; } --want; }
+                    }
+                }
                 if (m > b) { pa = b; pbb = m; code = pair_code(S, m, b, hbonds); }
             }
             double tij = 0.0;
@@ -939,23 +962,24 @@ __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
 /* ------------------------------------------------------------------ */
 /* footprints of a batch candidate                                     */
 /* ------------------------------------------------------------------ */
-/* Claim (claim = true) or test the footprint of one candidate.  A claim
- * raises owner[b] to the candidate's ticket, (batch sequence) * 64 +
- * (63 - position), so that after the claims every bead holds the ticket of
- * the earliest candidate that touches it; the test reports whether an
- * earlier candidate holds any bead of this one.  Tickets grow from batch to
- * batch, so the array needs no reset.  The set covers every bead the event
- * reads or writes in the serial order: i, j, their extra_repuls, their
- * H-bond helpers and those of their H-bond partners, both neighbour lists of
- * i and j, and for every bead that may need a full re-prediction its up
- * list and extras. */
-__device__ bool warp_footprint(const DSys &S, WarpArea &W, unsigned long long ticket, int i, int j, bool claim) {
+/* Claim the footprint of one candidate: raise own[b] to the candidate's
+ * ticket, (batch sequence) * 32 + (31 - position), for every bead b the
+ * event reads or writes in the serial order, and list those beads in W.rset.
+ * After all claims every bead holds the ticket of the earliest candidate that
+ * touches it, so warp_footprint_test() finds whether an earlier candidate
+ * holds any bead of this one.  Tickets grow from batch to batch, so the table
+ * needs no reset.  The set: i, j, their extra_repuls, their H-bond helpers and
+ * those of their H-bond partners, both neighbour lists of i and j, and for
+ * every bead that may need a full re-prediction its up list and extras. */
+__device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
     int lane = threadIdx.x & 31;
-    bool conflict = false;
+    if (lane == 0) { W.nrset = 0; W.casc_over = 0; }
+    __syncwarp();
     auto visit = [&](int b) {
         if (b < 0) return;
-        if (claim) atomicMax(&S.owner[b], ticket);
-        else if (S.owner[b] > ticket) conflict = true;
+        atomicMax(&own[b], ticket);
+        int pos = atomicAdd(&W.nrset, 1);
+        if (pos < RSET_MAX) W.rset[pos] = b;
     };
     /* fixed part: 18 entries on lanes 0..17 */
     if (lane < 18) {
@@ -981,37 +1005,34 @@ __device__ bool warp_footprint(const DSys &S, WarpArea &W, unsigned long long ti
     for (int q = lane; q < di; q += 32) visit(DI[q]);
     for (int q = lane; q < uj; q += 32) visit(UJ[q]);
     for (int q = lane; q < dj; q += 32) visit(DJ[q]);
-    /* beads that may be fully re-predicted (listed once, at the claim) */
-    if (claim) {
-        int nc = 0;
-        for (int base = 0; base < di + dj; base += 32) {
-            int q = base + lane;
-            int l = -1;
-            if (q < di) { l = DI[q]; if (S.nptnr[l] != i) l = -1; }
-            else if (q < di + dj) { l = DJ[q - di]; if (S.nptnr[l] != j) l = -1; }
-            unsigned m = __ballot_sync(FULL, l >= 0);
-            int pos = nc + __popc(m & ((1u << lane) - 1));
-            if (l >= 0 && pos < CASC_MAX - 10) W.casc[pos] = l;
-            nc += __popc(m);
-        }
-        if (lane == 0) W.casc_over = nc > CASC_MAX - 10;
-        nc = min(nc, CASC_MAX - 10);
-        if (lane < 10) {
-            int b;
-            if (lane < 3) b = S.er[4 * i + lane];
-            else if (lane < 6) b = S.er[4 * j + lane - 3];
-            else {
-                int x = lane < 8 ? i : j, h1, h2;
-                own_helpers(S, x, h1, h2);
-                b = (lane & 1) ? h2 : h1;
-            }
-            W.casc[nc + lane] = b;
-        }
-        if (lane == 0) W.ncasc = nc + 10;
-        __syncwarp();
+    /* beads that may be fully re-predicted */
+    int nc = 0;
+    for (int base = 0; base < di + dj; base += 32) {
+        int q = base + lane;
+        int l = -1;
+        if (q < di) { l = DI[q]; if (S.nptnr[l] != i) l = -1; }
+        else if (q < di + dj) { l = DJ[q - di]; if (S.nptnr[l] != j) l = -1; }
+        unsigned m = __ballot_sync(FULL, l >= 0);
+        int pos = nc + __popc(m & ((1u << lane) - 1));
+        if (l >= 0 && pos < CASC_MAX - 10) W.casc[pos] = l;
+        nc += __popc(m);
     }
+    bool over = nc > CASC_MAX - 10;
+    nc = min(nc, CASC_MAX - 10);
+    if (lane < 10) {
+        int b;
+        if (lane < 3) b = S.er[4 * i + lane];
+        else if (lane < 6) b = S.er[4 * j + lane - 3];
+        else {
+            int x = lane < 8 ? i : j, h1, h2;
+            own_helpers(S, x, h1, h2);
+            b = (lane & 1) ? h2 : h1;
+        }
+        W.casc[nc + lane] = b;
+    }
+    __syncwarp();
     /* their up lists and extras, one cascade bead per lane */
-    int nc = W.ncasc;
+    nc += 10;
     for (int c = lane; c < nc; c += 32) {
         int l = W.casc[c];
         if (l < 0) continue;
@@ -1020,6 +1041,16 @@ __device__ bool warp_footprint(const DSys &S, WarpArea &W, unsigned long long ti
         for (int q = 0; q < ul; ++q) visit(UL[q]);
         visit(S.er[4 * l + 0]); visit(S.er[4 * l + 1]); visit(S.er[4 * l + 2]);
     }
+    __syncwarp();
+    /* an incomplete list (cascade or bead list overflow) ends the batch here */
+    if (lane == 0) W.casc_over = over || W.nrset > RSET_MAX;
+    __syncwarp();
+}
+__device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, unsigned ticket) {
+    int lane = threadIdx.x & 31;
+    bool conflict = false;
+    int n = min(W.nrset, RSET_MAX);
+    for (int q = lane; q < n; q += 32) conflict |= own[W.rset[q]] > ticket;
     return __any_sync(FULL, conflict);
 }
 
@@ -1386,7 +1417,7 @@ __device__ int cta_candidates(const DSys &S, SharedState &sh, int root, long lon
         long long kc = sh.kcut;
         /* groups whose minimum lies below the cut */
         for (int g = threadIdx.x; g < S.nl1; g += blockDim.x) {
-            if (S.key[S.l1i[g]] < kc) {
+            if (S.l1k[g] < kc) {
                 int s = atomicAdd(&sh.ngroups, 1);
                 if (s < 256) sh.groups[s] = g;
             }
@@ -1458,7 +1489,6 @@ __global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int 
     const DSys &S = S_sh;
     int hbonds = hbonds_mask & 1;
     if (threadIdx.x == 0) { sh.sc = *S.sc; }
-    for (int b = threadIdx.x; b < S.N; b += blockDim.x) S.owner[b] = 0ull;
     __syncthreads();
     cta_rebuild(S, sh, hbonds);
     if (threadIdx.x == 0) *S.sc = sh.sc;
@@ -1466,7 +1496,7 @@ __global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int 
 
 __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target, int hbonds_mask,
                                                      const int *chain_start, const int *chain_len,
-                                                     const int *chain_off, dmd_diag *outputs) {
+                                                     const int *chain_off, dmd_diag *outputs, int own_cap) {
     extern __shared__ WarpArea warea[];
     __shared__ SharedState sh;
     __shared__ DSys S_sh;
@@ -1485,7 +1515,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     if (threadIdx.x == 0) {
         sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0;
         sh.delta = sh.sc.interval * 0.05;
+        sh.bseq = 0;
     }
+    /* footprint claim table: shared memory for systems that fit, else the
+     * system's global array; cleared at every launch */
+    unsigned *own = N <= own_cap ? (unsigned *)(warea + NWARPS) : S.owner;
+    for (int b = threadIdx.x; b < N; b += blockDim.x) own[b] = 0u;
     __syncthreads();
     DMD_PHASE_START();
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
@@ -1532,20 +1567,28 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             /* footprints: claim, test, release */
             int P = m;
             if (m > 1) {
-                unsigned long long ticket = (unsigned long long)(sh.sc.bseq + 1) * 64ull + (unsigned long long)(63 - warp);
+                if (sh.bseq >= DMD_TICKET_SEQ_MAX) {   /* tickets exhausted: clear the table */
+                    __syncthreads();
+                    for (int b = threadIdx.x; b < N; b += blockDim.x) own[b] = 0u;
+                    __syncthreads();
+                    if (threadIdx.x == 0) sh.bseq = 0;
+                    __syncthreads();
+                }
+                unsigned ticket = ((unsigned)(sh.bseq + 1) << 5) | (unsigned)(31 - warp);
                 if (warp < m) {
                     int i = sh.sort_idx[warp];
-                    warp_footprint(S, W, ticket, i, S.nptnr[i], true);
+                    warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
                 }
                 __syncthreads();
+                DMD_PHASE(10);
                 if (warp < m) {
-                    int i = sh.sort_idx[warp];
-                    bool c = warp_footprint(S, W, ticket, i, S.nptnr[i], false);
+                    bool c = warp_footprint_test(W, own, ticket);
                     if (lane == 0) W.conflict = c;
                 }
                 __syncthreads();
+                DMD_PHASE(11);
                 if (threadIdx.x == 0) {
-                    sh.sc.bseq += 1;
+                    sh.bseq += 1;
                     /* the longest conflict-free prefix; an incomplete footprint
                      * (cascade list overflow) ends the batch after its event */
                     int p = m;
@@ -1717,14 +1760,17 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, cons
 /* ------------------------------------------------------------------ */
 /* launch wrappers                                                     */
 /* ------------------------------------------------------------------ */
-static size_t run_smem() { return sizeof(WarpArea) * NWARPS; }
+static_assert(sizeof(WarpArea) * NWARPS + OWN_SMEM_MAX * sizeof(unsigned) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
+              "k_run shared memory above the 227 KB a block may use");
+static size_t run_smem(int own_cap) { return sizeof(WarpArea) * NWARPS + (size_t)own_cap * sizeof(unsigned); }
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st) {
     k_init<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
     return cudaGetLastError();
 }
-cudaError_t dmd_launch_run(DSys *d_systems, int nsys, long long target, int hbonds, const int *chain_start,
-                           const int *chain_len, const int *chain_off, dmd_diag *outputs, cudaStream_t st) {
+cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, long long target, int hbonds,
+                           const int *chain_start, const int *chain_len, const int *chain_off, dmd_diag *outputs,
+                           cudaStream_t st) {
     static std::mutex mu;
     static bool done[256];
     int dev = 0;
@@ -1733,12 +1779,14 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, long long target, int hbon
     {
         std::lock_guard<std::mutex> lock(mu);
         if (dev >= 0 && dev < 256 && !done[dev]) {
-            e = cudaFuncSetAttribute(k_run, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem());
+            e = cudaFuncSetAttribute(k_run, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(OWN_SMEM_MAX));
             if (e != cudaSuccess) return e;
             done[dev] = true;
         }
     }
-    k_run<<<nsys, NTHREADS, run_smem(), st>>>(d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off, outputs);
+    int own_cap = max_beads <= OWN_SMEM_MAX ? max_beads : 0;
+    k_run<<<nsys, NTHREADS, run_smem(own_cap), st>>>(d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off,
+                                                     outputs, own_cap);
     return cudaGetLastError();
 }
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,

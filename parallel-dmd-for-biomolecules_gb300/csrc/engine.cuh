@@ -57,6 +57,8 @@ struct DTab {
      * bonded H-bond pair's inner core (code 15), the bond windows */
     double core_sq[14][DMD_NT][DMD_NT];
     double ncfac_sq[DMD_NT][DMD_NT];
+    double core15_sq[DMD_NT][DMD_NT];    /* eventdyn.f's bonded H-bond core (code 15) */
+    double rmass[DMD_NT][DMD_NT];        /* 2*m_a*m_b/(m_a+m_b), code/eventdyn.f:40 */
     double evp2_sq[DMD_NC], evp3_sq[DMD_NC];
 };
 __host__ __device__ __forceinline__ int core_slot(int code) { return code <= 3 ? code : code - 13; }
@@ -99,13 +101,14 @@ struct DSys {
     int8_t *colt;
     uint8_t *queued;
     long long *key;                /* ordered integer key of (queued ? tim : +inf), N + 3 entries */
-    unsigned long long *owner;     /* footprint tickets, N entries (0 = never claimed) */
+    unsigned int *owner;           /* footprint tickets, N entries, when not in shared memory */
     int *up, *dn;                  /* neighbour lists [N*cap] */
     int8_t *upc;                   /* static pair code of each up entry */
     int *upn, *dnn;
     int *cell_count, *cell_start, *cell_beads;  /* rebuild grid */
     int *l1i;                      /* tournament level 1: argmin of 32 entries */
     int *l2i;                      /* level 2: argmin of 32 level-1 groups */
+    long long *l1k, *l2k;          /* the keys of those minima */
     int nl1, nl2;
     void *log;                     /* dmd_event ring or NULL */
     long long log_cap;
