@@ -220,6 +220,14 @@ int dmd_batch_get_state(dmd_batch *b, int32_t r, double *x, double *y, double *z
                         double *t, double *tfalse, int64_t *coll);
 int dmd_batch_diagnostics(dmd_batch *b, int32_t r, dmd_diag *out);
 double dmd_batch_last_run_ms(dmd_batch *b);
+/* CTAs (one thread-block cluster) that advance each system: 1, 2, 4 or 8,
+ * or 0 (default) to let the library choose from the number of systems and
+ * what the GPU can hold at once.  Results do not depend on it: the
+ * committed event sequence is the serial one for every value. */
+int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas);
+int dmd_set_cluster(dmd_handle *h, int32_t ctas);
+/* the cluster size the last run used */
+int32_t dmd_batch_cluster(dmd_batch *b);
 void dmd_batch_destroy(dmd_batch *b);
 const char *dmd_batch_last_error(dmd_batch *b);
 

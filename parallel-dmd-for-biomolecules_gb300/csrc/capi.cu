@@ -391,7 +391,9 @@ struct Pool {
     }
 };
 
-size_t layout(const HostSys &H, DSys &d, char *base) {
+/* for_run: the arrays only the event loop uses (down-list codes, claim
+ * tables); the allocation-free prediction pass leaves them out */
+size_t layout(const HostSys &H, DSys &d, char *base, bool for_run = true) {
     Pool P{base, 0};
     size_t N = H.N, NE = H.N + 3, cap = H.cap;
     size_t nc3 = (size_t)H.ncell * H.ncell * H.ncell;
@@ -410,11 +412,12 @@ size_t layout(const HostSys &H, DSys &d, char *base) {
     d.ovc = P.take<int8_t>(4 * N);
     d.tim = P.take<double>(NE); d.nptnr = P.take<int>(NE); d.colt = P.take<int8_t>(NE); d.queued = P.take<uint8_t>(NE);
     d.up = P.take<int>(N * cap); d.dn = P.take<int>(N * cap); d.upc = P.take<int8_t>(N * cap);
+    d.dnc = for_run ? P.take<int8_t>(N * cap) : nullptr;
     d.upn = P.take<int>(N); d.dnn = P.take<int>(N);
     d.cell_count = P.take<int>(nc3 + 1); d.cell_start = P.take<int>(nc3 + 1); d.cell_beads = P.take<int>(N);
     d.l1i = P.take<int>(H.nl1); d.l2i = P.take<int>(H.nl2);
     d.l1k = P.take<long long>(H.nl1); d.l2k = P.take<long long>(H.nl2);
-    d.key = P.take<long long>(NE); d.owner = P.take<unsigned int>(N);
+    d.key = P.take<long long>(NE); d.owner = for_run ? P.take<unsigned int>(3 * N) : nullptr;
     return P.off + 256;
 }
 
@@ -441,10 +444,28 @@ struct dmd_batch {
     double last_ms = 0.0;
     std::string err;
     int ready = 0;
+    int cluster = 0;        /* CTAs per system: 1, 2, 4, 8, or 0 = chosen at run time */
+    int last_cluster = 0;   /* what the last run used */
 };
 struct dmd_handle { dmd_batch b; };
 
 namespace {
+
+/* CTAs per system when the caller has not chosen: the largest of 4 and 2
+ * for which every system's cluster can be resident at once, else 1 */
+int auto_cluster(int nsys) {
+    static int max_active[9] = {0};
+    for (int C : {4, 2}) {
+        if (max_active[C] == 0) {
+            int v = 0;
+            if (dmd_max_active_clusters(C, &v) != cudaSuccess) v = -1;
+            cudaGetLastError();
+            max_active[C] = v;
+        }
+        if (max_active[C] > 0 && nsys <= max_active[C]) return C;
+    }
+    return 1;
+}
 
 int upload(dmd_batch &B) {
     std::string &err = B.err;
@@ -587,7 +608,9 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     CK(cudaEventRecord(B.ev0, B.st));
     int max_beads = 0;
     for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
-    CK(dmd_launch_run(B.d_sys, n, max_beads, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr,
+    int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
+    B.last_cluster = C;
+    CK(dmd_launch_run(B.d_sys, n, max_beads, C, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr,
                       B.st));
     CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
@@ -703,6 +726,14 @@ void dmd_batch_destroy(dmd_batch *b) {
 }
 const char *dmd_batch_last_error(dmd_batch *b) { return b ? b->err.c_str() : "null handle"; }
 double dmd_batch_last_run_ms(dmd_batch *b) { return b ? b->last_ms : 0.0; }
+int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas) {
+    if (!b) return DMD_E_INPUT;
+    if (ctas != 0 && ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8) { b->err = "cluster size must be 0, 1, 2, 4 or 8"; return DMD_E_INPUT; }
+    b->cluster = ctas;
+    return 0;
+}
+int32_t dmd_batch_cluster(dmd_batch *b) { return b ? b->last_cluster : 0; }
+int dmd_set_cluster(dmd_handle *h, int32_t ctas) { return h ? dmd_batch_set_cluster(&h->b, ctas) : DMD_E_INPUT; }
 double dmd_last_run_ms(dmd_handle *h) { return h ? h->b.last_ms : 0.0; }
 
 int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, dmd_handle **out) {
@@ -815,7 +846,7 @@ int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, co
     cudaError_t ce = dmd_noalloc_scratch(&base);
     if (ce != cudaSuccess) return fail_msg(DMD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce));
     DSys d{};
-    size_t bytes = layout(H, d, (char *)base);
+    size_t bytes = layout(H, d, (char *)base, false);
     if (bytes > DMD_NOALLOC_SCRATCH_BYTES)
         return fail_msg(DMD_E_CAPACITY, "dmd_predict_all_noalloc: system needs " + std::to_string(bytes) +
                                             " scratch bytes, the array holds " + std::to_string(DMD_NOALLOC_SCRATCH_BYTES));

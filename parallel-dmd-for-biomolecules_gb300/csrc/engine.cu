@@ -34,6 +34,7 @@
 #include <stdint.h>
 #include <limits.h>
 
+#include <cooperative_groups.h>
 #include <mutex>
 
 #include "dmd.h"
@@ -46,10 +47,13 @@
 #define CAND_MAX 64
 #define META_MAX 16
 #define TG_MAX 64         /* full re-predictions per round (i, j, marked beads) */
+#define TMAP_MAX 256
 #define CASC_MAX 64
 #define RSET_MAX 384
-#define OWN_SMEM_MAX 16384   /* systems up to this size keep the claim table in shared memory */
-#define DMD_TICKET_SEQ_MAX ((1 << 27) - 2)
+#define WSET_MAX 16
+#define QSET_MAX 160
+#define OWN_SMEM_MAX 6144    /* systems up to this size keep the claim tables in shared memory */
+#define DMD_TICKET_SEQ_MAX ((1 << 25) - 2)
 #define FULL 0xffffffffu
 
 /* Optional phase timers of k_run (build with -DDMD_PHASE_TIMERS): thread 0
@@ -59,13 +63,24 @@
 #define DMD_PHASE_SLOTS 16
 #define DMD_PHASE_CTAS 1024
 __device__ long long g_phase_cycles[DMD_PHASE_CTAS][DMD_PHASE_SLOTS];
-#define DMD_PHASE_START() long long ph_t_ = clock64()
+#define DMD_PHASE_START(row) long long ph_t_ = clock64(); const int ph_row_ = (row)
 #define DMD_PHASE(k)                                                                       \
     do {                                                                                   \
-        if (threadIdx.x == 0 && blockIdx.x < DMD_PHASE_CTAS) {                             \
+        if (threadIdx.x == 0 && ph_row_ >= 0 && ph_row_ < DMD_PHASE_CTAS) {                \
             long long now_ = clock64();                                                    \
-            g_phase_cycles[blockIdx.x][(k)] += now_ - ph_t_;                               \
+            g_phase_cycles[ph_row_][(k)] += now_ - ph_t_;                                  \
             ph_t_ = now_;                                                                  \
+        }                                                                                  \
+    } while (0)
+/* sub-phases of one event's processing, on warp 0 of the first CTA only
+ * (row DMD_PHASE_CTAS - 1) */
+__device__ long long g_sub_last;
+#define DMD_SUB(k)                                                                         \
+    do {                                                                                   \
+        if (blockIdx.x == 0 && threadIdx.x == 0) {                                         \
+            long long now_ = clock64();                                                    \
+            if ((k) >= 0) g_phase_cycles[DMD_PHASE_CTAS - 1][(k)] += now_ - g_sub_last;    \
+            g_sub_last = now_;                                                             \
         }                                                                                  \
     } while (0)
 extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
@@ -73,8 +88,9 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
     return (int)cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(long long) * DMD_PHASE_SLOTS * nctas);
 }
 #else
-#define DMD_PHASE_START() do {} while (0)
+#define DMD_PHASE_START(row) do { (void)(row); } while (0)
 #define DMD_PHASE(k) do { (void)(k); } while (0)
+#define DMD_SUB(k) do { } while (0)
 #endif
 
 /* per-warp working area of one event (dynamic shared memory) */
@@ -83,6 +99,7 @@ struct WarpArea {
     /* down-list operations (bead, source) in the reference's order, and
      * the prediction of each operation's pair (time + tfalse, type) */
     int ops_l[OPS_MAX], ops_s[OPS_MAX];
+    int8_t ops_c[OPS_MAX];        /* static code of the pair, -1 if not listed */
     double op_t[OPS_MAX];
     int8_t op_y[OPS_MAX];
     /* distinct operation beads: bead, first operation, full-redo mark */
@@ -97,6 +114,7 @@ struct WarpArea {
     int tg_p[TG_MAX];
     double tg_raw[TG_MAX];
     int8_t tg_y[TG_MAX];
+    int8_t tmap[TMAP_MAX];        /* task -> target of the round */
     /* buffered predictions: bead, time, partner, type, queued */
     int pb[OPS_MAX + 2];
     double pt[OPS_MAX + 2];
@@ -113,8 +131,10 @@ struct WarpArea {
     double sij[12];
     int8_t colt_i;
     int casc[CASC_MAX];
-    int rset[RSET_MAX];            /* beads of the footprint claim */
-    int nrset;
+    int rset[RSET_MAX];            /* beads of the footprint claim: read, written, queue */
+    int wset[WSET_MAX];
+    int qset[QSET_MAX];
+    int nrset, nwset, nqset;
     /* the event */
     int i, j, ct, evcode, xpulse, conflict, casc_over;
     int err, err_info;
@@ -131,7 +151,7 @@ struct SharedState {
     int cand_idx[CAND_MAX];
     long long sort_key[CAND_MAX];
     int sort_idx[CAND_MAX];
-    int ncand, m, nbatch, nvalid, overflow;
+    int ncand, m, nbatch, nvalid, tick_reset;
     long long kcut;
     double delta;        /* time window of the candidate cut */
     int groups[256];
@@ -141,7 +161,26 @@ struct SharedState {
     int rebuild;
     int touched[8];
     int bseq;            /* footprint claims of this launch (ticket base) */
+    /* cluster exchange: the leader CTA (rank 0) publishes the batch, every
+     * CTA's warps report their candidate's results into the leader's slots,
+     * and the other CTAs copy what they need into their own fields */
+    int exitf, P, V;
+    long long coll0, log0;
+    double imax, tnow, tf_iv;
+    int c_conflict[CAND_MAX], c_over[CAND_MAX];
+    long long c_tnew_key[CAND_MAX];
+    int c_tnew_idx[CAND_MAX], c_err[CAND_MAX], c_err_info[CAND_MAX], c_ct[CAND_MAX];
+    double c_tf[CAND_MAX];
+    double red_max[16];
 };
+
+namespace cg = cooperative_groups;
+/* barrier over the CTAs of one system (the cluster), with release/acquire
+ * ordering of global and shared memory at cluster scope */
+__device__ __forceinline__ void csync(int C) {
+    if (C == 1) __syncthreads();
+    else cg::this_cluster().sync();
+}
 
 /* where an error goes: the system's status, or the status of one
  * speculative event (raised only if that event is committed) */
@@ -196,17 +235,17 @@ __device__ void l1_update(const DSys &S, int g, int NE) {
 __device__ void l2_update(const DSys &S, int h) {
     int lo = h * 32, n = min(32, S.nl1 - lo);
     long long k[32];
+    int ix[32];
 #pragma unroll
-    for (int q = 0; q < 32; ++q) k[q] = q < n ? S.l1k[lo + q] : DMD_KEY_INF;
-    int best = S.l1i[lo];
+    for (int q = 0; q < 32; ++q) {
+        k[q] = q < n ? S.l1k[lo + q] : DMD_KEY_INF;
+        ix[q] = q < n ? S.l1i[lo + q] : INT_MAX;
+    }
+    int best = ix[0];
     long long bk = k[0];
 #pragma unroll
-    for (int q = 1; q < 32; ++q) {
-        if (q < n) {
-            int e = S.l1i[lo + q];
-            if (key_less(k[q], e, bk, best)) { bk = k[q]; best = e; }
-        }
-    }
+    for (int q = 1; q < 32; ++q)
+        if (key_less(k[q], ix[q], bk, best)) { bk = k[q]; best = ix[q]; }
     S.l2i[h] = best;
     S.l2k[h] = bk;
 }
@@ -235,14 +274,10 @@ __device__ int warp_tree_root(const DSys &S, long long &kroot) {
     kroot = bk;
     return bk == DMD_KEY_INF ? -1 : best;
 }
-/* warp: refresh the level-1 groups of the given entries (level 2 after a sync) */
+/* warp: refresh the level-1 groups of the given entries */
 __device__ void warp_l1_refresh(const DSys &S, const int *entries, int n) {
     int lane = threadIdx.x & 31;
     for (int q = lane; q < n; q += 32) { int e = entries[q]; if (e >= 0) l1_update(S, e >> 5, S.N + 3); }
-}
-__device__ void warp_l2_refresh(const DSys &S, const int *entries, int n) {
-    int lane = threadIdx.x & 31;
-    for (int q = lane; q < n; q += 32) { int e = entries[q]; if (e >= 0) l2_update(S, e >> 10); }
 }
 
 /* ------------------------------------------------------------------ */
@@ -490,26 +525,13 @@ __device__ double warp_check_sigma(const DSys &S, int i, int j, double tf) {  /*
 /* one event on one warp                                               */
 /* ------------------------------------------------------------------ */
 /* snapshot of everything the collision of (i, j) may write */
+/* The positions, velocities and coltype of i and j, taken before every
+ * collision; the H-bond bookkeeping state (identity, partner, extra_repuls,
+ * overrides) of the beads it may touch is taken by lane_meta_snapshot()
+ * only when the collision is about to write it. */
 __device__ void warp_snapshot(const DSys &S, WarpArea &W, int i, int j) {
     int lane = threadIdx.x & 31;
-    if (lane == 0) {
-        int n = 0;
-        auto add = [&](int b) { if (b >= 0 && n < META_MAX) W.mb[n++] = b; };
-        add(i); add(j);
-        for (int k = 0; k < 4; ++k) { add(S.er[4 * i + k]); add(S.er[4 * j + k]); }
-        int h1, h2;
-        own_helpers(S, i, h1, h2); add(h1); add(h2);
-        own_helpers(S, j, h1, h2); add(h1); add(h2);
-        W.nmeta = n;
-        W.colt_i = S.colt[i];
-    }
-    __syncwarp();
-    for (int q = lane; q < W.nmeta; q += 32) {
-        int b = W.mb[q];
-        W.mident[q] = S.ident[b];
-        W.mbp[q] = S.bptnr[b];
-        for (int k = 0; k < 4; ++k) { W.mer[q][k] = S.er[4 * b + k]; W.movp[q][k] = S.ovp[4 * b + k]; W.movc[q][k] = S.ovc[4 * b + k]; }
-    }
+    if (lane == 0) { W.nmeta = 0; W.colt_i = S.colt[i]; }
     if (lane < 12) {
         int b = lane < 6 ? i : j, f = lane % 6;
         const double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
@@ -533,6 +555,23 @@ __device__ void warp_restore(const DSys &S, WarpArea &W) {
     }
     if (lane == 0) S.colt[W.i] = W.colt_i;
     __syncwarp();
+}
+
+__device__ void lane_meta_snapshot(const DSys &S, WarpArea &W, int i, int j) {
+    int n = 0;
+    auto add = [&](int b) { if (b >= 0 && n < META_MAX) W.mb[n++] = b; };
+    add(i); add(j);
+    for (int k = 0; k < 4; ++k) { add(S.er[4 * i + k]); add(S.er[4 * j + k]); }
+    int h1, h2;
+    own_helpers(S, i, h1, h2); add(h1); add(h2);
+    own_helpers(S, j, h1, h2); add(h1); add(h2);
+    for (int q = 0; q < n; ++q) {
+        int b = W.mb[q];
+        W.mident[q] = S.ident[b];
+        W.mbp[q] = S.bptnr[b];
+        for (int k = 0; k < 4; ++k) { W.mer[q][k] = S.er[4 * b + k]; W.movp[q][k] = S.ovp[4 * b + k]; W.movc[q][k] = S.ovc[4 * b + k]; }
+    }
+    W.nmeta = n;
 }
 
 /* worker block (code/main.F90:1432-1956) and master application
@@ -605,6 +644,7 @@ __device__ void warp_collision(const DSys &S, Err E, WarpArea &W, int i, int j, 
     }
     if (ct == 14 || ct == 15 || ct == 16) warp_bumpoff(S, i, j, evcode, tf);
     if (lane == 0) {
+        if (ct == 20 || ct == 21 || ct == 24 || ct == 25 || ct == 14 || ct == 16) lane_meta_snapshot(S, W, i, j);
         if (ct == 20) {
             if (id[i] + id[j] == 5) {
                 S.bptnr[i] = j; S.bptnr[j] = i;
@@ -715,38 +755,63 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
     {
         int cnt = S.dnn[i];
         const int *dn = S.dn + (size_t)i * S.cap;
-        for (int q = lane; q < cnt; q += 32) { W.ops_l[q] = dn[q]; W.ops_s[q] = i; }
+        const int8_t *dc = S.dnc ? S.dnc + (size_t)i * S.cap : nullptr;
+        for (int q = lane; q < cnt; q += 32) { W.ops_l[q] = dn[q]; W.ops_s[q] = i; W.ops_c[q] = dc ? dc[q] : (int8_t)-1; }
         n = cnt;
         if (lane == 0)
             for (int k = 0; k < 3; ++k) {
                 int l = S.er[4 * i + k];
-                if (l >= 0 && l < i) { W.ops_l[n] = l; W.ops_s[n] = i; ++n; }
+                if (l >= 0 && l < i) { W.ops_l[n] = l; W.ops_s[n] = i; W.ops_c[n] = -1; ++n; }
             }
         n = __shfl_sync(FULL, n, 0);
         if (j >= 0) {
             int cj = S.dnn[j];
             const int *dj = S.dn + (size_t)j * S.cap;
+            const int8_t *dcj = S.dnc ? S.dnc + (size_t)j * S.cap : nullptr;
             for (int base = 0; base < cj; base += 32) {
                 int q = base + lane;
                 int l = q < cj ? dj[q] : -1;
                 bool keep = q < cj && l != i;
                 unsigned m = __ballot_sync(FULL, keep);
                 int pos = n + __popc(m & ((1u << lane) - 1));
-                if (keep) { W.ops_l[pos] = l; W.ops_s[pos] = j; }
+                if (keep) { W.ops_l[pos] = l; W.ops_s[pos] = j; W.ops_c[pos] = dcj ? dcj[q] : (int8_t)-1; }
                 n += __popc(m);
             }
             if (lane == 0)
                 for (int k = 0; k < 3; ++k) {
                     int l = S.er[4 * j + k];
-                    if (l >= 0 && l < j) { W.ops_l[n] = l; W.ops_s[n] = j; ++n; }
+                    if (l >= 0 && l < j) { W.ops_l[n] = l; W.ops_s[n] = j; W.ops_c[n] = -1; ++n; }
                 }
             n = __shfl_sync(FULL, n, 0);
         }
     }
     __syncwarp();
+    DMD_SUB(2);
     /* 2. distinct beads (leaders), their first operation and mark */
     int nl = 0, nm = 0;
-    for (int base = 0; base < n; base += 32) {
+    if (n <= 32) {
+        /* one pass: lanes holding the same bead find each other in one step */
+        int q = lane;
+        bool in = q < n;
+        int l = in ? W.ops_l[q] : -1 - lane;
+        int src = in ? W.ops_s[q] : -1;
+        unsigned peers = __match_any_sync(FULL, l);
+        bool lead = in && (__ffs(peers) - 1) == lane;
+        int p0 = (in && l != i) ? S.nptnr[l] : -2;
+        unsigned hit = __ballot_sync(FULL, in && src == p0);
+        unsigned same = __match_any_sync(FULL, in ? ((long long)l << 32) | (unsigned)src : -1LL - lane);
+        unsigned dup = __ballot_sync(FULL, in && __popc(same) > 1);
+        bool mark = lead && l != i && ((hit | dup) & peers) != 0;
+        unsigned m = __ballot_sync(FULL, lead);
+        int pos = __popc(m & ((1u << lane) - 1));
+        unsigned mm = __ballot_sync(FULL, mark);
+        int mpos = __popc(mm & ((1u << lane) - 1));
+        if (lead) { W.lead_l[pos] = l; W.lead_q[pos] = (int16_t)q; W.lead_m[pos] = mark; }
+        if (mark) W.mk[mpos] = (int16_t)pos;
+        nl = __popc(m);
+        nm = __popc(mm);
+    }
+    for (int base = 0; n > 32 && base < n; base += 32) {
         int q = base + lane;
         bool lead = false, mark = false;
         int l = -1;
@@ -779,6 +844,7 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
         W.pb[0] = i; W.pb[1] = j;
     }
     __syncwarp();
+    DMD_SUB(3);
     const double Hraw = imax + DMD_LTSTEP - tf;   /* eventredo_up's starting time */
     const long long Hkey = okey(Hraw), imax_key = okey(imax);
     const int per_round = TG_MAX - 2;
@@ -813,28 +879,41 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
         }
         if (lane == 0) W.tg_base[ntg] = run;
         __syncwarp();
+        const bool mapped = run <= TMAP_MAX;
+        if (mapped) {   /* task -> target map, one target per lane */
+            for (int t = lane; t < ntg; t += 32)
+                for (int q = W.tg_base[t]; q < W.tg_base[t + 1]; ++q) W.tmap[q] = (int8_t)t;
+            __syncwarp();
+        }
         int nop = rd == 0 ? n : 0;
         int ntask = nop + run;
+        DMD_SUB(4);
         /* 4. every task of the round, 32 per pass, one predictor call site */
         for (int base = 0; base < ntask; base += 32) {
             int q = base + lane;
             int pa = -1, pbb = -1, code = 1, tgt = -1;
+            int st = -1;    /* the pair's static code when a list holds it */
             if (q < nop) {
                 pa = W.ops_l[q]; pbb = W.ops_s[q];
-                code = pair_code(S, pa, pbb, hbonds);
+                st = W.ops_c[q];
             } else if (q < ntask) {
                 int rel = q - nop;
-                int lo = 0, hi = ntg - 1;        /* last target with tg_base <= rel */
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (W.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
+                int lo;
+                if (mapped) lo = W.tmap[rel];
+                else {
+                    int hi = ntg - 1;                /* last target with tg_base <= rel */
+                    lo = 0;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (W.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
+                    }
                 }
                 tgt = lo;
                 int b = W.tg_b[lo];
                 int k = rel - W.tg_base[lo];
                 int nu = S.upn[b];
                 int m;
-                if (k < nu) m = S.up[(size_t)b * S.cap + k];
+                if (k < nu) { m = S.up[(size_t)b * S.cap + k]; st = S.upc[(size_t)b * S.cap + k]; }
                 else {
                     int want = k - nu;
                     m = -1;
@@ -843,7 +922,12 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
                         if (e > b) { if (want == 0) { m = e; break; } --want; }
                     }
                 }
-                if (m > b) { pa = b; pbb = m; code = pair_code(S, m, b, hbonds); }
+                if (m > b) { pa = b; pbb = m; }
+            }
+            /* ev_code(l, source) for a down operation, ev_code(m, b) for a full one */
+            if (pa >= 0) {
+                int a1 = q < nop ? pa : pbb, a2 = q < nop ? pbb : pa;
+                code = st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
             }
             double tij = 0.0;
             int ty = 0;
@@ -878,6 +962,7 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             }
             __syncwarp();
         }
+        DMD_SUB(5);
         /* 5. the full results: time = minimum + tfalse */
         for (int t = lane; t < ntg; t += 32) W.tg_raw[t] = W.tg_raw[t] + tf;
         __syncwarp();
@@ -930,6 +1015,7 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
         }
         __syncwarp();
     }
+    DMD_SUB(7);
     /* 7. the earliest new queued entry of this event */
     long long bk = DMD_KEY_INF;
     int bb = INT_MAX;
@@ -962,26 +1048,52 @@ __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
 /* ------------------------------------------------------------------ */
 /* footprints of a batch candidate                                     */
 /* ------------------------------------------------------------------ */
-/* Claim the footprint of one candidate: raise own[b] to the candidate's
- * ticket, (batch sequence) * 32 + (31 - position), for every bead b the
- * event reads or writes in the serial order, and list those beads in W.rset.
- * After all claims every bead holds the ticket of the earliest candidate that
- * touches it, so warp_footprint_test() finds whether an earlier candidate
- * holds any bead of this one.  Tickets grow from batch to batch, so the table
- * needs no reset.  The set: i, j, their extra_repuls, their H-bond helpers and
- * those of their H-bond partners, both neighbour lists of i and j, and for
- * every bead that may need a full re-prediction its up list and extras. */
+/* Footprint of one candidate, as three sets of beads:
+ *   R: beads whose state (position, velocity, identity, H-bond partner,
+ *      extra_repuls, pair-type overrides) the event reads: i, j, their
+ *      extra_repuls, the H-bond helpers of i, j and of their H-bond
+ *      partners, both neighbour lists of i and j, and for every bead that may
+ *      need a full re-prediction its up list and extras;
+ *   W: beads whose state the collision may write: i, j, their extra_repuls
+ *      and their own helpers (code/repuls_add.f, repuls_del_b.f, the
+ *      shoulders of main.F90:825-868) - W is part of R;
+ *   Q: beads whose event-queue entry the event reads and rewrites: i, j, the
+ *      down lists, the lower extras and the helpers that become extras.
+ * Candidate k conflicts with an earlier k' when R(k) meets W(k'), W(k) meets
+ * R(k') or Q(k) meets Q(k'): then the two do not commute.  Reading the same
+ * neighbour is no conflict.  A claim raises the three tables (own, own + N,
+ * own + 2N) to the candidate's ticket, (batch sequence) * 64 + (63 - slot),
+ * so that after all claims each entry holds the ticket of the earliest
+ * candidate whose set has the bead; tickets grow from batch to batch and
+ * the tables need no reset.  The beads are listed in W.rset/wset/qset for
+ * warp_footprint_test(). */
 __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
     int lane = threadIdx.x & 31;
-    if (lane == 0) { W.nrset = 0; W.casc_over = 0; }
+    const int N = S.N;
+    unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
+    if (lane == 0) { W.nrset = 0; W.nwset = 0; W.nqset = 0; W.casc_over = 0; }
     __syncwarp();
-    auto visit = [&](int b) {
+    auto visit_r = [&](int b) {
         if (b < 0) return;
-        atomicMax(&own[b], ticket);
+        atomicMax(&own_r[b], ticket);
         int pos = atomicAdd(&W.nrset, 1);
         if (pos < RSET_MAX) W.rset[pos] = b;
     };
-    /* fixed part: 18 entries on lanes 0..17 */
+    auto visit_w = [&](int b) {
+        if (b < 0) return;
+        atomicMax(&own_w[b], ticket);
+        int pos = atomicAdd(&W.nwset, 1);
+        if (pos < WSET_MAX) W.wset[pos] = b;
+        visit_r(b);
+    };
+    auto visit_q = [&](int b) {
+        if (b < 0) return;
+        atomicMax(&own_q[b], ticket);
+        int pos = atomicAdd(&W.nqset, 1);
+        if (pos < QSET_MAX) W.qset[pos] = b;
+        visit_r(b);
+    };
+    /* fixed part on lanes 0..17 */
     if (lane < 18) {
         int b = -1;
         if (lane == 0) b = i;
@@ -995,16 +1107,20 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
             own_helpers(S, x, h1, h2);
             b = (lane & 1) ? h2 : h1;
         }
-        visit(b);
+        if (lane < 14) visit_w(b);   /* i, j, extras, own helpers */
+        else visit_r(b);             /* the partners' helpers: read only */
+        /* queue entries: i, j, the lower extras (0..2) and the helpers */
+        bool q = lane < 2 || (lane >= 2 && lane < 5) || (lane >= 6 && lane < 9) || (lane >= 10 && lane < 14);
+        if (q) visit_q(b);
     }
     /* neighbour lists of i and j */
     int ui = S.upn[i], di = S.dnn[i], uj = S.upn[j], dj = S.dnn[j];
     const int *UI = S.up + (size_t)i * S.cap, *DI = S.dn + (size_t)i * S.cap;
     const int *UJ = S.up + (size_t)j * S.cap, *DJ = S.dn + (size_t)j * S.cap;
-    for (int q = lane; q < ui; q += 32) visit(UI[q]);
-    for (int q = lane; q < di; q += 32) visit(DI[q]);
-    for (int q = lane; q < uj; q += 32) visit(UJ[q]);
-    for (int q = lane; q < dj; q += 32) visit(DJ[q]);
+    for (int q = lane; q < ui; q += 32) visit_r(UI[q]);
+    for (int q = lane; q < di; q += 32) visit_q(DI[q]);
+    for (int q = lane; q < uj; q += 32) visit_r(UJ[q]);
+    for (int q = lane; q < dj; q += 32) visit_q(DJ[q]);
     /* beads that may be fully re-predicted */
     int nc = 0;
     for (int base = 0; base < di + dj; base += 32) {
@@ -1038,19 +1154,22 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
         if (l < 0) continue;
         int ul = S.upn[l];
         const int *UL = S.up + (size_t)l * S.cap;
-        for (int q = 0; q < ul; ++q) visit(UL[q]);
-        visit(S.er[4 * l + 0]); visit(S.er[4 * l + 1]); visit(S.er[4 * l + 2]);
+        for (int q = 0; q < ul; ++q) visit_r(UL[q]);
+        visit_r(S.er[4 * l + 0]); visit_r(S.er[4 * l + 1]); visit_r(S.er[4 * l + 2]);
     }
     __syncwarp();
-    /* an incomplete list (cascade or bead list overflow) ends the batch here */
-    if (lane == 0) W.casc_over = over || W.nrset > RSET_MAX;
+    /* an incomplete list (cascade or set overflow) ends the batch here */
+    if (lane == 0) W.casc_over = over || W.nrset > RSET_MAX || W.nwset > WSET_MAX || W.nqset > QSET_MAX;
     __syncwarp();
 }
-__device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, unsigned ticket) {
+__device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, int N, unsigned ticket) {
     int lane = threadIdx.x & 31;
+    const volatile unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
     bool conflict = false;
-    int n = min(W.nrset, RSET_MAX);
-    for (int q = lane; q < n; q += 32) conflict |= own[W.rset[q]] > ticket;
+    int nr = min(W.nrset, RSET_MAX), nw = min(W.nwset, WSET_MAX), nq = min(W.nqset, QSET_MAX);
+    for (int q = lane; q < nr; q += 32) conflict |= own_w[W.rset[q]] > ticket;
+    for (int q = lane; q < nw; q += 32) conflict |= own_r[W.wset[q]] > ticket;
+    for (int q = lane; q < nq; q += 32) conflict |= own_q[W.qset[q]] > ticket;
     return __any_sync(FULL, conflict);
 }
 
@@ -1163,7 +1282,10 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
                 if (nu < S.cap) { up[nu] = c; upc[nu] = (int8_t)static_code(ib, S.info[c], hbonds); }
                 ++nu;
             } else {
-                if (nd < S.cap) dn[nd] = c;
+                if (nd < S.cap) {
+                    dn[nd] = c;
+                    if (S.dnc) S.dnc[(size_t)b * S.cap + nd] = (int8_t)static_code(ib, S.info[c], hbonds);
+                }
                 ++nd;
             }
         };
@@ -1228,29 +1350,48 @@ __device__ void cta_rebuild(const DSys &S, SharedState &sh, int hbonds) {
     cta_tree_rebuild(S);
 }
 
-/* interval event N+2 (code/main.F90:1126-1187, code/displ.f) */
-__device__ bool cta_interval(const DSys &S, SharedState &sh, int hbonds) {
+/* interval event N+2 (code/main.F90:1126-1187, code/displ.f), spread over the
+ * C CTAs of the system: each shifts the times and advances the positions of
+ * its slice of the beads; the leader (L, rank 0) takes the maximum
+ * displacement and decides on a rebuild, which it does alone.  sh.tf_iv
+ * holds tfalse of the event on every CTA. */
+__device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L, int rank, int C, int hbonds) {
     const int N = S.N;
-    double tf = sh.sc.tfalse;
+    const double tf = sh.tf_iv;
     const DTab &T = *S.tab;
-    __syncthreads();
-    for (int k = threadIdx.x; k < N + 3; k += blockDim.x) {
+    const int stride = C * blockDim.x, t0 = rank * blockDim.x + threadIdx.x;
+    for (int k = t0; k < N + 3; k += stride) {
         double tn = S.tim[k] - tf;
         S.tim[k] = tn;
         S.key[k] = S.queued[k] ? okey(tn) : DMD_KEY_INF;
     }
     /* displ.f: the largest squared displacement over hdelr; dividing after
-     * the maximum gives the same value, division being monotone */
-    double dmax = 0.0;
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+     * the maximum gives the same value, division being monotone.  The
+     * squared displacements are non-negative: their maximum is taken on the
+     * bit patterns. */
+    long long dmax_bits = 0;
+    for (int k = t0; k < N; k += stride) {
         double px = S.x[k] + S.vx[k] * tf, py = S.y[k] + S.vy[k] * tf, pz = S.z[k] + S.vz[k] * tf;
         S.x[k] = px; S.y[k] = py; S.z[k] = pz;
         double a = S.ox[k] - px, b = S.oy[k] - py, c = S.oz[k] - pz;
         double dis = a * a + b * b + c * c;
-        if (dis > dmax) dmax = dis;
+        long long db = dbits(dis);
+        if (db > dmax_bits) dmax_bits = db;
     }
-    dmax = cta_max(sh, dmax);
+    for (int o = 16; o > 0; o >>= 1) { long long v = __shfl_xor_sync(FULL, dmax_bits, o); if (v > dmax_bits) dmax_bits = v; }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh.red_d[threadIdx.x >> 5] = __longlong_as_double(dmax_bits);
+    __syncthreads();
     if (threadIdx.x == 0) {
+        long long m = 0;
+        for (int w = 0; w < NWARPS; ++w) { long long v = dbits(sh.red_d[w]); if (v > m) m = v; }
+        L->red_max[rank] = __longlong_as_double(m);
+    }
+    csync(C);
+    if (rank == 0 && threadIdx.x == 0) {
+        long long mb = 0;
+        for (int q = 0; q < C; ++q) { long long v = dbits(sh.red_max[q]); if (v > mb) mb = v; }
+        double dmax = __longlong_as_double(mb);
         double moved_far = 0.0;
         double moved = dmax / T.hdelr;
         if (moved > moved_far) moved_far = moved;
@@ -1273,16 +1414,22 @@ __device__ bool cta_interval(const DSys &S, SharedState &sh, int hbonds) {
             sh.rebuild = 1;
         }
     }
+    if (rank == 0) {
+        __syncthreads();
+        if (sh.rebuild) {
+            for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
+            __syncthreads();
+            cta_rebuild(S, sh, hbonds);
+        }
+        if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
+    }
+    csync(C);
+    if (threadIdx.x == 0 && rank != 0) sh.rebuild = L->rebuild;
     __syncthreads();
     bool rb = sh.rebuild != 0;
-    if (rb) {
-        for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
-        __syncthreads();
-        cta_rebuild(S, sh, hbonds);
-    }
-    if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
-    __syncthreads();
-    cta_tree_rebuild(S);
+    /* level 1 of the tournament, spread over the CTAs (level 2 follows at
+     * the leader's next selection) */
+    for (int g = t0; g < S.nl1; g += stride) l1_update(S, g, N + 3);
     return rb;
 }
 
@@ -1494,14 +1641,20 @@ __global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int 
     if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
+/* The event loop of code/main.F90:484-1258 for nsys systems, each advanced
+ * by one cluster of C CTAs (C = 1: one CTA).  The leader CTA (rank 0)
+ * selects events and keeps the counters; a batch's candidates go one per
+ * warp over all CTAs of the cluster. */
 __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target, int hbonds_mask,
                                                      const int *chain_start, const int *chain_len,
-                                                     const int *chain_off, dmd_diag *outputs, int own_cap) {
+                                                     const int *chain_off, dmd_diag *outputs, int own_cap, int C) {
     extern __shared__ WarpArea warea[];
     __shared__ SharedState sh;
     __shared__ DSys S_sh;
-    int r = blockIdx.x;
-    if (r >= nsys) return;
+    const int rank = C > 1 ? (int)cg::this_cluster().block_rank() : 0;
+    const int r = blockIdx.x / C;
+    if (r >= nsys) return;             /* whole clusters only */
+    const bool leader = rank == 0;
     if (threadIdx.x == 0) S_sh = systems[r];
     __syncthreads();
     const DSys &S = S_sh;
@@ -1511,178 +1664,223 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     const bool stop_out = (S.flags & DMD_FLAG_STOP_AT_OUTPUT) != 0;
     const bool serial = (S.flags & DMD_FLAG_SERIAL) != 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gw = rank * NWARPS + warp;          /* candidate slot of this warp */
+    const int slots = min(C * NWARPS, CAND_MAX);
     WarpArea &W = warea[warp];
+    SharedState *L = C > 1 ? cg::this_cluster().map_shared_rank(&sh, 0) : &sh;
     if (threadIdx.x == 0) {
         sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0;
         sh.delta = sh.sc.interval * 0.05;
         sh.bseq = 0;
+        sh.exitf = 0;
     }
-    /* footprint claim table: shared memory for systems that fit, else the
-     * system's global array; cleared at every launch */
-    unsigned *own = N <= own_cap ? (unsigned *)(warea + NWARPS) : S.owner;
-    for (int b = threadIdx.x; b < N; b += blockDim.x) own[b] = 0u;
-    __syncthreads();
-    DMD_PHASE_START();
+    /* footprint claim table: shared memory when one CTA holds the system and
+     * it fits, else the system's global array; cleared at every launch */
+    unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)(warea + NWARPS) : S.owner;
+    for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
+    csync(C);
+    DMD_PHASE_START(leader ? r : -1);
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
     const long long max_iter = 16 * target + 1000000;
     long long iter = 0;
     while (true) {
-        if (sh.sc.done >= target || sh.sc.err || sh.sc.stop) break;
-        if (++iter > max_iter) {
-            if (threadIdx.x == 0) set_err(sh, DMD_E_DEVICE_TIMEOUT, 0);
+        /* ---- the leader selects the next event (and a batch) ---- */
+        if (leader) {
+            for (int h = threadIdx.x; h < S.nl2; h += blockDim.x) l2_update(S, h);
             __syncthreads();
-            break;
-        }
-        if (warp == 0) {
-            long long kroot;
-            int e = warp_tree_root(S, kroot);
-            if (lane == 0) {
-                sh.ev = e;
-                sh.kcut = kroot;
-                if (e < 0) set_err(sh, DMD_E_STATE, 0);
+            if (threadIdx.x == 0) {
+                bool ex = sh.sc.done >= target || sh.sc.err || sh.sc.stop;
+                if (!ex && ++iter > max_iter) { set_err(sh, DMD_E_DEVICE_TIMEOUT, 0); ex = true; }
+                sh.exitf = ex;
+            }
+            __syncthreads();
+            if (!sh.exitf && warp == 0) {
+                long long kroot;
+                int e = warp_tree_root(S, kroot);
+                if (lane == 0) {
+                    sh.ev = e;
+                    sh.kcut = kroot;
+                    if (e < 0) { set_err(sh, DMD_E_STATE, 0); sh.exitf = 1; }
+                }
+            }
+            __syncthreads();
+            DMD_PHASE(0);
+            if (!sh.exitf && sh.ev < N) {
+                int e = sh.ev;
+                long long kroot = sh.kcut;
+                long long left = target - sh.sc.done;
+                int m;
+                if (serial || left <= 1) {
+                    if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = e; }
+                    __syncthreads();
+                    m = 1;
+                } else {
+                    m = cta_candidates(S, sh, e, kroot);
+                    if (m > slots) m = slots;
+                    if (m > left) m = (int)left;
+                }
+                if (threadIdx.x == 0) {
+                    sh.m = m;
+                    sh.tick_reset = m > 1 && sh.bseq >= DMD_TICKET_SEQ_MAX;
+                }
+                DMD_PHASE(1);
+            } else if (!sh.exitf && threadIdx.x == 0) {
+                /* a pseudo event: its counter and time */
+                sh.sc.coll += 1;
+                sh.tf_iv = S.tim[sh.ev];
+                if (sh.ev != N) sh.sc.tfalse = sh.tf_iv;
+            }
+            if (threadIdx.x == 0) {
+                sh.coll0 = sh.sc.coll; sh.log0 = sh.sc.log_count; sh.imax = sh.sc.interval_max; sh.tnow = sh.sc.t;
             }
         }
-        __syncthreads();
-        DMD_PHASE(0);
+        csync(C);
+        /* ---- the other CTAs copy the leader's decision ---- */
+        if (!leader) {
+            if (threadIdx.x == 0) {
+                sh.exitf = L->exitf; sh.ev = L->ev; sh.m = L->m; sh.tick_reset = L->tick_reset; sh.bseq = L->bseq;
+                sh.coll0 = L->coll0; sh.log0 = L->log0; sh.imax = L->imax; sh.tnow = L->tnow; sh.tf_iv = L->tf_iv;
+            }
+            if (threadIdx.x < NWARPS) {
+                int k = rank * NWARPS + threadIdx.x;
+                if (k < CAND_MAX) { sh.sort_idx[k] = L->sort_idx[k]; sh.sort_key[k] = L->sort_key[k]; }
+            }
+            __syncthreads();
+        }
+        if (sh.exitf) break;
         int ph_kind __attribute__((unused)) = 9;
-        int e = sh.ev;
-        if (e < 0) break;
+        const int e = sh.ev;
         if (e < N) {
             ph_kind = 5;
             /* ---- a batch of pair events ---- */
-            long long kroot = sh.kcut;
-            int m;
-            long long left = target - sh.sc.done;
-            __syncthreads();
-            if (serial || left <= 1) {
-                if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = e; }
-                __syncthreads();
-                m = 1;
-            } else {
-                m = cta_candidates(S, sh, e, kroot);
-                DMD_PHASE(1);
-                if (m > NWARPS) m = NWARPS;
-                if (m > left) m = (int)left;
-            }
-            /* footprints: claim, test, release */
-            int P = m;
+            const int m = sh.m;
+            int P = 1;
             if (m > 1) {
-                if (sh.bseq >= DMD_TICKET_SEQ_MAX) {   /* tickets exhausted: clear the table */
-                    __syncthreads();
-                    for (int b = threadIdx.x; b < N; b += blockDim.x) own[b] = 0u;
-                    __syncthreads();
+                if (sh.tick_reset) {   /* tickets exhausted: clear the table */
+                    for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
+                    csync(C);
                     if (threadIdx.x == 0) sh.bseq = 0;
                     __syncthreads();
                 }
-                unsigned ticket = ((unsigned)(sh.bseq + 1) << 5) | (unsigned)(31 - warp);
-                if (warp < m) {
-                    int i = sh.sort_idx[warp];
+                unsigned ticket = ((unsigned)(sh.bseq + 1) << 6) | (unsigned)(63 - gw);
+                if (gw < m) {
+                    int i = sh.sort_idx[gw];
                     warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
                 }
-                __syncthreads();
+                csync(C);
                 DMD_PHASE(10);
-                if (warp < m) {
-                    bool c = warp_footprint_test(W, own, ticket);
-                    if (lane == 0) W.conflict = c;
+                if (gw < m) {
+                    bool c = warp_footprint_test(W, own, N, ticket);
+                    if (lane == 0) { L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over; }
                 }
-                __syncthreads();
+                csync(C);
                 DMD_PHASE(11);
-                if (threadIdx.x == 0) {
-                    sh.bseq += 1;
+                if (leader && threadIdx.x == 0) {
+                    sh.bseq = sh.tick_reset ? 1 : sh.bseq + 1;
                     /* the longest conflict-free prefix; an incomplete footprint
                      * (cascade list overflow) ends the batch after its event */
                     int p = m;
                     for (int k = 0; k < m; ++k) {
-                        if (k > 0 && warea[k].conflict) { p = k; break; }
-                        if (warea[k].casc_over) { p = k > 0 ? k : 1; break; }
+                        if (k > 0 && sh.c_conflict[k]) { p = k; break; }
+                        if (sh.c_over[k]) { p = k > 0 ? k : 1; break; }
                     }
-                    sh.nbatch = p;
+                    sh.P = p;
                 }
+                csync(C);
+                if (!leader && threadIdx.x == 0) sh.P = L->P;
                 __syncthreads();
-                P = sh.nbatch;
+                P = sh.P;
                 DMD_PHASE(2);
             }
             /* speculative commit of each event on its warp */
-            long long coll0 = sh.sc.coll;
-            double imax = sh.sc.interval_max;
-            if (warp < P) {
-                int i = sh.sort_idx[warp];
+            const long long coll0 = sh.coll0;
+            const double imax = sh.imax;
+            if (gw < P) {
+                int i = sh.sort_idx[gw];
                 int j = S.nptnr[i];
                 double tf = S.tim[i];
-                if (lane == 0) { W.i = i; W.j = j; W.tf = tf; W.coll = coll0 + warp + 1; }
+                if (lane == 0) { W.i = i; W.j = j; W.tf = tf; W.coll = coll0 + gw + 1; }
                 __syncwarp();
+                DMD_SUB(-1);
                 warp_snapshot(S, W, i, j);
+                DMD_SUB(0);
                 if (lane == 0) { W.err = 0; W.err_info = 0; }
                 __syncwarp();
                 Err E{&W.err, &W.err_info};
-                warp_collision(S, E, W, i, j, tf, coll0 + warp + 1, hbonds);
+                warp_collision(S, E, W, i, j, tf, coll0 + gw + 1, hbonds);
+                DMD_SUB(1);
                 warp_repredict(S, E, W, i, j, tf, imax, hbonds);
+                DMD_SUB(8);
                 if (lane == 0 && W.xpulse) {
                     if (S.ident[i] < S.ident[j]) repuls_del_b(S, i, j); else repuls_del_b(S, j, i);
                 }
                 __syncwarp();
+                if (lane == 0) {
+                    L->c_tnew_key[gw] = W.tnew_key; L->c_tnew_idx[gw] = W.tnew_idx;
+                    L->c_err[gw] = W.err; L->c_err_info[gw] = W.err_info;
+                    L->c_ct[gw] = W.ct; L->c_tf[gw] = W.tf;
+                }
             }
-            __syncthreads();
+            csync(C);
             DMD_PHASE(3);
-            /* validation: event k stands if it precedes every new entry of events 0..k-1 */
-            if (threadIdx.x == 0) {
+            /* validation: event k stands if it precedes every new entry of
+             * events 0..k-1; the leader also books the committed events */
+            if (leader && threadIdx.x == 0) {
                 int v = P;
                 long long bk = DMD_KEY_INF;
                 int bb = INT_MAX;
                 for (int k = 0; k < P; ++k) {
                     if (k > 0 && !key_less(sh.sort_key[k], sh.sort_idx[k], bk, bb)) { v = k; break; }
-                    if (warea[k].err) {   /* the run stops after the first event in error */
-                        set_err(sh, warea[k].err, warea[k].err_info);
+                    if (sh.c_err[k]) {   /* the run stops after the first event in error */
+                        set_err(sh, sh.c_err[k], sh.c_err_info[k]);
                         v = k + 1;
                         break;
                     }
-                    if (key_less(warea[k].tnew_key, warea[k].tnew_idx, bk, bb)) { bk = warea[k].tnew_key; bb = warea[k].tnew_idx; }
+                    if (key_less(sh.c_tnew_key[k], sh.c_tnew_idx[k], bk, bb)) { bk = sh.c_tnew_key[k]; bb = sh.c_tnew_idx[k]; }
                 }
-                sh.nvalid = v;
+                sh.V = v;
+                for (int k = 0; k < v; ++k) {
+                    int ct = sh.c_ct[k];
+                    if (ct >= 1 && ct < 32) sh.sc.nevents[ct] += 1;
+                }
+                sh.sc.coll = coll0 + v;
+                sh.sc.n_pair += v;
+                sh.sc.n_batches += 1;
+                sh.sc.n_rolled_back += P - v;
+                sh.sc.n_candidates += m;
+                sh.sc.done += v;
+                sh.sc.tfalse = sh.c_tf[v - 1];
+                sh.sc.old_tfalse = sh.c_tf[v - 1];
+                if (S.log && S.log_cap > 0) sh.sc.log_count += v;
             }
+            csync(C);
+            if (!leader && threadIdx.x == 0) sh.V = L->V;
             __syncthreads();
             DMD_PHASE(4);
-            int V = sh.nvalid;
-            if (warp < P) {
-                if (warp < V) {
+            const int V = sh.V;
+            if (gw < P) {
+                if (gw < V) {
                     warp_commit_preds(S, W);
-                    if (lane == 0) log_event(S, sh.sc.log_count + warp, W.coll, sh.sc.t, W.tf, W.i, W.j, W.ct, W.evcode);
+                    if (lane == 0) log_event(S, sh.log0 + gw, W.coll, sh.tnow, W.tf, W.i, W.j, W.ct, W.evcode);
                 } else {
                     warp_restore(S, W);
                 }
             }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int k = 0; k < V; ++k) {
-                    int ct = warea[k].ct;
-                    if (ct >= 1 && ct < 32) sh.sc.nevents[ct] += 1;
-                }
-                sh.sc.coll = coll0 + V;
-                sh.sc.n_pair += V;
-                sh.sc.n_batches += 1;
-                sh.sc.n_rolled_back += P - V;
-                sh.sc.n_candidates += m;
-                sh.sc.done += V;
-                sh.sc.tfalse = warea[V - 1].tf;
-                sh.sc.old_tfalse = warea[V - 1].tf;
-                if (S.log && S.log_cap > 0) sh.sc.log_count += V;
-            }
-            if (warp < V) warp_l1_refresh(S, W.pb, W.npred);
-            __syncthreads();
-            if (warp < V) warp_l2_refresh(S, W.pb, W.npred);
+            csync(C);   /* every commit lands before any level-1 group is recomputed */
+            if (gw < V) warp_l1_refresh(S, W.pb, W.npred);
         } else if (e == N) {
             ph_kind = 6;
-            /* ---- ghost collision: alone ---- */
-            if (warp == 0) {
-                double tf = S.tim[N];
+            /* ---- ghost collision: leader warp 0 ---- */
+            if (leader && warp == 0) {
+                double tf = sh.tf_iv;
                 if (lane == 0) {
-                    sh.sc.coll += 1;
                     int i = lane_ghost(S, sh, tf);
                     W.i = i; W.tf = tf;
                 }
                 __syncwarp();
                 int i = W.i;
                 tf = W.tf;
+                DMD_SUB(-1);
                 warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds);
                 warp_commit_preds(S, W);
                 if (lane == 0) {
@@ -1695,17 +1893,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 }
                 __syncwarp();
                 warp_l1_refresh(S, W.pb, W.npred + 1);
-                __syncwarp();
-                warp_l2_refresh(S, W.pb, W.npred + 1);
             }
         } else if (e == N + 1) {
             ph_kind = 7;
-            /* ---- interval ---- */
-            if (threadIdx.x == 0) { sh.sc.coll += 1; sh.sc.tfalse = S.tim[N + 1]; }
-            __syncthreads();
-            double t_before = sh.sc.t, tf = sh.sc.tfalse;
-            bool rb = cta_interval(S, sh, hbonds);
-            if (threadIdx.x == 0) {
+            /* ---- interval: all CTAs ---- */
+            double t_before = sh.tnow, tf = sh.tf_iv;
+            bool rb = cluster_interval(S, sh, L, rank, C, hbonds);
+            if (leader && threadIdx.x == 0) {
                 sh.sc.n_interval += 1;
                 log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
                 if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
@@ -1714,33 +1908,32 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             }
         } else {
             ph_kind = 8;
-            /* ---- output ---- */
-            if (threadIdx.x == 0) { sh.sc.coll += 1; sh.sc.tfalse = S.tim[N + 2]; }
-            __syncthreads();
-            cta_diag(S, sh, cs, cl, outputs ? outputs + r : nullptr);
-            if (threadIdx.x == 0) {
-                sh.sc.n_output += 1;
-                double tn = 3.3 / (sqrt(S.tab->setemp)) + 5 + sh.sc.tfalse;
-                set_pred(S, N + 2, tn, -2, -2, tn < sh.sc.interval_max);
-                log_event(S, sh.sc.log_count, sh.sc.coll, sh.sc.t, sh.sc.tfalse, N + 2, -1, DMD_EV_OUTPUT, 0);
-                if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
-                sh.sc.old_tfalse = sh.sc.tfalse;
-                if (!phys) sh.sc.done += 1;
-                if (stop_out) sh.sc.stop = 1;
-                sh.touched[0] = N + 2;
-            }
-            __syncthreads();
-            if (warp == 0) {
-                warp_l1_refresh(S, sh.touched, 1);
-                __syncwarp();
-                warp_l2_refresh(S, sh.touched, 1);
+            /* ---- output: the leader CTA ---- */
+            if (leader) {
+                cta_diag(S, sh, cs, cl, outputs ? outputs + r : nullptr);
+                if (threadIdx.x == 0) {
+                    sh.sc.n_output += 1;
+                    double tn = 3.3 / (sqrt(S.tab->setemp)) + 5 + sh.sc.tfalse;
+                    set_pred(S, N + 2, tn, -2, -2, tn < sh.sc.interval_max);
+                    log_event(S, sh.sc.log_count, sh.sc.coll, sh.sc.t, sh.sc.tfalse, N + 2, -1, DMD_EV_OUTPUT, 0);
+                    if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
+                    sh.sc.old_tfalse = sh.sc.tfalse;
+                    if (!phys) sh.sc.done += 1;
+                    if (stop_out) sh.sc.stop = 1;
+                    sh.touched[0] = N + 2;
+                }
+                __syncthreads();
+                if (warp == 0) warp_l1_refresh(S, sh.touched, 1);
             }
         }
-        __syncthreads();
+        csync(C);
         DMD_PHASE(ph_kind);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) *S.sc = sh.sc;
+    if (leader) {
+        __syncthreads();
+        if (threadIdx.x == 0) *S.sc = sh.sc;
+    }
+    if (C > 1) cg::this_cluster().sync();   /* no CTA leaves while others may read its shared memory */
 }
 
 __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, const int *chain_start, const int *chain_len,
@@ -1760,34 +1953,67 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, cons
 /* ------------------------------------------------------------------ */
 /* launch wrappers                                                     */
 /* ------------------------------------------------------------------ */
-static_assert(sizeof(WarpArea) * NWARPS + OWN_SMEM_MAX * sizeof(unsigned) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
+static_assert(sizeof(WarpArea) * NWARPS + OWN_SMEM_MAX * 3 * sizeof(unsigned) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
               "k_run shared memory above the 227 KB a block may use");
-static size_t run_smem(int own_cap) { return sizeof(WarpArea) * NWARPS + (size_t)own_cap * sizeof(unsigned); }
+static size_t run_smem(int own_cap) { return sizeof(WarpArea) * NWARPS + (size_t)own_cap * 3 * sizeof(unsigned); }
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st) {
     k_init<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
     return cudaGetLastError();
 }
-cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, long long target, int hbonds,
-                           const int *chain_start, const int *chain_len, const int *chain_off, dmd_diag *outputs,
-                           cudaStream_t st) {
+static cudaError_t k_run_attributes() {
     static std::mutex mu;
     static bool done[256];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    {
-        std::lock_guard<std::mutex> lock(mu);
-        if (dev >= 0 && dev < 256 && !done[dev]) {
-            e = cudaFuncSetAttribute(k_run, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(OWN_SMEM_MAX));
-            if (e != cudaSuccess) return e;
-            done[dev] = true;
-        }
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 0 && dev < 256 && !done[dev]) {
+        e = cudaFuncSetAttribute(k_run, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(OWN_SMEM_MAX));
+        if (e != cudaSuccess) return e;
+        done[dev] = true;
     }
-    int own_cap = max_beads <= OWN_SMEM_MAX ? max_beads : 0;
-    k_run<<<nsys, NTHREADS, run_smem(own_cap), st>>>(d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off,
-                                                     outputs, own_cap);
-    return cudaGetLastError();
+    return cudaSuccess;
+}
+
+static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, int nsys, int C, size_t smem,
+                           cudaStream_t st) {
+    cfg = cudaLaunchConfig_t{};
+    cfg.gridDim = dim3((unsigned)(nsys * C), 1, 1);
+    cfg.blockDim = dim3(NTHREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+}
+
+/* k_run with one cluster of C CTAs per system (C = 1, 2, 4 or 8) */
+cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, int hbonds,
+                           const int *chain_start, const int *chain_len, const int *chain_off, dmd_diag *outputs,
+                           cudaStream_t st) {
+    if (C != 1 && C != 2 && C != 4 && C != 8) return cudaErrorInvalidValue;
+    cudaError_t e = k_run_attributes();
+    if (e != cudaSuccess) return e;
+    int own_cap = (C == 1 && max_beads <= OWN_SMEM_MAX) ? max_beads : 0;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    cluster_config(cfg, attr, nsys, C, run_smem(own_cap), st);
+    return cudaLaunchKernelEx(&cfg, k_run, d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off, outputs,
+                              own_cap, C);
+}
+
+/* how many clusters of C CTAs of k_run can be resident at once */
+cudaError_t dmd_max_active_clusters(int C, int *n) {
+    cudaError_t e = k_run_attributes();
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    cluster_config(cfg, attr, 1, C, run_smem(C == 1 ? OWN_SMEM_MAX : 0), 0);
+    return cudaOccupancyMaxActiveClusters(n, k_run, &cfg);
 }
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st) {

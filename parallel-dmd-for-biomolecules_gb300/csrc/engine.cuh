@@ -101,9 +101,10 @@ struct DSys {
     int8_t *colt;
     uint8_t *queued;
     long long *key;                /* ordered integer key of (queued ? tim : +inf), N + 3 entries */
-    unsigned int *owner;           /* footprint tickets, N entries, when not in shared memory */
+    unsigned int *owner;           /* footprint tickets (read, write, queue: 3N entries), when not in shared memory */
     int *up, *dn;                  /* neighbour lists [N*cap] */
     int8_t *upc;                   /* static pair code of each up entry */
+    int8_t *dnc;                   /* ... and of each down entry (event loop only; may be NULL) */
     int *upn, *dnn;
     int *cell_count, *cell_start, *cell_beads;  /* rebuild grid */
     int *l1i;                      /* tournament level 1: argmin of 32 entries */
@@ -176,6 +177,14 @@ __host__ __device__ __forceinline__ int static_code(const BeadInfo &A, const Bea
     return 1;
 }
 
+/* ev_code(a,b) when the static code of the pair is already known */
+__device__ __forceinline__ int pair_code_st(const DSys &S, int a, int b, int st) {
+    const int *op = S.ovp + 4 * a;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        if (op[s] == b) return S.ovc[4 * a + s];
+    return st;
+}
 /* ev_code(a,b): the rule plus the H-bond shoulder overrides of repuls_add */
 __device__ __forceinline__ int pair_code(const DSys &S, int a, int b, int hbonds) {
     const int *op = S.ovp + 4 * a;

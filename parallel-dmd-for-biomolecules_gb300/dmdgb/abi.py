@@ -102,6 +102,7 @@ ENGINE_SYMBOLS = [
     "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
+    "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster",
 ]
 
 
@@ -155,6 +156,12 @@ def _declare(lib) -> None:
     lib.dmd_last_run_ms.restype = C.c_double
     lib.dmd_batch_last_run_ms.argtypes = [C.c_void_p]
     lib.dmd_batch_last_run_ms.restype = C.c_double
+    lib.dmd_batch_set_cluster.argtypes = [C.c_void_p, C.c_int32]
+    lib.dmd_batch_set_cluster.restype = C.c_int
+    lib.dmd_set_cluster.argtypes = [C.c_void_p, C.c_int32]
+    lib.dmd_set_cluster.restype = C.c_int
+    lib.dmd_batch_cluster.argtypes = [C.c_void_p]
+    lib.dmd_batch_cluster.restype = C.c_int32
     lib.dmd_predict_all_noalloc.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System),
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int32]
     lib.dmd_predict_all_noalloc.restype = C.c_int

@@ -30,7 +30,8 @@ def _check(rc: int, lib, handle, fn="dmd_last_error"):
 class Engine:
     """One system on the GPU (the plain one-system-per-launch path)."""
 
-    def __init__(self, spec: SystemSpec, tables: Optional[Tables] = None, flags: int = 0, list_cap: int = 0):
+    def __init__(self, spec: SystemSpec, tables: Optional[Tables] = None, flags: int = 0, list_cap: int = 0,
+                 cluster: int = 0):
         self.lib = abi.load_engine()
         self.spec = spec
         self.n = spec.n_beads
@@ -45,6 +46,8 @@ class Engine:
             self.lib.dmd_destroy(h)
             self.h = None
             raise DMDError(rc, msg.decode() if msg else "")
+        if cluster:
+            _check(self.lib.dmd_set_cluster(self.h, int(cluster)), self.lib, self.h)
 
     def close(self):
         if getattr(self, "h", None):
@@ -112,7 +115,8 @@ class Engine:
 class Batch:
     """Many independent systems advanced by one persistent launch."""
 
-    def __init__(self, specs: Sequence[SystemSpec], tables: Optional[Tables] = None, flags: int = 0, list_cap: int = 0):
+    def __init__(self, specs: Sequence[SystemSpec], tables: Optional[Tables] = None, flags: int = 0, list_cap: int = 0,
+                 cluster: int = 0):
         self.lib = abi.load_engine()
         self.specs = list(specs)
         n = len(self.specs)
@@ -127,6 +131,17 @@ class Batch:
             self.lib.dmd_batch_destroy(h)
             self.h = None
             raise DMDError(rc, msg.decode() if msg else "")
+        if cluster:
+            self.set_cluster(cluster)
+
+    def set_cluster(self, ctas: int):
+        """CTAs per system (1, 2, 4, 8; 0 = automatic).  Results do not depend on it."""
+        _check(self.lib.dmd_batch_set_cluster(self.h, int(ctas)), self.lib, self.h, "dmd_batch_last_error")
+
+    @property
+    def cluster(self) -> int:
+        """The cluster size the last run used."""
+        return int(self.lib.dmd_batch_cluster(self.h))
 
     def close(self):
         if getattr(self, "h", None):

@@ -117,3 +117,37 @@ def test_c3_replicas_batched(built):
         for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity"):
             assert np.array_equal(st[key], ost[key]), (r, key)
     b.close()
+
+
+@pytest.mark.parametrize("ctas", [1, 2, 4, 8])
+def test_cluster_sizes(built, ctas):
+    """The same systems advanced with 1, 2, 4 or 8 CTAs per system commit
+    the oracle's event sequence."""
+    specs = systems.config_c3(32, seed=2)
+    pick = [sorted(specs, key=lambda s: s.n_beads)[0], specs[7], specs[30]]
+    for s in pick:
+        systems.generate(s)
+    n = 20000
+    b = Batch(pick, cluster=ctas)
+    logs = b.run(n, log_capacity=n + 64)
+    assert b.cluster == ctas
+    for r, s in enumerate(pick):
+        ora = Oracle(s)
+        olog = ora.run(n, log_capacity=n + 64)
+        k = first_mismatch(logs[r], olog)
+        assert k < 0, f"C={ctas} replica {r}: logs diverge at {k}:\n{describe(logs[r], olog, k)}"
+        st, ost = b.state(r), ora.state()
+        for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity"):
+            assert np.array_equal(st[key], ost[key]), (ctas, r, key)
+    b.close()
+
+
+def test_cluster_hbond_plain(built):
+    """The plain path on a cluster of 4 CTAs, on the H-bond-rich system."""
+    spec = dense_system(n_chains=10, L=10, box=38.0, tstar=0.12, seed=21, rng_seed=5)
+    with Engine(spec, cluster=4) as eng:
+        glog = eng.run(200000, log_capacity=200064)
+    ora = Oracle(spec)
+    olog = ora.run(200000, log_capacity=200064)
+    k = first_mismatch(glog, olog)
+    assert k < 0, f"logs diverge at {k}:\n{describe(glog, olog, k)}"
