@@ -405,6 +405,7 @@ size_t layout(const HostSys &H, DSys &d, char *base, bool for_run = true) {
     d.x = P.take<double>(N); d.y = P.take<double>(N); d.z = P.take<double>(N);
     d.vx = P.take<double>(N); d.vy = P.take<double>(N); d.vz = P.take<double>(N);
     d.ox = P.take<double>(N); d.oy = P.take<double>(N); d.oz = P.take<double>(N);
+    d.xf = P.take<float>(N); d.yf = P.take<float>(N); d.zf = P.take<float>(N);
     d.ident = P.take<int8_t>(N);
     d.bptnr = P.take<int>(N);
     d.er = P.take<int>(4 * N);

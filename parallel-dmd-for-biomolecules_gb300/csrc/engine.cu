@@ -93,6 +93,18 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
 #define DMD_SUB(k) do { } while (0)
 #endif
 
+/* per-warp scratch of the full re-predictions of up to TG_MAX beads: bead,
+ * first task, running minimum (key, partner, time, type), task -> bead map */
+struct FullScratch {
+    int tg_b[TG_MAX];
+    int tg_base[TG_MAX + 1];
+    long long tg_k[TG_MAX];
+    int tg_p[TG_MAX];
+    double tg_raw[TG_MAX];
+    int8_t tg_y[TG_MAX];
+    int8_t tmap[TMAP_MAX];
+};
+
 /* per-warp working area of one event (dynamic shared memory) */
 struct WarpArea {
     int nops, nlead, npred, nmeta, ncasc, ntg, nmarked;
@@ -107,14 +119,7 @@ struct WarpArea {
     int16_t lead_q[OPS_MAX];
     int8_t lead_m[OPS_MAX];
     int16_t mk[OPS_MAX];          /* marked leaders, in leader order */
-    /* full re-predictions of one round: bead, first task, running minimum */
-    int tg_b[TG_MAX];
-    int tg_base[TG_MAX + 1];
-    long long tg_k[TG_MAX];
-    int tg_p[TG_MAX];
-    double tg_raw[TG_MAX];
-    int8_t tg_y[TG_MAX];
-    int8_t tmap[TMAP_MAX];        /* task -> target of the round */
+    FullScratch fs;               /* full re-predictions of one round */
     /* buffered predictions: bead, time, partner, type, queued */
     int pb[OPS_MAX + 2];
     double pt[OPS_MAX + 2];
@@ -858,15 +863,15 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             if (t == 0) b = rd == 0 ? i : -1;
             else if (t == 1) b = rd == 0 ? j : -1;
             else b = W.lead_l[W.mk[m0 + t - 2]];
-            W.tg_b[t] = b;
-            W.tg_k[t] = Hkey; W.tg_p[t] = -1; W.tg_raw[t] = Hraw; W.tg_y[t] = -1;
+            W.fs.tg_b[t] = b;
+            W.fs.tg_k[t] = Hkey; W.fs.tg_p[t] = -1; W.fs.tg_raw[t] = Hraw; W.fs.tg_y[t] = -1;
         }
         /* task offsets: an inclusive scan over the targets of the up-list
          * length plus the extras above the bead */
         int run = 0;
         for (int base = 0; base < ntg; base += 32) {
             int t = base + lane;
-            int b = t < ntg ? W.tg_b[t] : -1;
+            int b = t < ntg ? W.fs.tg_b[t] : -1;
             int c = 0;
             if (b >= 0) {
                 c = S.upn[b];
@@ -874,15 +879,15 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             }
             int incl = c;
             for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
-            if (t < ntg) W.tg_base[t] = run + incl - c;
+            if (t < ntg) W.fs.tg_base[t] = run + incl - c;
             run += __shfl_sync(FULL, incl, 31);
         }
-        if (lane == 0) W.tg_base[ntg] = run;
+        if (lane == 0) W.fs.tg_base[ntg] = run;
         __syncwarp();
         const bool mapped = run <= TMAP_MAX;
         if (mapped) {   /* task -> target map, one target per lane */
             for (int t = lane; t < ntg; t += 32)
-                for (int q = W.tg_base[t]; q < W.tg_base[t + 1]; ++q) W.tmap[q] = (int8_t)t;
+                for (int q = W.fs.tg_base[t]; q < W.fs.tg_base[t + 1]; ++q) W.fs.tmap[q] = (int8_t)t;
             __syncwarp();
         }
         int nop = rd == 0 ? n : 0;
@@ -899,18 +904,18 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             } else if (q < ntask) {
                 int rel = q - nop;
                 int lo;
-                if (mapped) lo = W.tmap[rel];
+                if (mapped) lo = W.fs.tmap[rel];
                 else {
                     int hi = ntg - 1;                /* last target with tg_base <= rel */
                     lo = 0;
                     while (lo < hi) {
                         int mid = (lo + hi + 1) >> 1;
-                        if (W.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
+                        if (W.fs.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
                     }
                 }
                 tgt = lo;
-                int b = W.tg_b[lo];
-                int k = rel - W.tg_base[lo];
+                int b = W.fs.tg_b[lo];
+                int k = rel - W.fs.tg_base[lo];
                 int nu = S.upn[b];
                 int m;
                 if (k < nu) { m = S.up[(size_t)b * S.cap + k]; st = S.upc[(size_t)b * S.cap + k]; }
@@ -957,18 +962,18 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             }
             int gprev = __shfl_up_sync(FULL, tgt, 1);
             bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
-            if (head && key_less(k, p, W.tg_k[tgt], W.tg_p[tgt])) {
-                W.tg_k[tgt] = k; W.tg_p[tgt] = p; W.tg_raw[tgt] = rt; W.tg_y[tgt] = (int8_t)y;
+            if (head && key_less(k, p, W.fs.tg_k[tgt], W.fs.tg_p[tgt])) {
+                W.fs.tg_k[tgt] = k; W.fs.tg_p[tgt] = p; W.fs.tg_raw[tgt] = rt; W.fs.tg_y[tgt] = (int8_t)y;
             }
             __syncwarp();
         }
         DMD_SUB(5);
         /* 5. the full results: time = minimum + tfalse */
-        for (int t = lane; t < ntg; t += 32) W.tg_raw[t] = W.tg_raw[t] + tf;
+        for (int t = lane; t < ntg; t += 32) W.fs.tg_raw[t] = W.fs.tg_raw[t] + tf;
         __syncwarp();
         if (rd == 0 && lane < 2 && (lane == 0 || j >= 0)) {
-            double tn = W.tg_raw[lane];
-            W.pt[lane] = tn; W.pn[lane] = W.tg_p[lane]; W.pc[lane] = W.tg_y[lane];
+            double tn = W.fs.tg_raw[lane];
+            W.pt[lane] = tn; W.pn[lane] = W.fs.tg_p[lane]; W.pc[lane] = W.fs.tg_y[lane];
             W.pq[lane] = okey(tn) < imax_key;
         }
         __syncwarp();
@@ -990,14 +995,14 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
             double t;
             int p, y;
             bool qq;
-            if (l == i) { t = W.tg_raw[0]; p = W.tg_p[0]; y = W.tg_y[0]; qq = okey(t) < imax_key; }
+            if (l == i) { t = W.fs.tg_raw[0]; p = W.fs.tg_p[0]; y = W.fs.tg_y[0]; qq = okey(t) < imax_key; }
             else { t = S.tim[l]; p = S.nptnr[l]; y = S.colt[l]; qq = S.queued[l] != 0; }
             for (int pp = W.lead_q[ld]; pp < n; ++pp) {
                 if (W.ops_l[pp] != l) continue;
                 int src = W.ops_s[pp];
                 if (p == src) {
                     if (ft < 0) { set_err(E, DMD_E_STATE, l); break; }
-                    t = W.tg_raw[ft]; p = W.tg_p[ft]; y = W.tg_y[ft]; qq = okey(t) < imax_key;
+                    t = W.fs.tg_raw[ft]; p = W.fs.tg_p[ft]; y = W.fs.tg_y[ft]; qq = okey(t) < imax_key;
                 } else if (W.op_y[pp] != -128) {
                     double tn = W.op_t[pp];
                     long long kn = okey(tn);
@@ -1266,38 +1271,59 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
         int8_t *upc = S.upc + (size_t)b * S.cap;
         const BeadInfo ib = S.info[b];
         double xb = S.x[b], yb = S.y[b], zb = S.z[b];
+        const float xbf = S.xf[b], ybf = S.yf[b], zbf = S.zf[b];
         auto consider = [&](int c) {
             if (c == b) return;
-            int code = pair_code(S, c, b, hbonds);
+            int st = static_code(S.info[c], ib, hbonds);
+            int code = pair_code_st(S, c, b, st);
             bool take;
             if ((code >= 4 && code <= 12) || (code >= 17 && code < 27)) take = true;
             else {
-                double rx = xb - S.x[c], ry = yb - S.y[c], rz = zb - S.z[c];
-                rx = rx - d_nint(rx); ry = ry - d_nint(ry); rz = rz - d_nint(rz);
-                double r2 = rx * rx + ry * ry + rz * rz;
-                take = r2 <= T.rlsq[code];
+                /* Single-precision prefilter.  Positions lie in [-0.5, 0.5]
+                 * at a rebuild, so each wrapped single-precision component
+                 * is within 1e-7 of the double one and r2 within
+                 * 4e-7 + 4e-7 * r2; only pairs that close to the cutoff are
+                 * decided in double precision, as the reference does. */
+                float fx = xbf - S.xf[c], fy = ybf - S.yf[c], fz = zbf - S.zf[c];
+                fx = fx - rintf(fx); fy = fy - rintf(fy); fz = fz - rintf(fz);
+                float r2f = fx * fx + fy * fy + fz * fz;
+                float cut = (float)T.rlsq[code];
+                float margin = 4e-7f + 4e-7f * cut;
+                if (r2f > cut + margin) take = false;
+                else if (r2f < cut - margin) take = true;
+                else {
+                    double rx = xb - S.x[c], ry = yb - S.y[c], rz = zb - S.z[c];
+                    rx = rx - d_nint(rx); ry = ry - d_nint(ry); rz = rz - d_nint(rz);
+                    double r2 = rx * rx + ry * ry + rz * rz;
+                    take = r2 <= T.rlsq[code];
+                }
             }
             if (!take) return;
             if (c > b) {
-                if (nu < S.cap) { up[nu] = c; upc[nu] = (int8_t)static_code(ib, S.info[c], hbonds); }
+                if (nu < S.cap) { up[nu] = c; upc[nu] = (int8_t)st; }
                 ++nu;
             } else {
                 if (nd < S.cap) {
                     dn[nd] = c;
-                    if (S.dnc) S.dnc[(size_t)b * S.cap + nd] = (int8_t)static_code(ib, S.info[c], hbonds);
+                    if (S.dnc) S.dnc[(size_t)b * S.cap + nd] = (int8_t)st;
                 }
                 ++nd;
             }
         };
         if (nc >= 3) {
             int cx = cell_coord(xb, nc), cy = cell_coord(yb, nc), cz = cell_coord(zb, nc);
-            for (int dz = -1; dz <= 1; ++dz)
-                for (int dy = -1; dy <= 1; ++dy)
-                    for (int dx = -1; dx <= 1; ++dx) {
-                        int gx = (cx + dx + nc) % nc, gy = (cy + dy + nc) % nc, gz = (cz + dz + nc) % nc;
-                        int c0 = (gz * nc + gy) * nc + gx;
-                        for (int q = S.cell_start[c0]; q < S.cell_start[c0 + 1]; ++q) consider(S.cell_beads[q]);
-                    }
+            /* the 27 cell ranges are loaded before the first one is walked */
+            int lo[27], hi[27];
+#pragma unroll
+            for (int s27 = 0; s27 < 27; ++s27) {
+                int dx = s27 % 3 - 1, dy = (s27 / 3) % 3 - 1, dz = s27 / 9 - 1;
+                int gx = (cx + dx + nc) % nc, gy = (cy + dy + nc) % nc, gz = (cz + dz + nc) % nc;
+                int c0 = (gz * nc + gy) * nc + gx;
+                lo[s27] = S.cell_start[c0];
+                hi[s27] = S.cell_start[c0 + 1];
+            }
+            for (int s27 = 0; s27 < 27; ++s27)
+                for (int q = lo[s27]; q < hi[s27]; ++q) consider(S.cell_beads[q]);
         } else {
             for (int c = 0; c < N; ++c) consider(c);
         }
@@ -1308,26 +1334,115 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
     __syncthreads();
 }
 
-/* events(): every bead over its up list and extras (code/events.f:23-123) */
-__device__ void cta_predict_all(const DSys &S, SharedState &sh, double interval_max, int hbonds) {
-    const int N = S.N;
-    for (int b = threadIdx.x; b < N; b += blockDim.x) {
-        double bt = interval_max + DMD_LTSTEP;
-        long long bk = okey(bt);
-        int bp = -1, by = -1;
-        const int *up = S.up + (size_t)b * S.cap;
-        int nu = S.upn[b];
-        for (int k = 0; k < nu + 3; ++k) {
-            int m = k < nu ? up[k] : S.er[4 * b + (k - nu)];
-            if (m <= b) continue;
-            double tij; int ty;
-            if (!d_predict_c(S, b, m, pair_code(S, m, b, hbonds), 0.0, tij, ty)) { set_err(sh, DMD_E_INPUT, b); continue; }
-            check_tij(cta_err(sh), tij, b);
-            long long kk = okey(tij);
-            if (key_less(kk, m, bk, bp)) { bk = kk; bt = tij; bp = m; by = ty; }
-        }
-        set_pred(S, b, bt, bp, by, bt < interval_max);
+/* events() for beads b0 .. b0+nb-1 (nb <= TG_MAX) on one warp: every
+ * (bead, partner) pair of the up lists and extras is one task, 32 per pass,
+ * and the minimum per bead is a segmented reduction over the lanes
+ * (code/events.f:23-123) */
+__device__ void warp_predict_beads(const DSys &S, Err E, FullScratch &F, int b0, int nb, double interval_max,
+                                   int hbonds) {
+    int lane = threadIdx.x & 31;
+    const double H = interval_max + DMD_LTSTEP;
+    const long long Hkey = okey(H), imax_key = okey(interval_max);
+    for (int t = lane; t < nb; t += 32) {
+        F.tg_b[t] = b0 + t;
+        F.tg_k[t] = Hkey; F.tg_p[t] = -1; F.tg_raw[t] = H; F.tg_y[t] = -1;
     }
+    int run = 0;
+    for (int base = 0; base < nb; base += 32) {
+        int t = base + lane;
+        int c = 0;
+        if (t < nb) {
+            int b = b0 + t;
+            c = S.upn[b];
+            for (int k = 0; k < 3; ++k) c += S.er[4 * b + k] > b;
+        }
+        int incl = c;
+        for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
+        if (t < nb) F.tg_base[t] = run + incl - c;
+        run += __shfl_sync(FULL, incl, 31);
+    }
+    if (lane == 0) F.tg_base[nb] = run;
+    __syncwarp();
+    const bool mapped = run <= TMAP_MAX;
+    if (mapped) {
+        for (int t = lane; t < nb; t += 32)
+            for (int q = F.tg_base[t]; q < F.tg_base[t + 1]; ++q) F.tmap[q] = (int8_t)t;
+        __syncwarp();
+    }
+    for (int base = 0; base < run; base += 32) {
+        int q = base + lane;
+        int tgt = -1, pa = -1, pbb = -1, st = -1;
+        if (q < run) {
+            int lo;
+            if (mapped) lo = F.tmap[q];
+            else {
+                int hi = nb - 1;
+                lo = 0;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (F.tg_base[mid] <= q) lo = mid; else hi = mid - 1;
+                }
+            }
+            tgt = lo;
+            int b = b0 + lo;
+            int k = q - F.tg_base[lo];
+            int nu = S.upn[b];
+            int m;
+            if (k < nu) { m = S.up[(size_t)b * S.cap + k]; st = S.upc[(size_t)b * S.cap + k]; }
+            else {
+                int want = k - nu;
+                m = -1;
+                for (int k2 = 0; k2 < 3; ++k2) {
+                    int e = S.er[4 * b + k2];
+                    if (e > b) { if (want == 0) { m = e; break; } --want; }
+                }
+            }
+            if (m > b) { pa = b; pbb = m; }
+        }
+        double tij = 0.0;
+        int ty = 0;
+        bool ok = false;
+        if (pa >= 0) {
+            int code = st >= 0 ? pair_code_st(S, pbb, pa, st) : pair_code(S, pbb, pa, hbonds);
+            ok = d_predict_c(S, pa, pbb, code, 0.0, tij, ty);
+            if (!ok) set_err(E, DMD_E_INPUT, pa);
+            else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
+        }
+        long long k = (tgt >= 0 && ok) ? okey(tij) : DMD_KEY_INF;
+        int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
+        double rt = tij;
+        int y = ty;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long k2 = __shfl_down_sync(FULL, k, o);
+            int p2 = __shfl_down_sync(FULL, p, o);
+            double r2 = __shfl_down_sync(FULL, rt, o);
+            int y2 = __shfl_down_sync(FULL, y, o);
+            int g2 = __shfl_down_sync(FULL, tgt, o);
+            if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
+        }
+        int gprev = __shfl_up_sync(FULL, tgt, 1);
+        bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
+        if (head && key_less(k, p, F.tg_k[tgt], F.tg_p[tgt])) {
+            F.tg_k[tgt] = k; F.tg_p[tgt] = p; F.tg_raw[tgt] = rt; F.tg_y[tgt] = (int8_t)y;
+        }
+        __syncwarp();
+    }
+    for (int t = lane; t < nb; t += 32)
+        set_pred(S, b0 + t, F.tg_raw[t], F.tg_p[t], F.tg_y[t], F.tg_k[t] < imax_key);
+    __syncwarp();
+}
+
+/* events(): every bead over its up list and extras, TG_MAX beads per warp
+ * at a time */
+/* the scratch of warp w is at fs0 + w * stride bytes */
+struct ScratchRef { char *fs0; size_t stride; };
+__device__ void cta_predict_all(const DSys &S, SharedState &sh, ScratchRef fr, double interval_max, int hbonds) {
+    const int N = S.N;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    FullScratch &F = *(FullScratch *)(fr.fs0 + (size_t)warp * fr.stride);
+    for (int b0 = warp * TG_MAX; b0 < N; b0 += nwarps * TG_MAX)
+        warp_predict_beads(S, cta_err(sh), F, b0, min(TG_MAX, N - b0), interval_max, hbonds);
     if (threadIdx.x < 3) {
         int e = N + threadIdx.x;
         bool q = S.tim[e] < interval_max;
@@ -1337,16 +1452,20 @@ __device__ void cta_predict_all(const DSys &S, SharedState &sh, double interval_
     __syncthreads();
 }
 
-__device__ void cta_rebuild(const DSys &S, SharedState &sh, int hbonds) {
+__device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int hbonds) {
+    DMD_SUB(-1);
     for (int b = threadIdx.x; b < S.N; b += blockDim.x) {
         double px = S.x[b], py = S.y[b], pz = S.z[b];
         px = px - d_nint(px); py = py - d_nint(py); pz = pz - d_nint(pz);
         S.x[b] = px; S.y[b] = py; S.z[b] = pz;
         S.ox[b] = px; S.oy[b] = py; S.oz[b] = pz;
+        S.xf[b] = (float)px; S.yf[b] = (float)py; S.zf[b] = (float)pz;
     }
     __syncthreads();
     cta_build_lists(S, sh, hbonds);
-    cta_predict_all(S, sh, sh.sc.interval_max, hbonds);
+    DMD_SUB(13);
+    cta_predict_all(S, sh, fr, sh.sc.interval_max, hbonds);
+    DMD_SUB(14);
     cta_tree_rebuild(S);
 }
 
@@ -1355,31 +1474,63 @@ __device__ void cta_rebuild(const DSys &S, SharedState &sh, int hbonds) {
  * its slice of the beads; the leader (L, rank 0) takes the maximum
  * displacement and decides on a rebuild, which it does alone.  sh.tf_iv
  * holds tfalse of the event on every CTA. */
-__device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L, int rank, int C, int hbonds) {
+__device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L, int rank, int C, ScratchRef fr,
+                                 int hbonds) {
     const int N = S.N;
     const double tf = sh.tf_iv;
     const DTab &T = *S.tab;
     const int stride = C * blockDim.x, t0 = rank * blockDim.x + threadIdx.x;
-    for (int k = t0; k < N + 3; k += stride) {
-        double tn = S.tim[k] - tf;
-        S.tim[k] = tn;
-        S.key[k] = S.queued[k] ? okey(tn) : DMD_KEY_INF;
+    DMD_SUB(-1);
+    for (int k0 = t0; k0 < N + 3; k0 += 4 * stride) {   /* four entries in flight per thread */
+        double tv[4];
+        uint8_t qv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int k = k0 + u * stride;
+            if (k < N + 3) { tv[u] = S.tim[k]; qv[u] = S.queued[k]; }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int k = k0 + u * stride;
+            if (k < N + 3) {
+                double tn = tv[u] - tf;
+                S.tim[k] = tn;
+                S.key[k] = qv[u] ? okey(tn) : DMD_KEY_INF;
+            }
+        }
     }
     /* displ.f: the largest squared displacement over hdelr; dividing after
      * the maximum gives the same value, division being monotone.  The
      * squared displacements are non-negative: their maximum is taken on the
      * bit patterns. */
     long long dmax_bits = 0;
-    for (int k = t0; k < N; k += stride) {
-        double px = S.x[k] + S.vx[k] * tf, py = S.y[k] + S.vy[k] * tf, pz = S.z[k] + S.vz[k] * tf;
-        S.x[k] = px; S.y[k] = py; S.z[k] = pz;
-        double a = S.ox[k] - px, b = S.oy[k] - py, c = S.oz[k] - pz;
-        double dis = a * a + b * b + c * c;
-        long long db = dbits(dis);
-        if (db > dmax_bits) dmax_bits = db;
+    for (int k0 = t0; k0 < N; k0 += 2 * stride) {   /* two beads in flight per thread */
+        double p[2][9];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            int k = k0 + u * stride;
+            if (k < N) {
+                p[u][0] = S.x[k]; p[u][1] = S.y[k]; p[u][2] = S.z[k];
+                p[u][3] = S.vx[k]; p[u][4] = S.vy[k]; p[u][5] = S.vz[k];
+                p[u][6] = S.ox[k]; p[u][7] = S.oy[k]; p[u][8] = S.oz[k];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            int k = k0 + u * stride;
+            if (k < N) {
+                double px = p[u][0] + p[u][3] * tf, py = p[u][1] + p[u][4] * tf, pz = p[u][2] + p[u][5] * tf;
+                S.x[k] = px; S.y[k] = py; S.z[k] = pz;
+                double a = p[u][6] - px, b = p[u][7] - py, c = p[u][8] - pz;
+                double dis = a * a + b * b + c * c;
+                long long db = dbits(dis);
+                if (db > dmax_bits) dmax_bits = db;
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) { long long v = __shfl_xor_sync(FULL, dmax_bits, o); if (v > dmax_bits) dmax_bits = v; }
     __syncthreads();
+    DMD_SUB(9);
     if ((threadIdx.x & 31) == 0) sh.red_d[threadIdx.x >> 5] = __longlong_as_double(dmax_bits);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1416,10 +1567,12 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     }
     if (rank == 0) {
         __syncthreads();
+        DMD_SUB(10);
         if (sh.rebuild) {
             for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
             __syncthreads();
-            cta_rebuild(S, sh, hbonds);
+            cta_rebuild(S, sh, fr, hbonds);
+            DMD_SUB(11);
         }
         if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
     }
@@ -1430,6 +1583,7 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     /* level 1 of the tournament, spread over the CTAs (level 2 follows at
      * the leader's next selection) */
     for (int g = t0; g < S.nl1; g += stride) l1_update(S, g, N + 3);
+    DMD_SUB(12);
     return rb;
 }
 
@@ -1626,7 +1780,7 @@ __device__ void log_event(const DSys &S, long long slot, long long coll, double 
     L->i = i + 1; L->j = j + 1; L->type = type; L->evcode = evcode;
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int hbonds_mask) {
+__global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, int hbonds_mask) {
     __shared__ SharedState sh;
     __shared__ DSys S_sh;
     int r = blockIdx.x;
@@ -1637,7 +1791,8 @@ __global__ void __launch_bounds__(NTHREADS) k_init(DSys *systems, int nsys, int 
     int hbonds = hbonds_mask & 1;
     if (threadIdx.x == 0) { sh.sc = *S.sc; }
     __syncthreads();
-    cta_rebuild(S, sh, hbonds);
+    __shared__ FullScratch fs[NWARPS];
+    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds);
     if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
@@ -1898,7 +2053,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             ph_kind = 7;
             /* ---- interval: all CTAs ---- */
             double t_before = sh.tnow, tf = sh.tf_iv;
-            bool rb = cluster_interval(S, sh, L, rank, C, hbonds);
+            bool rb = cluster_interval(S, sh, L, rank, C, ScratchRef{(char *)&warea[0].fs, sizeof(WarpArea)}, hbonds);
             if (leader && threadIdx.x == 0) {
                 sh.sc.n_interval += 1;
                 log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
@@ -2033,14 +2188,15 @@ cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, c
  * race on it. */
 static __device__ __align__(256) unsigned char g_noalloc_scratch[DMD_NOALLOC_SCRATCH_BYTES];
 
-__global__ void __launch_bounds__(NTHREADS) k_predict_noalloc(DSys S_in, int hbonds, double *tim_out,
+__global__ void __launch_bounds__(NTHREADS, 1) k_predict_noalloc(DSys S_in, int hbonds, double *tim_out,
                                                               int *nptnr_out, int *colt_out) {
     __shared__ SharedState sh;
     __shared__ DSys S_sh;
+    __shared__ FullScratch fs[NWARPS];
     if (threadIdx.x == 0) { S_sh = S_in; sh.sc = *S_in.sc; }
     __syncthreads();
     const DSys &S = S_sh;
-    cta_rebuild(S, sh, hbonds);
+    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds);
     for (int b = threadIdx.x; b < S.N; b += blockDim.x) {
         tim_out[b] = S.tim[b];
         int p = S.nptnr[b];

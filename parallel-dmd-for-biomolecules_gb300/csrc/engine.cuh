@@ -91,6 +91,7 @@ struct DSys {
     const double *blmin_sq, *blmax_sq;   /* their squares */
     double *x, *y, *z, *vx, *vy, *vz;
     double *ox, *oy, *oz;          /* positions at the last list rebuild */
+    float *xf, *yf, *zf;           /* the same in single precision (list-build prefilter) */
     int8_t *ident;                 /* identity 1..28 (5..8: bonded backbone) */
     int *bptnr;                    /* H-bond partner or -1 */
     int *er;                       /* extra_repuls(b,1..4) at er[4b+0..3], -1 = none */
