@@ -231,6 +231,37 @@ int32_t dmd_batch_cluster(dmd_batch *b);
 void dmd_batch_destroy(dmd_batch *b);
 const char *dmd_batch_last_error(dmd_batch *b);
 
+/* ---- serving: continuous batching of independent simulation requests (no
+ * reference counterpart: the reference runs one system per MPI job).
+ * Requests are admitted first in, first out while slots and the
+ * device-memory budget allow; every dmd_server_step() advances all running
+ * requests by up to chunk_events in one launch while the next requests are
+ * uploaded on a second stream, then hands back the finished ones.  A
+ * request's result does not depend on what runs beside it. */
+#define DMD_REQ_QUEUED 0
+#define DMD_REQ_ACTIVE 1
+#define DMD_REQ_DONE   2
+#define DMD_REQ_FAILED 3
+typedef struct dmd_server dmd_server;
+/* hbm_budget_bytes <= 0: 90 % of the free device memory at creation */
+int dmd_server_create(int32_t max_slots, int64_t hbm_budget_bytes, int64_t chunk_events, dmd_server **out);
+/* thread-safe with respect to dmd_server_step; the set-up work runs on the
+ * calling thread */
+int dmd_server_submit(dmd_server *s, const dmd_run_cfg *cfg, const dmd_tables *tables,
+                      const dmd_system *sys, int64_t n_events, int64_t *id);
+int dmd_server_step(dmd_server *s, int32_t *n_active, int32_t *n_finished);
+/* times are seconds of a monotonic host clock */
+int dmd_server_status(dmd_server *s, int64_t id, int32_t *state, int64_t *events_done,
+                      double *t_submit, double *t_admit, double *t_finish);
+int dmd_server_result(dmd_server *s, int64_t id, dmd_diag *diag, double *x, double *y, double *z,
+                      double *vx, double *vy, double *vz, int32_t *bptnr, int32_t *identity,
+                      double *t, double *tfalse, int64_t *coll);
+int dmd_server_release(dmd_server *s, int64_t id);
+int dmd_server_stats(dmd_server *s, int64_t *steps, int64_t *events, double *kernel_ms,
+                     int32_t *n_waiting, int32_t *n_active, int64_t *bytes_used, int64_t *bytes_budget);
+const char *dmd_server_last_error(dmd_server *s);
+void dmd_server_destroy(dmd_server *s);
+
 /* ---- synthetic systems (restates the insertion and velocity steps of
  * genconfig/gen_config_random-SQZ.f90:665-891 on an extended template). */
 typedef struct dmd_gen_spec {

@@ -10,7 +10,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <deque>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -468,6 +471,59 @@ int auto_cluster(int nsys) {
     return 1;
 }
 
+/* one system's pool: allocation (stream-ordered when a stream is given),
+ * layout and the upload of the host state and the pseudo-event times */
+int upload_system(HostSys &H, DevSys &D, cudaStream_t st, std::string &err) {
+    DSys tmp{};
+    size_t bytes = layout(H, tmp, nullptr);
+    if (st) CK(cudaMallocAsync(&D.pool, bytes, st));
+    else CK(cudaMalloc(&D.pool, bytes));
+    D.bytes = bytes;
+    DSys &d = D.d;
+    layout(H, d, (char *)D.pool);
+    d.N = H.N; d.nchains = H.nchains; d.cap = H.cap; d.ncell = H.ncell;
+    d.seed = H.cfg.seed; d.canon = H.cfg.canon; d.flags = H.cfg.flags;
+    d.nl1 = H.nl1; d.nl2 = H.nl2;
+    d.log = nullptr; d.log_cap = 0;
+    size_t N = H.N;
+    /* pseudo events (code/main.F90:408-423) and bead placeholders */
+    std::vector<double> tim(N + 3, H.sc.interval_max + DMD_LTSTEP);
+    std::vector<int> np(N + 3, -1);
+    std::vector<int8_t> ct(N + 3, -1);
+    std::vector<uint8_t> q(N + 3, 0);
+    if (H.cfg.canon) {
+        double tgho = 0.0;
+        uint32_t k = 0;
+        while ((tgho < 1e-18) || (tgho == 1.0)) tgho = dmd_uniform(H.cfg.seed, DMD_STREAM_GHOST0, 0, k++);
+        tim[N] = -1.0 * dmd_log(tgho) * H.tab.avegtime * .0000001;
+    } else {
+        tim[N] = 1000000000.0;
+    }
+    tim[N + 1] = H.sc.interval;
+    tim[N + 2] = 3.3 / (std::sqrt(H.tab.setemp)) + 5;
+    np[N] = np[N + 1] = np[N + 2] = -2;
+    ct[N] = ct[N + 1] = ct[N + 2] = -2;
+    struct Cp { void *dst; const void *src; size_t n; };
+    const Cp cps[] = {
+        {(void *)d.tab, &H.tab, sizeof(DTab)}, {d.sc, &H.sc, sizeof(DScal)},
+        {(void *)d.info, H.info.data(), N * sizeof(BeadInfo)}, {(void *)d.bm, H.bm.data(), N * 8},
+        {(void *)d.blmin, H.blmin.data(), N * 8}, {(void *)d.blmax, H.blmax.data(), N * 8},
+        {(void *)d.blmin_sq, H.blmin_sq.data(), N * 8}, {(void *)d.blmax_sq, H.blmax_sq.data(), N * 8},
+        {d.x, H.x.data(), N * 8}, {d.y, H.y.data(), N * 8}, {d.z, H.z.data(), N * 8},
+        {d.vx, H.vx.data(), N * 8}, {d.vy, H.vy.data(), N * 8}, {d.vz, H.vz.data(), N * 8},
+        {d.ident, H.ident.data(), N}, {d.bptnr, H.bptnr.data(), N * 4}, {d.er, H.er.data(), 4 * N * 4},
+        {d.ovp, H.ovp.data(), 4 * N * 4}, {d.ovc, H.ovc.data(), 4 * N},
+        {d.tim, tim.data(), (N + 3) * 8}, {d.nptnr, np.data(), (N + 3) * 4}, {d.colt, ct.data(), N + 3},
+        {d.queued, q.data(), N + 3},
+    };
+    for (const Cp &c : cps) {
+        if (st) CK(cudaMemcpyAsync(c.dst, c.src, c.n, cudaMemcpyHostToDevice, st));
+        else CK(cudaMemcpy(c.dst, c.src, c.n, cudaMemcpyHostToDevice));
+    }
+    if (st) CK(cudaStreamSynchronize(st));   /* the host vectors above go out of scope */
+    return DMD_OK;
+}
+
 int upload(dmd_batch &B) {
     std::string &err = B.err;
     int n = (int)B.hs.size();
@@ -479,59 +535,9 @@ int upload(dmd_batch &B) {
     std::vector<int> cstart, clen, coff;
     for (int r = 0; r < n; ++r) {
         HostSys &H = B.hs[r];
-        DevSys &D = B.ds[r];
-        DSys tmp{};
-        size_t bytes = layout(H, tmp, nullptr);
-        CK(cudaMalloc(&D.pool, bytes));
-        D.bytes = bytes;
-        DSys &d = D.d;
-        layout(H, d, (char *)D.pool);
-        d.N = H.N; d.nchains = H.nchains; d.cap = H.cap; d.ncell = H.ncell;
-        d.seed = H.cfg.seed; d.canon = H.cfg.canon; d.flags = H.cfg.flags;
-        d.nl1 = H.nl1; d.nl2 = H.nl2;
-        d.log = nullptr; d.log_cap = 0;
-        size_t N = H.N;
-        CK(cudaMemcpy((void *)d.tab, &H.tab, sizeof(DTab), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.sc, &H.sc, sizeof(DScal), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy((void *)d.info, H.info.data(), N * sizeof(BeadInfo), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy((void *)d.bm, H.bm.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy((void *)d.blmin, H.blmin.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy((void *)d.blmax, H.blmax.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy((void *)d.blmin_sq, H.blmin_sq.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy((void *)d.blmax_sq, H.blmax_sq.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.x, H.x.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.y, H.y.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.z, H.z.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.vx, H.vx.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.vy, H.vy.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.vz, H.vz.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.ident, H.ident.data(), N, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.bptnr, H.bptnr.data(), N * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.er, H.er.data(), 4 * N * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.ovp, H.ovp.data(), 4 * N * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.ovc, H.ovc.data(), 4 * N, cudaMemcpyHostToDevice));
-        /* pseudo events (code/main.F90:408-423) and bead placeholders */
-        std::vector<double> tim(N + 3, H.sc.interval_max + DMD_LTSTEP);
-        std::vector<int> np(N + 3, -1);
-        std::vector<int8_t> ct(N + 3, -1);
-        std::vector<uint8_t> q(N + 3, 0);
-        if (H.cfg.canon) {
-            double tgho = 0.0;
-            uint32_t k = 0;
-            while ((tgho < 1e-18) || (tgho == 1.0)) tgho = dmd_uniform(H.cfg.seed, DMD_STREAM_GHOST0, 0, k++);
-            tim[N] = -1.0 * dmd_log(tgho) * H.tab.avegtime * .0000001;
-        } else {
-            tim[N] = 1000000000.0;
-        }
-        tim[N + 1] = H.sc.interval;
-        tim[N + 2] = 3.3 / (std::sqrt(H.tab.setemp)) + 5;
-        np[N] = np[N + 1] = np[N + 2] = -2;
-        ct[N] = ct[N + 1] = ct[N + 2] = -2;
-        CK(cudaMemcpy(d.tim, tim.data(), (N + 3) * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.nptnr, np.data(), (N + 3) * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.colt, ct.data(), N + 3, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d.queued, q.data(), N + 3, cudaMemcpyHostToDevice));
-        hd[r] = d;
+        int rc = upload_system(H, B.ds[r], nullptr, err);
+        if (rc != DMD_OK) return rc;
+        hd[r] = B.ds[r].d;
         coff.push_back((int)cstart.size());
         for (int c = 0; c < H.nchains; ++c) { cstart.push_back(H.chain_start[c]); clen.push_back(H.chain_len[c]); }
     }
@@ -611,8 +617,8 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
     int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
     B.last_cluster = C;
-    CK(dmd_launch_run(B.d_sys, n, max_beads, C, (long long)n_events, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr,
-                      B.st));
+    CK(dmd_launch_run(B.d_sys, n, max_beads, C, (long long)n_events, nullptr, B.hbonds, B.d_cstart, B.d_clen, B.d_coff,
+                      nullptr, B.st));
     CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
     float ms = 0.f;
@@ -687,6 +693,230 @@ void batch_free(dmd_batch &B) {
     if (B.ev1) cudaEventDestroy(B.ev1);
     if (B.st) cudaStreamDestroy(B.st);
     B.ds.clear();
+}
+
+
+/* ---------------------------------------------------------------------- */
+/* serving: continuous batching of independent requests                   */
+/* ---------------------------------------------------------------------- */
+struct ServerReq {
+    long long id = 0;
+    HostSys H;
+    DevSys D;
+    long long total = 0, done = 0;      /* events requested / committed */
+    int state = DMD_REQ_QUEUED;
+    int rc = 0;
+    std::string err;
+    double t_submit = 0, t_admit = 0, t_finish = 0;
+    size_t need = 0;                    /* device bytes of its pool */
+    dmd_diag diag{};
+    std::vector<double> x, y, z, vx, vy, vz;
+    std::vector<int32_t> bptnr, ident;
+    double t = 0, tfalse = 0;
+    long long coll = 0;
+};
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct dmd_server {
+    int max_slots = 0;
+    size_t budget = 0, used = 0;
+    long long chunk = 0;
+    int hbonds = -1;
+    cudaStream_t run_st = nullptr, copy_st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::mutex mu;                              /* submit may come from another host thread */
+    std::map<long long, ServerReq *> reqs;
+    std::deque<ServerReq *> waiting;
+    std::vector<ServerReq *> active;
+    long long next_id = 1;
+    /* device arrays of the active set, grown as needed */
+    DSys *d_sys = nullptr;
+    long long *d_targets = nullptr;
+    int *d_cstart = nullptr, *d_clen = nullptr, *d_coff = nullptr;
+    size_t cap_sys = 0, cap_chains = 0;
+    dmd_diag *d_diag = nullptr;
+    /* statistics */
+    long long steps = 0, events = 0;
+    double kernel_ms = 0;
+    std::string err;
+};
+
+namespace {
+
+int server_grow(dmd_server &V, size_t nsys, size_t nch) {
+    std::string &err = V.err;
+    if (nsys > V.cap_sys) {
+        if (V.d_sys) cudaFree(V.d_sys);
+        if (V.d_targets) cudaFree(V.d_targets);
+        if (V.d_coff) cudaFree(V.d_coff);
+        if (V.d_diag) cudaFree(V.d_diag);
+        size_t c = std::max<size_t>(nsys, 2 * V.cap_sys);
+        CK(cudaMalloc(&V.d_sys, c * sizeof(DSys)));
+        CK(cudaMalloc(&V.d_targets, c * sizeof(long long)));
+        CK(cudaMalloc(&V.d_coff, c * sizeof(int)));
+        CK(cudaMalloc(&V.d_diag, c * sizeof(dmd_diag)));
+        V.cap_sys = c;
+    }
+    if (nch > V.cap_chains) {
+        if (V.d_cstart) cudaFree(V.d_cstart);
+        if (V.d_clen) cudaFree(V.d_clen);
+        size_t c = std::max<size_t>(nch, 2 * V.cap_chains);
+        CK(cudaMalloc(&V.d_cstart, c * sizeof(int)));
+        CK(cudaMalloc(&V.d_clen, c * sizeof(int)));
+        V.cap_chains = c;
+    }
+    return DMD_OK;
+}
+
+/* Admit queued requests, first in first out, while slots and the
+ * device-memory budget allow: allocate, upload and build the lists on the
+ * copy stream (concurrently with the running launch). */
+void server_admit(dmd_server &V, int n_running, std::vector<ServerReq *> &admitted) {
+    while (true) {
+        ServerReq *R;
+        {
+            std::lock_guard<std::mutex> lock(V.mu);
+            if (V.waiting.empty()) break;
+            if (n_running + (int)admitted.size() >= V.max_slots) break;
+            R = V.waiting.front();
+            if (V.used + R->need > V.budget) break;
+            V.waiting.pop_front();
+            V.used += R->need;
+        }
+        std::string e;
+        int rc = upload_system(R->H, R->D, V.copy_st, e);
+        if (rc == DMD_OK) {
+            DSys *one = nullptr;
+            cudaError_t ce = cudaMallocAsync((void **)&one, sizeof(DSys), V.copy_st);
+            if (ce == cudaSuccess) ce = cudaMemcpyAsync(one, &R->D.d, sizeof(DSys), cudaMemcpyHostToDevice, V.copy_st);
+            if (ce == cudaSuccess) ce = dmd_launch_init(one, 1, R->H.cfg.hbonds != 0, V.copy_st);
+            if (ce == cudaSuccess) ce = cudaFreeAsync(one, V.copy_st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(V.copy_st);
+            if (ce != cudaSuccess) { rc = DMD_E_CUDA; e = cudaGetErrorString(ce); }
+        }
+        if (rc == DMD_OK) {
+            DScal sc;
+            if (cudaMemcpy(&sc, R->D.d.sc, sizeof sc, cudaMemcpyDeviceToHost) != cudaSuccess) { rc = DMD_E_CUDA; e = "read-back"; }
+            else if (sc.err) { rc = sc.err; e = "device error during the list build"; }
+        }
+        std::lock_guard<std::mutex> lock(V.mu);
+        if (rc != DMD_OK) {
+            R->state = DMD_REQ_FAILED; R->rc = rc; R->err = e; R->t_finish = now_s();
+            if (R->D.pool) { cudaFree(R->D.pool); R->D.pool = nullptr; }
+            V.used -= R->need;
+            continue;
+        }
+        R->state = DMD_REQ_ACTIVE;
+        R->t_admit = now_s();
+        admitted.push_back(R);
+    }
+}
+
+/* a finished request: its state and diagnostics to host memory */
+int server_retire(dmd_server &V, ServerReq &R, int slot) {
+    std::string &err = V.err;
+    size_t N = R.H.N;
+    const DSys &d = R.D.d;
+    R.x.resize(N); R.y.resize(N); R.z.resize(N); R.vx.resize(N); R.vy.resize(N); R.vz.resize(N);
+    CK(cudaMemcpy(R.x.data(), d.x, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(R.y.data(), d.y, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(R.z.data(), d.z, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(R.vx.data(), d.vx, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(R.vy.data(), d.vy, N * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(R.vz.data(), d.vz, N * 8, cudaMemcpyDeviceToHost));
+    std::vector<int> b(N);
+    CK(cudaMemcpy(b.data(), d.bptnr, N * 4, cudaMemcpyDeviceToHost));
+    R.bptnr.resize(N);
+    for (size_t k = 0; k < N; ++k) R.bptnr[k] = b[k] + 1;
+    std::vector<int8_t> id(N);
+    CK(cudaMemcpy(id.data(), d.ident, N, cudaMemcpyDeviceToHost));
+    R.ident.assign(id.begin(), id.end());
+    CK(cudaMemcpy(&R.diag, V.d_diag + slot, sizeof(dmd_diag), cudaMemcpyDeviceToHost));
+    R.t = R.H.sc.t; R.tfalse = R.H.sc.tfalse; R.coll = R.H.sc.coll;
+    return DMD_OK;
+}
+
+/* One round: launch the running requests for up to chunk events each,
+ * admit queued requests on the copy stream meanwhile, then retire the
+ * finished ones; the admitted requests run from the next round on. */
+int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
+    std::string &err = V.err;
+    std::vector<ServerReq *> act;
+    {
+        std::lock_guard<std::mutex> lock(V.mu);
+        act = V.active;
+    }
+    int n = (int)act.size();
+    int finished = 0;
+    std::vector<ServerReq *> keep, admitted;
+    if (n > 0) {
+        std::vector<DSys> hd(n);
+        std::vector<long long> tg(n);
+        std::vector<int> cstart, clen, coff;
+        int max_beads = 0;
+        for (int r = 0; r < n; ++r) {
+            ServerReq &R = *act[r];
+            hd[r] = R.D.d;
+            tg[r] = std::min(V.chunk, R.total - R.done);
+            coff.push_back((int)cstart.size());
+            for (int c = 0; c < R.H.nchains; ++c) { cstart.push_back(R.H.chain_start[c]); clen.push_back(R.H.chain_len[c]); }
+            max_beads = std::max(max_beads, R.H.N);
+        }
+        int rc = server_grow(V, n, cstart.size());
+        if (rc != DMD_OK) return rc;
+        CK(cudaMemcpyAsync(V.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice, V.run_st));
+        CK(cudaMemcpyAsync(V.d_targets, tg.data(), n * sizeof(long long), cudaMemcpyHostToDevice, V.run_st));
+        CK(cudaMemcpyAsync(V.d_cstart, cstart.data(), cstart.size() * 4, cudaMemcpyHostToDevice, V.run_st));
+        CK(cudaMemcpyAsync(V.d_clen, clen.data(), clen.size() * 4, cudaMemcpyHostToDevice, V.run_st));
+        CK(cudaMemcpyAsync(V.d_coff, coff.data(), coff.size() * 4, cudaMemcpyHostToDevice, V.run_st));
+        CK(cudaEventRecord(V.e0, V.run_st));
+        CK(dmd_launch_run(V.d_sys, n, max_beads, 1, 0, V.d_targets, V.hbonds, V.d_cstart, V.d_clen, V.d_coff, nullptr,
+                          V.run_st));
+        CK(cudaEventRecord(V.e1, V.run_st));
+        CK(dmd_launch_diag(V.d_sys, n, V.d_cstart, V.d_clen, V.d_coff, V.d_diag, V.run_st));
+        server_admit(V, n, admitted);          /* overlaps the launch */
+        CK(cudaStreamSynchronize(V.run_st));   /* (the host vectors above outlive the copies) */
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, V.e0, V.e1) == cudaSuccess) V.kernel_ms += ms;
+        for (int r = 0; r < n; ++r) {
+            ServerReq &R = *act[r];
+            DScal sc;
+            CK(cudaMemcpy(&sc, R.D.d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+            R.H.sc = sc;
+            R.done += sc.done;
+            V.events += sc.done;
+            if (sc.err) {
+                R.state = DMD_REQ_FAILED; R.rc = sc.err;
+                R.err = "device error " + std::to_string(sc.err) + " (info " + std::to_string(sc.err_info) + ")";
+            } else if (R.done >= R.total) {
+                rc = server_retire(V, R, r);
+                if (rc != DMD_OK) return rc;
+                R.state = DMD_REQ_DONE;
+            }
+            if (R.state == DMD_REQ_ACTIVE) { keep.push_back(&R); continue; }
+            R.t_finish = now_s();
+            CK(cudaFreeAsync(R.D.pool, V.copy_st));
+            R.D.pool = nullptr;
+            ++finished;
+            std::lock_guard<std::mutex> lock(V.mu);
+            V.used -= R.need;
+        }
+        ++V.steps;
+    } else {
+        server_admit(V, 0, admitted);
+    }
+    std::lock_guard<std::mutex> lock(V.mu);
+    V.active = keep;
+    for (ServerReq *R : admitted) V.active.push_back(R);
+    if (n_finished) *n_finished = finished;
+    if (n_active) *n_active = (int)V.active.size();
+    return DMD_OK;
 }
 
 }  // namespace
@@ -914,6 +1144,134 @@ int dmd_inspect(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_syst
     int m = (int)(sizeof v / sizeof v[0]);
     for (int k = 0; k < n && k < m; ++k) out[k] = v[k];
     return m;
+}
+
+
+/* ---- serving ---- */
+int dmd_server_create(int32_t max_slots, int64_t hbm_budget_bytes, int64_t chunk_events, dmd_server **out) {
+    if (!out) return DMD_E_INPUT;
+    dmd_server *V = new dmd_server();
+    *out = V;
+    std::string &err = V->err;
+    if (max_slots <= 0 || chunk_events <= 0) { err = "max_slots and chunk_events must be positive"; return DMD_E_INPUT; }
+    V->max_slots = max_slots;
+    V->chunk = chunk_events;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    size_t cap = (size_t)(0.9 * (double)free_b);
+    V->budget = hbm_budget_bytes > 0 ? std::min<size_t>((size_t)hbm_budget_bytes, cap) : cap;
+    CK(cudaStreamCreateWithFlags(&V->run_st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&V->copy_st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&V->e0));
+    CK(cudaEventCreate(&V->e1));
+    return DMD_OK;
+}
+int dmd_server_submit(dmd_server *V, const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,
+                      int64_t n_events, int64_t *id) {
+    if (!V || !cfg || !tables || !sys || !id) return DMD_E_INPUT;
+    if (n_events <= 0) { V->err = "n_events must be positive"; return DMD_E_INPUT; }
+    ServerReq *R = new ServerReq();
+    std::string e;
+    if (!setup_host(R->H, cfg, tables, sys, e)) { delete R; V->err = e; return DMD_E_INPUT; }
+    DSys tmp{};
+    R->need = layout(R->H, tmp, nullptr);
+    R->total = n_events;
+    R->t_submit = now_s();
+    std::lock_guard<std::mutex> lock(V->mu);
+    int hb = cfg->hbonds != 0;
+    if (V->hbonds < 0) V->hbonds = hb;
+    if (V->hbonds != hb) { delete R; V->err = "all requests of a server share the hbonds flag"; return DMD_E_INPUT; }
+    if (R->need > V->budget) { delete R; V->err = "request larger than the device-memory budget"; return DMD_E_CAPACITY; }
+    R->id = V->next_id++;
+    V->reqs[R->id] = R;
+    V->waiting.push_back(R);
+    *id = R->id;
+    return DMD_OK;
+}
+int dmd_server_step(dmd_server *V, int32_t *n_active, int32_t *n_finished) {
+    if (!V) return DMD_E_INPUT;
+    return server_step(*V, n_active, n_finished);
+}
+int dmd_server_status(dmd_server *V, int64_t id, int32_t *state, int64_t *events_done, double *t_submit,
+                      double *t_admit, double *t_finish) {
+    if (!V) return DMD_E_INPUT;
+    std::lock_guard<std::mutex> lock(V->mu);
+    auto it = V->reqs.find(id);
+    if (it == V->reqs.end()) { V->err = "unknown request"; return DMD_E_INPUT; }
+    ServerReq &R = *it->second;
+    if (state) *state = R.state;
+    if (events_done) *events_done = R.done;
+    if (t_submit) *t_submit = R.t_submit;
+    if (t_admit) *t_admit = R.t_admit;
+    if (t_finish) *t_finish = R.t_finish;
+    return R.state == DMD_REQ_FAILED ? R.rc : DMD_OK;
+}
+int dmd_server_result(dmd_server *V, int64_t id, dmd_diag *diag, double *x, double *y, double *z, double *vx,
+                      double *vy, double *vz, int32_t *bptnr, int32_t *identity, double *t, double *tfalse,
+                      int64_t *coll) {
+    if (!V) return DMD_E_INPUT;
+    std::lock_guard<std::mutex> lock(V->mu);
+    auto it = V->reqs.find(id);
+    if (it == V->reqs.end()) { V->err = "unknown request"; return DMD_E_INPUT; }
+    ServerReq &R = *it->second;
+    if (R.state == DMD_REQ_FAILED) { V->err = R.err; return R.rc; }
+    if (R.state != DMD_REQ_DONE) { V->err = "request not finished"; return DMD_E_STATE; }
+    size_t N = R.H.N;
+    if (diag) *diag = R.diag;
+    if (x) { std::memcpy(x, R.x.data(), N * 8); std::memcpy(y, R.y.data(), N * 8); std::memcpy(z, R.z.data(), N * 8); }
+    if (vx) { std::memcpy(vx, R.vx.data(), N * 8); std::memcpy(vy, R.vy.data(), N * 8); std::memcpy(vz, R.vz.data(), N * 8); }
+    if (bptnr) std::memcpy(bptnr, R.bptnr.data(), N * 4);
+    if (identity) std::memcpy(identity, R.ident.data(), N * 4);
+    if (t) *t = R.t;
+    if (tfalse) *tfalse = R.tfalse;
+    if (coll) *coll = R.coll;
+    return DMD_OK;
+}
+int dmd_server_release(dmd_server *V, int64_t id) {
+    if (!V) return DMD_E_INPUT;
+    std::lock_guard<std::mutex> lock(V->mu);
+    auto it = V->reqs.find(id);
+    if (it == V->reqs.end()) { V->err = "unknown request"; return DMD_E_INPUT; }
+    if (it->second->state == DMD_REQ_QUEUED || it->second->state == DMD_REQ_ACTIVE) {
+        V->err = "request still queued or running"; return DMD_E_STATE;
+    }
+    delete it->second;
+    V->reqs.erase(it);
+    return DMD_OK;
+}
+int dmd_server_stats(dmd_server *V, int64_t *steps, int64_t *events, double *kernel_ms, int32_t *n_waiting,
+                     int32_t *n_active, int64_t *bytes_used, int64_t *bytes_budget) {
+    if (!V) return DMD_E_INPUT;
+    std::lock_guard<std::mutex> lock(V->mu);
+    if (steps) *steps = V->steps;
+    if (events) *events = V->events;
+    if (kernel_ms) *kernel_ms = V->kernel_ms;
+    if (n_waiting) *n_waiting = (int32_t)V->waiting.size();
+    if (n_active) *n_active = (int32_t)V->active.size();
+    if (bytes_used) *bytes_used = (int64_t)V->used;
+    if (bytes_budget) *bytes_budget = (int64_t)V->budget;
+    return DMD_OK;
+}
+const char *dmd_server_last_error(dmd_server *V) { return V ? V->err.c_str() : "null handle"; }
+void dmd_server_destroy(dmd_server *V) {
+    if (!V) return;
+    if (V->run_st) cudaStreamSynchronize(V->run_st);
+    if (V->copy_st) cudaStreamSynchronize(V->copy_st);
+    for (auto &kv : V->reqs) {
+        if (kv.second->D.pool) cudaFree(kv.second->D.pool);
+        delete kv.second;
+    }
+    if (V->d_sys) cudaFree(V->d_sys);
+    if (V->d_targets) cudaFree(V->d_targets);
+    if (V->d_cstart) cudaFree(V->d_cstart);
+    if (V->d_clen) cudaFree(V->d_clen);
+    if (V->d_coff) cudaFree(V->d_coff);
+    if (V->d_diag) cudaFree(V->d_diag);
+    if (V->e0) cudaEventDestroy(V->e0);
+    if (V->e1) cudaEventDestroy(V->e1);
+    if (V->run_st) cudaStreamDestroy(V->run_st);
+    if (V->copy_st) cudaStreamDestroy(V->copy_st);
+    delete V;
 }
 
 }  // extern "C"

@@ -1800,7 +1800,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, i
  * by one cluster of C CTAs (C = 1: one CTA).  The leader CTA (rank 0)
  * selects events and keeps the counters; a batch's candidates go one per
  * warp over all CTAs of the cluster. */
-__global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target, int hbonds_mask,
+__global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target_all,
+                                                     const long long *targets, int hbonds_mask,
                                                      const int *chain_start, const int *chain_len,
                                                      const int *chain_off, dmd_diag *outputs, int own_cap, int C) {
     extern __shared__ WarpArea warea[];
@@ -1809,6 +1810,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     const int rank = C > 1 ? (int)cg::this_cluster().block_rank() : 0;
     const int r = blockIdx.x / C;
     if (r >= nsys) return;             /* whole clusters only */
+    const long long target = targets ? targets[r] : target_all;   /* events for this system */
     const bool leader = rank == 0;
     if (threadIdx.x == 0) S_sh = systems[r];
     __syncthreads();
@@ -2147,9 +2149,9 @@ static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, i
 }
 
 /* k_run with one cluster of C CTAs per system (C = 1, 2, 4 or 8) */
-cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, int hbonds,
-                           const int *chain_start, const int *chain_len, const int *chain_off, dmd_diag *outputs,
-                           cudaStream_t st) {
+cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, const long long *targets,
+                           int hbonds, const int *chain_start, const int *chain_len, const int *chain_off,
+                           dmd_diag *outputs, cudaStream_t st) {
     if (C != 1 && C != 2 && C != 4 && C != 8) return cudaErrorInvalidValue;
     cudaError_t e = k_run_attributes();
     if (e != cudaSuccess) return e;
@@ -2157,8 +2159,8 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
     cluster_config(cfg, attr, nsys, C, run_smem(own_cap), st);
-    return cudaLaunchKernelEx(&cfg, k_run, d_systems, nsys, target, hbonds, chain_start, chain_len, chain_off, outputs,
-                              own_cap, C);
+    return cudaLaunchKernelEx(&cfg, k_run, d_systems, nsys, target, targets, hbonds, chain_start, chain_len, chain_off,
+                              outputs, own_cap, C);
 }
 
 /* how many clusters of C CTAs of k_run can be resident at once */

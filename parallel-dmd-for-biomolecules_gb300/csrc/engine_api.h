@@ -9,9 +9,10 @@
 #include "engine.cuh"
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st);
-cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, int hbonds,
-                           const int *chain_start, const int *chain_len, const int *chain_off, dmd_diag *outputs,
-                           cudaStream_t st);
+/* targets: per-system event counts (device array), or NULL for target */
+cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, const long long *targets,
+                           int hbonds, const int *chain_start, const int *chain_len, const int *chain_off,
+                           dmd_diag *outputs, cudaStream_t st);
 cudaError_t dmd_max_active_clusters(int C, int *n);
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st);

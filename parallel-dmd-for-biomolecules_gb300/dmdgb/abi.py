@@ -103,7 +103,11 @@ ENGINE_SYMBOLS = [
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
     "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster",
+    "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
+    "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
 ]
+
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
 def tables_struct(t) -> Tables:
@@ -169,6 +173,25 @@ def _declare(lib) -> None:
     lib.dmd_static_evcode.restype = C.c_int
     lib.dmd_inspect.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), dbl_p, C.c_int32, C.c_char_p, C.c_int32]
     lib.dmd_inspect.restype = C.c_int
+    lib.dmd_server_create.argtypes = [C.c_int32, C.c_int64, C.c_int64, C.POINTER(C.c_void_p)]
+    lib.dmd_server_create.restype = C.c_int
+    lib.dmd_server_submit.argtypes = [C.c_void_p, C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), C.c_int64,
+                                      i64_p]
+    lib.dmd_server_submit.restype = C.c_int
+    lib.dmd_server_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.dmd_server_step.restype = C.c_int
+    lib.dmd_server_status.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), i64_p, dbl_p, dbl_p, dbl_p]
+    lib.dmd_server_status.restype = C.c_int
+    lib.dmd_server_result.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Diag)] + [dbl_p] * 6 + [i32_p] * 2 + [dbl_p, dbl_p, i64_p]
+    lib.dmd_server_result.restype = C.c_int
+    lib.dmd_server_release.argtypes = [C.c_void_p, C.c_int64]
+    lib.dmd_server_release.restype = C.c_int
+    lib.dmd_server_stats.argtypes = [C.c_void_p, i64_p, i64_p, dbl_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), i64_p, i64_p]
+    lib.dmd_server_stats.restype = C.c_int
+    lib.dmd_server_last_error.argtypes = [C.c_void_p]
+    lib.dmd_server_last_error.restype = C.c_char_p
+    lib.dmd_server_destroy.argtypes = [C.c_void_p]
+    lib.dmd_server_destroy.restype = None
 
 
 _engine = None
