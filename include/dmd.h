@@ -228,6 +228,20 @@ int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas);
 int dmd_set_cluster(dmd_handle *h, int32_t ctas);
 /* the cluster size the last run used */
 int32_t dmd_batch_cluster(dmd_batch *b);
+/* Rebuild grid: cells per side of the finest grid (cells as wide as the
+ * list cutoff) divided by div (1..8, at least 3 cells per side).  Lists
+ * and results do not depend on it. */
+int dmd_batch_set_cell_div(dmd_batch *b, int32_t div);
+/* n_launches launches of n_events each, captured into a CUDA graph on the
+ * first call (and again when the sizes or the cluster size change) and
+ * replayed; the same result as dmd_batch_run with n_events * n_launches. */
+int dmd_batch_run_graph(dmd_batch *b, int64_t n_events, int32_t n_launches);
+/* Autotuner: trial runs of a copy of the batch (from its create-time inputs)
+ * for each cluster size that fits and rebuild grids with div 1 and 2; keeps
+ * the fastest for this batch and reports it (best_ms: device time of its
+ * trial).  The batch's own state is not advanced. */
+int dmd_batch_autotune(dmd_batch *b, int64_t trial_events, int32_t *cluster, int32_t *cell_div,
+                       double *best_ms);
 void dmd_batch_destroy(dmd_batch *b);
 const char *dmd_batch_last_error(dmd_batch *b);
 

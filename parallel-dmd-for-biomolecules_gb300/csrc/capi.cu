@@ -450,10 +450,22 @@ struct dmd_batch {
     int ready = 0;
     int cluster = 0;        /* CTAs per system: 1, 2, 4, 8, or 0 = chosen at run time */
     int last_cluster = 0;   /* what the last run used */
+    int cell_div = 1;       /* rebuild grid: the finest grid's cells per side divided by this */
+    cudaGraphExec_t graph = nullptr;   /* captured launches of dmd_batch_run_graph */
+    long long graph_events = 0;
+    int graph_launches = 0, graph_cluster = 0;
 };
 struct dmd_handle { dmd_batch b; };
 
 namespace {
+
+/* cells per side of a coarser rebuild grid: cells stay at least as wide
+ * as the finest grid's (the cutoff), so the lists are the same */
+int coarse_cells(int ncell, int div) {
+    if (ncell < 3 || div <= 1) return ncell;
+    int c = ncell / div;
+    return c >= 3 ? c : 3;
+}
 
 /* CTAs per system when the caller has not chosen: the largest of 4 and 2
  * for which every system's cluster can be resident at once, else 1 */
@@ -604,6 +616,7 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     std::vector<long long> count0(n, 0);
     for (int r = 0; r < n; ++r) {
         hd[r] = B.ds[r].d;
+        hd[r].ncell = coarse_cells(B.hs[r].ncell, B.cell_div);
         if (logs && logs[r].capacity > 0) { hd[r].log = B.d_log + (size_t)r * cap; hd[r].log_cap = logs[r].capacity; }
         else { hd[r].log = nullptr; hd[r].log_cap = 0; }
         DScal sc;
@@ -681,7 +694,96 @@ int diagnostics(dmd_batch &B, int r, dmd_diag *out) {
     return DMD_OK;
 }
 
+/* n_launches consecutive launches of n_events each, captured once into a
+ * CUDA graph (captured again when the sizes or the cluster change) and
+ * replayed; the result equals one run of n_events * n_launches events */
+int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
+    std::string &err = B.err;
+    if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    if (n_launches <= 0 || n_events < 0) { err = "bad launch count"; return DMD_E_INPUT; }
+    int n = (int)B.hs.size();
+    int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
+    int probe = 0;
+    CK(dmd_max_active_clusters(C, &probe));   /* kernel attributes are set outside the capture */
+    std::vector<DSys> hd(n);
+    for (int r = 0; r < n; ++r) {
+        hd[r] = B.ds[r].d;
+        hd[r].ncell = coarse_cells(B.hs[r].ncell, B.cell_div);
+        hd[r].log = nullptr; hd[r].log_cap = 0;
+    }
+    CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
+    if (!B.graph || B.graph_events != n_events || B.graph_launches != n_launches || B.graph_cluster != C) {
+        if (B.graph) cudaGraphExecDestroy(B.graph);
+        B.graph = nullptr;
+        int max_beads = 0;
+        for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaSuccess;
+        for (int k = 0; k < n_launches && ce == cudaSuccess; ++k)
+            ce = dmd_launch_run(B.d_sys, n, max_beads, C, (long long)n_events, nullptr, B.hbonds, B.d_cstart, B.d_clen,
+                                B.d_coff, nullptr, B.st);
+        cudaError_t ce2 = cudaStreamEndCapture(B.st, &g);
+        if (ce != cudaSuccess) { err = cudaGetErrorString(ce); if (ce2 == cudaSuccess) cudaGraphDestroy(g); return DMD_E_CUDA; }
+        CK(ce2);
+        cudaError_t ce3 = cudaGraphInstantiate(&B.graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(ce3);
+        B.graph_events = n_events; B.graph_launches = n_launches; B.graph_cluster = C;
+    }
+    B.last_cluster = C;
+    CK(cudaEventRecord(B.ev0, B.st));
+    CK(cudaGraphLaunch(B.graph, B.st));
+    CK(cudaEventRecord(B.ev1, B.st));
+    int rc = sync_check(B);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) B.last_ms = ms;
+    return rc;
+}
+
+void batch_free(dmd_batch &B);
+
+/* Autotuner: times trial runs of a copy of the batch (made from its
+ * create-time inputs) for each cluster size that fits and two rebuild
+ * grids, and keeps the fastest.  The committed events do not depend on
+ * either choice, so only the speed is compared. */
+int batch_autotune(dmd_batch &B, int64_t trial_events, int32_t *best_cluster, int32_t *best_cell_div, double *best_ms) {
+    std::string &err = B.err;
+    if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    if (trial_events <= 0) { err = "trial_events must be positive"; return DMD_E_INPUT; }
+    dmd_batch T;
+    T.hs = B.hs;
+    T.hbonds = B.hbonds;
+    int rc = upload(T);
+    if (rc != DMD_OK) { err = T.err; batch_free(T); return rc; }
+    int n = (int)B.hs.size();
+    double bms = 1e300;
+    int bc = 1, bd = 1;
+    for (int C : {1, 2, 4}) {
+        int act = 0;
+        if (dmd_max_active_clusters(C, &act) != cudaSuccess) { cudaGetLastError(); continue; }
+        if (C > 1 && act < n) continue;
+        for (int div : {1, 2}) {
+            T.cluster = C;
+            T.cell_div = div;
+            rc = batch_run(T, trial_events, nullptr);          /* warm-up */
+            if (rc == DMD_OK) rc = batch_run(T, trial_events, nullptr);
+            if (rc != DMD_OK) { err = T.err; batch_free(T); return rc; }
+            if (T.last_ms < bms) { bms = T.last_ms; bc = C; bd = div; }
+        }
+    }
+    batch_free(T);
+    B.cluster = bc;
+    B.cell_div = bd;
+    if (best_cluster) *best_cluster = bc;
+    if (best_cell_div) *best_cell_div = bd;
+    if (best_ms) *best_ms = bms;
+    return DMD_OK;
+}
+
 void batch_free(dmd_batch &B) {
+    if (B.graph) cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
     for (auto &D : B.ds) if (D.pool) cudaFree(D.pool);
     if (B.d_sys) cudaFree(B.d_sys);
     if (B.d_cstart) cudaFree(B.d_cstart);
@@ -964,6 +1066,20 @@ int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas) {
     return 0;
 }
 int32_t dmd_batch_cluster(dmd_batch *b) { return b ? b->last_cluster : 0; }
+int dmd_batch_run_graph(dmd_batch *b, int64_t n_events, int32_t n_launches) {
+    if (!b) return DMD_E_INPUT;
+    return batch_run_graph(*b, n_events, n_launches);
+}
+int dmd_batch_autotune(dmd_batch *b, int64_t trial_events, int32_t *cluster, int32_t *cell_div, double *best_ms) {
+    if (!b) return DMD_E_INPUT;
+    return batch_autotune(*b, trial_events, cluster, cell_div, best_ms);
+}
+int dmd_batch_set_cell_div(dmd_batch *b, int32_t div) {
+    if (!b) return DMD_E_INPUT;
+    if (div < 1 || div > 8) { b->err = "cell_div must be 1..8"; return DMD_E_INPUT; }
+    b->cell_div = div;
+    return 0;
+}
 int dmd_set_cluster(dmd_handle *h, int32_t ctas) { return h ? dmd_batch_set_cluster(&h->b, ctas) : DMD_E_INPUT; }
 double dmd_last_run_ms(dmd_handle *h) { return h ? h->b.last_ms : 0.0; }
 

@@ -102,7 +102,8 @@ ENGINE_SYMBOLS = [
     "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
-    "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster",
+    "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster", "dmd_batch_set_cell_div",
+    "dmd_batch_run_graph", "dmd_batch_autotune",
     "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
     "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
 ]
@@ -166,6 +167,12 @@ def _declare(lib) -> None:
     lib.dmd_set_cluster.restype = C.c_int
     lib.dmd_batch_cluster.argtypes = [C.c_void_p]
     lib.dmd_batch_cluster.restype = C.c_int32
+    lib.dmd_batch_set_cell_div.argtypes = [C.c_void_p, C.c_int32]
+    lib.dmd_batch_set_cell_div.restype = C.c_int
+    lib.dmd_batch_run_graph.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
+    lib.dmd_batch_run_graph.restype = C.c_int
+    lib.dmd_batch_autotune.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dbl_p]
+    lib.dmd_batch_autotune.restype = C.c_int
     lib.dmd_predict_all_noalloc.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System),
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int32]
     lib.dmd_predict_all_noalloc.restype = C.c_int

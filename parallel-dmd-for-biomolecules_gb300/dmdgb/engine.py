@@ -143,6 +143,23 @@ class Batch:
         """The cluster size the last run used."""
         return int(self.lib.dmd_batch_cluster(self.h))
 
+    def set_cell_div(self, div: int):
+        """Coarser rebuild grid (finest cells per side / div); results do not depend on it."""
+        _check(self.lib.dmd_batch_set_cell_div(self.h, int(div)), self.lib, self.h, "dmd_batch_last_error")
+
+    def run_graph(self, n_events: int, n_launches: int):
+        """n_launches launches of n_events each, replayed from a captured CUDA graph."""
+        _check(self.lib.dmd_batch_run_graph(self.h, int(n_events), int(n_launches)), self.lib, self.h,
+               "dmd_batch_last_error")
+
+    def autotune(self, trial_events: int = 5000) -> dict:
+        """Pick the cluster size and rebuild grid by timing trial runs on a copy."""
+        c, d = C.c_int32(), C.c_int32()
+        ms = C.c_double()
+        _check(self.lib.dmd_batch_autotune(self.h, int(trial_events), C.byref(c), C.byref(d), C.byref(ms)), self.lib,
+               self.h, "dmd_batch_last_error")
+        return {"cluster": c.value, "cell_div": d.value, "trial_ms": ms.value}
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.dmd_batch_destroy(self.h)

@@ -151,3 +151,43 @@ def test_cluster_hbond_plain(built):
     olog = ora.run(200000, log_capacity=200064)
     k = first_mismatch(glog, olog)
     assert k < 0, f"logs diverge at {k}:\n{describe(glog, olog, k)}"
+
+
+def test_graph_replay_and_grid(built):
+    """Launches replayed from a captured CUDA graph, and a coarser rebuild
+    grid, commit the same events as one plain run."""
+    specs = systems.config_c3(32, seed=3)[:3]
+    for s in specs:
+        systems.generate(s)
+    ref = Batch(specs)
+    ref.run(24000)
+    want = [ref.state(r) for r in range(3)]
+    ref.close()
+    g = Batch(specs)
+    g.set_cell_div(2)
+    g.run_graph(6000, 2)
+    g.run_graph(6000, 2)      # the second call replays the same graph
+    for r in range(3):
+        st = g.state(r)
+        for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity"):
+            assert np.array_equal(st[key], want[r][key]), (r, key)
+        assert st["coll"] == want[r]["coll"]
+    g.close()
+
+
+def test_autotune_keeps_state(built):
+    specs = systems.config_c3(32, seed=4)[:4]
+    for s in specs:
+        systems.generate(s)
+    b = Batch(specs)
+    before = [b.state(r) for r in range(4)]
+    cfg = b.autotune(3000)
+    assert cfg["cluster"] in (1, 2, 4) and cfg["cell_div"] in (1, 2) and cfg["trial_ms"] > 0
+    for r in range(4):
+        st = b.state(r)
+        assert np.array_equal(st["x"], before[r]["x"]) and st["coll"] == before[r]["coll"]
+    logs = b.run(10000, log_capacity=10064)
+    for r, s in enumerate(specs):
+        olog = Oracle(s).run(10000, log_capacity=10064)
+        assert first_mismatch(logs[r], olog) < 0, r
+    b.close()
