@@ -117,23 +117,30 @@ class ClockSampler:
 
 # ------------------------------------------------------------ CPU baseline
 def _cpu_worker(args):
-    spec, n_events = args
+    """One host process: its share of the replicas, one after another."""
+    part, n_events = args
     sys.path.insert(0, REPO)
     sys.path.insert(0, PKG)
     from oracle.oracle import Oracle
 
-    o = Oracle(spec)
-    t0 = time.perf_counter()
-    o.run(n_events)
-    return n_events, time.perf_counter() - t0
+    busy = 0.0
+    for spec in part:
+        o = Oracle(spec)
+        t0 = time.perf_counter()
+        o.run(n_events)
+        busy += time.perf_counter() - t0
+    return n_events * len(part), busy
 
 
 def cpu_rate(specs, events_per_replica: int, cores: int):
-    """Aggregate events/s of the CPU restatement, one replica per core."""
-    work = [(specs[k % len(specs)], events_per_replica) for k in range(cores)]
+    """Aggregate events/s of the CPU restatement: every replica advanced by
+    events_per_replica, the replicas dealt round-robin to `cores` processes;
+    the rate is all events over the busiest process's time."""
+    parts = [specs[k::cores] for k in range(min(cores, len(specs)))]
+    work = [(p, events_per_replica) for p in parts if p]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
+    with ctx.Pool(len(work)) as pool:
         res = pool.map(_cpu_worker, work)
     wall = time.perf_counter() - t0
     total = sum(r[0] for r in res)
@@ -186,7 +193,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc, "events_per_replica_per_step": n_ev},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes, one C3 replica each, {n_ev} events per step"},
+                         "sample": f"all {len(specs)} replicas, {n_ev} events each, dealt to {cores} processes"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -216,6 +223,7 @@ def run_ours(args):
     E = args.events
     batch = Batch(specs)
     lib = batch.lib
+    tuned = batch.autotune(max(2000, E // 4)) if not args.no_tune else None
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -289,13 +297,16 @@ def run_ours(args):
     serving = None
     if rank == 0 and not args.no_serve:
         serving = run_serving(args)
+    single = None
+    if rank == 0 and not args.no_single:
+        single = run_single_systems(E)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = max(1, min(os.cpu_count() or 1, 64))
         r, tot, wall = cpu_rate(specs, args.cpu_events, cores)
         cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"CPU restatement, {cores} processes, one replica each, {args.cpu_events} events, {wall:.1f} s"}
+               "sample": f"CPU restatement: all {len(specs)} replicas, {args.cpu_events} events each, dealt to {cores} processes, {wall:.1f} s wall"}
 
     if rank == 0:
         line = {
@@ -304,7 +315,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": desc, "replicas": len(specs), "events_per_replica_per_step": E,
                        "beads_total": int(sum(s.n_beads for s in specs)), "l2": "flushed (256 MB write) between steps",
-                       "parallelism": f"replicas: one CTA per system, {world} GPU(s)"},
+                       "parallelism": f"replicas: one cluster of {batch.cluster} CTA(s) per system, {world} GPU(s)",
+                       "autotuned": tuned},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "plain_gpu": {"value": plain_value, "unit": UNIT, "replicas_timed": n_plain,
                           "note": "same replicas, one system per launch, one after another"},
@@ -315,10 +327,32 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "serving": serving,
+            "single_system": single,
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_single_systems(E: int) -> dict:
+    """The single-system workloads on the plain path (one system per launch,
+    autotuned cluster): 48 x KLVFFAE (1,344 beads) and 1,000 random 10-mers
+    (40,000 beads), committed events/s over E events after a warm-up."""
+    from dmdgb import systems
+    from dmdgb.engine import Engine
+
+    out = {}
+    for name, spec in (("c2_1344_beads", systems.config_c2()), ("c4_40000_beads", systems.config_c4())):
+        systems.generate(spec)
+        from dmdgb.engine import Batch
+        b = Batch([spec])
+        t = b.autotune(max(2000, E // 4))
+        b.run(E)
+        b.run(E)
+        ms = b.lib.dmd_batch_last_run_ms(b.h)
+        out[name] = {"events_per_s": E / ms * 1e3, "cluster": t["cluster"], "cell_div": t["cell_div"]}
+        b.close()
+    return out
 
 
 def run_serving(args) -> dict:
@@ -353,10 +387,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c3")
     ap.add_argument("--events", type=int, default=20000, help="events per replica per step")
-    ap.add_argument("--cpu-events", type=int, default=200000)
+    ap.add_argument("--cpu-events", type=int, default=300000, help="CPU baseline: events per replica")
     ap.add_argument("--plain-replicas", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-scale", type=float, default=0.01)
     ap.add_argument("--serve-slots", type=int, default=256)

@@ -448,6 +448,8 @@ struct dmd_batch {
     double last_ms = 0.0;
     std::string err;
     int ready = 0;
+    std::vector<dmd_diag> diag_cache;   /* diagnostics of all systems, valid until the next run */
+    bool diag_valid = false;
     int cluster = 0;        /* CTAs per system: 1, 2, 4, 8, or 0 = chosen at run time */
     int last_cluster = 0;   /* what the last run used */
     int cell_div = 1;       /* rebuild grid: the finest grid's cells per side divided by this */
@@ -467,10 +469,13 @@ int coarse_cells(int ncell, int div) {
     return c >= 3 ? c : 3;
 }
 
-/* CTAs per system when the caller has not chosen: the largest of 4 and 2
- * for which every system's cluster can be resident at once, else 1 */
+/* CTAs per system when the caller has not chosen: one CTA per system for
+ * many systems (a system's batches rarely fill more than one CTA's warps),
+ * else the largest of 4 and 2 for which every system's cluster can be
+ * resident at once */
 int auto_cluster(int nsys) {
     static int max_active[9] = {0};
+    if (nsys >= 16) return 1;
     for (int C : {4, 2}) {
         if (max_active[C] == 0) {
             int v = 0;
@@ -602,6 +607,7 @@ int sync_check(dmd_batch &B) {
 int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     std::string &err = B.err;
     if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    B.diag_valid = false;
     int n = (int)B.hs.size();
     /* event logs: one device ring per system for this call */
     std::vector<DSys> hd(n);
@@ -685,12 +691,19 @@ int get_state(dmd_batch &B, int r, double *x, double *y, double *z, double *vx, 
     return DMD_OK;
 }
 
+/* diagnostics of every system in one launch, kept until the next run */
 int diagnostics(dmd_batch &B, int r, dmd_diag *out) {
     std::string &err = B.err;
-    if (r < 0 || r >= (int)B.hs.size() || !out) { err = "bad argument"; return DMD_E_INPUT; }
-    CK(dmd_launch_diag(B.d_sys, (int)B.hs.size(), B.d_cstart, B.d_clen, B.d_coff, B.d_diag, B.st));
-    CK(cudaStreamSynchronize(B.st));
-    CK(cudaMemcpy(out, B.d_diag + r, sizeof(dmd_diag), cudaMemcpyDeviceToHost));
+    int n = (int)B.hs.size();
+    if (r < 0 || r >= n || !out) { err = "bad argument"; return DMD_E_INPUT; }
+    if (!B.diag_valid) {
+        CK(dmd_launch_diag(B.d_sys, n, B.d_cstart, B.d_clen, B.d_coff, B.d_diag, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        B.diag_cache.resize(n);
+        CK(cudaMemcpy(B.diag_cache.data(), B.d_diag, n * sizeof(dmd_diag), cudaMemcpyDeviceToHost));
+        B.diag_valid = true;
+    }
+    *out = B.diag_cache[r];
     return DMD_OK;
 }
 
@@ -701,6 +714,7 @@ int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
     std::string &err = B.err;
     if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
     if (n_launches <= 0 || n_events < 0) { err = "bad launch count"; return DMD_E_INPUT; }
+    B.diag_valid = false;
     int n = (int)B.hs.size();
     int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
     int probe = 0;

@@ -1700,7 +1700,7 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
 /* The bead events below the cut, sorted in (key, index) order into
  * sh.sort_*; returns how many there are (1 when the window could not be
  * made small enough: the root alone). */
-__device__ int cta_candidates(const DSys &S, SharedState &sh, int root, long long kroot) {
+__device__ int cta_candidates(const DSys &S, SharedState &sh, int root, long long kroot, int slots) {
     const int N = S.N;
     long long kp = min(min(S.key[N], S.key[N + 1]), S.key[N + 2]);
     bool ok = false;
@@ -1761,8 +1761,8 @@ __device__ int cta_candidates(const DSys &S, SharedState &sh, int root, long lon
     }
     if (threadIdx.x == 0) {
         /* aim at about one to four candidates per warp */
-        if (nc < NWARPS) sh.delta = sh.delta * 2.0;
-        else if (nc > 4 * NWARPS) sh.delta = sh.delta * 0.5;
+        if (nc < slots) sh.delta = sh.delta * 2.0;
+        else if (nc > 4 * slots) sh.delta = sh.delta * 0.5;
         if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
     }
     __syncthreads();
@@ -1872,7 +1872,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     __syncthreads();
                     m = 1;
                 } else {
-                    m = cta_candidates(S, sh, e, kroot);
+                    m = cta_candidates(S, sh, e, kroot, slots);
                     if (m > slots) m = slots;
                     if (m > left) m = (int)left;
                 }
