@@ -41,10 +41,10 @@ UNIT = "events/s"
 
 # --------------------------------------------------------------- workloads
 def make_workload(name: str, rank: int = 0):
-    from dmdgb import systems
+    from dmdgb import sharding, systems
 
     if name == "c3":
-        specs = systems.config_c3(32, seed=1 + 1000 * rank)
+        specs = systems.config_c3(32, seed=sharding.replica_seed(rank))
         desc = "C3: 32 replicas, 8-96 chains x 16-mer random sequences, 5 mM, T* 0.18-0.50"
     elif name == "c2":
         specs = [systems.config_c2(seed=1 + rank)]
@@ -248,10 +248,8 @@ def run_ours(args):
     d1 = [batch.diagnostics(r) for r in range(len(specs))]
     step_s = sum(ms) / 1000.0
     events = E * len(specs) * args.steps
-    if world > 1:
-        t = torch.tensor([step_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_s = float(t.item())
+    from dmdgb import sharding
+    step_s = sharding.max_over_ranks(step_s, device="cuda")   # the slowest rank's time
     value = events * world / step_s
     pair_events = sum(b["n_pair"] - a["n_pair"] for a, b in zip(d0, d1))
     nbr = float(np.mean([d["nbr_mean"] for d in d1]))

@@ -143,8 +143,10 @@ int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables,
  * log may be NULL. */
 int dmd_run(dmd_handle *h, int64_t n_events, dmd_event_log *log);
 
-/* Full prediction pass of code/events.f:11-127 on the current state:
- * tim/nptnr/coltype per bead (1-based partners, times relative to t). */
+/* The per-bead event predictions: after dmd_create the full pass of
+ * code/events.f:11-127; after a run the queue's current entries (those the
+ * partial re-predictions of code/partial_events.f left).  tim/nptnr/coltype
+ * per bead (1-based partners, times relative to t). */
 int dmd_predict_all(dmd_handle *h, double *tim, int32_t *nptnr, int32_t *coltype);
 
 /* State read-back: the stored positions (box units; the position at the
