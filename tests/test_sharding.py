@@ -1,6 +1,7 @@
 """The multi-process path of bench.py on CPU: two gloo ranks on 127.0.0.1,
 each with its own replica set, agree on the slowest rank's step time."""
 import os
+import re
 import subprocess
 import sys
 import textwrap
@@ -46,5 +47,5 @@ def test_two_gloo_ranks_max(tmp_path):
            "--master-addr", "127.0.0.1", "--master-port", "29541", str(script)]
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=240, env=env)
     assert out.returncode == 0, out.stderr[-2000:]
-    lines = [l for l in out.stdout.splitlines() if l.startswith("rank")]
-    assert sorted(lines) == ["rank 0 max 2.5", "rank 1 max 2.5"]
+    found = sorted(re.findall(r"rank (\d) max ([0-9.]+)", out.stdout))
+    assert found == [("0", "2.5"), ("1", "2.5")], out.stdout
