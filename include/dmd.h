@@ -169,6 +169,16 @@ int dmd_get_evcode(dmd_handle *h, int8_t *out);
  * events on the stream it was launched on (no reference counterpart). */
 double dmd_last_run_ms(dmd_handle *h);
 
+/* Checkpoint of the whole engine state of a system (positions, velocities,
+ * H-bond state, lists, event queue, counters, random-stream position), so
+ * that a run resumes bit-identically (the reference's restart from
+ * .config/.bptnr/.lastvel records, code/main.F90:240-321, rebuilds the
+ * queue and restarts the intervals instead).  Load into a handle created
+ * from the same system. */
+int64_t dmd_state_bytes(dmd_handle *h);
+int dmd_save_state(dmd_handle *h, void *buf, int64_t n);
+int dmd_load_state(dmd_handle *h, const void *buf, int64_t n);
+
 void dmd_destroy(dmd_handle *h);
 
 const char *dmd_last_error(dmd_handle *h);

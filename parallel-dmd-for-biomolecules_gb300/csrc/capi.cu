@@ -1404,4 +1404,53 @@ void dmd_server_destroy(dmd_server *V) {
     delete V;
 }
 
+
+/* ---- checkpoint: the whole device state of a system ---- */
+namespace {
+struct CkptHeader {
+    char magic[8];                 /* "DMDGBCK1" */
+    int64_t n_beads, cap, ncell, bytes;
+};
+}
+int64_t dmd_state_bytes(dmd_handle *h) {
+    if (!h || !h->b.ready) return DMD_E_STATE;
+    return (int64_t)(sizeof(CkptHeader) + h->b.ds[0].bytes);
+}
+int dmd_save_state(dmd_handle *h, void *buf, int64_t n) {
+    if (!h || !h->b.ready) return DMD_E_STATE;
+    dmd_batch &B = h->b;
+    std::string &err = B.err;
+    const DevSys &D = B.ds[0];
+    if (!buf || n < (int64_t)(sizeof(CkptHeader) + D.bytes)) { err = "buffer smaller than dmd_state_bytes()"; return DMD_E_INPUT; }
+    CkptHeader hd{};
+    std::memcpy(hd.magic, "DMDGBCK1", 8);
+    hd.n_beads = B.hs[0].N; hd.cap = B.hs[0].cap; hd.ncell = B.hs[0].ncell; hd.bytes = (int64_t)D.bytes;
+    std::memcpy(buf, &hd, sizeof hd);
+    CK(cudaStreamSynchronize(B.st));
+    CK(cudaMemcpy((char *)buf + sizeof hd, D.pool, D.bytes, cudaMemcpyDeviceToHost));
+    return DMD_OK;
+}
+int dmd_load_state(dmd_handle *h, const void *buf, int64_t n) {
+    if (!h || !h->b.ready) return DMD_E_STATE;
+    dmd_batch &B = h->b;
+    std::string &err = B.err;
+    const DevSys &D = B.ds[0];
+    CkptHeader hd{};
+    if (!buf || n < (int64_t)sizeof hd) { err = "buffer too small"; return DMD_E_INPUT; }
+    std::memcpy(&hd, buf, sizeof hd);
+    if (std::memcmp(hd.magic, "DMDGBCK1", 8) != 0) { err = "not a checkpoint of this engine"; return DMD_E_INPUT; }
+    if (hd.n_beads != B.hs[0].N || hd.cap != B.hs[0].cap || hd.ncell != B.hs[0].ncell || hd.bytes != (int64_t)D.bytes ||
+        n < (int64_t)(sizeof hd + D.bytes)) {
+        err = "checkpoint of a different system shape (beads, list capacity or grid)";
+        return DMD_E_INPUT;
+    }
+    CK(cudaStreamSynchronize(B.st));
+    CK(cudaMemcpy(D.pool, (const char *)buf + sizeof hd, D.bytes, cudaMemcpyHostToDevice));
+    DScal sc;
+    CK(cudaMemcpy(&sc, D.d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+    B.hs[0].sc = sc;
+    B.diag_valid = false;
+    return DMD_OK;
+}
+
 }  // extern "C"

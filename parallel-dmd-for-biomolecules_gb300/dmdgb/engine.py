@@ -77,6 +77,20 @@ class Engine:
         _check(rc, self.lib, self.h)
         return None
 
+    def save_state(self) -> bytes:
+        """The whole engine state (resumes bit-identically with load_state)."""
+        n = int(self.lib.dmd_state_bytes(self.h))
+        if n < 0:
+            _check(n, self.lib, self.h)
+        buf = C.create_string_buffer(n)
+        _check(self.lib.dmd_save_state(self.h, buf, n), self.lib, self.h)
+        return buf.raw
+
+    def load_state(self, blob: bytes):
+        """Restore a state saved from an engine created from the same system."""
+        buf = C.create_string_buffer(blob, len(blob))
+        _check(self.lib.dmd_load_state(self.h, buf, len(blob)), self.lib, self.h)
+
     def predictions(self):
         tim = np.zeros(self.n)
         np_ = np.zeros(self.n, np.int32)
