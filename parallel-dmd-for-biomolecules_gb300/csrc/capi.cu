@@ -37,7 +37,7 @@ struct HostSys {
     int N = 0, nchains = 0, cap = 128, ncell = 0, nl1 = 0, nl2 = 0;
     std::vector<int> chain_start, chain_len;
     std::vector<BeadInfo> info;
-    std::vector<double> bm, blmin, blmax, blmin_sq, blmax_sq;
+    std::vector<double> bm, blmin, blmax, blmin_sq, blmax_sq, rblmin_sq, rblmax_sq;
     std::vector<double> x, y, z, vx, vy, vz;
     std::vector<int8_t> ident;
     std::vector<int> bptnr, er, ovp;
@@ -126,7 +126,10 @@ void build_tables(HostSys &H, const dmd_tables *T, double boxl) {
             D.ncfac_sq[a][b] = D.sigma_sq[a][b] * p * p;
             D.core15_sq[a][b] = D.sigma_sq[a][b] * (p * p);
         }
-    for (int l = 0; l < DMD_NC; ++l) { D.evp2_sq[l] = D.evp2[l] * D.evp2[l]; D.evp3_sq[l] = D.evp3[l] * D.evp3[l]; }
+    for (int l = 0; l < DMD_NC; ++l) {
+        D.evp2_sq[l] = D.evp2[l] * D.evp2[l]; D.evp3_sq[l] = D.evp3[l] * D.evp3[l];
+        D.revp2_sq[l] = 1.0 / D.evp2_sq[l]; D.revp3_sq[l] = 1.0 / D.evp3_sq[l];
+    }
     /* kept for nbor_setup: scaled bead diameters and the side-chain wells */
     for (int k = 1; k <= 28; ++k) { H.sigma_raw[k] = sigma[k]; H.welldia_raw[k] = welldia[k]; }
     (void)wel;
@@ -310,7 +313,13 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
     for (int b = 0; b < H.N; ++b) H.bm[b] = bmass[H.ident[b]];
     H.blmin_sq.assign(H.N, 0.0);
     H.blmax_sq.assign(H.N, 0.0);
-    for (int b = 0; b < H.N; ++b) { H.blmin_sq[b] = H.blmin[b] * H.blmin[b]; H.blmax_sq[b] = H.blmax[b] * H.blmax[b]; }
+    H.rblmin_sq.assign(H.N, 0.0);
+    H.rblmax_sq.assign(H.N, 0.0);
+    for (int b = 0; b < H.N; ++b) {
+        H.blmin_sq[b] = H.blmin[b] * H.blmin[b]; H.blmax_sq[b] = H.blmax[b] * H.blmax[b];
+        if (H.blmin_sq[b] != 0.0) H.rblmin_sq[b] = 1.0 / H.blmin_sq[b];
+        if (H.blmax_sq[b] != 0.0) H.rblmax_sq[b] = 1.0 / H.blmax_sq[b];
+    }
 
     build_tables(H, T, S->boxl);
     for (int a = 0; a < DMD_NT; ++a)
@@ -318,6 +327,7 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
             double bmi = bmass[a], bmj = bmass[b];
             H.tab.rmass[a][b] = (bmi + bmj) != 0.0 ? 2 * bmi * bmj / (bmi + bmj) : 0.0;
         }
+    for (int a = 0; a < DMD_NT; ++a) H.tab.rbm[a] = bmass[a] != 0.0 ? 1.0 / bmass[a] : 0.0;
     H.tab.setemp = cfg->tstar * 12.0;
     H.tab.avegtime = 0.00005 / std::sqrt(H.tab.setemp);
 
@@ -405,6 +415,7 @@ size_t layout(const HostSys &H, DSys &d, char *base, bool for_run = true) {
     d.info = P.take<BeadInfo>(N);
     d.bm = P.take<double>(N); d.blmin = P.take<double>(N); d.blmax = P.take<double>(N);
     d.blmin_sq = P.take<double>(N); d.blmax_sq = P.take<double>(N);
+    d.rblmin_sq = P.take<double>(N); d.rblmax_sq = P.take<double>(N);
     d.x = P.take<double>(N); d.y = P.take<double>(N); d.z = P.take<double>(N);
     d.vx = P.take<double>(N); d.vy = P.take<double>(N); d.vz = P.take<double>(N);
     d.ox = P.take<double>(N); d.oy = P.take<double>(N); d.oz = P.take<double>(N);
@@ -526,6 +537,7 @@ int upload_system(HostSys &H, DevSys &D, cudaStream_t st, std::string &err) {
         {(void *)d.info, H.info.data(), N * sizeof(BeadInfo)}, {(void *)d.bm, H.bm.data(), N * 8},
         {(void *)d.blmin, H.blmin.data(), N * 8}, {(void *)d.blmax, H.blmax.data(), N * 8},
         {(void *)d.blmin_sq, H.blmin_sq.data(), N * 8}, {(void *)d.blmax_sq, H.blmax_sq.data(), N * 8},
+        {(void *)d.rblmin_sq, H.rblmin_sq.data(), N * 8}, {(void *)d.rblmax_sq, H.rblmax_sq.data(), N * 8},
         {d.x, H.x.data(), N * 8}, {d.y, H.y.data(), N * 8}, {d.z, H.z.data(), N * 8},
         {d.vx, H.vx.data(), N * 8}, {d.vy, H.vy.data(), N * 8}, {d.vz, H.vz.data(), N * 8},
         {d.ident, H.ident.data(), N}, {d.bptnr, H.bptnr.data(), N * 4}, {d.er, H.er.data(), 4 * N * 4},
@@ -1238,6 +1250,7 @@ int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, co
         {(void *)d.info, H.info.data(), N * sizeof(BeadInfo)}, {(void *)d.bm, H.bm.data(), N * 8},
         {(void *)d.blmin, H.blmin.data(), N * 8}, {(void *)d.blmax, H.blmax.data(), N * 8},
         {(void *)d.blmin_sq, H.blmin_sq.data(), N * 8}, {(void *)d.blmax_sq, H.blmax_sq.data(), N * 8},
+        {(void *)d.rblmin_sq, H.rblmin_sq.data(), N * 8}, {(void *)d.rblmax_sq, H.rblmax_sq.data(), N * 8},
         {d.x, H.x.data(), N * 8}, {d.y, H.y.data(), N * 8}, {d.z, H.z.data(), N * 8},
         {d.vx, H.vx.data(), N * 8}, {d.vy, H.vy.data(), N * 8}, {d.vz, H.vz.data(), N * 8},
         {d.ident, H.ident.data(), N}, {d.bptnr, H.bptnr.data(), N * 4}, {d.er, H.er.data(), 4 * N * 4},

@@ -408,10 +408,12 @@ __device__ void warp_impulse(const DSys &S, int i, int j, const WRel &w, double 
             bool minus = (bump < 0) != isj;
             p = minus ? p - bd * r : p + bd * r;
         }
-        double bmb = S.bm[b];
+        double bmb = S.bm[b], rbmb = S.tab->rbm[S.ident[b]];   /* bm(b) = mass(identity(b)) */
         double delv = ratio * r;
-        V[b] = isj ? V[b] + delv / bmb : V[b] - delv / bmb;
-        p = isj ? p - delv * tf / bmb : p + delv * tf / bmb;
+        double dv = div_by(delv, bmb, rbmb);
+        double dp = div_by(delv * tf, bmb, rbmb);
+        V[b] = isj ? V[b] + dv : V[b] - dv;
+        p = isj ? p - dp : p + dp;
         P[b] = p;
     }
     __syncwarp();
@@ -436,6 +438,7 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
     int lane = threadIdx.x & 31;
     const DTab &T = *S.tab;
     WRel w = warp_rel(S, i, j, tf);
+    DMD_SUB(12);
     double ratio = 0.0, bd = 0.0;
     int bump = 0;
     if (lane == 0) {
@@ -447,10 +450,12 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
         bool side = evcode >= 10 && evcode <= 12;
         if (ct == 2) {
             double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];
-            ratio = rmass * bij / lo;
+            double rlo = side ? S.rblmin_sq[i] : T.revp2_sq[evcode];
+            ratio = div_by(rmass * bij, lo, rlo);
         } else if (ct == 3) {
             double hi = side ? S.blmax_sq[i] : T.evp3_sq[evcode];
-            ratio = rmass * bij / hi;
+            double rhi = side ? S.rblmax_sq[i] : T.revp3_sq[evcode];
+            ratio = div_by(rmass * bij, hi, rhi);
         } else if (ct == 1) {
             double sigsq;
             if (evcode == 15) sigsq = S.bptnr[i] == j ? T.core15_sq[a][b] : T.sigma_sq[a][b];
@@ -509,7 +514,9 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
     bd = __shfl_sync(FULL, bd, 0);
     bump = __shfl_sync(FULL, bump, 0);
     ct = __shfl_sync(FULL, ct, 0);
+    DMD_SUB(13);
     warp_impulse(S, i, j, w, ratio, bd, bump, tf);
+    DMD_SUB(14);
     return ct;
 }
 /* code/bumped.f:1-47 */
@@ -641,6 +648,7 @@ __device__ void warp_collision(const DSys &S, Err E, WarpArea &W, int i, int j, 
         __syncwarp();
         return;
     }
+    DMD_SUB(15);
     if (ct < 14) ct = warp_eventdyn(S, i, j, evcode, ct, tf);
     if ((ct == 24 || ct == 25) && (evcode < 45 ? er[4 * i + 3] : er[4 * j + 3]) < 0) {
         if (lane == 0) { set_err(E, DMD_E_STATE, i); W.ct = ct; W.evcode = evcode; W.xpulse = 0; }
@@ -1463,9 +1471,7 @@ __device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int h
     }
     __syncthreads();
     cta_build_lists(S, sh, hbonds);
-    DMD_SUB(13);
     cta_predict_all(S, sh, fr, sh.sc.interval_max, hbonds);
-    DMD_SUB(14);
     cta_tree_rebuild(S);
 }
 
@@ -1530,7 +1536,6 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     }
     for (int o = 16; o > 0; o >>= 1) { long long v = __shfl_xor_sync(FULL, dmax_bits, o); if (v > dmax_bits) dmax_bits = v; }
     __syncthreads();
-    DMD_SUB(9);
     if ((threadIdx.x & 31) == 0) sh.red_d[threadIdx.x >> 5] = __longlong_as_double(dmax_bits);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1567,12 +1572,10 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     }
     if (rank == 0) {
         __syncthreads();
-        DMD_SUB(10);
         if (sh.rebuild) {
             for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
             __syncthreads();
             cta_rebuild(S, sh, fr, hbonds);
-            DMD_SUB(11);
         }
         if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
     }
@@ -1583,7 +1586,6 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     /* level 1 of the tournament, spread over the CTAs (level 2 follows at
      * the leader's next selection) */
     for (int g = t0; g < S.nl1; g += stride) l1_update(S, g, N + 3);
-    DMD_SUB(12);
     return rb;
 }
 

@@ -59,6 +59,8 @@ struct DTab {
     double ncfac_sq[DMD_NT][DMD_NT];
     double core15_sq[DMD_NT][DMD_NT];    /* eventdyn.f's bonded H-bond core (code 15) */
     double rmass[DMD_NT][DMD_NT];        /* 2*m_a*m_b/(m_a+m_b), code/eventdyn.f:40 */
+    double rbm[DMD_NT];                  /* 1/mass, rounded to nearest (for div_by) */
+    double revp2_sq[DMD_NC], revp3_sq[DMD_NC];   /* 1/evp2_sq, 1/evp3_sq */
     double evp2_sq[DMD_NC], evp3_sq[DMD_NC];
 };
 __host__ __device__ __forceinline__ int core_slot(int code) { return code <= 3 ? code : code - 13; }
@@ -89,6 +91,7 @@ struct DSys {
     const double *bm;
     const double *blmin, *blmax;  /* side-chain bond window of a backbone bead (codes 10/11/12) */
     const double *blmin_sq, *blmax_sq;   /* their squares */
+    const double *rblmin_sq, *rblmax_sq; /* and the reciprocals of those, rounded to nearest */
     double *x, *y, *z, *vx, *vy, *vz;
     double *ox, *oy, *oz;          /* positions at the last list rebuild */
     float *xf, *yf, *zf;           /* the same in single precision (list-build prefilter) */
@@ -246,6 +249,19 @@ __device__ __forceinline__ bool d_lt0(double x) { long long b = dbits(x); return
 __device__ __forceinline__ bool d_gt0(double x) { return dbits(x) > 0; }
 /* a < b for a, b >= +0.0 (non-negative, not NaN) */
 __device__ __forceinline__ bool d_lt_nn(double a, double b) { return dbits(a) < dbits(b); }
+/* a / b rounded to nearest, given rb = RN(1/b) (an IEEE division on the
+ * host): q = RN(a*rb) is within one ulp of a/b, the remainder a - b*q is
+ * exact in one fused multiply-add, and RN(q + remainder*rb) is then the
+ * correctly rounded quotient (Markstein's theorem, IBM J. Res. Dev. 34(1),
+ * 1990; no overflow or underflow in this engine's ranges).  Three FP64
+ * instructions instead of a full division; a zero numerator keeps its
+ * sign. */
+__device__ __forceinline__ double div_by(double a, double b, double rb) {
+    double q = a * rb;
+    if ((__double_as_longlong(a) & 0x7fffffffffffffffLL) == 0) return q;
+    double r = fma(-q, b, a);
+    return fma(r, rb, q);
+}
 __device__ __forceinline__ double d_negate(double x) { return __longlong_as_double(dbits(x) ^ (long long)0x8000000000000000ULL); }
 /* x - nint(x); skips the rounding where |x| < 0.5 and x is not -0.0 */
 __device__ __forceinline__ double d_wrap(double x) {
