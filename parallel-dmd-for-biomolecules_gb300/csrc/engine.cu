@@ -52,7 +52,7 @@
 #define RSET_MAX 384
 #define WSET_MAX 16
 #define QSET_MAX 160
-#define OWN_SMEM_MAX 6144    /* systems up to this size keep the claim tables in shared memory */
+#define OWN_SMEM_MAX 5632    /* systems up to this size keep the claim tables in shared memory */
 #define DMD_TICKET_SEQ_MAX ((1 << 25) - 2)
 #define FULL 0xffffffffu
 
@@ -105,9 +105,22 @@ struct FullScratch {
     int8_t tmap[TMAP_MAX];
 };
 
+/* The prediction tasks of all events of a batch on one CTA, executed by all
+ * its warps together (a task: bead, partner, static code or -1, flags =
+ * down-operation bit | owner warp << 1; result: time, type, valid). */
+#define PTASK_MAX 512
+struct TaskPool {
+    int n;
+    int a[PTASK_MAX], b[PTASK_MAX];
+    int8_t st[PTASK_MAX], flag[PTASK_MAX];
+    double t[PTASK_MAX];
+    int8_t ty[PTASK_MAX], ok[PTASK_MAX];
+};
+
 /* per-warp working area of one event (dynamic shared memory) */
 struct WarpArea {
-    int nops, nlead, npred, nmeta, ncasc, ntg, nmarked;
+    int nops, nlead, npred, nmeta, ncasc, ntg, nmarked, ntask;
+    int pooled, pool_base;        /* this event's tasks in the CTA's TaskPool, from pool_base */
     /* down-list operations (bead, source) in the reference's order, and
      * the prediction of each operation's pair (time + tfalse, type) */
     int ops_l[OPS_MAX], ops_s[OPS_MAX];
@@ -760,8 +773,26 @@ __device__ __forceinline__ bool check_tij(Err E, double tij, int i) {
  * partner before the event is one of its sources or a source repeats;
  * those beads ("marked") are fully re-predicted up front, in rounds of at
  * most TG_MAX - 2. */
-__device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, double imax,
-                               int hbonds) {
+/* Steps of partial_events(i, j) (code/partial_events.f:5-205; j = -1
+ * after a ghost), run on one warp into W's buffer.
+ *
+ * The reference updates beads one operation at a time: the full
+ * re-prediction of i and of j (eventredo_up over the up list and the
+ * extras), then for every bead l of the down lists and the lower extras of
+ * i and then j, either a full re-prediction of l (when l's current partner
+ * is the source) or a comparison with the pair (l, source)
+ * (eventredo_down).  No prediction depends on another: all read the state
+ * after the collision.  So the pairs are predicted as one flat task list
+ * (32 per pass, one call site; or pooled with the other events of a batch,
+ * see k_run) and the order-dependent part - which candidate wins, when a
+ * full re-prediction is due - is replayed per bead on integer keys.  A bead
+ * needs its full re-prediction only if its partner before the event is one
+ * of its sources or a source repeats; those beads ("marked") are fully
+ * re-predicted up front, in rounds of at most TG_MAX - 2. */
+
+/* 1-2: the down-list operations in the reference's order, and the distinct
+ * beads among them (leaders) with their first operation and mark */
+__device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
     int lane = threadIdx.x & 31;
     /* 1. the down-list operations in the reference's order */
     int n = 0;
@@ -853,183 +884,218 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
         nm += __popc(mm);
     }
     if (lane == 0) {
+        W.nops = n;
         W.nlead = nl; W.nmarked = nm; W.npred = 2 + nl;
         W.pb[0] = i; W.pb[1] = j;
     }
     __syncwarp();
-    DMD_SUB(3);
-    const double Hraw = imax + DMD_LTSTEP - tf;   /* eventredo_up's starting time */
-    const long long Hkey = okey(Hraw), imax_key = okey(imax);
+}
+
+/* 3: the full re-predictions of round rd (i, j in round 0, then marked
+ * beads), their running minima and task offsets; W.ntg, W.ntask */
+__device__ void warp_rp_targets(const DSys &S, WarpArea &W, int i, int j, int rd, double Hraw, long long Hkey) {
+    int lane = threadIdx.x & 31;
     const int per_round = TG_MAX - 2;
-    int rounds = nm > 0 ? (nm + per_round - 1) / per_round : 1;
-    for (int rd = 0; rd < rounds; ++rd) {
-        /* 3. this round's full re-predictions: i, j (round 0), marked beads */
-        int m0 = rd * per_round, m1 = min(nm, m0 + per_round);
-        int ntg = 2 + (m1 - m0);
-        for (int t = lane; t < ntg; t += 32) {
-            int b;
-            if (t == 0) b = rd == 0 ? i : -1;
-            else if (t == 1) b = rd == 0 ? j : -1;
-            else b = W.lead_l[W.mk[m0 + t - 2]];
-            W.fs.tg_b[t] = b;
-            W.fs.tg_k[t] = Hkey; W.fs.tg_p[t] = -1; W.fs.tg_raw[t] = Hraw; W.fs.tg_y[t] = -1;
+    const int nm = W.nmarked;
+    /* 3. this round's full re-predictions: i, j (round 0), marked beads */
+    int m0 = rd * per_round, m1 = min(nm, m0 + per_round);
+    int ntg = 2 + (m1 - m0);
+    for (int t = lane; t < ntg; t += 32) {
+        int b;
+        if (t == 0) b = rd == 0 ? i : -1;
+        else if (t == 1) b = rd == 0 ? j : -1;
+        else b = W.lead_l[W.mk[m0 + t - 2]];
+        W.fs.tg_b[t] = b;
+        W.fs.tg_k[t] = Hkey; W.fs.tg_p[t] = -1; W.fs.tg_raw[t] = Hraw; W.fs.tg_y[t] = -1;
+    }
+    /* task offsets: an inclusive scan over the targets of the up-list
+     * length plus the extras above the bead */
+    int run = 0;
+    for (int base = 0; base < ntg; base += 32) {
+        int t = base + lane;
+        int b = t < ntg ? W.fs.tg_b[t] : -1;
+        int c = 0;
+        if (b >= 0) {
+            c = S.upn[b];
+            for (int k = 0; k < 3; ++k) c += S.er[4 * b + k] > b;
         }
-        /* task offsets: an inclusive scan over the targets of the up-list
-         * length plus the extras above the bead */
-        int run = 0;
-        for (int base = 0; base < ntg; base += 32) {
-            int t = base + lane;
-            int b = t < ntg ? W.fs.tg_b[t] : -1;
-            int c = 0;
-            if (b >= 0) {
-                c = S.upn[b];
-                for (int k = 0; k < 3; ++k) c += S.er[4 * b + k] > b;
-            }
-            int incl = c;
-            for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
-            if (t < ntg) W.fs.tg_base[t] = run + incl - c;
-            run += __shfl_sync(FULL, incl, 31);
-        }
-        if (lane == 0) W.fs.tg_base[ntg] = run;
+        int incl = c;
+        for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
+        if (t < ntg) W.fs.tg_base[t] = run + incl - c;
+        run += __shfl_sync(FULL, incl, 31);
+    }
+    if (lane == 0) W.fs.tg_base[ntg] = run;
+    __syncwarp();
+    const bool mapped = run <= TMAP_MAX;
+    if (mapped) {   /* task -> target map, one target per lane */
+        for (int t = lane; t < ntg; t += 32)
+            for (int q = W.fs.tg_base[t]; q < W.fs.tg_base[t + 1]; ++q) W.fs.tmap[q] = (int8_t)t;
         __syncwarp();
-        const bool mapped = run <= TMAP_MAX;
-        if (mapped) {   /* task -> target map, one target per lane */
-            for (int t = lane; t < ntg; t += 32)
-                for (int q = W.fs.tg_base[t]; q < W.fs.tg_base[t + 1]; ++q) W.fs.tmap[q] = (int8_t)t;
-            __syncwarp();
+    }
+    if (lane == 0) { W.ntg = ntg; W.ntask = (rd == 0 ? W.nops : 0) + run; }
+    __syncwarp();
+}
+
+/* the task q of round rd as (bead, partner, static code or -1, target or
+ * -1 for a down operation); pa < 0 when the slot holds no pair */
+__device__ __forceinline__ void rp_task(const DSys &S, const WarpArea &W, int q, int nop, int &pa, int &pbb, int &st,
+                                        int &tgt) {
+    pa = -1; pbb = -1; st = -1; tgt = -1;
+    if (q < nop) {
+        pa = W.ops_l[q]; pbb = W.ops_s[q];
+        st = W.ops_c[q];
+        return;
+    }
+    int rel = q - nop;
+    int ntg = W.ntg;
+    int run = W.fs.tg_base[ntg];
+    int lo;
+    if (run <= TMAP_MAX) lo = W.fs.tmap[rel];
+    else {
+        int hi = ntg - 1;                /* last target with tg_base <= rel */
+        lo = 0;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (W.fs.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
         }
-        int nop = rd == 0 ? n : 0;
-        int ntask = nop + run;
-        DMD_SUB(4);
-        /* 4. every task of the round, 32 per pass, one predictor call site */
-        for (int base = 0; base < ntask; base += 32) {
-            int q = base + lane;
-            int pa = -1, pbb = -1, code = 1, tgt = -1;
-            int st = -1;    /* the pair's static code when a list holds it */
-            if (q < nop) {
-                pa = W.ops_l[q]; pbb = W.ops_s[q];
-                st = W.ops_c[q];
-            } else if (q < ntask) {
-                int rel = q - nop;
-                int lo;
-                if (mapped) lo = W.fs.tmap[rel];
-                else {
-                    int hi = ntg - 1;                /* last target with tg_base <= rel */
-                    lo = 0;
-                    while (lo < hi) {
-                        int mid = (lo + hi + 1) >> 1;
-                        if (W.fs.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
-                    }
-                }
-                tgt = lo;
-                int b = W.fs.tg_b[lo];
-                int k = rel - W.fs.tg_base[lo];
-                int nu = S.upn[b];
-                int m;
-                if (k < nu) { m = S.up[(size_t)b * S.cap + k]; st = S.upc[(size_t)b * S.cap + k]; }
-                else {
-                    int want = k - nu;
-                    m = -1;
-                    for (int k2 = 0; k2 < 3; ++k2) {
-                        int e = S.er[4 * b + k2];
-                        if (e > b) { if (want == 0) { m = e; break; } --want; }
-                    }
-                }
-                if (m > b) { pa = b; pbb = m; }
-            }
-            /* ev_code(l, source) for a down operation, ev_code(m, b) for a full one */
-            if (pa >= 0) {
-                int a1 = q < nop ? pa : pbb, a2 = q < nop ? pbb : pa;
-                code = st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
-            }
-            double tij = 0.0;
-            int ty = 0;
-            bool ok = false;
-            if (pa >= 0) {
-                ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
-                if (!ok) set_err(E, DMD_E_INPUT, pa);
-                else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
-            }
-            /* a down operation's candidate time is tij + tfalse; a full
-             * re-prediction adds tfalse after its minimum (x + (-0.0) == x) */
-            double tt = tij + (q < nop ? tf : -0.0);
-            if (q < nop) { W.op_t[q] = tt; W.op_y[q] = ok ? (int8_t)ty : (int8_t)-128; }
-            /* segmented minimum of the full tasks, segment = target */
-            long long k = (tgt >= 0 && ok) ? okey(tt) : DMD_KEY_INF;
-            int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
-            double rt = tt;
-            int y = ty;
+    }
+    tgt = lo;
+    int b = W.fs.tg_b[lo];
+    int k = rel - W.fs.tg_base[lo];
+    int nu = S.upn[b];
+    int m;
+    if (k < nu) { m = S.up[(size_t)b * S.cap + k]; st = S.upc[(size_t)b * S.cap + k]; }
+    else {
+        int want = k - nu;
+        m = -1;
+        for (int k2 = 0; k2 < 3; ++k2) {
+            int e = S.er[4 * b + k2];
+            if (e > b) { if (want == 0) { m = e; break; } --want; }
+        }
+    }
+    if (m > b) { pa = b; pbb = m; }
+}
+
+/* one prediction task: ev_code(l, source) for a down operation, ev_code(m, b)
+ * for a full one; the time is tij + tfalse for a down operation and tij for
+ * a full one (tfalse is added after its minimum; x + (-0.0) == x) */
+__device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb, int st, bool is_op, double tf,
+                                           int hbonds, double &tt, int &ty) {
+    double tij = 0.0;
+    ty = 0;
+    bool ok = false;
+    if (pa >= 0) {
+        int a1 = is_op ? pa : pbb, a2 = is_op ? pbb : pa;
+        int code = st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
+        ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
+        if (!ok) set_err(E, DMD_E_INPUT, pa);
+        else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
+    }
+    tt = tij + (is_op ? tf : -0.0);
+    return ok;
+}
+
+/* 4: the tasks of the round on this warp, 32 per pass */
+__device__ void warp_rp_tasks(const DSys &S, Err E, WarpArea &W, int rd, double tf, int hbonds) {
+    int lane = threadIdx.x & 31;
+    const int nop = rd == 0 ? W.nops : 0;
+    const int ntask = W.ntask;
+    for (int base = 0; base < ntask; base += 32) {
+        int q = base + lane;
+        int pa = -1, pbb = -1, st = -1, tgt = -1;
+        if (q < ntask) rp_task(S, W, q, nop, pa, pbb, st, tgt);
+        double tt;
+        int ty;
+        bool ok = rp_predict(S, E, pa, pbb, st, q < nop, tf, hbonds, tt, ty);
+        if (q < nop) { W.op_t[q] = tt; W.op_y[q] = ok ? (int8_t)ty : (int8_t)-128; }
+        /* segmented minimum of the full tasks, segment = target */
+        long long k = (tgt >= 0 && ok) ? okey(tt) : DMD_KEY_INF;
+        int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
+        double rt = tt;
+        int y = ty;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                long long k2 = __shfl_down_sync(FULL, k, o);
-                int p2 = __shfl_down_sync(FULL, p, o);
-                double r2 = __shfl_down_sync(FULL, rt, o);
-                int y2 = __shfl_down_sync(FULL, y, o);
-                int g2 = __shfl_down_sync(FULL, tgt, o);
-                if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
-            }
-            int gprev = __shfl_up_sync(FULL, tgt, 1);
-            bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
-            if (head && key_less(k, p, W.fs.tg_k[tgt], W.fs.tg_p[tgt])) {
-                W.fs.tg_k[tgt] = k; W.fs.tg_p[tgt] = p; W.fs.tg_raw[tgt] = rt; W.fs.tg_y[tgt] = (int8_t)y;
-            }
-            __syncwarp();
+        for (int o = 1; o < 32; o <<= 1) {
+            long long k2 = __shfl_down_sync(FULL, k, o);
+            int p2 = __shfl_down_sync(FULL, p, o);
+            double r2 = __shfl_down_sync(FULL, rt, o);
+            int y2 = __shfl_down_sync(FULL, y, o);
+            int g2 = __shfl_down_sync(FULL, tgt, o);
+            if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
         }
-        DMD_SUB(5);
-        /* 5. the full results: time = minimum + tfalse */
-        for (int t = lane; t < ntg; t += 32) W.fs.tg_raw[t] = W.fs.tg_raw[t] + tf;
-        __syncwarp();
-        if (rd == 0 && lane < 2 && (lane == 0 || j >= 0)) {
-            double tn = W.fs.tg_raw[lane];
-            W.pt[lane] = tn; W.pn[lane] = W.fs.tg_p[lane]; W.pc[lane] = W.fs.tg_y[lane];
-            W.pq[lane] = okey(tn) < imax_key;
-        }
-        __syncwarp();
-        /* 6. replay of the operations per bead: round 0 replays the
-         * unmarked beads and i, each round its marked beads */
-        int nrep = rd == 0 ? nl : 0;
-        int nrep_m = m1 - m0;
-        for (int q = lane; q < nrep + nrep_m; q += 32) {
-            int ld, ft;
-            if (q < nrep) {
-                ld = q;
-                if (W.lead_m[ld]) continue;          /* replayed in its round */
-                ft = W.lead_l[ld] == i ? 0 : -1;
-            } else {
-                ld = W.mk[m0 + q - nrep];
-                ft = 2 + (q - nrep);
-            }
-            int l = W.lead_l[ld];
-            double t;
-            int p, y;
-            bool qq;
-            if (l == i) { t = W.fs.tg_raw[0]; p = W.fs.tg_p[0]; y = W.fs.tg_y[0]; qq = okey(t) < imax_key; }
-            else { t = S.tim[l]; p = S.nptnr[l]; y = S.colt[l]; qq = S.queued[l] != 0; }
-            for (int pp = W.lead_q[ld]; pp < n; ++pp) {
-                if (W.ops_l[pp] != l) continue;
-                int src = W.ops_s[pp];
-                if (p == src) {
-                    if (ft < 0) { set_err(E, DMD_E_STATE, l); break; }
-                    t = W.fs.tg_raw[ft]; p = W.fs.tg_p[ft]; y = W.fs.tg_y[ft]; qq = okey(t) < imax_key;
-                } else if (W.op_y[pp] != -128) {
-                    double tn = W.op_t[pp];
-                    long long kn = okey(tn);
-                    if (key_less(kn, src, okey(t), p)) { t = tn; p = src; y = W.op_y[pp]; qq = kn < imax_key; }
-                }
-            }
-            int slot = 2 + ld;
-            if (l == i) {
-                W.pb[slot] = -1;
-                W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq;
-            } else {
-                W.pb[slot] = l;
-                W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
-            }
+        int gprev = __shfl_up_sync(FULL, tgt, 1);
+        bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
+        if (head && key_less(k, p, W.fs.tg_k[tgt], W.fs.tg_p[tgt])) {
+            W.fs.tg_k[tgt] = k; W.fs.tg_p[tgt] = p; W.fs.tg_raw[tgt] = rt; W.fs.tg_y[tgt] = (int8_t)y;
         }
         __syncwarp();
     }
-    DMD_SUB(7);
-    /* 7. the earliest new queued entry of this event */
+}
+
+/* 5-6: the full results (minimum + tfalse) and the replay of the operations
+ * per bead: round 0 replays the unmarked beads and i, each round its marked
+ * beads */
+__device__ void warp_rp_finish(const DSys &S, Err E, WarpArea &W, int i, int j, int rd, double tf, double imax) {
+    int lane = threadIdx.x & 31;
+    const int per_round = TG_MAX - 2;
+    const int n = W.nops, nl = W.nlead, nm = W.nmarked, ntg = W.ntg;
+    const int m0 = rd * per_round, m1 = min(nm, m0 + per_round);
+    const long long imax_key = okey(imax);
+    /* 5. the full results: time = minimum + tfalse */
+    for (int t = lane; t < ntg; t += 32) W.fs.tg_raw[t] = W.fs.tg_raw[t] + tf;
+    __syncwarp();
+    if (rd == 0 && lane < 2 && (lane == 0 || j >= 0)) {
+        double tn = W.fs.tg_raw[lane];
+        W.pt[lane] = tn; W.pn[lane] = W.fs.tg_p[lane]; W.pc[lane] = W.fs.tg_y[lane];
+        W.pq[lane] = okey(tn) < imax_key;
+    }
+    __syncwarp();
+    /* 6. replay of the operations per bead: round 0 replays the
+     * unmarked beads and i, each round its marked beads */
+    int nrep = rd == 0 ? nl : 0;
+    int nrep_m = m1 - m0;
+    for (int q = lane; q < nrep + nrep_m; q += 32) {
+        int ld, ft;
+        if (q < nrep) {
+            ld = q;
+            if (W.lead_m[ld]) continue;          /* replayed in its round */
+            ft = W.lead_l[ld] == i ? 0 : -1;
+        } else {
+            ld = W.mk[m0 + q - nrep];
+            ft = 2 + (q - nrep);
+        }
+        int l = W.lead_l[ld];
+        double t;
+        int p, y;
+        bool qq;
+        if (l == i) { t = W.fs.tg_raw[0]; p = W.fs.tg_p[0]; y = W.fs.tg_y[0]; qq = okey(t) < imax_key; }
+        else { t = S.tim[l]; p = S.nptnr[l]; y = S.colt[l]; qq = S.queued[l] != 0; }
+        for (int pp = W.lead_q[ld]; pp < n; ++pp) {
+            if (W.ops_l[pp] != l) continue;
+            int src = W.ops_s[pp];
+            if (p == src) {
+                if (ft < 0) { set_err(E, DMD_E_STATE, l); break; }
+                t = W.fs.tg_raw[ft]; p = W.fs.tg_p[ft]; y = W.fs.tg_y[ft]; qq = okey(t) < imax_key;
+            } else if (W.op_y[pp] != -128) {
+                double tn = W.op_t[pp];
+                long long kn = okey(tn);
+                if (key_less(kn, src, okey(t), p)) { t = tn; p = src; y = W.op_y[pp]; qq = kn < imax_key; }
+            }
+        }
+        int slot = 2 + ld;
+        if (l == i) {
+            W.pb[slot] = -1;
+            W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq;
+        } else {
+            W.pb[slot] = l;
+            W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
+        }
+    }
+    __syncwarp();
+}
+
+/* 7: the earliest new queued entry of this event */
+__device__ void warp_rp_tnew(WarpArea &W) {
+    int lane = threadIdx.x & 31;
     long long bk = DMD_KEY_INF;
     int bb = INT_MAX;
     for (int q = lane; q < W.npred; q += 32) {
@@ -1046,6 +1112,26 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
     }
     if (lane == 0) { W.tnew_key = bk; W.tnew_idx = bb; }
     __syncwarp();
+}
+
+__device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, double imax,
+                               int hbonds) {
+    warp_rp_lists(S, W, i, j);
+    DMD_SUB(3);
+    const double Hraw = imax + DMD_LTSTEP - tf;   /* eventredo_up's starting time */
+    const long long Hkey = okey(Hraw);
+    const int nm = W.nmarked;
+    const int per_round = TG_MAX - 2;
+    int rounds = nm > 0 ? (nm + per_round - 1) / per_round : 1;
+    for (int rd = 0; rd < rounds; ++rd) {
+        warp_rp_targets(S, W, i, j, rd, Hraw, Hkey);
+        DMD_SUB(4);
+        warp_rp_tasks(S, E, W, rd, tf, hbonds);
+        DMD_SUB(5);
+        warp_rp_finish(S, E, W, i, j, rd, tf, imax);
+    }
+    DMD_SUB(7);
+    warp_rp_tnew(W);
 }
 
 __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
@@ -1835,7 +1921,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     }
     /* footprint claim table: shared memory when one CTA holds the system and
      * it fits, else the system's global array; cleared at every launch */
-    unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)(warea + NWARPS) : S.owner;
+    TaskPool &TP = *(TaskPool *)(warea + NWARPS);
+    unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)((char *)(warea + NWARPS) + sizeof(TaskPool)) : S.owner;
+    if (threadIdx.x == 0) TP.n = 0;
     for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
     csync(C);
     DMD_PHASE_START(leader ? r : -1);
@@ -1968,7 +2056,76 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 Err E{&W.err, &W.err_info};
                 warp_collision(S, E, W, i, j, tf, coll0 + gw + 1, hbonds);
                 DMD_SUB(1);
-                warp_repredict(S, E, W, i, j, tf, imax, hbonds);
+                /* the re-prediction's lists and tasks; the tasks go to the
+                 * CTA's pool when they fit (one round of full
+                 * re-predictions), else this warp runs them after the pool */
+                warp_rp_lists(S, W, i, j);
+                bool pooled = W.nmarked <= TG_MAX - 2;
+                int base = 0;
+                if (pooled) {
+                    const double Hraw = imax + DMD_LTSTEP - tf;
+                    warp_rp_targets(S, W, i, j, 0, Hraw, okey(Hraw));
+                    int nt = W.ntask, nop = W.nops;
+                    if (lane == 0) base = atomicAdd(&TP.n, nt);
+                    base = __shfl_sync(FULL, base, 0);
+                    pooled = base + nt <= PTASK_MAX;
+                    for (int q = lane; q < nt && base + q < PTASK_MAX; q += 32) {
+                        int pa = -1, pbb = -1, st = -1, tgt = -1;
+                        if (pooled) rp_task(S, W, q, nop, pa, pbb, st, tgt);
+                        TP.a[base + q] = pa; TP.b[base + q] = pbb; TP.st[base + q] = (int8_t)st;
+                        TP.flag[base + q] = (int8_t)((q < nop ? 1 : 0) | (warp << 1));
+                    }
+                }
+                if (lane == 0) { W.pooled = pooled; W.pool_base = base; }
+                __syncwarp();
+            }
+            __syncthreads();
+            /* every pooled prediction task of this CTA's events, all warps */
+            {
+                const int ntot = min(TP.n, PTASK_MAX);
+                for (int q = threadIdx.x; q < ntot; q += blockDim.x) {
+                    int pa = TP.a[q];
+                    if (pa < 0) { TP.ok[q] = 0; continue; }
+                    int owner = TP.flag[q] >> 1;
+                    WarpArea &O = warea[owner];
+                    Err EO{&O.err, &O.err_info};
+                    double tt;
+                    int ty;
+                    bool ok = rp_predict(S, EO, pa, TP.b[q], TP.st[q], (TP.flag[q] & 1) != 0, O.tf, hbonds, tt, ty);
+                    TP.t[q] = tt; TP.ty[q] = (int8_t)ty; TP.ok[q] = ok;
+                }
+            }
+            __syncthreads();
+            if (gw < P) {
+                const int i = W.i, j = W.j;
+                const double tf = W.tf;
+                Err E{&W.err, &W.err_info};
+                if (W.pooled) {
+                    /* down operations' times, and the minimum per full
+                     * re-prediction over its contiguous tasks */
+                    const int base = W.pool_base, nop = W.nops, ntg = W.ntg;
+                    for (int q = lane; q < nop; q += 32) {
+                        W.op_t[q] = TP.t[base + q];
+                        W.op_y[q] = TP.ok[base + q] ? TP.ty[base + q] : (int8_t)-128;
+                    }
+                    for (int t = lane; t < ntg; t += 32) {
+                        long long bk = W.fs.tg_k[t];
+                        int bp = W.fs.tg_p[t];
+                        double braw = W.fs.tg_raw[t];
+                        int by = W.fs.tg_y[t];
+                        for (int x = base + nop + W.fs.tg_base[t]; x < base + nop + W.fs.tg_base[t + 1]; ++x) {
+                            if (!TP.ok[x]) continue;
+                            long long k = okey(TP.t[x]);
+                            if (key_less(k, TP.b[x], bk, bp)) { bk = k; bp = TP.b[x]; braw = TP.t[x]; by = TP.ty[x]; }
+                        }
+                        W.fs.tg_k[t] = bk; W.fs.tg_p[t] = bp; W.fs.tg_raw[t] = braw; W.fs.tg_y[t] = (int8_t)by;
+                    }
+                    __syncwarp();
+                    warp_rp_finish(S, E, W, i, j, 0, tf, imax);
+                    warp_rp_tnew(W);
+                } else {
+                    warp_repredict(S, E, W, i, j, tf, imax, hbonds);
+                }
                 DMD_SUB(8);
                 if (lane == 0 && W.xpulse) {
                     if (S.ident[i] < S.ident[j]) repuls_del_b(S, i, j); else repuls_del_b(S, j, i);
@@ -1980,6 +2137,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     L->c_ct[gw] = W.ct; L->c_tf[gw] = W.tf;
                 }
             }
+            if (threadIdx.x == 0) TP.n = 0;   /* the pool is free until the next batch */
             csync(C);
             DMD_PHASE(3);
             /* validation: event k stands if it precedes every new entry of
@@ -2112,9 +2270,12 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, cons
 /* ------------------------------------------------------------------ */
 /* launch wrappers                                                     */
 /* ------------------------------------------------------------------ */
-static_assert(sizeof(WarpArea) * NWARPS + OWN_SMEM_MAX * 3 * sizeof(unsigned) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
+static_assert(sizeof(WarpArea) * NWARPS + sizeof(TaskPool) + OWN_SMEM_MAX * 3 * sizeof(unsigned) + sizeof(SharedState) +
+                  sizeof(DSys) <= 227 * 1024,
               "k_run shared memory above the 227 KB a block may use");
-static size_t run_smem(int own_cap) { return sizeof(WarpArea) * NWARPS + (size_t)own_cap * 3 * sizeof(unsigned); }
+static size_t run_smem(int own_cap) {
+    return sizeof(WarpArea) * NWARPS + sizeof(TaskPool) + (size_t)own_cap * 3 * sizeof(unsigned);
+}
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st) {
     k_init<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
