@@ -149,6 +149,7 @@ struct WarpArea {
     double sij[12];
     int8_t colt_i;
     int casc[CASC_MAX];
+    int cbase[CASC_MAX + 1];      /* offsets of the cascade beads' claim entries */
     int rset[RSET_MAX];            /* beads of the footprint claim: read, written, queue */
     int wset[WSET_MAX];
     int qset[QSET_MAX];
@@ -1246,15 +1247,31 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
         W.casc[nc + lane] = b;
     }
     __syncwarp();
-    /* their up lists and extras, one cascade bead per lane */
+    /* their up lists and extras as one flat range over the lanes: entry
+     * offsets by a warp scan, then each lane finds its cascade bead */
     nc += 10;
-    for (int c = lane; c < nc; c += 32) {
-        int l = W.casc[c];
-        if (l < 0) continue;
-        int ul = S.upn[l];
-        const int *UL = S.up + (size_t)l * S.cap;
-        for (int q = 0; q < ul; ++q) visit_r(UL[q]);
-        visit_r(S.er[4 * l + 0]); visit_r(S.er[4 * l + 1]); visit_r(S.er[4 * l + 2]);
+    int run = 0;
+    for (int base = 0; base < nc; base += 32) {
+        int c = base + lane;
+        int l = c < nc ? W.casc[c] : -1;
+        int cnt = l >= 0 ? S.upn[l] + 3 : 0;
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
+        if (c < nc) W.cbase[c] = run + incl - cnt;
+        run += __shfl_sync(FULL, incl, 31);
+    }
+    if (lane == 0) W.cbase[nc] = run;
+    __syncwarp();
+    for (int q = lane; q < run; q += 32) {
+        int lo = 0, hi = nc - 1;          /* last cascade bead with cbase <= q */
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (W.cbase[mid] <= q) lo = mid; else hi = mid - 1;
+        }
+        int l = W.casc[lo];
+        int k = q - W.cbase[lo];
+        int ul = W.cbase[lo + 1] - W.cbase[lo] - 3;
+        visit_r(k < ul ? S.up[(size_t)l * S.cap + k] : S.er[4 * l + (k - ul)]);
     }
     __syncwarp();
     /* an incomplete list (cascade or set overflow) ends the batch here */
