@@ -278,12 +278,12 @@ def run_ours(args):
     e2e_times, h2d, d2h = [], 0, 0
     for s in specs:
         n = s.n_beads
-        h2d += 6 * 8 * n + 4 * len(s.chain_len) + 4 * len(s.residues) + abi.C.sizeof(abi.Tables) + abi.C.sizeof(abi.RunCfg)
         d2h += 6 * 8 * n + 3 * 4 * n + 4 * 4 * n + 24
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         b2 = Batch(specs)
+        h2d = int(b2.lib.dmd_batch_device_bytes(b2.h))   # the pools' host image, one copy
         b2.run(E)
         states = [b2.state(r) for r in range(len(specs))]
         torch.cuda.synchronize()

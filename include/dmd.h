@@ -240,6 +240,9 @@ int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas);
 int dmd_set_cluster(dmd_handle *h, int32_t ctas);
 /* the cluster size the last run used */
 int32_t dmd_batch_cluster(dmd_batch *b);
+/* device bytes of the batch's system pools (what dmd_batch_create copies
+ * from host memory in one transfer) */
+int64_t dmd_batch_device_bytes(dmd_batch *b);
 /* Rebuild grid: cells per side of the finest grid (cells as wide as the
  * list cutoff) divided by div (1..8, at least 3 cells per side).  Lists
  * and results do not depend on it. */

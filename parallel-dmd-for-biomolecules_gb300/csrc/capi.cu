@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <deque>
@@ -19,6 +20,7 @@
 #include <map>
 #include <set>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dmd.h"
@@ -459,6 +461,7 @@ struct dmd_batch {
     double last_ms = 0.0;
     std::string err;
     int ready = 0;
+    void *pool_all = nullptr;           /* the pools of all systems, one allocation */
     std::vector<dmd_diag> diag_cache;   /* diagnostics of all systems, valid until the next run */
     bool diag_valid = false;
     int cluster = 0;        /* CTAs per system: 1, 2, 4, 8, or 0 = chosen at run time */
@@ -501,38 +504,30 @@ int auto_cluster(int nsys) {
 
 /* one system's pool: allocation (stream-ordered when a stream is given),
  * layout and the upload of the host state and the pseudo-event times */
-int upload_system(HostSys &H, DevSys &D, cudaStream_t st, std::string &err) {
-    DSys tmp{};
-    size_t bytes = layout(H, tmp, nullptr);
-    if (st) CK(cudaMallocAsync(&D.pool, bytes, st));
-    else CK(cudaMalloc(&D.pool, bytes));
-    D.bytes = bytes;
-    DSys &d = D.d;
-    layout(H, d, (char *)D.pool);
-    d.N = H.N; d.nchains = H.nchains; d.cap = H.cap; d.ncell = H.ncell;
-    d.seed = H.cfg.seed; d.canon = H.cfg.canon; d.flags = H.cfg.flags;
-    d.nl1 = H.nl1; d.nl2 = H.nl2;
-    d.log = nullptr; d.log_cap = 0;
+/* The host data of one system's pool: (destination in the pool laid out at
+ * d, source, bytes).  `keep` owns the temporary arrays the list points to. */
+struct PoolCopy { void *dst; const void *src; size_t n; };
+struct PoolTemps { std::vector<double> tim; std::vector<int> np; std::vector<int8_t> ct; std::vector<uint8_t> q; };
+void pool_copies(HostSys &H, const DSys &d, PoolTemps &keep, std::vector<PoolCopy> &out) {
     size_t N = H.N;
     /* pseudo events (code/main.F90:408-423) and bead placeholders */
-    std::vector<double> tim(N + 3, H.sc.interval_max + DMD_LTSTEP);
-    std::vector<int> np(N + 3, -1);
-    std::vector<int8_t> ct(N + 3, -1);
-    std::vector<uint8_t> q(N + 3, 0);
+    keep.tim.assign(N + 3, H.sc.interval_max + DMD_LTSTEP);
+    keep.np.assign(N + 3, -1);
+    keep.ct.assign(N + 3, -1);
+    keep.q.assign(N + 3, 0);
     if (H.cfg.canon) {
         double tgho = 0.0;
         uint32_t k = 0;
         while ((tgho < 1e-18) || (tgho == 1.0)) tgho = dmd_uniform(H.cfg.seed, DMD_STREAM_GHOST0, 0, k++);
-        tim[N] = -1.0 * dmd_log(tgho) * H.tab.avegtime * .0000001;
+        keep.tim[N] = -1.0 * dmd_log(tgho) * H.tab.avegtime * .0000001;
     } else {
-        tim[N] = 1000000000.0;
+        keep.tim[N] = 1000000000.0;
     }
-    tim[N + 1] = H.sc.interval;
-    tim[N + 2] = 3.3 / (std::sqrt(H.tab.setemp)) + 5;
-    np[N] = np[N + 1] = np[N + 2] = -2;
-    ct[N] = ct[N + 1] = ct[N + 2] = -2;
-    struct Cp { void *dst; const void *src; size_t n; };
-    const Cp cps[] = {
+    keep.tim[N + 1] = H.sc.interval;
+    keep.tim[N + 2] = 3.3 / (std::sqrt(H.tab.setemp)) + 5;
+    keep.np[N] = keep.np[N + 1] = keep.np[N + 2] = -2;
+    keep.ct[N] = keep.ct[N + 1] = keep.ct[N + 2] = -2;
+    out = {
         {(void *)d.tab, &H.tab, sizeof(DTab)}, {d.sc, &H.sc, sizeof(DScal)},
         {(void *)d.info, H.info.data(), N * sizeof(BeadInfo)}, {(void *)d.bm, H.bm.data(), N * 8},
         {(void *)d.blmin, H.blmin.data(), N * 8}, {(void *)d.blmax, H.blmax.data(), N * 8},
@@ -542,14 +537,37 @@ int upload_system(HostSys &H, DevSys &D, cudaStream_t st, std::string &err) {
         {d.vx, H.vx.data(), N * 8}, {d.vy, H.vy.data(), N * 8}, {d.vz, H.vz.data(), N * 8},
         {d.ident, H.ident.data(), N}, {d.bptnr, H.bptnr.data(), N * 4}, {d.er, H.er.data(), 4 * N * 4},
         {d.ovp, H.ovp.data(), 4 * N * 4}, {d.ovc, H.ovc.data(), 4 * N},
-        {d.tim, tim.data(), (N + 3) * 8}, {d.nptnr, np.data(), (N + 3) * 4}, {d.colt, ct.data(), N + 3},
-        {d.queued, q.data(), N + 3},
+        {d.tim, keep.tim.data(), (N + 3) * 8}, {d.nptnr, keep.np.data(), (N + 3) * 4}, {d.colt, keep.ct.data(), N + 3},
+        {d.queued, keep.q.data(), N + 3},
     };
-    for (const Cp &c : cps) {
+}
+
+void set_scalars(const HostSys &H, DSys &d) {
+    d.N = H.N; d.nchains = H.nchains; d.cap = H.cap; d.ncell = H.ncell;
+    d.seed = H.cfg.seed; d.canon = H.cfg.canon; d.flags = H.cfg.flags;
+    d.nl1 = H.nl1; d.nl2 = H.nl2;
+    d.log = nullptr; d.log_cap = 0;
+}
+
+/* one system's own pool: allocation (stream-ordered when a stream is
+ * given), layout and upload */
+int upload_system(HostSys &H, DevSys &D, cudaStream_t st, std::string &err) {
+    DSys tmp{};
+    size_t bytes = layout(H, tmp, nullptr);
+    if (st) CK(cudaMallocAsync(&D.pool, bytes, st));
+    else CK(cudaMalloc(&D.pool, bytes));
+    D.bytes = bytes;
+    DSys &d = D.d;
+    layout(H, d, (char *)D.pool);
+    set_scalars(H, d);
+    PoolTemps keep;
+    std::vector<PoolCopy> cps;
+    pool_copies(H, d, keep, cps);
+    for (const PoolCopy &c : cps) {
         if (st) CK(cudaMemcpyAsync(c.dst, c.src, c.n, cudaMemcpyHostToDevice, st));
         else CK(cudaMemcpy(c.dst, c.src, c.n, cudaMemcpyHostToDevice));
     }
-    if (st) CK(cudaStreamSynchronize(st));   /* the host vectors above go out of scope */
+    if (st) CK(cudaStreamSynchronize(st));   /* `keep` goes out of scope */
     return DMD_OK;
 }
 
@@ -560,16 +578,39 @@ int upload(dmd_batch &B) {
     CK(cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking));
     CK(cudaEventCreate(&B.ev0));
     CK(cudaEventCreate(&B.ev1));
+    /* all systems' pools in one allocation, filled from one pinned host
+     * image by one copy */
+    std::vector<size_t> off(n + 1, 0);
+    for (int r = 0; r < n; ++r) {
+        DSys tmp{};
+        size_t bytes = (layout(B.hs[r], tmp, nullptr) + 255) & ~(size_t)255;
+        B.ds[r].bytes = bytes;
+        off[r + 1] = off[r] + bytes;
+    }
+    size_t total = off[n];
+    CK(cudaMalloc(&B.pool_all, total));
+    char *stage = nullptr;
+    CK(cudaMallocHost((void **)&stage, total));
     std::vector<DSys> hd(n);
     std::vector<int> cstart, clen, coff;
     for (int r = 0; r < n; ++r) {
         HostSys &H = B.hs[r];
-        int rc = upload_system(H, B.ds[r], nullptr, err);
-        if (rc != DMD_OK) return rc;
-        hd[r] = B.ds[r].d;
+        DevSys &D = B.ds[r];
+        D.pool = nullptr;                      /* part of pool_all */
+        layout(H, D.d, (char *)B.pool_all + off[r]);
+        set_scalars(H, D.d);
+        PoolTemps keep;
+        std::vector<PoolCopy> cps;
+        pool_copies(H, D.d, keep, cps);
+        for (const PoolCopy &c : cps)
+            std::memcpy(stage + ((char *)c.dst - (char *)B.pool_all), c.src, c.n);
+        hd[r] = D.d;
         coff.push_back((int)cstart.size());
         for (int c = 0; c < H.nchains; ++c) { cstart.push_back(H.chain_start[c]); clen.push_back(H.chain_len[c]); }
     }
+    cudaError_t ce = cudaMemcpy(B.pool_all, stage, total, cudaMemcpyHostToDevice);
+    cudaFreeHost(stage);
+    CK(ce);
     CK(cudaMalloc(&B.d_sys, n * sizeof(DSys)));
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
     CK(cudaMalloc(&B.d_cstart, cstart.size() * 4));
@@ -594,10 +635,22 @@ int batch_create(dmd_batch &B, int n, const dmd_run_cfg *cfgs, const dmd_tables 
     if (n <= 0 || !cfgs || !tables || !systems) { B.err = "null or empty argument"; return DMD_E_INPUT; }
     B.hs.resize(n);
     B.hbonds = cfgs[0].hbonds != 0;
-    for (int r = 0; r < n; ++r) {
+    for (int r = 0; r < n; ++r)
         if ((cfgs[r].hbonds != 0) != (B.hbonds != 0)) { B.err = "all replicas of a batch share the hbonds flag"; return DMD_E_INPUT; }
-        if (!setup_host(B.hs[r], &cfgs[r], tables, &systems[r], B.err)) return DMD_E_INPUT;
-    }
+    /* the host set-up of the systems on parallel threads */
+    std::vector<std::string> errs(n);
+    std::vector<char> ok(n, 0);
+    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)n);
+    std::atomic<int> next(0);
+    auto work = [&]() {
+        for (int r = next++; r < n; r = next++) ok[r] = setup_host(B.hs[r], &cfgs[r], tables, &systems[r], errs[r]);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    for (int r = 0; r < n; ++r)
+        if (!ok[r]) { B.err = "system " + std::to_string(r) + ": " + errs[r]; return DMD_E_INPUT; }
     return upload(B);
 }
 
@@ -811,6 +864,8 @@ void batch_free(dmd_batch &B) {
     if (B.graph) cudaGraphExecDestroy(B.graph);
     B.graph = nullptr;
     for (auto &D : B.ds) if (D.pool) cudaFree(D.pool);
+    if (B.pool_all) cudaFree(B.pool_all);
+    B.pool_all = nullptr;
     if (B.d_sys) cudaFree(B.d_sys);
     if (B.d_cstart) cudaFree(B.d_cstart);
     if (B.d_clen) cudaFree(B.d_clen);
@@ -1092,6 +1147,12 @@ int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas) {
     return 0;
 }
 int32_t dmd_batch_cluster(dmd_batch *b) { return b ? b->last_cluster : 0; }
+int64_t dmd_batch_device_bytes(dmd_batch *b) {
+    if (!b) return 0;
+    int64_t s = 0;
+    for (const DevSys &D : b->ds) s += (int64_t)D.bytes;
+    return s;
+}
 int dmd_batch_run_graph(dmd_batch *b, int64_t n_events, int32_t n_launches) {
     if (!b) return DMD_E_INPUT;
     return batch_run_graph(*b, n_events, n_launches);
@@ -1440,7 +1501,7 @@ int dmd_save_state(dmd_handle *h, void *buf, int64_t n) {
     hd.n_beads = B.hs[0].N; hd.cap = B.hs[0].cap; hd.ncell = B.hs[0].ncell; hd.bytes = (int64_t)D.bytes;
     std::memcpy(buf, &hd, sizeof hd);
     CK(cudaStreamSynchronize(B.st));
-    CK(cudaMemcpy((char *)buf + sizeof hd, D.pool, D.bytes, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy((char *)buf + sizeof hd, (const void *)D.d.tab, D.bytes, cudaMemcpyDeviceToHost));
     return DMD_OK;
 }
 int dmd_load_state(dmd_handle *h, const void *buf, int64_t n) {
@@ -1458,7 +1519,7 @@ int dmd_load_state(dmd_handle *h, const void *buf, int64_t n) {
         return DMD_E_INPUT;
     }
     CK(cudaStreamSynchronize(B.st));
-    CK(cudaMemcpy(D.pool, (const char *)buf + sizeof hd, D.bytes, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void *)D.d.tab, (const char *)buf + sizeof hd, D.bytes, cudaMemcpyHostToDevice));
     DScal sc;
     CK(cudaMemcpy(&sc, D.d.sc, sizeof sc, cudaMemcpyDeviceToHost));
     B.hs[0].sc = sc;
