@@ -295,6 +295,8 @@ def run_ours(args):
     serving = None
     if rank == 0 and not args.no_serve:
         serving = run_serving(args)
+        # the same arrivals with 10x the events: the server saturates (1e5-1e6 events per request)
+        serving["saturated"] = run_serving(args, scale=10 * args.serve_scale)
     single = None
     if rank == 0 and not args.no_single:
         single = run_single_systems(E)
@@ -353,7 +355,7 @@ def run_single_systems(E: int) -> dict:
     return out
 
 
-def run_serving(args) -> dict:
+def run_serving(args, scale: float = None) -> dict:
     """The serving workload: Poisson arrivals at 20 requests/s of systems of
     4-200 chains x 6-40 residues, 2-10 mM, T* 0.15-0.30, replayed for
     --serve-seconds with each request's 1e6-1e7 events scaled by
@@ -366,11 +368,12 @@ def run_serving(args) -> dict:
     reqs = []
     for k in range(len(arr)):
         spec = systems.generate(systems.serving_request(k, seed=1))
-        reqs.append((spec, max(1000, int(spec.n_events * args.serve_scale))))
+        reqs.append((spec, max(1000, int(spec.n_events * (scale if scale is not None else args.serve_scale)))))
     with Server(max_slots=args.serve_slots, chunk_events=args.serve_chunk) as srv:
         res = serve_trace(srv, arr, reqs)
     out = res.summary()
-    out.update({"arrival_rate_per_s": 20.0, "trace_seconds": args.serve_seconds, "events_scale": args.serve_scale,
+    out.update({"arrival_rate_per_s": 20.0, "trace_seconds": args.serve_seconds,
+                "events_scale": scale if scale is not None else args.serve_scale,
                 "slots": args.serve_slots, "chunk_events": args.serve_chunk,
                 "beads_per_request_mean": float(np.mean([s.n_beads for s, _ in reqs])) if reqs else 0.0,
                 "note": "latency = completion - arrival on the host clock; events/s over the trace's wall time"})

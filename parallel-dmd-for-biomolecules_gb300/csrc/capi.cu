@@ -892,6 +892,7 @@ struct ServerReq {
     std::string err;
     double t_submit = 0, t_admit = 0, t_finish = 0;
     size_t need = 0;                    /* device bytes of its pool */
+    double cpe = 0;                     /* measured SM cycles per event (0: not yet) */
     dmd_diag diag{};
     std::vector<double> x, y, z, vx, vy, vz;
     std::vector<int32_t> bptnr, ident;
@@ -1043,10 +1044,24 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
         std::vector<long long> tg(n);
         std::vector<int> cstart, clen, coff;
         int max_beads = 0;
+        /* Balance the round: every request gets about the SM time that
+         * the typical one needs for chunk events (from each request's
+         * measured cycles per event), so that no CTA idles while the
+         * slowest finishes. */
+        std::vector<double> cpes;
+        for (ServerReq *R : act) if (R->cpe > 0) cpes.push_back(R->cpe);
+        double budget = 0;
+        if (!cpes.empty()) {
+            std::nth_element(cpes.begin(), cpes.begin() + cpes.size() / 2, cpes.end());
+            budget = cpes[cpes.size() / 2] * (double)V.chunk;
+        }
         for (int r = 0; r < n; ++r) {
             ServerReq &R = *act[r];
             hd[r] = R.D.d;
-            tg[r] = std::min(V.chunk, R.total - R.done);
+            long long want = V.chunk;
+            if (budget > 0 && R.cpe > 0)
+                want = std::max<long long>(V.chunk / 8, std::min<long long>(4 * V.chunk, (long long)(budget / R.cpe)));
+            tg[r] = std::min(want, R.total - R.done);
             coff.push_back((int)cstart.size());
             for (int c = 0; c < R.H.nchains; ++c) { cstart.push_back(R.H.chain_start[c]); clen.push_back(R.H.chain_len[c]); }
             max_beads = std::max(max_beads, R.H.N);
@@ -1074,6 +1089,7 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
             R.H.sc = sc;
             R.done += sc.done;
             V.events += sc.done;
+            if (sc.done > 0 && sc.run_cycles > 0) R.cpe = (double)sc.run_cycles / (double)sc.done;
             if (sc.err) {
                 R.state = DMD_REQ_FAILED; R.rc = sc.err;
                 R.err = "device error " + std::to_string(sc.err) + " (info " + std::to_string(sc.err_info) + ")";

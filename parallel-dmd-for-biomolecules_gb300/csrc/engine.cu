@@ -1946,6 +1946,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     DMD_PHASE_START(leader ? r : -1);
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
     const long long max_iter = 16 * target + 1000000;
+    const long long t_start = clock64();
     long long iter = 0;
     while (true) {
         /* ---- the leader selects the next event (and a batch) ---- */
@@ -2265,7 +2266,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     }
     if (leader) {
         __syncthreads();
-        if (threadIdx.x == 0) *S.sc = sh.sc;
+        if (threadIdx.x == 0) {
+            sh.sc.run_cycles = clock64() - t_start;
+            *S.sc = sh.sc;
+        }
     }
     if (C > 1) cg::this_cluster().sync();   /* no CTA leaves while others may read its shared memory */
 }

@@ -78,6 +78,7 @@ struct DScal {
     int pad;
     long long n_batches, n_rolled_back, n_candidates;   /* batch statistics */
     long long bseq;       /* footprint claims made so far (ticket base) */
+    long long run_cycles; /* SM clock cycles of this system's last launch (scheduling hint) */
 };
 
 /* device view of one system; all arrays in global memory */
