@@ -187,6 +187,7 @@ struct SharedState {
     long long coll0, log0;
     double imax, tnow, tf_iv;
     int c_conflict[CAND_MAX], c_over[CAND_MAX];
+    int8_t c_simple[CAND_MAX];    /* the event's collision cannot change H-bond state (coltype 1-3) */
     long long c_tnew_key[CAND_MAX];
     int c_tnew_idx[CAND_MAX], c_err[CAND_MAX], c_err_info[CAND_MAX], c_ct[CAND_MAX];
     double c_tf[CAND_MAX];
@@ -994,6 +995,33 @@ __device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb
     }
     tt = tij + (is_op ? tf : -0.0);
     return ok;
+}
+
+/* 1-4 into the CTA's task pool for the event of warp `owner` (its tasks
+ * must fit one round and the pool), else W.pooled = 0 and the owner warp
+ * runs warp_repredict() after the pool */
+__device__ void warp_rp_prepare(const DSys &S, WarpArea &W, TaskPool &TP, int owner, int i, int j, double tf,
+                                double imax) {
+    int lane = threadIdx.x & 31;
+    warp_rp_lists(S, W, i, j);
+    bool pooled = W.nmarked <= TG_MAX - 2;
+    int base = 0;
+    if (pooled) {
+        const double Hraw = imax + DMD_LTSTEP - tf;
+        warp_rp_targets(S, W, i, j, 0, Hraw, okey(Hraw));
+        int nt = W.ntask, nop = W.nops;
+        if (lane == 0) base = atomicAdd(&TP.n, nt);
+        base = __shfl_sync(FULL, base, 0);
+        pooled = base + nt <= PTASK_MAX;
+        for (int q = lane; q < nt && base + q < PTASK_MAX; q += 32) {
+            int pa = -1, pbb = -1, st = -1, tgt = -1;
+            if (pooled) rp_task(S, W, q, nop, pa, pbb, st, tgt);
+            TP.a[base + q] = pa; TP.b[base + q] = pbb; TP.st[base + q] = (int8_t)st;
+            TP.flag[base + q] = (int8_t)((q < nop ? 1 : 0) | (owner << 1));
+        }
+    }
+    if (lane == 0) { W.pooled = pooled; W.pool_base = base; }
+    __syncwarp();
 }
 
 /* 4: the tasks of the round on this warp, 32 per pass */
@@ -1987,6 +2015,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 if (threadIdx.x == 0) {
                     sh.m = m;
                     sh.tick_reset = m > 1 && sh.bseq >= DMD_TICKET_SEQ_MAX;
+                    sh.c_simple[0] = 0;    /* set by the footprint test when m > 1 */
                 }
                 DMD_PHASE(1);
             } else if (!sh.exitf && threadIdx.x == 0) {
@@ -2036,7 +2065,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 DMD_PHASE(10);
                 if (gw < m) {
                     bool c = warp_footprint_test(W, own, N, ticket);
-                    if (lane == 0) { L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over; }
+                    if (lane == 0) {
+                        int ct0 = S.colt[sh.sort_idx[gw]];
+                        L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over;
+                        L->c_simple[gw] = ct0 >= 1 && ct0 <= 3;
+                    }
                 }
                 csync(C);
                 DMD_PHASE(11);
@@ -2060,6 +2093,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             /* speculative commit of each event on its warp */
             const long long coll0 = sh.coll0;
             const double imax = sh.imax;
+            const bool split = C == 1 && P <= NWARPS / 2;
             if (gw < P) {
                 int i = sh.sort_idx[gw];
                 int j = S.nptnr[i];
@@ -2076,26 +2110,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 DMD_SUB(1);
                 /* the re-prediction's lists and tasks; the tasks go to the
                  * CTA's pool when they fit (one round of full
-                 * re-predictions), else this warp runs them after the pool */
-                warp_rp_lists(S, W, i, j);
-                bool pooled = W.nmarked <= TG_MAX - 2;
-                int base = 0;
-                if (pooled) {
-                    const double Hraw = imax + DMD_LTSTEP - tf;
-                    warp_rp_targets(S, W, i, j, 0, Hraw, okey(Hraw));
-                    int nt = W.ntask, nop = W.nops;
-                    if (lane == 0) base = atomicAdd(&TP.n, nt);
-                    base = __shfl_sync(FULL, base, 0);
-                    pooled = base + nt <= PTASK_MAX;
-                    for (int q = lane; q < nt && base + q < PTASK_MAX; q += 32) {
-                        int pa = -1, pbb = -1, st = -1, tgt = -1;
-                        if (pooled) rp_task(S, W, q, nop, pa, pbb, st, tgt);
-                        TP.a[base + q] = pa; TP.b[base + q] = pbb; TP.st[base + q] = (int8_t)st;
-                        TP.flag[base + q] = (int8_t)((q < nop ? 1 : 0) | (warp << 1));
-                    }
-                }
-                if (lane == 0) { W.pooled = pooled; W.pool_base = base; }
-                __syncwarp();
+                 * re-predictions), else this warp runs them after the pool.
+                 * In a batch of at most NWARPS/2 events, a second warp
+                 * prepares them while this one computes the collision,
+                 * when the collision cannot change the H-bond state they
+                 * read (coltype 1-3). */
+                if (!(split && sh.c_simple[gw])) warp_rp_prepare(S, W, TP, warp, i, j, tf, imax);
+            } else if (split && warp >= NWARPS / 2 && warp - NWARPS / 2 < P && sh.c_simple[warp - NWARPS / 2]) {
+                const int k = warp - NWARPS / 2;
+                const int i = sh.sort_idx[k];
+                warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
             }
             __syncthreads();
             /* every pooled prediction task of this CTA's events, all warps */
