@@ -121,7 +121,8 @@ typedef struct dmd_event_log {
 /* Diagnostics of code/energy.f, code/radgyr.f, code/end2end.f plus counters. */
 typedef struct dmd_diag {
     double  e_total, temperature, rg, e2e, ehh_ii, ehh_ij, e_kin;
-    int32_t hb_alpha, hb_ii, hb_ij, pad;
+    int32_t hb_alpha, hb_ii, hb_ij;
+    int32_t max_down;         /* engine: the longest down neighbour list at the last rebuild */
     int64_t nevents[32];      /* per final coltype */
     int64_t coll, n_pair, n_ghost, n_interval, n_output, n_updates, n_forced_updates;
     double  t, tfalse;
@@ -247,6 +248,14 @@ int64_t dmd_batch_device_bytes(dmd_batch *b);
  * list cutoff) divided by div (1..8, at least 3 cells per side).  Lists
  * and results do not depend on it. */
 int dmd_batch_set_cell_div(dmd_batch *b, int32_t div);
+/* Event-loop variant: the compact one (per-warp event areas sized for down
+ * neighbour lists of at most 32 beads, which leaves most of the SM's
+ * shared memory to the L1 cache) runs while every system's longest down
+ * list is at most max_down; a system whose lists outgrow it at a rebuild
+ * finishes the run on the full variant.  max_down 0..32 (default 32; 0:
+ * always the full variant).  Results do not depend on it. */
+int dmd_batch_set_compact_limit(dmd_batch *b, int32_t max_down);
+int dmd_set_compact_limit(dmd_handle *h, int32_t max_down);
 /* n_launches launches of n_events each, captured into a CUDA graph on the
  * first call (and again when the sizes or the cluster size change) and
  * replayed; the same result as dmd_batch_run with n_events * n_launches. */

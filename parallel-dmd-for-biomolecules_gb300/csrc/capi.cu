@@ -469,7 +469,9 @@ struct dmd_batch {
     int cell_div = 1;       /* rebuild grid: the finest grid's cells per side divided by this */
     cudaGraphExec_t graph = nullptr;   /* captured launches of dmd_batch_run_graph */
     long long graph_events = 0;
-    int graph_launches = 0, graph_cluster = 0;
+    int graph_launches = 0, graph_cluster = 0, graph_compact = -1;
+    long long *d_targets = nullptr;    /* per-system event targets of a follow-up launch */
+    int compact_dn = DMD_COMPACT_DN;   /* down-list limit of the compact variant, 0: never */
 };
 struct dmd_handle { dmd_batch b; };
 
@@ -669,6 +671,18 @@ int sync_check(dmd_batch &B) {
     return DMD_OK;
 }
 
+/* A follow-up launch of the full variant with per-system targets rem[] (0:
+ * the system only enters and leaves). */
+int run_full_remainder(dmd_batch &B, const std::vector<long long> &rem, int C, int max_beads) {
+    std::string &err = B.err;
+    int n = (int)B.hs.size();
+    if (!B.d_targets) CK(cudaMalloc(&B.d_targets, (size_t)n * sizeof(long long)));
+    CK(cudaMemcpyAsync(B.d_targets, rem.data(), (size_t)n * sizeof(long long), cudaMemcpyHostToDevice, B.st));
+    CK(dmd_launch_run(B.d_sys, n, max_beads, C, 0, 0, B.d_targets, B.hbonds, B.d_cstart, B.d_clen, B.d_coff, nullptr,
+                      B.st));
+    return sync_check(B);
+}
+
 int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     std::string &err = B.err;
     if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
@@ -685,6 +699,7 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
         B.log_cap = cap;
     }
     std::vector<long long> count0(n, 0);
+    int compact = B.compact_dn;   /* the compact variant when every system's lists fit it */
     for (int r = 0; r < n; ++r) {
         hd[r] = B.ds[r].d;
         hd[r].ncell = coarse_cells(B.hs[r].ncell, B.cell_div);
@@ -693,6 +708,7 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
         DScal sc;
         CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
         sc.log_count = 0;
+        if (sc.max_dn > B.compact_dn) compact = 0;
         CK(cudaMemcpy(B.ds[r].d.sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
     }
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
@@ -701,10 +717,23 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
     int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
     B.last_cluster = C;
-    CK(dmd_launch_run(B.d_sys, n, max_beads, C, (long long)n_events, nullptr, B.hbonds, B.d_cstart, B.d_clen, B.d_coff,
-                      nullptr, B.st));
+    CK(dmd_launch_run(B.d_sys, n, max_beads, C, compact, (long long)n_events, nullptr, B.hbonds, B.d_cstart, B.d_clen,
+                      B.d_coff, nullptr, B.st));
     CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
+    if (rc == DMD_OK && compact) {
+        /* systems whose lists outgrew the compact variant at a rebuild go
+         * on with the full one for the rest of their events */
+        std::vector<long long> rem(n, 0);
+        bool any = false;
+        for (int r = 0; r < n; ++r)
+            if (B.hs[r].sc.need_full) { rem[r] = std::max<long long>(0, (long long)n_events - B.hs[r].sc.done); any = true; }
+        if (any) {
+            rc = run_full_remainder(B, rem, C, max_beads);
+            CK(cudaEventRecord(B.ev1, B.st));
+            CK(cudaEventSynchronize(B.ev1));
+        }
+    }
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) B.last_ms = ms;
     if (logs) {
@@ -785,36 +814,59 @@ int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
     int probe = 0;
     CK(dmd_max_active_clusters(C, &probe));   /* kernel attributes are set outside the capture */
     std::vector<DSys> hd(n);
+    std::vector<long long> done0(n);
+    int compact = B.compact_dn;   /* the compact variant when every system's lists fit it */
     for (int r = 0; r < n; ++r) {
         hd[r] = B.ds[r].d;
         hd[r].ncell = coarse_cells(B.hs[r].ncell, B.cell_div);
         hd[r].log = nullptr; hd[r].log_cap = 0;
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        done0[r] = sc.done_all;
+        if (sc.max_dn > B.compact_dn) compact = 0;
     }
+    int max_beads = 0;
+    for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
-    if (!B.graph || B.graph_events != n_events || B.graph_launches != n_launches || B.graph_cluster != C) {
+    if (!B.graph || B.graph_events != n_events || B.graph_launches != n_launches || B.graph_cluster != C ||
+        B.graph_compact != compact) {
         if (B.graph) cudaGraphExecDestroy(B.graph);
         B.graph = nullptr;
-        int max_beads = 0;
-        for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal));
         cudaError_t ce = cudaSuccess;
         for (int k = 0; k < n_launches && ce == cudaSuccess; ++k)
-            ce = dmd_launch_run(B.d_sys, n, max_beads, C, (long long)n_events, nullptr, B.hbonds, B.d_cstart, B.d_clen,
-                                B.d_coff, nullptr, B.st);
+            ce = dmd_launch_run(B.d_sys, n, max_beads, C, compact, (long long)n_events, nullptr, B.hbonds, B.d_cstart,
+                                B.d_clen, B.d_coff, nullptr, B.st);
         cudaError_t ce2 = cudaStreamEndCapture(B.st, &g);
         if (ce != cudaSuccess) { err = cudaGetErrorString(ce); if (ce2 == cudaSuccess) cudaGraphDestroy(g); return DMD_E_CUDA; }
         CK(ce2);
         cudaError_t ce3 = cudaGraphInstantiate(&B.graph, g, 0);
         cudaGraphDestroy(g);
         CK(ce3);
-        B.graph_events = n_events; B.graph_launches = n_launches; B.graph_cluster = C;
+        B.graph_events = n_events; B.graph_launches = n_launches; B.graph_cluster = C; B.graph_compact = compact;
     }
     B.last_cluster = C;
     CK(cudaEventRecord(B.ev0, B.st));
     CK(cudaGraphLaunch(B.graph, B.st));
     CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
+    if (rc == DMD_OK && compact) {
+        /* a system whose lists outgrew the compact variant left its later
+         * launches at once: its remaining events run on the full one */
+        std::vector<long long> rem(n, 0);
+        bool any = false;
+        for (int r = 0; r < n; ++r)
+            if (B.hs[r].sc.need_full) {
+                rem[r] = std::max<long long>(0, (long long)n_events * n_launches - (B.hs[r].sc.done_all - done0[r]));
+                any = true;
+            }
+        if (any) {
+            rc = run_full_remainder(B, rem, C, max_beads);
+            CK(cudaEventRecord(B.ev1, B.st));
+            CK(cudaEventSynchronize(B.ev1));
+        }
+    }
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) B.last_ms = ms;
     return rc;
@@ -833,6 +885,7 @@ int batch_autotune(dmd_batch &B, int64_t trial_events, int32_t *best_cluster, in
     dmd_batch T;
     T.hs = B.hs;
     T.hbonds = B.hbonds;
+    T.compact_dn = B.compact_dn;
     int rc = upload(T);
     if (rc != DMD_OK) { err = T.err; batch_free(T); return rc; }
     int n = (int)B.hs.size();
@@ -872,6 +925,7 @@ void batch_free(dmd_batch &B) {
     if (B.d_coff) cudaFree(B.d_coff);
     if (B.d_diag) cudaFree(B.d_diag);
     if (B.d_log) cudaFree(B.d_log);
+    if (B.d_targets) cudaFree(B.d_targets);
     if (B.ev0) cudaEventDestroy(B.ev0);
     if (B.ev1) cudaEventDestroy(B.ev1);
     if (B.st) cudaStreamDestroy(B.st);
@@ -1074,8 +1128,13 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
         CK(cudaMemcpyAsync(V.d_clen, clen.data(), clen.size() * 4, cudaMemcpyHostToDevice, V.run_st));
         CK(cudaMemcpyAsync(V.d_coff, coff.data(), coff.size() * 4, cudaMemcpyHostToDevice, V.run_st));
         CK(cudaEventRecord(V.e0, V.run_st));
-        CK(dmd_launch_run(V.d_sys, n, max_beads, 1, 0, V.d_targets, V.hbonds, V.d_cstart, V.d_clen, V.d_coff, nullptr,
-                          V.run_st));
+        /* the compact variant unless a request's lists are known to need the
+         * full one (a request that finds out at a rebuild stops there and
+         * goes on in the next round) */
+        int compact = DMD_COMPACT_DN;
+        for (ServerReq *R : act) if (R->H.sc.max_dn > DMD_COMPACT_DN) compact = 0;
+        CK(dmd_launch_run(V.d_sys, n, max_beads, 1, compact, 0, V.d_targets, V.hbonds, V.d_cstart, V.d_clen, V.d_coff,
+                          nullptr, V.run_st));
         CK(cudaEventRecord(V.e1, V.run_st));
         CK(dmd_launch_diag(V.d_sys, n, V.d_cstart, V.d_clen, V.d_coff, V.d_diag, V.run_st));
         server_admit(V, n, admitted);          /* overlaps the launch */
@@ -1184,6 +1243,15 @@ int dmd_batch_set_cell_div(dmd_batch *b, int32_t div) {
     return 0;
 }
 int dmd_set_cluster(dmd_handle *h, int32_t ctas) { return h ? dmd_batch_set_cluster(&h->b, ctas) : DMD_E_INPUT; }
+int dmd_batch_set_compact_limit(dmd_batch *b, int32_t max_down) {
+    if (!b) return DMD_E_INPUT;
+    if (max_down < 0 || max_down > DMD_COMPACT_DN) { b->err = "max_down must be 0..32"; return DMD_E_INPUT; }
+    b->compact_dn = max_down;
+    return 0;
+}
+int dmd_set_compact_limit(dmd_handle *h, int32_t max_down) {
+    return h ? dmd_batch_set_compact_limit(&h->b, max_down) : DMD_E_INPUT;
+}
 double dmd_last_run_ms(dmd_handle *h) { return h ? h->b.last_ms : 0.0; }
 
 int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys, dmd_handle **out) {

@@ -35,6 +35,7 @@
 #include <limits.h>
 
 #include <cooperative_groups.h>
+#include <algorithm>
 #include <mutex>
 
 #include "dmd.h"
@@ -43,16 +44,16 @@
 
 #define NTHREADS 256
 #define NWARPS (NTHREADS / 32)
-#define OPS_MAX 264        /* 2 * list capacity (128) + 6 extras + slack */
 #define CAND_MAX 64
 #define META_MAX 16
 #define TG_MAX 64         /* full re-predictions per round (i, j, marked beads) */
 #define TMAP_MAX 256
 #define CASC_MAX 64
-#define RSET_MAX 384
 #define WSET_MAX 16
-#define QSET_MAX 160
-#define OWN_SMEM_MAX 5632    /* systems up to this size keep the claim tables in shared memory */
+/* systems up to this size keep the claim tables in shared memory (full and
+ * compact variants of k_run); larger ones use their global array */
+#define OWN_SMEM_FULL 2048
+#define OWN_SMEM_COMPACT 1536
 #define DMD_TICKET_SEQ_MAX ((1 << 25) - 2)
 #define FULL 0xffffffffu
 
@@ -115,52 +116,6 @@ struct TaskPool {
     int8_t st[PTASK_MAX], flag[PTASK_MAX];
     double t[PTASK_MAX];
     int8_t ty[PTASK_MAX], ok[PTASK_MAX];
-};
-
-/* per-warp working area of one event (dynamic shared memory) */
-struct WarpArea {
-    int nops, nlead, npred, nmeta, ncasc, ntg, nmarked, ntask;
-    int pooled, pool_base;        /* this event's tasks in the CTA's TaskPool, from pool_base */
-    /* down-list operations (bead, source) in the reference's order, and
-     * the prediction of each operation's pair (time + tfalse, type) */
-    int ops_l[OPS_MAX], ops_s[OPS_MAX];
-    int8_t ops_c[OPS_MAX];        /* static code of the pair, -1 if not listed */
-    double op_t[OPS_MAX];
-    int8_t op_y[OPS_MAX];
-    /* distinct operation beads: bead, first operation, full-redo mark */
-    int lead_l[OPS_MAX];
-    int16_t lead_q[OPS_MAX];
-    int8_t lead_m[OPS_MAX];
-    int16_t mk[OPS_MAX];          /* marked leaders, in leader order */
-    FullScratch fs;               /* full re-predictions of one round */
-    /* buffered predictions: bead, time, partner, type, queued */
-    int pb[OPS_MAX + 2];
-    double pt[OPS_MAX + 2];
-    int pn[OPS_MAX + 2];
-    int8_t pc[OPS_MAX + 2];
-    uint8_t pq[OPS_MAX + 2];
-    /* snapshot of what the collision may write */
-    int mb[META_MAX];
-    int8_t mident[META_MAX];
-    int mbp[META_MAX];
-    int mer[META_MAX][4];
-    int movp[META_MAX][4];
-    int8_t movc[META_MAX][4];
-    double sij[12];
-    int8_t colt_i;
-    int casc[CASC_MAX];
-    int cbase[CASC_MAX + 1];      /* offsets of the cascade beads' claim entries */
-    int rset[RSET_MAX];            /* beads of the footprint claim: read, written, queue */
-    int wset[WSET_MAX];
-    int qset[QSET_MAX];
-    int nrset, nwset, nqset;
-    /* the event */
-    int i, j, ct, evcode, xpulse, conflict, casc_over;
-    int err, err_info;
-    long long coll;
-    double tf;
-    long long tnew_key;
-    int tnew_idx;
 };
 
 struct SharedState {
@@ -358,966 +313,6 @@ __device__ void repuls_del_b(const DSys &S, int i, int j) {
 }
 
 /* ------------------------------------------------------------------ */
-/* warp-collective pair geometry: components on lanes 0..2             */
-/* ------------------------------------------------------------------ */
-struct WRel { double rx, ry, rz, bij, rijsq, vijsq; };
-
-/* relative position at tfalse with the minimum image, and the products of
- * code/core.f:14-26 (sums kept in the reference's left-to-right order) */
-__device__ WRel warp_rel(const DSys &S, int i, int j, double tf) {
-    int lane = threadIdx.x & 31;
-    int d = lane % 3;
-    const double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
-    const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
-    double v = V[i] - V[j];
-    double r = P[i] - P[j] + v * tf;
-    r = d_wrap(r);
-    double pb = r * v, pr = r * r, pv = v * v;
-    WRel w;
-    w.rx = __shfl_sync(FULL, r, 0); w.ry = __shfl_sync(FULL, r, 1); w.rz = __shfl_sync(FULL, r, 2);
-    double b0 = __shfl_sync(FULL, pb, 0), b1 = __shfl_sync(FULL, pb, 1), b2 = __shfl_sync(FULL, pb, 2);
-    double r0 = __shfl_sync(FULL, pr, 0), r1 = __shfl_sync(FULL, pr, 1), r2 = __shfl_sync(FULL, pr, 2);
-    double v0 = __shfl_sync(FULL, pv, 0), v1 = __shfl_sync(FULL, pv, 1), v2 = __shfl_sync(FULL, pv, 2);
-    /* three independent sums on three lanes, then broadcast */
-    double s = lane == 0 ? b0 + b1 + b2 : (lane == 1 ? r0 + r1 + r2 : v0 + v1 + v2);
-    w.bij = __shfl_sync(FULL, s, 0);
-    w.rijsq = __shfl_sync(FULL, s, 1);
-    w.vijsq = __shfl_sync(FULL, s, 2);
-    return w;
-}
-
-/* four distances at tfalse (code/repuls_check.f), pair q on lanes 3q..3q+2 */
-__device__ void warp_dist4(const DSys &S, const int *a, const int *b, double tf, double *dout) {
-    int lane = threadIdx.x & 31;
-    int q = lane / 3 < 4 ? lane / 3 : 3, d = lane % 3;
-    int ia = a[q], ib = b[q];
-    const double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
-    const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
-    double v = V[ia] - V[ib];
-    double r = P[ia] - P[ib] + v * tf;
-    r = d_wrap(r);
-    double p = r * r;
-    double c0 = __shfl_sync(FULL, p, 3 * (lane & 3));
-    double c1 = __shfl_sync(FULL, p, 3 * (lane & 3) + 1);
-    double c2 = __shfl_sync(FULL, p, 3 * (lane & 3) + 2);
-    double dd = c0 + c1 + c2;
-    double dist = sqrt(dd);
-    for (int k = 0; k < 4; ++k) dout[k] = __shfl_sync(FULL, dist, k);
-}
-
-/* the per-component tail of code/eventdyn.f:357-381 after the bumpdist push:
- * lanes 0..5 = (bead i/j) x (x,y,z) */
-__device__ void warp_impulse(const DSys &S, int i, int j, const WRel &w, double ratio, double bd, int bump,
-                             double tf) {
-    int lane = threadIdx.x & 31;
-    if (lane < 6) {
-        int d = lane % 3;
-        bool isj = lane >= 3;
-        int b = isj ? j : i;
-        double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
-        double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
-        double r = d == 0 ? w.rx : (d == 1 ? w.ry : w.rz);
-        double p = P[b];
-        /* bump = -1: pair pushed together (i - bd*r, j + bd*r); +1: apart; 0: none */
-        if (bump != 0) {
-            bool minus = (bump < 0) != isj;
-            p = minus ? p - bd * r : p + bd * r;
-        }
-        double bmb = S.bm[b], rbmb = S.tab->rbm[S.ident[b]];   /* bm(b) = mass(identity(b)) */
-        double delv = ratio * r;
-        double dv = div_by(delv, bmb, rbmb);
-        double dp = div_by(delv * tf, bmb, rbmb);
-        V[b] = isj ? V[b] + dv : V[b] - dv;
-        p = isj ? p - dp : p + dp;
-        P[b] = p;
-    }
-    __syncwarp();
-}
-__device__ void warp_bump_only(const DSys &S, int i, int j, const WRel &w, double bd, int bump) {
-    int lane = threadIdx.x & 31;
-    if (lane < 6) {
-        int d = lane % 3;
-        bool isj = lane >= 3;
-        int b = isj ? j : i;
-        double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
-        double r = d == 0 ? w.rx : (d == 1 ? w.ry : w.rz);
-        bool minus = (bump < 0) != isj;
-        double p = P[b];
-        P[b] = minus ? p - bd * r : p + bd * r;
-    }
-    __syncwarp();
-}
-
-/* code/eventdyn.f:4-385: ratio on lane 0, the six component updates on lanes 0..5 */
-__device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, double tf) {
-    int lane = threadIdx.x & 31;
-    const DTab &T = *S.tab;
-    WRel w = warp_rel(S, i, j, tf);
-    DMD_SUB(12);
-    double ratio = 0.0, bd = 0.0;
-    int bump = 0;
-    if (lane == 0) {
-        double bij = w.bij;
-        int a = S.ident[i], b = S.ident[j];
-        /* the masses, squared diameters and bond windows come from tables
-         * computed in the same operation order (bm(i) = mass(identity(i))) */
-        double rmass = T.rmass[a][b];
-        bool side = evcode >= 10 && evcode <= 12;
-        if (ct == 2) {
-            double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];
-            double rlo = side ? S.rblmin_sq[i] : T.revp2_sq[evcode];
-            ratio = div_by(rmass * bij, lo, rlo);
-        } else if (ct == 3) {
-            double hi = side ? S.blmax_sq[i] : T.evp3_sq[evcode];
-            double rhi = side ? S.rblmax_sq[i] : T.revp3_sq[evcode];
-            ratio = div_by(rmass * bij, hi, rhi);
-        } else if (ct == 1) {
-            double sigsq;
-            if (evcode == 15) sigsq = S.bptnr[i] == j ? T.core15_sq[a][b] : T.sigma_sq[a][b];
-            else sigsq = T.core_sq[core_slot(evcode)][a][b];
-            ratio = rmass * bij / sigsq;
-        } else if (ct == 4) {
-            double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
-            double del_pe = 4.0 * wellsq * epsave / rmass;
-            bd = DMD_SMDIST * sqrt(wellsq);
-            if (bij * bij + del_pe > 0.0) {
-                ratio = rmass * (sqrt((4.0 * wellsq * epsave / rmass) + bij * bij) + bij) / (2.0 * wellsq);
-                ct = 20; bump = -1;
-            } else {
-                ratio = rmass * bij / wellsq;
-                ct = 22; bump = 1;
-            }
-        } else if (ct == 8) {
-            double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
-            double del_pe = 4.0 * wellsq * epsave / rmass;
-            bd = DMD_SMDIST * sqrt(wellsq);
-            if (bij * bij > del_pe) {
-                ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
-                ct = 21; bump = 1;
-            } else {
-                ratio = rmass * bij / wellsq;
-                ct = 22; bump = -1;
-            }
-        } else if (ct == 9) {
-            double wellsq = T.welldia_sq[a][b];
-            ratio = rmass * bij / wellsq;
-            ct = 23; bump = 1; bd = DMD_SMDIST * sqrt(wellsq);
-        } else if (ct == 5) {
-            double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
-            double del_pe = 4.0 * wellsq * epsave / rmass;
-            bd = DMD_SMDIST * sqrt(wellsq);
-            ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
-            ct = 24; bump = 1;
-        } else if (ct == 6) {
-            double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
-            double del_pe = 4.0 * wellsq * epsave / rmass;
-            bd = DMD_SMDIST * sqrt(wellsq);
-            if (bij * bij > -del_pe) {
-                ratio = rmass * (sqrt(del_pe + bij * bij) + bij) / (2.0 * wellsq);
-                ct = 25; bump = -1;
-            } else {
-                ratio = rmass * bij / wellsq;
-                ct = 26; bump = 1;
-            }
-        } else if (ct == 13) {
-            double wellsq = T.shlddia_sq[a][b];
-            ratio = rmass * bij / wellsq;
-            ct = 27; bump = 1; bd = DMD_SMDIST * sqrt(wellsq);
-        }
-    }
-    ratio = __shfl_sync(FULL, ratio, 0);
-    bd = __shfl_sync(FULL, bd, 0);
-    bump = __shfl_sync(FULL, bump, 0);
-    ct = __shfl_sync(FULL, ct, 0);
-    DMD_SUB(13);
-    warp_impulse(S, i, j, w, ratio, bd, bump, tf);
-    DMD_SUB(14);
-    return ct;
-}
-/* code/bumped.f:1-47 */
-__device__ void warp_bumpoff(const DSys &S, int i, int j, int evcode, double tf) {
-    WRel w = warp_rel(S, i, j, tf);
-    const DTab &T = *S.tab;
-    int a = S.ident[i], b = S.ident[j];
-    double bd = (evcode >= 40) ? DMD_SMDIST * sqrt(T.shlddia_sq[a][b]) : DMD_SMDIST * sqrt(T.welldia_sq[a][b]);
-    warp_bump_only(S, i, j, w, bd, w.bij < 0.0 ? -1 : 1);
-}
-__device__ double warp_check_sigma(const DSys &S, int i, int j, double tf) {  /* code/check_sigma.f */
-    WRel w = warp_rel(S, i, j, tf);
-    double diff = w.rijsq - S.tab->sigma_sq[S.ident[i]][S.ident[j]];
-    return diff < 0.0 ? 10.0 : 11.0;
-}
-
-/* ------------------------------------------------------------------ */
-/* one event on one warp                                               */
-/* ------------------------------------------------------------------ */
-/* snapshot of everything the collision of (i, j) may write */
-/* The positions, velocities and coltype of i and j, taken before every
- * collision; the H-bond bookkeeping state (identity, partner, extra_repuls,
- * overrides) of the beads it may touch is taken by lane_meta_snapshot()
- * only when the collision is about to write it. */
-__device__ void warp_snapshot(const DSys &S, WarpArea &W, int i, int j) {
-    int lane = threadIdx.x & 31;
-    if (lane == 0) { W.nmeta = 0; W.colt_i = S.colt[i]; }
-    if (lane < 12) {
-        int b = lane < 6 ? i : j, f = lane % 6;
-        const double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
-        W.sij[lane] = A[b];
-    }
-    __syncwarp();
-}
-__device__ void warp_restore(const DSys &S, WarpArea &W) {
-    int lane = threadIdx.x & 31;
-    /* entries naming the same bead hold the same values, so order does not matter */
-    for (int q = lane; q < W.nmeta; q += 32) {
-        int b = W.mb[q];
-        S.ident[b] = W.mident[q];
-        S.bptnr[b] = W.mbp[q];
-        for (int k = 0; k < 4; ++k) { S.er[4 * b + k] = W.mer[q][k]; S.ovp[4 * b + k] = W.movp[q][k]; S.ovc[4 * b + k] = W.movc[q][k]; }
-    }
-    if (lane < 12) {
-        int b = lane < 6 ? W.i : W.j, f = lane % 6;
-        double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
-        A[b] = W.sij[lane];
-    }
-    if (lane == 0) S.colt[W.i] = W.colt_i;
-    __syncwarp();
-}
-
-__device__ void lane_meta_snapshot(const DSys &S, WarpArea &W, int i, int j) {
-    int n = 0;
-    auto add = [&](int b) { if (b >= 0 && n < META_MAX) W.mb[n++] = b; };
-    add(i); add(j);
-    for (int k = 0; k < 4; ++k) { add(S.er[4 * i + k]); add(S.er[4 * j + k]); }
-    int h1, h2;
-    own_helpers(S, i, h1, h2); add(h1); add(h2);
-    own_helpers(S, j, h1, h2); add(h1); add(h2);
-    for (int q = 0; q < n; ++q) {
-        int b = W.mb[q];
-        W.mident[q] = S.ident[b];
-        W.mbp[q] = S.bptnr[b];
-        for (int k = 0; k < 4; ++k) { W.mer[q][k] = S.er[4 * b + k]; W.movp[q][k] = S.ovp[4 * b + k]; W.movc[q][k] = S.ovc[4 * b + k]; }
-    }
-    W.nmeta = n;
-}
-
-/* worker block (code/main.F90:1432-1956) and master application
- * (code/main.F90:646-943) of the pair event (i, j), warp-wide */
-__device__ void warp_collision(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, long long coll,
-                               int hbonds) {
-    int lane = threadIdx.x & 31;
-    int8_t *id = S.ident;
-    int *er = S.er;
-    int ct = S.colt[i];
-    int evcode = pair_code(S, i, j, hbonds);
-    bool nonend = !S.info[i].is_end && !S.info[j].is_end;
-    int xpulse = 0;
-    int nb = id[i] < id[j] ? i : j;
-    int cb = id[i] < id[j] ? j : i;
-    int err = 0;
-    if (ct == 7) {
-        if (er[4 * i + 3] < 0 && er[4 * j + 3] < 0) {
-            if (nonend) {
-                int ncim1, ncai, ncaj, nnjp1;
-                helpers_of(S, nb, cb, ncim1, ncai, ncaj, nnjp1);
-                int a[4] = {nb, nb, cb, cb}, b[4] = {ncaj, nnjp1, ncai, ncim1};
-                double d[4];
-                warp_dist4(S, a, b, tf, d);
-                const DTab &T = *S.tab;
-                double rating = ((d[0] > T.shd1) && (d[1] > T.shd2) && (d[2] > T.shd3) && (d[3] > T.shd4)) ? 10.0 : 11.0;
-                ct = rating <= 10.0 ? 4 : 14;
-            } else {
-                double ran_non = dmd_uniform(S.seed, DMD_STREAM_CAPTURE, (uint64_t)coll, 0);
-                ct = ran_non <= 0.2 ? 4 : 9;
-            }
-        } else {
-            ct = 9;
-        }
-    } else if (ct == 10 || ct == 12) {
-        int hb = evcode < 45 ? er[4 * i + 3] : er[4 * j + 3];
-        if (hb < 0) err = 1;
-        else if (ct == 10) {
-            /* code/repuls_check_3.f with (n, c, k) */
-            int x = evcode < 45 ? i : j, k = evcode < 45 ? j : i;
-            int n = id[x] < id[hb] ? x : hb, c = id[x] < id[hb] ? hb : x;
-            int ncim1, ncai, ncaj, nnjp1;
-            helpers_of(S, n, c, ncim1, ncai, ncaj, nnjp1);
-            int a[4] = {n, n, c, c}, b[4] = {ncaj, nnjp1, ncai, ncim1};
-            double d[4];
-            warp_dist4(S, a, b, tf, d);
-            const DTab &T = *S.tab;
-            int m = 0;
-            if ((ncaj != k) && (d[0] > T.shd1)) m = m + 1;
-            if ((nnjp1 != k) && (d[1] > T.shd2)) m = m + 1;
-            if ((ncai != k) && (d[2] > T.shd3)) m = m + 1;
-            if ((ncim1 != k) && (d[3] > T.shd4)) m = m + 1;
-            ct = (m == 3 ? 10.0 : 11.0) <= 10.0 ? 5 : 15;
-        } else {
-            int x = evcode < 45 ? i : j;
-            if (S.bptnr[x] == hb) ct = warp_check_sigma(S, x, hb, tf) > 10.0 ? 6 : 13;
-            else ct = 15;
-        }
-    }
-    if (err) {
-        if (lane == 0) { set_err(E, DMD_E_STATE, i); W.ct = ct; W.evcode = evcode; W.xpulse = 0; }
-        __syncwarp();
-        return;
-    }
-    DMD_SUB(15);
-    if (ct < 14) ct = warp_eventdyn(S, i, j, evcode, ct, tf);
-    if ((ct == 24 || ct == 25) && (evcode < 45 ? er[4 * i + 3] : er[4 * j + 3]) < 0) {
-        if (lane == 0) { set_err(E, DMD_E_STATE, i); W.ct = ct; W.evcode = evcode; W.xpulse = 0; }
-        __syncwarp();
-        return;
-    }
-    if (ct == 14 || ct == 15 || ct == 16) warp_bumpoff(S, i, j, evcode, tf);
-    if (lane == 0) {
-        if (ct == 20 || ct == 21 || ct == 24 || ct == 25 || ct == 14 || ct == 16) lane_meta_snapshot(S, W, i, j);
-        if (ct == 20) {
-            if (id[i] + id[j] == 5) {
-                S.bptnr[i] = j; S.bptnr[j] = i;
-                id[i] = id[i] + 4; id[j] = id[j] + 4;
-                if (nonend) { if (id[i] < id[j]) repuls_add(S, E, i, j, hbonds); else repuls_add(S, E, j, i, hbonds); }
-            }
-        } else if (ct == 21) {
-            if (id[i] <= 8) {
-                if (nonend) {
-                    xpulse = 1;
-                    if (id[i] < id[j]) shoulders_off(S, E, i, j, hbonds); else shoulders_off(S, E, j, i, hbonds);
-                }
-                if (S.bptnr[i] == j) {
-                    S.bptnr[i] = -1; S.bptnr[j] = -1;
-                    id[i] = id[i] - 4; id[j] = id[j] - 4;
-                }
-            }
-        } else if (ct == 24) {
-            int x = evcode < 45 ? i : j, hb = er[4 * x + 3];
-            if (id[x] + id[hb] == 5) { S.bptnr[x] = hb; S.bptnr[hb] = x; id[x] += 4; id[hb] += 4; }
-        } else if (ct == 25) {
-            int x = evcode < 45 ? i : j, hb = er[4 * x + 3];
-            if (id[x] >= 5) { S.bptnr[x] = -1; S.bptnr[hb] = -1; id[x] -= 4; id[hb] -= 4; }
-        } else if (ct == 14) {
-            if (nonend) { if (id[i] < id[j]) repuls_add(S, E, i, j, hbonds); else repuls_add(S, E, j, i, hbonds); }
-        } else if (ct == 16) {
-            if (nonend) {
-                xpulse = 1;
-                if (id[i] < id[j]) shoulders_off(S, E, i, j, hbonds); else shoulders_off(S, E, j, i, hbonds);
-            }
-        }
-        S.colt[i] = (int8_t)ct;
-        W.ct = ct; W.evcode = evcode; W.xpulse = xpulse;
-    }
-    __syncwarp();
-}
-
-/* Andersen ghost collision (code/main.F90:997-1121) up to the re-prediction;
- * lane 0, returns the bead and the (possibly clamped) event time */
-__device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
-    const DTab &T = *S.tab;
-    long long g = sh.sc.ghost_index++;
-    uint32_t k = 0;
-    int N = S.N;
-    int i;
-    do { i = (int)(dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) * N) + 1; } while (i == N + 1 && k < 64);
-    if (i > N) i = N;
-    i -= 1;
-    sh.sc.n_ghost += 1;
-    S.x[i] = S.x[i] + S.vx[i] * tfalse; S.y[i] = S.y[i] + S.vy[i] * tfalse; S.z[i] = S.z[i] + S.vz[i] * tfalse;
-    double v1, v2, r;
-    double bmi = S.bm[i];
-    do {
-        v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
-        v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
-        r = v1 * v1 + v2 * v2;
-    } while (((r == 0.0) || (r >= 1.0)) && k < 4096);
-    double fact = sqrt(-2.0 * T.setemp * bmi * dmd_log(r) / r);
-    S.vx[i] = v1 * fact / bmi;
-    S.vy[i] = v2 * fact / bmi;
-    do {
-        v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
-        v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
-        r = v1 * v1 + v2 * v2;
-    } while (((r == 0.0) || (r >= 1.0)) && k < 8192);
-    fact = sqrt(-2.0 * T.setemp * bmi * dmd_log(r) / r);
-    S.vz[i] = v1 * fact / bmi;
-    S.x[i] = S.x[i] - S.vx[i] * tfalse; S.y[i] = S.y[i] - S.vy[i] * tfalse; S.z[i] = S.z[i] - S.vz[i] * tfalse;
-    double tgho = 0.0;
-    while (((tgho < 1e-18) || (tgho == 1.0)) && k < 12288) tgho = dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++);
-    if (r == 0.0 || r >= 1.0 || tgho < 1e-18) set_err(sh, DMD_E_STATE, -1);
-    double tn = -1.0 * dmd_log(tgho) * T.avegtime + tfalse;
-    set_pred(S, N, tn, -2, -2, tn < sh.sc.interval_max);
-    if (tfalse < sh.sc.old_tfalse) tfalse = sh.sc.old_tfalse;
-    return i;
-}
-
-/* ------------------------------------------------------------------ */
-/* re-prediction into the warp's buffer (code/partial_events.f)         */
-/* ------------------------------------------------------------------ */
-__device__ __forceinline__ bool check_tij(Err E, double tij, int i) {
-    /* reference debug check: negative time beyond 1e-10 (code/eventredo_up.f:58-74) */
-    if (tij < 0.0 && fabs(tij) > 1.0e-10) { set_err(E, DMD_E_NEG_TIME, i); return false; }
-    return true;
-}
-
-/* warp: partial_events(i, j) (code/partial_events.f:5-205; j = -1 after a
- * ghost) into W's buffer.
- *
- * The reference updates beads one operation at a time: the full
- * re-prediction of i and of j (eventredo_up over the up list and the
- * extras), then for every bead l of the down lists and the lower extras of
- * i and then j, either a full re-prediction of l (when l's current partner
- * is the source) or a comparison with the pair (l, source)
- * (eventredo_down).  No prediction depends on another: all read the state
- * after the collision.  So the pairs are predicted as one flat task list,
- * 32 per pass with one call site, and the order-dependent part - which
- * candidate wins, when a full re-prediction is due - is replayed per bead
- * on integer keys.  A bead needs its full re-prediction only if its
- * partner before the event is one of its sources or a source repeats;
- * those beads ("marked") are fully re-predicted up front, in rounds of at
- * most TG_MAX - 2. */
-/* Steps of partial_events(i, j) (code/partial_events.f:5-205; j = -1
- * after a ghost), run on one warp into W's buffer.
- *
- * The reference updates beads one operation at a time: the full
- * re-prediction of i and of j (eventredo_up over the up list and the
- * extras), then for every bead l of the down lists and the lower extras of
- * i and then j, either a full re-prediction of l (when l's current partner
- * is the source) or a comparison with the pair (l, source)
- * (eventredo_down).  No prediction depends on another: all read the state
- * after the collision.  So the pairs are predicted as one flat task list
- * (32 per pass, one call site; or pooled with the other events of a batch,
- * see k_run) and the order-dependent part - which candidate wins, when a
- * full re-prediction is due - is replayed per bead on integer keys.  A bead
- * needs its full re-prediction only if its partner before the event is one
- * of its sources or a source repeats; those beads ("marked") are fully
- * re-predicted up front, in rounds of at most TG_MAX - 2. */
-
-/* 1-2: the down-list operations in the reference's order, and the distinct
- * beads among them (leaders) with their first operation and mark */
-__device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
-    int lane = threadIdx.x & 31;
-    /* 1. the down-list operations in the reference's order */
-    int n = 0;
-    {
-        int cnt = S.dnn[i];
-        const int *dn = S.dn + (size_t)i * S.cap;
-        const int8_t *dc = S.dnc ? S.dnc + (size_t)i * S.cap : nullptr;
-        for (int q = lane; q < cnt; q += 32) { W.ops_l[q] = dn[q]; W.ops_s[q] = i; W.ops_c[q] = dc ? dc[q] : (int8_t)-1; }
-        n = cnt;
-        if (lane == 0)
-            for (int k = 0; k < 3; ++k) {
-                int l = S.er[4 * i + k];
-                if (l >= 0 && l < i) { W.ops_l[n] = l; W.ops_s[n] = i; W.ops_c[n] = -1; ++n; }
-            }
-        n = __shfl_sync(FULL, n, 0);
-        if (j >= 0) {
-            int cj = S.dnn[j];
-            const int *dj = S.dn + (size_t)j * S.cap;
-            const int8_t *dcj = S.dnc ? S.dnc + (size_t)j * S.cap : nullptr;
-            for (int base = 0; base < cj; base += 32) {
-                int q = base + lane;
-                int l = q < cj ? dj[q] : -1;
-                bool keep = q < cj && l != i;
-                unsigned m = __ballot_sync(FULL, keep);
-                int pos = n + __popc(m & ((1u << lane) - 1));
-                if (keep) { W.ops_l[pos] = l; W.ops_s[pos] = j; W.ops_c[pos] = dcj ? dcj[q] : (int8_t)-1; }
-                n += __popc(m);
-            }
-            if (lane == 0)
-                for (int k = 0; k < 3; ++k) {
-                    int l = S.er[4 * j + k];
-                    if (l >= 0 && l < j) { W.ops_l[n] = l; W.ops_s[n] = j; W.ops_c[n] = -1; ++n; }
-                }
-            n = __shfl_sync(FULL, n, 0);
-        }
-    }
-    __syncwarp();
-    DMD_SUB(2);
-    /* 2. distinct beads (leaders), their first operation and mark */
-    int nl = 0, nm = 0;
-    if (n <= 32) {
-        /* one pass: lanes holding the same bead find each other in one step */
-        int q = lane;
-        bool in = q < n;
-        int l = in ? W.ops_l[q] : -1 - lane;
-        int src = in ? W.ops_s[q] : -1;
-        unsigned peers = __match_any_sync(FULL, l);
-        bool lead = in && (__ffs(peers) - 1) == lane;
-        int p0 = (in && l != i) ? S.nptnr[l] : -2;
-        unsigned hit = __ballot_sync(FULL, in && src == p0);
-        unsigned same = __match_any_sync(FULL, in ? ((long long)l << 32) | (unsigned)src : -1LL - lane);
-        unsigned dup = __ballot_sync(FULL, in && __popc(same) > 1);
-        bool mark = lead && l != i && ((hit | dup) & peers) != 0;
-        unsigned m = __ballot_sync(FULL, lead);
-        int pos = __popc(m & ((1u << lane) - 1));
-        unsigned mm = __ballot_sync(FULL, mark);
-        int mpos = __popc(mm & ((1u << lane) - 1));
-        if (lead) { W.lead_l[pos] = l; W.lead_q[pos] = (int16_t)q; W.lead_m[pos] = mark; }
-        if (mark) W.mk[mpos] = (int16_t)pos;
-        nl = __popc(m);
-        nm = __popc(mm);
-    }
-    for (int base = 0; n > 32 && base < n; base += 32) {
-        int q = base + lane;
-        bool lead = false, mark = false;
-        int l = -1;
-        if (q < n) {
-            l = W.ops_l[q];
-            lead = true;
-            for (int p = 0; p < q; ++p) if (W.ops_l[p] == l) { lead = false; break; }
-            if (lead && l != i) {
-                int p0 = S.nptnr[l];
-                int s1 = -1, s2 = -1;   /* sources are i or j: two at most */
-                for (int pp = q; pp < n; ++pp) {
-                    if (W.ops_l[pp] != l) continue;
-                    int src = W.ops_s[pp];
-                    if (src == p0 || src == s1 || src == s2) mark = true;
-                    if (s1 < 0) s1 = src; else s2 = src;
-                }
-            }
-        }
-        unsigned m = __ballot_sync(FULL, lead);
-        int pos = nl + __popc(m & ((1u << lane) - 1));
-        unsigned mm = __ballot_sync(FULL, lead && mark);
-        int mpos = nm + __popc(mm & ((1u << lane) - 1));
-        if (lead) { W.lead_l[pos] = l; W.lead_q[pos] = (int16_t)q; W.lead_m[pos] = mark; }
-        if (lead && mark) W.mk[mpos] = (int16_t)pos;
-        nl += __popc(m);
-        nm += __popc(mm);
-    }
-    if (lane == 0) {
-        W.nops = n;
-        W.nlead = nl; W.nmarked = nm; W.npred = 2 + nl;
-        W.pb[0] = i; W.pb[1] = j;
-    }
-    __syncwarp();
-}
-
-/* 3: the full re-predictions of round rd (i, j in round 0, then marked
- * beads), their running minima and task offsets; W.ntg, W.ntask */
-__device__ void warp_rp_targets(const DSys &S, WarpArea &W, int i, int j, int rd, double Hraw, long long Hkey) {
-    int lane = threadIdx.x & 31;
-    const int per_round = TG_MAX - 2;
-    const int nm = W.nmarked;
-    /* 3. this round's full re-predictions: i, j (round 0), marked beads */
-    int m0 = rd * per_round, m1 = min(nm, m0 + per_round);
-    int ntg = 2 + (m1 - m0);
-    for (int t = lane; t < ntg; t += 32) {
-        int b;
-        if (t == 0) b = rd == 0 ? i : -1;
-        else if (t == 1) b = rd == 0 ? j : -1;
-        else b = W.lead_l[W.mk[m0 + t - 2]];
-        W.fs.tg_b[t] = b;
-        W.fs.tg_k[t] = Hkey; W.fs.tg_p[t] = -1; W.fs.tg_raw[t] = Hraw; W.fs.tg_y[t] = -1;
-    }
-    /* task offsets: an inclusive scan over the targets of the up-list
-     * length plus the extras above the bead */
-    int run = 0;
-    for (int base = 0; base < ntg; base += 32) {
-        int t = base + lane;
-        int b = t < ntg ? W.fs.tg_b[t] : -1;
-        int c = 0;
-        if (b >= 0) {
-            c = S.upn[b];
-            for (int k = 0; k < 3; ++k) c += S.er[4 * b + k] > b;
-        }
-        int incl = c;
-        for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
-        if (t < ntg) W.fs.tg_base[t] = run + incl - c;
-        run += __shfl_sync(FULL, incl, 31);
-    }
-    if (lane == 0) W.fs.tg_base[ntg] = run;
-    __syncwarp();
-    const bool mapped = run <= TMAP_MAX;
-    if (mapped) {   /* task -> target map, one target per lane */
-        for (int t = lane; t < ntg; t += 32)
-            for (int q = W.fs.tg_base[t]; q < W.fs.tg_base[t + 1]; ++q) W.fs.tmap[q] = (int8_t)t;
-        __syncwarp();
-    }
-    if (lane == 0) { W.ntg = ntg; W.ntask = (rd == 0 ? W.nops : 0) + run; }
-    __syncwarp();
-}
-
-/* the task q of round rd as (bead, partner, static code or -1, target or
- * -1 for a down operation); pa < 0 when the slot holds no pair */
-__device__ __forceinline__ void rp_task(const DSys &S, const WarpArea &W, int q, int nop, int &pa, int &pbb, int &st,
-                                        int &tgt) {
-    pa = -1; pbb = -1; st = -1; tgt = -1;
-    if (q < nop) {
-        pa = W.ops_l[q]; pbb = W.ops_s[q];
-        st = W.ops_c[q];
-        return;
-    }
-    int rel = q - nop;
-    int ntg = W.ntg;
-    int run = W.fs.tg_base[ntg];
-    int lo;
-    if (run <= TMAP_MAX) lo = W.fs.tmap[rel];
-    else {
-        int hi = ntg - 1;                /* last target with tg_base <= rel */
-        lo = 0;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (W.fs.tg_base[mid] <= rel) lo = mid; else hi = mid - 1;
-        }
-    }
-    tgt = lo;
-    int b = W.fs.tg_b[lo];
-    int k = rel - W.fs.tg_base[lo];
-    int nu = S.upn[b];
-    int m;
-    if (k < nu) { m = S.up[(size_t)b * S.cap + k]; st = S.upc[(size_t)b * S.cap + k]; }
-    else {
-        int want = k - nu;
-        m = -1;
-        for (int k2 = 0; k2 < 3; ++k2) {
-            int e = S.er[4 * b + k2];
-            if (e > b) { if (want == 0) { m = e; break; } --want; }
-        }
-    }
-    if (m > b) { pa = b; pbb = m; }
-}
-
-/* one prediction task: ev_code(l, source) for a down operation, ev_code(m, b)
- * for a full one; the time is tij + tfalse for a down operation and tij for
- * a full one (tfalse is added after its minimum; x + (-0.0) == x) */
-__device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb, int st, bool is_op, double tf,
-                                           int hbonds, double &tt, int &ty) {
-    double tij = 0.0;
-    ty = 0;
-    bool ok = false;
-    if (pa >= 0) {
-        int a1 = is_op ? pa : pbb, a2 = is_op ? pbb : pa;
-        int code = st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
-        ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
-        if (!ok) set_err(E, DMD_E_INPUT, pa);
-        else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
-    }
-    tt = tij + (is_op ? tf : -0.0);
-    return ok;
-}
-
-/* 1-4 into the CTA's task pool for the event of warp `owner` (its tasks
- * must fit one round and the pool), else W.pooled = 0 and the owner warp
- * runs warp_repredict() after the pool */
-__device__ void warp_rp_prepare(const DSys &S, WarpArea &W, TaskPool &TP, int owner, int i, int j, double tf,
-                                double imax) {
-    int lane = threadIdx.x & 31;
-    warp_rp_lists(S, W, i, j);
-    bool pooled = W.nmarked <= TG_MAX - 2;
-    int base = 0;
-    if (pooled) {
-        const double Hraw = imax + DMD_LTSTEP - tf;
-        warp_rp_targets(S, W, i, j, 0, Hraw, okey(Hraw));
-        int nt = W.ntask, nop = W.nops;
-        if (lane == 0) base = atomicAdd(&TP.n, nt);
-        base = __shfl_sync(FULL, base, 0);
-        pooled = base + nt <= PTASK_MAX;
-        for (int q = lane; q < nt && base + q < PTASK_MAX; q += 32) {
-            int pa = -1, pbb = -1, st = -1, tgt = -1;
-            if (pooled) rp_task(S, W, q, nop, pa, pbb, st, tgt);
-            TP.a[base + q] = pa; TP.b[base + q] = pbb; TP.st[base + q] = (int8_t)st;
-            TP.flag[base + q] = (int8_t)((q < nop ? 1 : 0) | (owner << 1));
-        }
-    }
-    if (lane == 0) { W.pooled = pooled; W.pool_base = base; }
-    __syncwarp();
-}
-
-/* 4: the tasks of the round on this warp, 32 per pass */
-__device__ void warp_rp_tasks(const DSys &S, Err E, WarpArea &W, int rd, double tf, int hbonds) {
-    int lane = threadIdx.x & 31;
-    const int nop = rd == 0 ? W.nops : 0;
-    const int ntask = W.ntask;
-    for (int base = 0; base < ntask; base += 32) {
-        int q = base + lane;
-        int pa = -1, pbb = -1, st = -1, tgt = -1;
-        if (q < ntask) rp_task(S, W, q, nop, pa, pbb, st, tgt);
-        double tt;
-        int ty;
-        bool ok = rp_predict(S, E, pa, pbb, st, q < nop, tf, hbonds, tt, ty);
-        if (q < nop) { W.op_t[q] = tt; W.op_y[q] = ok ? (int8_t)ty : (int8_t)-128; }
-        /* segmented minimum of the full tasks, segment = target */
-        long long k = (tgt >= 0 && ok) ? okey(tt) : DMD_KEY_INF;
-        int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
-        double rt = tt;
-        int y = ty;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            long long k2 = __shfl_down_sync(FULL, k, o);
-            int p2 = __shfl_down_sync(FULL, p, o);
-            double r2 = __shfl_down_sync(FULL, rt, o);
-            int y2 = __shfl_down_sync(FULL, y, o);
-            int g2 = __shfl_down_sync(FULL, tgt, o);
-            if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
-        }
-        int gprev = __shfl_up_sync(FULL, tgt, 1);
-        bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
-        if (head && key_less(k, p, W.fs.tg_k[tgt], W.fs.tg_p[tgt])) {
-            W.fs.tg_k[tgt] = k; W.fs.tg_p[tgt] = p; W.fs.tg_raw[tgt] = rt; W.fs.tg_y[tgt] = (int8_t)y;
-        }
-        __syncwarp();
-    }
-}
-
-/* 5-6: the full results (minimum + tfalse) and the replay of the operations
- * per bead: round 0 replays the unmarked beads and i, each round its marked
- * beads */
-__device__ void warp_rp_finish(const DSys &S, Err E, WarpArea &W, int i, int j, int rd, double tf, double imax) {
-    int lane = threadIdx.x & 31;
-    const int per_round = TG_MAX - 2;
-    const int n = W.nops, nl = W.nlead, nm = W.nmarked, ntg = W.ntg;
-    const int m0 = rd * per_round, m1 = min(nm, m0 + per_round);
-    const long long imax_key = okey(imax);
-    /* 5. the full results: time = minimum + tfalse */
-    for (int t = lane; t < ntg; t += 32) W.fs.tg_raw[t] = W.fs.tg_raw[t] + tf;
-    __syncwarp();
-    if (rd == 0 && lane < 2 && (lane == 0 || j >= 0)) {
-        double tn = W.fs.tg_raw[lane];
-        W.pt[lane] = tn; W.pn[lane] = W.fs.tg_p[lane]; W.pc[lane] = W.fs.tg_y[lane];
-        W.pq[lane] = okey(tn) < imax_key;
-    }
-    __syncwarp();
-    /* 6. replay of the operations per bead: round 0 replays the
-     * unmarked beads and i, each round its marked beads */
-    int nrep = rd == 0 ? nl : 0;
-    int nrep_m = m1 - m0;
-    for (int q = lane; q < nrep + nrep_m; q += 32) {
-        int ld, ft;
-        if (q < nrep) {
-            ld = q;
-            if (W.lead_m[ld]) continue;          /* replayed in its round */
-            ft = W.lead_l[ld] == i ? 0 : -1;
-        } else {
-            ld = W.mk[m0 + q - nrep];
-            ft = 2 + (q - nrep);
-        }
-        int l = W.lead_l[ld];
-        double t;
-        int p, y;
-        bool qq;
-        if (l == i) { t = W.fs.tg_raw[0]; p = W.fs.tg_p[0]; y = W.fs.tg_y[0]; qq = okey(t) < imax_key; }
-        else { t = S.tim[l]; p = S.nptnr[l]; y = S.colt[l]; qq = S.queued[l] != 0; }
-        for (int pp = W.lead_q[ld]; pp < n; ++pp) {
-            if (W.ops_l[pp] != l) continue;
-            int src = W.ops_s[pp];
-            if (p == src) {
-                if (ft < 0) { set_err(E, DMD_E_STATE, l); break; }
-                t = W.fs.tg_raw[ft]; p = W.fs.tg_p[ft]; y = W.fs.tg_y[ft]; qq = okey(t) < imax_key;
-            } else if (W.op_y[pp] != -128) {
-                double tn = W.op_t[pp];
-                long long kn = okey(tn);
-                if (key_less(kn, src, okey(t), p)) { t = tn; p = src; y = W.op_y[pp]; qq = kn < imax_key; }
-            }
-        }
-        int slot = 2 + ld;
-        if (l == i) {
-            W.pb[slot] = -1;
-            W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq;
-        } else {
-            W.pb[slot] = l;
-            W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
-        }
-    }
-    __syncwarp();
-}
-
-/* 7: the earliest new queued entry of this event */
-__device__ void warp_rp_tnew(WarpArea &W) {
-    int lane = threadIdx.x & 31;
-    long long bk = DMD_KEY_INF;
-    int bb = INT_MAX;
-    for (int q = lane; q < W.npred; q += 32) {
-        int b = W.pb[q];
-        if (b < 0 || !W.pq[q]) continue;
-        long long kk = okey(W.pt[q]);
-        if (key_less(kk, b, bk, bb)) { bk = kk; bb = b; }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        long long k2 = __shfl_xor_sync(FULL, bk, o);
-        int b2 = __shfl_xor_sync(FULL, bb, o);
-        if (key_less(k2, b2, bk, bb)) { bk = k2; bb = b2; }
-    }
-    if (lane == 0) { W.tnew_key = bk; W.tnew_idx = bb; }
-    __syncwarp();
-}
-
-__device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, double imax,
-                               int hbonds) {
-    warp_rp_lists(S, W, i, j);
-    DMD_SUB(3);
-    const double Hraw = imax + DMD_LTSTEP - tf;   /* eventredo_up's starting time */
-    const long long Hkey = okey(Hraw);
-    const int nm = W.nmarked;
-    const int per_round = TG_MAX - 2;
-    int rounds = nm > 0 ? (nm + per_round - 1) / per_round : 1;
-    for (int rd = 0; rd < rounds; ++rd) {
-        warp_rp_targets(S, W, i, j, rd, Hraw, Hkey);
-        DMD_SUB(4);
-        warp_rp_tasks(S, E, W, rd, tf, hbonds);
-        DMD_SUB(5);
-        warp_rp_finish(S, E, W, i, j, rd, tf, imax);
-    }
-    DMD_SUB(7);
-    warp_rp_tnew(W);
-}
-
-__device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
-    int lane = threadIdx.x & 31;
-    for (int q = lane; q < W.npred; q += 32) {
-        int b = W.pb[q];
-        if (b < 0) continue;
-        set_pred(S, b, W.pt[q], W.pn[q], W.pc[q], W.pq[q] != 0);
-    }
-    __syncwarp();
-}
-
-/* ------------------------------------------------------------------ */
-/* footprints of a batch candidate                                     */
-/* ------------------------------------------------------------------ */
-/* Footprint of one candidate, as three sets of beads:
- *   R: beads whose state (position, velocity, identity, H-bond partner,
- *      extra_repuls, pair-type overrides) the event reads: i, j, their
- *      extra_repuls, the H-bond helpers of i, j and of their H-bond
- *      partners, both neighbour lists of i and j, and for every bead that may
- *      need a full re-prediction its up list and extras;
- *   W: beads whose state the collision may write: i, j, their extra_repuls
- *      and their own helpers (code/repuls_add.f, repuls_del_b.f, the
- *      shoulders of main.F90:825-868) - W is part of R;
- *   Q: beads whose event-queue entry the event reads and rewrites: i, j, the
- *      down lists, the lower extras and the helpers that become extras.
- * Candidate k conflicts with an earlier k' when R(k) meets W(k'), W(k) meets
- * R(k') or Q(k) meets Q(k'): then the two do not commute.  Reading the same
- * neighbour is no conflict.  A claim raises the three tables (own, own + N,
- * own + 2N) to the candidate's ticket, (batch sequence) * 64 + (63 - slot),
- * so that after all claims each entry holds the ticket of the earliest
- * candidate whose set has the bead; tickets grow from batch to batch and
- * the tables need no reset.  The beads are listed in W.rset/wset/qset for
- * warp_footprint_test(). */
-__device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
-    int lane = threadIdx.x & 31;
-    const int N = S.N;
-    unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
-    if (lane == 0) { W.nrset = 0; W.nwset = 0; W.nqset = 0; W.casc_over = 0; }
-    __syncwarp();
-    auto visit_r = [&](int b) {
-        if (b < 0) return;
-        atomicMax(&own_r[b], ticket);
-        int pos = atomicAdd(&W.nrset, 1);
-        if (pos < RSET_MAX) W.rset[pos] = b;
-    };
-    auto visit_w = [&](int b) {
-        if (b < 0) return;
-        atomicMax(&own_w[b], ticket);
-        int pos = atomicAdd(&W.nwset, 1);
-        if (pos < WSET_MAX) W.wset[pos] = b;
-        visit_r(b);
-    };
-    auto visit_q = [&](int b) {
-        if (b < 0) return;
-        atomicMax(&own_q[b], ticket);
-        int pos = atomicAdd(&W.nqset, 1);
-        if (pos < QSET_MAX) W.qset[pos] = b;
-        visit_r(b);
-    };
-    /* fixed part on lanes 0..17 */
-    if (lane < 18) {
-        int b = -1;
-        if (lane == 0) b = i;
-        else if (lane == 1) b = j;
-        else if (lane < 6) b = S.er[4 * i + lane - 2];
-        else if (lane < 10) b = S.er[4 * j + lane - 6];
-        else {
-            int which = (lane - 10) >> 1;
-            int x = which == 0 ? i : which == 1 ? j : which == 2 ? S.er[4 * i + 3] : S.er[4 * j + 3];
-            int h1, h2;
-            own_helpers(S, x, h1, h2);
-            b = (lane & 1) ? h2 : h1;
-        }
-        if (lane < 14) visit_w(b);   /* i, j, extras, own helpers */
-        else visit_r(b);             /* the partners' helpers: read only */
-        /* queue entries: i, j, the lower extras (0..2) and the helpers */
-        bool q = lane < 2 || (lane >= 2 && lane < 5) || (lane >= 6 && lane < 9) || (lane >= 10 && lane < 14);
-        if (q) visit_q(b);
-    }
-    /* neighbour lists of i and j */
-    int ui = S.upn[i], di = S.dnn[i], uj = S.upn[j], dj = S.dnn[j];
-    const int *UI = S.up + (size_t)i * S.cap, *DI = S.dn + (size_t)i * S.cap;
-    const int *UJ = S.up + (size_t)j * S.cap, *DJ = S.dn + (size_t)j * S.cap;
-    for (int q = lane; q < ui; q += 32) visit_r(UI[q]);
-    for (int q = lane; q < di; q += 32) visit_q(DI[q]);
-    for (int q = lane; q < uj; q += 32) visit_r(UJ[q]);
-    for (int q = lane; q < dj; q += 32) visit_q(DJ[q]);
-    /* beads that may be fully re-predicted */
-    int nc = 0;
-    for (int base = 0; base < di + dj; base += 32) {
-        int q = base + lane;
-        int l = -1;
-        if (q < di) { l = DI[q]; if (S.nptnr[l] != i) l = -1; }
-        else if (q < di + dj) { l = DJ[q - di]; if (S.nptnr[l] != j) l = -1; }
-        unsigned m = __ballot_sync(FULL, l >= 0);
-        int pos = nc + __popc(m & ((1u << lane) - 1));
-        if (l >= 0 && pos < CASC_MAX - 10) W.casc[pos] = l;
-        nc += __popc(m);
-    }
-    bool over = nc > CASC_MAX - 10;
-    nc = min(nc, CASC_MAX - 10);
-    if (lane < 10) {
-        int b;
-        if (lane < 3) b = S.er[4 * i + lane];
-        else if (lane < 6) b = S.er[4 * j + lane - 3];
-        else {
-            int x = lane < 8 ? i : j, h1, h2;
-            own_helpers(S, x, h1, h2);
-            b = (lane & 1) ? h2 : h1;
-        }
-        W.casc[nc + lane] = b;
-    }
-    __syncwarp();
-    /* their up lists and extras as one flat range over the lanes: entry
-     * offsets by a warp scan, then each lane finds its cascade bead */
-    nc += 10;
-    int run = 0;
-    for (int base = 0; base < nc; base += 32) {
-        int c = base + lane;
-        int l = c < nc ? W.casc[c] : -1;
-        int cnt = l >= 0 ? S.upn[l] + 3 : 0;
-        int incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
-        if (c < nc) W.cbase[c] = run + incl - cnt;
-        run += __shfl_sync(FULL, incl, 31);
-    }
-    if (lane == 0) W.cbase[nc] = run;
-    __syncwarp();
-    for (int q = lane; q < run; q += 32) {
-        int lo = 0, hi = nc - 1;          /* last cascade bead with cbase <= q */
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (W.cbase[mid] <= q) lo = mid; else hi = mid - 1;
-        }
-        int l = W.casc[lo];
-        int k = q - W.cbase[lo];
-        int ul = W.cbase[lo + 1] - W.cbase[lo] - 3;
-        visit_r(k < ul ? S.up[(size_t)l * S.cap + k] : S.er[4 * l + (k - ul)]);
-    }
-    __syncwarp();
-    /* an incomplete list (cascade or set overflow) ends the batch here */
-    if (lane == 0) W.casc_over = over || W.nrset > RSET_MAX || W.nwset > WSET_MAX || W.nqset > QSET_MAX;
-    __syncwarp();
-}
-__device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, int N, unsigned ticket) {
-    int lane = threadIdx.x & 31;
-    const volatile unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
-    bool conflict = false;
-    int nr = min(W.nrset, RSET_MAX), nw = min(W.nwset, WSET_MAX), nq = min(W.nqset, QSET_MAX);
-    for (int q = lane; q < nr; q += 32) conflict |= own_w[W.rset[q]] > ticket;
-    for (int q = lane; q < nw; q += 32) conflict |= own_r[W.wset[q]] > ticket;
-    for (int q = lane; q < nq; q += 32) conflict |= own_q[W.qset[q]] > ticket;
-    return __any_sync(FULL, conflict);
-}
-
-/* ------------------------------------------------------------------ */
 /* CTA-wide reductions                                                 */
 /* ------------------------------------------------------------------ */
 __device__ double cta_max(SharedState &sh, double v) {
@@ -1404,6 +399,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
         }
         __syncthreads();
     }
+    int mdn = 0;
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
         int nu = 0, nd = 0;
         int *up = S.up + (size_t)b * S.cap, *dn = S.dn + (size_t)b * S.cap;
@@ -1469,6 +465,17 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
         if (nu > S.cap || nd > S.cap) set_err(sh, DMD_E_CAPACITY, b);
         S.upn[b] = min(nu, S.cap);
         S.dnn[b] = min(nd, S.cap);
+        mdn = max(mdn, min(nd, S.cap));
+    }
+    /* the longest down list, which selects the k_run variant */
+    mdn = __reduce_max_sync(FULL, mdn);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh.red_i[threadIdx.x >> 5] = mdn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int w = 0; w < NWARPS; ++w) m = max(m, sh.red_i[w]);
+        sh.sc.max_dn = m;
     }
     __syncthreads();
 }
@@ -1823,6 +830,7 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
         out->nbr_mean = nbr / (double)N;
         out->n_batches = sh.sc.n_batches; out->n_rolled_back = sh.sc.n_rolled_back;
         out->n_candidates = sh.sc.n_candidates;
+        out->max_down = sh.sc.max_dn;
     }
     __syncthreads();
 }
@@ -1929,374 +937,37 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, i
     if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
-/* The event loop of code/main.F90:484-1258 for nsys systems, each advanced
- * by one cluster of C CTAs (C = 1: one CTA).  The leader CTA (rank 0)
- * selects events and keeps the counters; a batch's candidates go one per
- * warp over all CTAs of the cluster. */
-__global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target_all,
-                                                     const long long *targets, int hbonds_mask,
-                                                     const int *chain_start, const int *chain_len,
-                                                     const int *chain_off, dmd_diag *outputs, int own_cap, int C) {
-    extern __shared__ WarpArea warea[];
-    __shared__ SharedState sh;
-    __shared__ DSys S_sh;
-    const int rank = C > 1 ? (int)cg::this_cluster().block_rank() : 0;
-    const int r = blockIdx.x / C;
-    if (r >= nsys) return;             /* whole clusters only */
-    const long long target = targets ? targets[r] : target_all;   /* events for this system */
-    const bool leader = rank == 0;
-    if (threadIdx.x == 0) S_sh = systems[r];
-    __syncthreads();
-    const DSys &S = S_sh;
-    const int N = S.N;
-    const int hbonds = hbonds_mask & 1;
-    const bool phys = (S.flags & DMD_FLAG_COUNT_PHYSICAL) != 0;
-    const bool stop_out = (S.flags & DMD_FLAG_STOP_AT_OUTPUT) != 0;
-    const bool serial = (S.flags & DMD_FLAG_SERIAL) != 0;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gw = rank * NWARPS + warp;          /* candidate slot of this warp */
-    const int slots = min(C * NWARPS, CAND_MAX);
-    WarpArea &W = warea[warp];
-    SharedState *L = C > 1 ? cg::this_cluster().map_shared_rank(&sh, 0) : &sh;
-    if (threadIdx.x == 0) {
-        sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0;
-        sh.delta = sh.sc.interval * 0.05;
-        sh.bseq = 0;
-        sh.exitf = 0;
-    }
-    /* footprint claim table: shared memory when one CTA holds the system and
-     * it fits, else the system's global array; cleared at every launch */
-    TaskPool &TP = *(TaskPool *)(warea + NWARPS);
-    unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)((char *)(warea + NWARPS) + sizeof(TaskPool)) : S.owner;
-    if (threadIdx.x == 0) TP.n = 0;
-    for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
-    csync(C);
-    DMD_PHASE_START(leader ? r : -1);
-    const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
-    const long long max_iter = 16 * target + 1000000;
-    const long long t_start = clock64();
-    long long iter = 0;
-    while (true) {
-        /* ---- the leader selects the next event (and a batch) ---- */
-        if (leader) {
-            for (int h = threadIdx.x; h < S.nl2; h += blockDim.x) l2_update(S, h);
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                bool ex = sh.sc.done >= target || sh.sc.err || sh.sc.stop;
-                if (!ex && ++iter > max_iter) { set_err(sh, DMD_E_DEVICE_TIMEOUT, 0); ex = true; }
-                sh.exitf = ex;
-            }
-            __syncthreads();
-            if (!sh.exitf && warp == 0) {
-                long long kroot;
-                int e = warp_tree_root(S, kroot);
-                if (lane == 0) {
-                    sh.ev = e;
-                    sh.kcut = kroot;
-                    if (e < 0) { set_err(sh, DMD_E_STATE, 0); sh.exitf = 1; }
-                }
-            }
-            __syncthreads();
-            DMD_PHASE(0);
-            if (!sh.exitf && sh.ev < N) {
-                int e = sh.ev;
-                long long kroot = sh.kcut;
-                long long left = target - sh.sc.done;
-                int m;
-                if (serial || left <= 1) {
-                    if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = e; }
-                    __syncthreads();
-                    m = 1;
-                } else {
-                    m = cta_candidates(S, sh, e, kroot, slots);
-                    if (m > slots) m = slots;
-                    if (m > left) m = (int)left;
-                }
-                if (threadIdx.x == 0) {
-                    sh.m = m;
-                    sh.tick_reset = m > 1 && sh.bseq >= DMD_TICKET_SEQ_MAX;
-                    sh.c_simple[0] = 0;    /* set by the footprint test when m > 1 */
-                }
-                DMD_PHASE(1);
-            } else if (!sh.exitf && threadIdx.x == 0) {
-                /* a pseudo event: its counter and time */
-                sh.sc.coll += 1;
-                sh.tf_iv = S.tim[sh.ev];
-                if (sh.ev != N) sh.sc.tfalse = sh.tf_iv;
-            }
-            if (threadIdx.x == 0) {
-                sh.coll0 = sh.sc.coll; sh.log0 = sh.sc.log_count; sh.imax = sh.sc.interval_max; sh.tnow = sh.sc.t;
-            }
-        }
-        csync(C);
-        /* ---- the other CTAs copy the leader's decision ---- */
-        if (!leader) {
-            if (threadIdx.x == 0) {
-                sh.exitf = L->exitf; sh.ev = L->ev; sh.m = L->m; sh.tick_reset = L->tick_reset; sh.bseq = L->bseq;
-                sh.coll0 = L->coll0; sh.log0 = L->log0; sh.imax = L->imax; sh.tnow = L->tnow; sh.tf_iv = L->tf_iv;
-            }
-            if (threadIdx.x < NWARPS) {
-                int k = rank * NWARPS + threadIdx.x;
-                if (k < CAND_MAX) { sh.sort_idx[k] = L->sort_idx[k]; sh.sort_key[k] = L->sort_key[k]; }
-            }
-            __syncthreads();
-        }
-        if (sh.exitf) break;
-        int ph_kind __attribute__((unused)) = 9;
-        const int e = sh.ev;
-        if (e < N) {
-            ph_kind = 5;
-            /* ---- a batch of pair events ---- */
-            const int m = sh.m;
-            int P = 1;
-            if (m > 1) {
-                if (sh.tick_reset) {   /* tickets exhausted: clear the table */
-                    for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
-                    csync(C);
-                    if (threadIdx.x == 0) sh.bseq = 0;
-                    __syncthreads();
-                }
-                unsigned ticket = ((unsigned)(sh.bseq + 1) << 6) | (unsigned)(63 - gw);
-                if (gw < m) {
-                    int i = sh.sort_idx[gw];
-                    warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
-                }
-                csync(C);
-                DMD_PHASE(10);
-                if (gw < m) {
-                    bool c = warp_footprint_test(W, own, N, ticket);
-                    if (lane == 0) {
-                        int ct0 = S.colt[sh.sort_idx[gw]];
-                        L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over;
-                        L->c_simple[gw] = ct0 >= 1 && ct0 <= 3;
-                    }
-                }
-                csync(C);
-                DMD_PHASE(11);
-                if (leader && threadIdx.x == 0) {
-                    sh.bseq = sh.tick_reset ? 1 : sh.bseq + 1;
-                    /* the longest conflict-free prefix; an incomplete footprint
-                     * (cascade list overflow) ends the batch after its event */
-                    int p = m;
-                    for (int k = 0; k < m; ++k) {
-                        if (k > 0 && sh.c_conflict[k]) { p = k; break; }
-                        if (sh.c_over[k]) { p = k > 0 ? k : 1; break; }
-                    }
-                    sh.P = p;
-                }
-                csync(C);
-                if (!leader && threadIdx.x == 0) sh.P = L->P;
-                __syncthreads();
-                P = sh.P;
-                DMD_PHASE(2);
-            }
-            /* speculative commit of each event on its warp */
-            const long long coll0 = sh.coll0;
-            const double imax = sh.imax;
-            const bool split = C == 1 && P <= NWARPS / 2;
-            if (gw < P) {
-                int i = sh.sort_idx[gw];
-                int j = S.nptnr[i];
-                double tf = S.tim[i];
-                if (lane == 0) { W.i = i; W.j = j; W.tf = tf; W.coll = coll0 + gw + 1; }
-                __syncwarp();
-                DMD_SUB(-1);
-                warp_snapshot(S, W, i, j);
-                DMD_SUB(0);
-                if (lane == 0) { W.err = 0; W.err_info = 0; }
-                __syncwarp();
-                Err E{&W.err, &W.err_info};
-                warp_collision(S, E, W, i, j, tf, coll0 + gw + 1, hbonds);
-                DMD_SUB(1);
-                /* the re-prediction's lists and tasks; the tasks go to the
-                 * CTA's pool when they fit (one round of full
-                 * re-predictions), else this warp runs them after the pool.
-                 * In a batch of at most NWARPS/2 events, a second warp
-                 * prepares them while this one computes the collision,
-                 * when the collision cannot change the H-bond state they
-                 * read (coltype 1-3). */
-                if (!(split && sh.c_simple[gw])) warp_rp_prepare(S, W, TP, warp, i, j, tf, imax);
-            } else if (split && warp >= NWARPS / 2 && warp - NWARPS / 2 < P && sh.c_simple[warp - NWARPS / 2]) {
-                const int k = warp - NWARPS / 2;
-                const int i = sh.sort_idx[k];
-                warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
-            }
-            __syncthreads();
-            /* every pooled prediction task of this CTA's events, all warps */
-            {
-                const int ntot = min(TP.n, PTASK_MAX);
-                for (int q = threadIdx.x; q < ntot; q += blockDim.x) {
-                    int pa = TP.a[q];
-                    if (pa < 0) { TP.ok[q] = 0; continue; }
-                    int owner = TP.flag[q] >> 1;
-                    WarpArea &O = warea[owner];
-                    Err EO{&O.err, &O.err_info};
-                    double tt;
-                    int ty;
-                    bool ok = rp_predict(S, EO, pa, TP.b[q], TP.st[q], (TP.flag[q] & 1) != 0, O.tf, hbonds, tt, ty);
-                    TP.t[q] = tt; TP.ty[q] = (int8_t)ty; TP.ok[q] = ok;
-                }
-            }
-            __syncthreads();
-            if (gw < P) {
-                const int i = W.i, j = W.j;
-                const double tf = W.tf;
-                Err E{&W.err, &W.err_info};
-                if (W.pooled) {
-                    /* down operations' times, and the minimum per full
-                     * re-prediction over its contiguous tasks */
-                    const int base = W.pool_base, nop = W.nops, ntg = W.ntg;
-                    for (int q = lane; q < nop; q += 32) {
-                        W.op_t[q] = TP.t[base + q];
-                        W.op_y[q] = TP.ok[base + q] ? TP.ty[base + q] : (int8_t)-128;
-                    }
-                    for (int t = lane; t < ntg; t += 32) {
-                        long long bk = W.fs.tg_k[t];
-                        int bp = W.fs.tg_p[t];
-                        double braw = W.fs.tg_raw[t];
-                        int by = W.fs.tg_y[t];
-                        for (int x = base + nop + W.fs.tg_base[t]; x < base + nop + W.fs.tg_base[t + 1]; ++x) {
-                            if (!TP.ok[x]) continue;
-                            long long k = okey(TP.t[x]);
-                            if (key_less(k, TP.b[x], bk, bp)) { bk = k; bp = TP.b[x]; braw = TP.t[x]; by = TP.ty[x]; }
-                        }
-                        W.fs.tg_k[t] = bk; W.fs.tg_p[t] = bp; W.fs.tg_raw[t] = braw; W.fs.tg_y[t] = (int8_t)by;
-                    }
-                    __syncwarp();
-                    warp_rp_finish(S, E, W, i, j, 0, tf, imax);
-                    warp_rp_tnew(W);
-                } else {
-                    warp_repredict(S, E, W, i, j, tf, imax, hbonds);
-                }
-                DMD_SUB(8);
-                if (lane == 0 && W.xpulse) {
-                    if (S.ident[i] < S.ident[j]) repuls_del_b(S, i, j); else repuls_del_b(S, j, i);
-                }
-                __syncwarp();
-                if (lane == 0) {
-                    L->c_tnew_key[gw] = W.tnew_key; L->c_tnew_idx[gw] = W.tnew_idx;
-                    L->c_err[gw] = W.err; L->c_err_info[gw] = W.err_info;
-                    L->c_ct[gw] = W.ct; L->c_tf[gw] = W.tf;
-                }
-            }
-            if (threadIdx.x == 0) TP.n = 0;   /* the pool is free until the next batch */
-            csync(C);
-            DMD_PHASE(3);
-            /* validation: event k stands if it precedes every new entry of
-             * events 0..k-1; the leader also books the committed events */
-            if (leader && threadIdx.x == 0) {
-                int v = P;
-                long long bk = DMD_KEY_INF;
-                int bb = INT_MAX;
-                for (int k = 0; k < P; ++k) {
-                    if (k > 0 && !key_less(sh.sort_key[k], sh.sort_idx[k], bk, bb)) { v = k; break; }
-                    if (sh.c_err[k]) {   /* the run stops after the first event in error */
-                        set_err(sh, sh.c_err[k], sh.c_err_info[k]);
-                        v = k + 1;
-                        break;
-                    }
-                    if (key_less(sh.c_tnew_key[k], sh.c_tnew_idx[k], bk, bb)) { bk = sh.c_tnew_key[k]; bb = sh.c_tnew_idx[k]; }
-                }
-                sh.V = v;
-                for (int k = 0; k < v; ++k) {
-                    int ct = sh.c_ct[k];
-                    if (ct >= 1 && ct < 32) sh.sc.nevents[ct] += 1;
-                }
-                sh.sc.coll = coll0 + v;
-                sh.sc.n_pair += v;
-                sh.sc.n_batches += 1;
-                sh.sc.n_rolled_back += P - v;
-                sh.sc.n_candidates += m;
-                sh.sc.done += v;
-                sh.sc.tfalse = sh.c_tf[v - 1];
-                sh.sc.old_tfalse = sh.c_tf[v - 1];
-                if (S.log && S.log_cap > 0) sh.sc.log_count += v;
-            }
-            csync(C);
-            if (!leader && threadIdx.x == 0) sh.V = L->V;
-            __syncthreads();
-            DMD_PHASE(4);
-            const int V = sh.V;
-            if (gw < P) {
-                if (gw < V) {
-                    warp_commit_preds(S, W);
-                    if (lane == 0) log_event(S, sh.log0 + gw, W.coll, sh.tnow, W.tf, W.i, W.j, W.ct, W.evcode);
-                } else {
-                    warp_restore(S, W);
-                }
-            }
-            csync(C);   /* every commit lands before any level-1 group is recomputed */
-            if (gw < V) warp_l1_refresh(S, W.pb, W.npred);
-        } else if (e == N) {
-            ph_kind = 6;
-            /* ---- ghost collision: leader warp 0 ---- */
-            if (leader && warp == 0) {
-                double tf = sh.tf_iv;
-                if (lane == 0) {
-                    int i = lane_ghost(S, sh, tf);
-                    W.i = i; W.tf = tf;
-                }
-                __syncwarp();
-                int i = W.i;
-                tf = W.tf;
-                DMD_SUB(-1);
-                warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds);
-                warp_commit_preds(S, W);
-                if (lane == 0) {
-                    W.pb[W.npred] = N;   /* the ghost entry itself */
-                    log_event(S, sh.sc.log_count, sh.sc.coll, sh.sc.t, tf, i, -1, DMD_EV_GHOST, 0);
-                    if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
-                    sh.sc.tfalse = tf;
-                    sh.sc.old_tfalse = tf;
-                    sh.sc.done += 1;
-                }
-                __syncwarp();
-                warp_l1_refresh(S, W.pb, W.npred + 1);
-            }
-        } else if (e == N + 1) {
-            ph_kind = 7;
-            /* ---- interval: all CTAs ---- */
-            double t_before = sh.tnow, tf = sh.tf_iv;
-            bool rb = cluster_interval(S, sh, L, rank, C, ScratchRef{(char *)&warea[0].fs, sizeof(WarpArea)}, hbonds);
-            if (leader && threadIdx.x == 0) {
-                sh.sc.n_interval += 1;
-                log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
-                if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
-                sh.sc.old_tfalse = sh.sc.tfalse;
-                if (!phys) sh.sc.done += 1;
-            }
-        } else {
-            ph_kind = 8;
-            /* ---- output: the leader CTA ---- */
-            if (leader) {
-                cta_diag(S, sh, cs, cl, outputs ? outputs + r : nullptr);
-                if (threadIdx.x == 0) {
-                    sh.sc.n_output += 1;
-                    double tn = 3.3 / (sqrt(S.tab->setemp)) + 5 + sh.sc.tfalse;
-                    set_pred(S, N + 2, tn, -2, -2, tn < sh.sc.interval_max);
-                    log_event(S, sh.sc.log_count, sh.sc.coll, sh.sc.t, sh.sc.tfalse, N + 2, -1, DMD_EV_OUTPUT, 0);
-                    if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
-                    sh.sc.old_tfalse = sh.sc.tfalse;
-                    if (!phys) sh.sc.done += 1;
-                    if (stop_out) sh.sc.stop = 1;
-                    sh.touched[0] = N + 2;
-                }
-                __syncthreads();
-                if (warp == 0) warp_l1_refresh(S, sh.touched, 1);
-            }
-        }
-        csync(C);
-        DMD_PHASE(ph_kind);
-    }
-    if (leader) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            sh.sc.run_cycles = clock64() - t_start;
-            *S.sc = sh.sc;
-        }
-    }
-    if (C > 1) cg::this_cluster().sync();   /* no CTA leaves while others may read its shared memory */
+/* k_run and its per-event functions, compiled in two variants that differ
+ * only in the size of the per-warp event areas in shared memory.  The full
+ * variant takes any list (down lists up to the capacity of 128); the
+ * compact one takes systems whose down lists hold at most 32 beads, and
+ * its smaller shared-memory footprint leaves about 150 KB of the SM's
+ * 256 KB to the L1 cache, which then holds a small system's bead state.
+ * A compact launch hands a system whose lists outgrow it back to the host
+ * (need_full) at the end of the rebuild that made them, and the host runs
+ * the rest of that system's events on the full variant. */
+#define DMD_RUN_OPS 264          /* 2 * list capacity (128) + 6 extras + slack */
+#define DMD_RUN_RSET 384
+#define DMD_RUN_QSET 160
+#define DMD_RUN_DN_LIMIT INT_MAX
+namespace run_full {
+#include "engine_run.cuh"
 }
+#undef DMD_RUN_OPS
+#undef DMD_RUN_RSET
+#undef DMD_RUN_QSET
+#undef DMD_RUN_DN_LIMIT
+#define DMD_RUN_OPS 72           /* 2 * 32 + 6 extras + slack */
+#define DMD_RUN_RSET 192
+#define DMD_RUN_QSET 96
+#define DMD_RUN_DN_LIMIT DMD_COMPACT_DN
+namespace run_compact {
+#include "engine_run.cuh"
+}
+#undef DMD_RUN_OPS
+#undef DMD_RUN_RSET
+#undef DMD_RUN_QSET
+#undef DMD_RUN_DN_LIMIT
 
 __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, const int *chain_start, const int *chain_len,
                                                    const int *chain_off, dmd_diag *out) {
@@ -2315,12 +986,19 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, cons
 /* ------------------------------------------------------------------ */
 /* launch wrappers                                                     */
 /* ------------------------------------------------------------------ */
-static_assert(sizeof(WarpArea) * NWARPS + sizeof(TaskPool) + OWN_SMEM_MAX * 3 * sizeof(unsigned) + sizeof(SharedState) +
-                  sizeof(DSys) <= 227 * 1024,
-              "k_run shared memory above the 227 KB a block may use");
-static size_t run_smem(int own_cap) {
-    return sizeof(WarpArea) * NWARPS + sizeof(TaskPool) + (size_t)own_cap * 3 * sizeof(unsigned);
+/* dynamic shared memory of k_run: the per-warp event areas, the task pool
+ * and, for systems of at most own_cap beads, the claim tables */
+template <typename WA> constexpr size_t run_smem_of(int own_cap) {
+    return sizeof(WA) * NWARPS + sizeof(TaskPool) + (size_t)own_cap * 3 * sizeof(unsigned);
 }
+static_assert(run_smem_of<run_full::WarpArea>(OWN_SMEM_FULL) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
+              "k_run shared memory above the 227 KB a block may use");
+static_assert(run_smem_of<run_compact::WarpArea>(OWN_SMEM_COMPACT) + sizeof(SharedState) + sizeof(DSys) <= 100 * 1024,
+              "compact k_run must leave the SM's 256 KB at least 156 KB of L1");
+static size_t run_smem(int compact, int own_cap) {
+    return compact ? run_smem_of<run_compact::WarpArea>(own_cap) : run_smem_of<run_full::WarpArea>(own_cap);
+}
+static int own_smem_max(int compact) { return compact ? OWN_SMEM_COMPACT : OWN_SMEM_FULL; }
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st) {
     k_init<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
@@ -2334,7 +1012,19 @@ static cudaError_t k_run_attributes() {
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(mu);
     if (dev >= 0 && dev < 256 && !done[dev]) {
-        e = cudaFuncSetAttribute(k_run, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)run_smem(OWN_SMEM_MAX));
+        /* the shared-memory carve-out is the smallest that holds a launch's
+         * blocks; the rest of the SM's 256 KB is L1 cache */
+        e = cudaFuncSetAttribute(run_full::k_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)run_smem(0, OWN_SMEM_FULL));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(run_compact::k_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)run_smem(1, OWN_SMEM_COMPACT));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(run_full::k_run, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxL1);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(run_compact::k_run, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxL1);
         if (e != cudaSuccess) return e;
         done[dev] = true;
     }
@@ -2357,18 +1047,22 @@ static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, i
 }
 
 /* k_run with one cluster of C CTAs per system (C = 1, 2, 4 or 8) */
-cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, const long long *targets,
-                           int hbonds, const int *chain_start, const int *chain_len, const int *chain_off,
-                           dmd_diag *outputs, cudaStream_t st) {
+cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int compact, long long target,
+                           const long long *targets, int hbonds, const int *chain_start, const int *chain_len,
+                           const int *chain_off, dmd_diag *outputs, cudaStream_t st) {
     if (C != 1 && C != 2 && C != 4 && C != 8) return cudaErrorInvalidValue;
     cudaError_t e = k_run_attributes();
     if (e != cudaSuccess) return e;
-    int own_cap = (C == 1 && max_beads <= OWN_SMEM_MAX) ? max_beads : 0;
+    /* claim tables in shared memory for the systems up to own_cap beads */
+    int own_cap = C == 1 ? std::min(max_beads, own_smem_max(compact)) : 0;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    cluster_config(cfg, attr, nsys, C, run_smem(own_cap), st);
-    return cudaLaunchKernelEx(&cfg, k_run, d_systems, nsys, target, targets, hbonds, chain_start, chain_len, chain_off,
-                              outputs, own_cap, C);
+    cluster_config(cfg, attr, nsys, C, run_smem(compact, own_cap), st);
+    if (compact)
+        return cudaLaunchKernelEx(&cfg, run_compact::k_run, d_systems, nsys, target, targets, hbonds, chain_start,
+                                  chain_len, chain_off, outputs, own_cap, C, std::min(compact, (int)DMD_COMPACT_DN));
+    return cudaLaunchKernelEx(&cfg, run_full::k_run, d_systems, nsys, target, targets, hbonds, chain_start, chain_len,
+                              chain_off, outputs, own_cap, C, INT_MAX);
 }
 
 /* how many clusters of C CTAs of k_run can be resident at once */
@@ -2377,8 +1071,8 @@ cudaError_t dmd_max_active_clusters(int C, int *n) {
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    cluster_config(cfg, attr, 1, C, run_smem(C == 1 ? OWN_SMEM_MAX : 0), 0);
-    return cudaOccupancyMaxActiveClusters(n, k_run, &cfg);
+    cluster_config(cfg, attr, 1, C, run_smem(0, C == 1 ? OWN_SMEM_FULL : 0), 0);
+    return cudaOccupancyMaxActiveClusters(n, run_full::k_run, &cfg);
 }
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st) {

@@ -75,10 +75,13 @@ struct DScal {
     int err;              /* DMD_E_* of the first device error, 0 if none */
     int err_info;
     int stop;             /* 1: stopped at an output event */
-    int pad;
+    int max_dn;           /* the longest down list of the last rebuild */
     long long n_batches, n_rolled_back, n_candidates;   /* batch statistics */
     long long bseq;       /* footprint claims made so far (ticket base) */
     long long run_cycles; /* SM clock cycles of this system's last launch (scheduling hint) */
+    long long done_all;   /* events over all launches since the host last cleared it */
+    int need_full;        /* 1: a compact launch stopped here; lists need the full variant */
+    int pad;
 };
 
 /* device view of one system; all arrays in global memory */

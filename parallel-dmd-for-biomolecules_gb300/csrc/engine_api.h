@@ -9,10 +9,16 @@
 #include "engine.cuh"
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st);
+/* The compact variant of the event loop takes systems whose down lists
+ * hold at most DMD_COMPACT_DN beads (DScal::max_dn); a system whose lists
+ * outgrow it stops with DScal::need_full set and continues on the full
+ * variant, which takes any list.  compact: 0 = the full variant, k > 0 =
+ * the compact one with the down-list limit min(k, DMD_COMPACT_DN). */
+#define DMD_COMPACT_DN 32
 /* targets: per-system event counts (device array), or NULL for target */
-cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, long long target, const long long *targets,
-                           int hbonds, const int *chain_start, const int *chain_len, const int *chain_off,
-                           dmd_diag *outputs, cudaStream_t st);
+cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int compact, long long target,
+                           const long long *targets, int hbonds, const int *chain_start, const int *chain_len,
+                           const int *chain_off, dmd_diag *outputs, cudaStream_t st);
 cudaError_t dmd_max_active_clusters(int C, int *n);
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st);

@@ -77,7 +77,7 @@ class Diag(C.Structure):
     _fields_ = [
         ("e_total", C.c_double), ("temperature", C.c_double), ("rg", C.c_double), ("e2e", C.c_double),
         ("ehh_ii", C.c_double), ("ehh_ij", C.c_double), ("e_kin", C.c_double),
-        ("hb_alpha", C.c_int32), ("hb_ii", C.c_int32), ("hb_ij", C.c_int32), ("pad", C.c_int32),
+        ("hb_alpha", C.c_int32), ("hb_ii", C.c_int32), ("hb_ij", C.c_int32), ("max_down", C.c_int32),
         ("nevents", C.c_int64 * 32),
         ("coll", C.c_int64), ("n_pair", C.c_int64), ("n_ghost", C.c_int64), ("n_interval", C.c_int64),
         ("n_output", C.c_int64), ("n_updates", C.c_int64), ("n_forced_updates", C.c_int64),
@@ -86,7 +86,7 @@ class Diag(C.Structure):
     ]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("nevents", "pad")}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("nevents",)}
         d["nevents"] = list(self.nevents)
         return d
 
@@ -103,6 +103,7 @@ ENGINE_SYMBOLS = [
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
     "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster", "dmd_batch_set_cell_div",
+    "dmd_batch_set_compact_limit", "dmd_set_compact_limit",
     "dmd_batch_run_graph", "dmd_batch_autotune", "dmd_batch_device_bytes", "dmd_state_bytes", "dmd_save_state", "dmd_load_state",
     "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
     "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
@@ -169,6 +170,9 @@ def _declare(lib) -> None:
     lib.dmd_batch_cluster.restype = C.c_int32
     lib.dmd_batch_set_cell_div.argtypes = [C.c_void_p, C.c_int32]
     lib.dmd_batch_set_cell_div.restype = C.c_int
+    for fn in ("dmd_batch_set_compact_limit", "dmd_set_compact_limit"):
+        getattr(lib, fn).argtypes = [C.c_void_p, C.c_int32]
+        getattr(lib, fn).restype = C.c_int
     lib.dmd_batch_device_bytes.argtypes = [C.c_void_p]
     lib.dmd_batch_device_bytes.restype = C.c_int64
     lib.dmd_batch_run_graph.argtypes = [C.c_void_p, C.c_int64, C.c_int32]

@@ -77,6 +77,11 @@ class Engine:
         _check(rc, self.lib, self.h)
         return None
 
+    def set_compact_limit(self, max_down: int):
+        """Longest down list (0..32) for which the compact event-loop variant
+        runs (0: always the full one); results do not depend on it."""
+        _check(self.lib.dmd_set_compact_limit(self.h, int(max_down)), self.lib, self.h)
+
     def save_state(self) -> bytes:
         """The whole engine state (resumes bit-identically with load_state)."""
         n = int(self.lib.dmd_state_bytes(self.h))
@@ -160,6 +165,11 @@ class Batch:
     def set_cell_div(self, div: int):
         """Coarser rebuild grid (finest cells per side / div); results do not depend on it."""
         _check(self.lib.dmd_batch_set_cell_div(self.h, int(div)), self.lib, self.h, "dmd_batch_last_error")
+
+    def set_compact_limit(self, max_down: int):
+        """Longest down list (0..32) for which the compact event-loop variant
+        runs (0: always the full one); results do not depend on it."""
+        _check(self.lib.dmd_batch_set_compact_limit(self.h, int(max_down)), self.lib, self.h, "dmd_batch_last_error")
 
     def run_graph(self, n_events: int, n_launches: int):
         """n_launches launches of n_events each, replayed from a captured CUDA graph."""

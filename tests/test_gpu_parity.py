@@ -191,3 +191,77 @@ def test_autotune_keeps_state(built):
         olog = Oracle(s).run(10000, log_capacity=10064)
         assert first_mismatch(logs[r], olog) < 0, r
     b.close()
+
+
+def test_capacity_error_is_reported(built):
+    """Neighbour lists larger than their capacity end in DMD_E_CAPACITY with
+    a message (at creation or at the first rebuild), no fault, and the
+    library stays usable."""
+    from dmdgb.engine import DMDError
+    spec = dense_system(seed=6)
+    with pytest.raises(DMDError) as ei:
+        with Engine(spec, list_cap=2) as eng:
+            eng.run(2000)
+    assert ei.value.rc == -7, str(ei.value)
+    with Engine(spec) as eng:          # a normal engine afterwards, still exact
+        glog = eng.run(2000, log_capacity=2064)
+    olog = Oracle(spec).run(2000, log_capacity=2064)
+    assert first_mismatch(glog, olog) < 0
+
+
+def test_compact_variant_hands_over(built):
+    """The compact event loop (down lists of at most max_down beads) stops a
+    system at the rebuild whose lists outgrow it and the full loop finishes
+    the run: the events are still the oracle's, and the switch happened."""
+    spec = dense_system(seed=8)
+    n, chunk = 60000, 6000
+    with Engine(spec) as eng:
+        limit = eng.diagnostics()["max_down"]
+        assert 0 < limit <= 32
+        eng.set_compact_limit(limit)
+        logs, crossed = [], False
+        for _ in range(n // chunk):
+            before = eng.diagnostics()["max_down"]
+            logs.append(eng.run(chunk, log_capacity=chunk + 64))
+            after = eng.diagnostics()["max_down"]
+            crossed |= before <= limit < after
+        gst = eng.state()
+    assert crossed, "the lists never outgrew the compact limit"
+    ora = Oracle(spec)
+    olog = ora.run(n, log_capacity=n + 64)
+    glog = np.concatenate(logs)
+    k = first_mismatch(glog, olog)
+    assert k < 0, f"event logs diverge at {k}:\n{describe(glog, olog, k)}"
+    ost = ora.state()
+    for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr"):
+        assert np.array_equal(gst[key], ost[key]), key
+
+
+def test_compact_variant_batch_and_graph(built):
+    """Replicas that cross the compact limit at different times, in a batch
+    run and in graph replay: the follow-up full launches give every replica
+    the events of one plain run."""
+    specs = systems.config_c3(32, seed=5)[:4]
+    for s in specs:
+        systems.generate(s)
+    ref = Batch(specs)
+    ref.set_compact_limit(0)          # the full variant throughout
+    ref.run(16000)
+    want = [ref.state(r) for r in range(4)]
+    ref.close()
+    b0 = Batch(specs)
+    limit = min(32, max(b0.diagnostics(r)["max_down"] for r in range(4)))
+    b0.close()
+    for graph in (False, True):
+        b = Batch(specs)
+        b.set_compact_limit(limit)
+        if graph:
+            b.run_graph(4000, 4)
+        else:
+            b.run(16000)
+        for r in range(4):
+            st = b.state(r)
+            for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity"):
+                assert np.array_equal(st[key], want[r][key]), (graph, r, key)
+            assert st["coll"] == want[r]["coll"], (graph, r)
+        b.close()
