@@ -73,17 +73,29 @@ __device__ long long g_phase_cycles[DMD_PHASE_CTAS][DMD_PHASE_SLOTS];
             ph_t_ = now_;                                                                  \
         }                                                                                  \
     } while (0)
-/* sub-phases of one event's processing, on warp 0 of the first CTA only
+/* sub-phases of one event's processing, on warp 0 of CTA g_sub_cta only
  * (row DMD_PHASE_CTAS - 1) */
 __device__ long long g_sub_last;
+__device__ int g_sub_cta;
 #define DMD_SUB(k)                                                                         \
     do {                                                                                   \
-        if (blockIdx.x == 0 && threadIdx.x == 0) {                                         \
+        if (blockIdx.x == g_sub_cta && threadIdx.x == 0) {                                 \
             long long now_ = clock64();                                                    \
             if ((k) >= 0) g_phase_cycles[DMD_PHASE_CTAS - 1][(k)] += now_ - g_sub_last;    \
             g_sub_last = now_;                                                             \
         }                                                                                  \
     } while (0)
+/* sub-phases of the interval event on CTA g_sub_cta (row DMD_PHASE_CTAS - 3) */
+__device__ long long g_isub_last;
+#define DMD_ISUB(k)                                                                        \
+    do {                                                                                   \
+        if (blockIdx.x == g_sub_cta && threadIdx.x == 0) {                                 \
+            long long now_ = clock64();                                                    \
+            if ((k) >= 0) g_phase_cycles[DMD_PHASE_CTAS - 3][(k)] += now_ - g_isub_last;   \
+            g_isub_last = now_;                                                            \
+        }                                                                                  \
+    } while (0)
+extern "C" int dmd_debug_set_sub_cta(int cta) { return (int)cudaMemcpyToSymbol(g_sub_cta, &cta, sizeof cta); }
 extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
     if (nctas > DMD_PHASE_CTAS) nctas = DMD_PHASE_CTAS;
     return (int)cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(long long) * DMD_PHASE_SLOTS * nctas);
@@ -92,6 +104,7 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
 #define DMD_PHASE_START(row) do { (void)(row); } while (0)
 #define DMD_PHASE(k) do { (void)(k); } while (0)
 #define DMD_SUB(k) do { } while (0)
+#define DMD_ISUB(k) do { } while (0)
 #endif
 
 /* per-warp scratch of the full re-predictions of up to TG_MAX beads: bead,
@@ -111,11 +124,12 @@ struct FullScratch {
  * down-operation bit | owner warp << 1; result: time, type, valid). */
 #define PTASK_MAX 512
 struct TaskPool {
-    int n;
+    int n, nlive;
     int a[PTASK_MAX], b[PTASK_MAX];
     int8_t st[PTASK_MAX], flag[PTASK_MAX];
     double t[PTASK_MAX];
     int8_t ty[PTASK_MAX], ok[PTASK_MAX];
+    int16_t live[PTASK_MAX];      /* the tasks left for double precision */
 };
 
 struct SharedState {
@@ -371,6 +385,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             atomicAdd(&S.cell_count[(cz * nc + cy) * nc + cx], 1);
         }
         __syncthreads();
+        DMD_ISUB(11);
         {
             int per = (ncell3 + blockDim.x - 1) / blockDim.x;
             int lo = threadIdx.x * per, hi = min(lo + per, ncell3);
@@ -391,6 +406,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             if (threadIdx.x == 0) S.cell_start[ncell3] = N;
             __syncthreads();
         }
+        DMD_ISUB(12);
         for (int b = threadIdx.x; b < N; b += blockDim.x) {
             int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc);
             int c = (cz * nc + cy) * nc + cx;
@@ -398,6 +414,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             S.cell_beads[S.cell_start[c] + slot] = b;
         }
         __syncthreads();
+        DMD_ISUB(13);
     }
     int mdn = 0;
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
@@ -470,6 +487,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
     /* the longest down list, which selects the k_run variant */
     mdn = __reduce_max_sync(FULL, mdn);
     __syncthreads();
+    DMD_ISUB(14);
     if ((threadIdx.x & 31) == 0) sh.red_i[threadIdx.x >> 5] = mdn;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -608,9 +626,13 @@ __device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int h
         S.xf[b] = (float)px; S.yf[b] = (float)py; S.zf[b] = (float)pz;
     }
     __syncthreads();
+    DMD_ISUB(7);
     cta_build_lists(S, sh, hbonds);
+    DMD_ISUB(8);
     cta_predict_all(S, sh, fr, sh.sc.interval_max, hbonds);
+    DMD_ISUB(9);
     cta_tree_rebuild(S);
+    DMD_ISUB(10);
 }
 
 /* interval event N+2 (code/main.F90:1126-1187, code/displ.f), spread over the
@@ -625,6 +647,7 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     const DTab &T = *S.tab;
     const int stride = C * blockDim.x, t0 = rank * blockDim.x + threadIdx.x;
     DMD_SUB(-1);
+    DMD_ISUB(-1);
     for (int k0 = t0; k0 < N + 3; k0 += 4 * stride) {   /* four entries in flight per thread */
         double tv[4];
         uint8_t qv[4];
@@ -673,7 +696,9 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
         }
     }
     for (int o = 16; o > 0; o >>= 1) { long long v = __shfl_xor_sync(FULL, dmax_bits, o); if (v > dmax_bits) dmax_bits = v; }
+    DMD_ISUB(0);
     __syncthreads();
+    DMD_ISUB(1);
     if ((threadIdx.x & 31) == 0) sh.red_d[threadIdx.x >> 5] = __longlong_as_double(dmax_bits);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -710,10 +735,12 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     }
     if (rank == 0) {
         __syncthreads();
+        DMD_ISUB(2);
         if (sh.rebuild) {
             for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
             __syncthreads();
             cta_rebuild(S, sh, fr, hbonds);
+            DMD_ISUB(3);
         }
         if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
     }
@@ -723,7 +750,9 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     bool rb = sh.rebuild != 0;
     /* level 1 of the tournament, spread over the CTAs (level 2 follows at
      * the leader's next selection) */
+    DMD_ISUB(4);
     for (int g = t0; g < S.nl1; g += stride) l1_update(S, g, N + 3);
+    DMD_ISUB(5);
     return rb;
 }
 
@@ -993,8 +1022,10 @@ template <typename WA> constexpr size_t run_smem_of(int own_cap) {
 }
 static_assert(run_smem_of<run_full::WarpArea>(OWN_SMEM_FULL) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
               "k_run shared memory above the 227 KB a block may use");
-static_assert(run_smem_of<run_compact::WarpArea>(OWN_SMEM_COMPACT) + sizeof(SharedState) + sizeof(DSys) <= 100 * 1024,
-              "compact k_run must leave the SM's 256 KB at least 156 KB of L1");
+static_assert(run_smem_of<run_compact::WarpArea>(OWN_SMEM_COMPACT) + sizeof(SharedState) + sizeof(DSys) + 1024 <=
+                  100 * 1024,
+              "compact k_run (with the 1 KB the system reserves per block) must fit the 100 KB carve-out, "
+              "leaving 156 KB of the SM's 256 KB to L1");
 static size_t run_smem(int compact, int own_cap) {
     return compact ? run_smem_of<run_compact::WarpArea>(own_cap) : run_smem_of<run_full::WarpArea>(own_cap);
 }

@@ -286,6 +286,96 @@ __device__ __forceinline__ Rel d_rel_c(const DSys &S, int i, int j, double tfals
     return r;
 }
 
+/* ------------------------------------------------------------------ */
+/* single-precision screen for "no event"                              */
+/* ------------------------------------------------------------------ */
+/* A double read as a float from its high word: the exponent rebiased and
+ * the mantissa truncated to 20 bits (relative error below 2^-20), in three
+ * integer operations.  Exact only for exponents that fit a normal float
+ * (2^-126 <= |x| < 2^128); `bad` collects the others (zeros among them). */
+__device__ __forceinline__ float f32_hi(unsigned hi, unsigned &bad) {
+    bad |= ((hi & 0x7ff00000u) - 0x38100000u) > (0x47e00000u - 0x38100000u);
+    return __uint_as_float(((hi - 0x38000000u) << 3) | (hi & 0x80000000u));
+}
+__device__ __forceinline__ unsigned d_hi(const double *p) { return reinterpret_cast<const unsigned *>(p)[1]; }
+
+/* True only when d_predict_c(S, i, j, evcode, tfalse) gives no event
+ * (k = PK_NONE, tij = DMD_BIG, type 0): the pair separates (bij > 0), or
+ * the discriminant of the shell it would meet is negative, and for the
+ * two-stage wells it is outside the well.  bij, rijsq, vijsq and the
+ * discriminant are evaluated in single precision from the doubles' high
+ * words, each with a bound on every error - the truncation of the inputs,
+ * the single-precision arithmetic and the double-precision arithmetic of
+ * d_rel_c - and a test is taken only when it holds beyond its bound; the
+ * minimum image is taken only away from half a box, and inputs outside the
+ * normal float range (zeros) decide nothing.  Bond pairs (always an
+ * event), bonded H-bond pairs and invalid codes are not screened.  tf_hi
+ * is the high word of tfalse. */
+__device__ __forceinline__ bool f32_no_event(const DSys &S, int i, int j, int evcode, unsigned tf_hi) {
+    /* every load first: positions and velocities, identities, H-bond partner */
+    unsigned h[12];
+    const double *P[6] = {S.x, S.y, S.z, S.vx, S.vy, S.vz};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { h[2 * k] = d_hi(P[k] + i); h[2 * k + 1] = d_hi(P[k] + j); }
+    const int a = S.ident[i], b = S.ident[j];
+    const bool core = evcode <= 3 || (evcode >= 17 && evcode <= 26);
+    const bool well = evcode == 15 || evcode == 16 || evcode >= 40;
+    if (!core && !well) return false;
+    if (evcode == 15 && a + b != 5 && S.bptnr[i] == j) return false;
+    const DTab &T = *S.tab;
+    const double *Rp = core ? &T.core_sq[core_slot(evcode)][a][b]
+                            : evcode >= 40 ? &T.shlddia_sq[a][b] : &T.welldia_sq[a][b];
+    const bool need_out = well && (evcode != 15 || a + b == 5);
+    const unsigned Rh = d_hi(Rp);
+    const float C1 = 3.814697265625e-06f;   /* 2^-18 */
+    const float C2 = 1.9073486328125e-06f;  /* 2^-19 */
+    const float C3 = 4.76837158203125e-07f; /* 2^-21 */
+    const float TINY = 1e-30f;
+    unsigned bad = 0;
+    const float tf = tf_hi == 0u ? 0.0f : f32_hi(tf_hi, bad);   /* tfalse is often exactly 0 */
+    const float atf = fabsf(tf);
+    float r[3], dv[3], Er[3], Edv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float xi = f32_hi(h[2 * k], bad), xj = f32_hi(h[2 * k + 1], bad);
+        const float vi = f32_hi(h[6 + 2 * k], bad), vj = f32_hi(h[6 + 2 * k + 1], bad);
+        const float d = vi - vj;
+        const float av = fabsf(vi) + fabsf(vj);
+        const float x = (xi - xj) + d * tf;
+        const float xr = x - rintf(x);
+        r[k] = xr;
+        dv[k] = d;
+        Er[k] = C1 * (fabsf(xi) + fabsf(xj) + av * atf + fabsf(x));
+        Edv[k] = C2 * av;
+        bad |= !(fabsf(xr) <= 0.45f);   /* near half a box, or NaN */
+    }
+    const float Rf = f32_hi(Rh, bad), ER = C2 * Rf;
+    if (bad) return false;
+    float bf = 0.f, r2 = 0.f, v2 = 0.f, Eb = TINY, Er2 = TINY, Ev2 = TINY, sb = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float ar = fabsf(r[k]), ad = fabsf(dv[k]);
+        bf = bf + r[k] * dv[k];
+        r2 = r2 + r[k] * r[k];
+        v2 = v2 + dv[k] * dv[k];
+        sb = sb + ar * ad;
+        Eb = Eb + Er[k] * (ad + Edv[k]) + (ar + Er[k]) * Edv[k];
+        Er2 = Er2 + (2.f * ar + Er[k]) * Er[k];
+        Ev2 = Ev2 + (2.f * ad + Edv[k]) * Edv[k];
+    }
+    Eb = Eb + C3 * sb;
+    Er2 = Er2 + C3 * r2;
+    Ev2 = Ev2 + C3 * v2;
+    if (need_out && !(r2 - Er2 > Rf + ER)) return false;
+    if (bf > Eb) return true;
+    const float c = r2 - Rf;
+    const float Ec = Er2 + ER + C3 * fabsf(c);
+    const float D = bf * bf - v2 * c;
+    const float ED = (2.f * fabsf(bf) + Eb) * Eb + Ev2 * fabsf(c) + (v2 + Ev2) * Ec +
+                     C3 * (bf * bf + fabsf(v2 * c)) + TINY;
+    return D + ED < 0.f;
+}
+
 #define PK_NONE 0
 #define PK_MINUS 1
 #define PK_PLUS 2

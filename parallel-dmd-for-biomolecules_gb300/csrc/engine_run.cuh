@@ -58,6 +58,7 @@ struct WarpArea {
     int err, err_info;
     long long coll;
     double tf;
+    double big_tf;                /* DMD_BIG + tf: a down operation's time when it has no event */
     long long tnew_key;
     int tnew_idx;
 };
@@ -686,22 +687,34 @@ __device__ __forceinline__ void rp_task(const DSys &S, const WarpArea &W, int q,
 /* one prediction task: ev_code(l, source) for a down operation, ev_code(m, b)
  * for a full one; the time is tij + tfalse for a down operation and tij for
  * a full one (tfalse is added after its minimum; x + (-0.0) == x) */
-__device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb, int st, bool is_op, double tf,
-                                           int hbonds, double &tt, int &ty) {
+__device__ __forceinline__ bool rp_predict_code(const DSys &S, Err E, int pa, int pbb, int code, bool is_op,
+                                                double tf, double &tt, int &ty) {
     double tij = 0.0;
     ty = 0;
-    bool ok = false;
-    if (pa >= 0) {
-        int a1 = is_op ? pa : pbb, a2 = is_op ? pbb : pa;
-        int code = st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
-        ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
-        if (!ok) set_err(E, DMD_E_INPUT, pa);
-        else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
+    bool ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
+#ifdef DMD_PHASE_TIMERS
+    {   /* double-precision predictions: all, no event while separating, no event while approaching */
+        unsigned long long *cnt = (unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 2][0];
+        atomicAdd(cnt, 1ull);
+        if (ok && ty == 0) atomicAdd(cnt + (d_lt0(d_rel_c(S, pa, pbb, tf).bij) ? 2 : 1), 1ull);
     }
+#endif
+    if (!ok) set_err(E, DMD_E_INPUT, pa);
+    else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
     tt = tij + (is_op ? tf : -0.0);
     return ok;
 }
-
+__device__ __forceinline__ int rp_code(const DSys &S, int pa, int pbb, int st, bool is_op, int hbonds) {
+    int a1 = is_op ? pa : pbb, a2 = is_op ? pbb : pa;
+    return st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
+}
+__device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb, int st, bool is_op, double tf,
+                                           int hbonds, double &tt, int &ty) {
+    if (pa >= 0) return rp_predict_code(S, E, pa, pbb, rp_code(S, pa, pbb, st, is_op, hbonds), is_op, tf, tt, ty);
+    ty = 0;
+    tt = 0.0 + (is_op ? tf : -0.0);
+    return false;
+}
 /* 1-4 into the CTA's task pool for the event of warp `owner` (its tasks
  * must fit one round and the pool), else W.pooled = 0 and the owner warp
  * runs warp_repredict() after the pool */
@@ -725,7 +738,7 @@ __device__ void warp_rp_prepare(const DSys &S, WarpArea &W, TaskPool &TP, int ow
             TP.flag[base + q] = (int8_t)((q < nop ? 1 : 0) | (owner << 1));
         }
     }
-    if (lane == 0) { W.pooled = pooled; W.pool_base = base; }
+    if (lane == 0) { W.pooled = pooled; W.pool_base = base; W.big_tf = DMD_BIG + tf; }
     __syncwarp();
 }
 
@@ -901,72 +914,72 @@ __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
  * the tables need no reset.  The beads are listed in W.rset/wset/qset for
  * warp_footprint_test(). */
 __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
-    int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
     const int N = S.N;
     unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
-    if (lane == 0) { W.nrset = 0; W.nwset = 0; W.nqset = 0; W.casc_over = 0; }
-    __syncwarp();
-    auto visit_r = [&](int b) {
-        if (b < 0) return;
-        atomicMax(&own_r[b], ticket);
-        int pos = atomicAdd(&W.nrset, 1);
-        if (pos < RSET_MAX) W.rset[pos] = b;
+    DMD_SUB(-1);
+    /* the sets are appended warp-wide: a ballot per chunk of 32 places each
+     * lane's bead; the counters stay in registers (warp-uniform) */
+    int nr = 0, nw = 0, nq = 0;
+    auto put = [&](int *arr, int cap, int &n, bool pred, int b) {
+        unsigned m = __ballot_sync(FULL, pred);
+        int pos = n + __popc(m & lt);
+        if (pred && pos < cap) arr[pos] = b;
+        n += __popc(m);
     };
-    auto visit_w = [&](int b) {
-        if (b < 0) return;
-        atomicMax(&own_w[b], ticket);
-        int pos = atomicAdd(&W.nwset, 1);
-        if (pos < WSET_MAX) W.wset[pos] = b;
-        visit_r(b);
-    };
-    auto visit_q = [&](int b) {
-        if (b < 0) return;
-        atomicMax(&own_q[b], ticket);
-        int pos = atomicAdd(&W.nqset, 1);
-        if (pos < QSET_MAX) W.qset[pos] = b;
-        visit_r(b);
-    };
-    /* fixed part on lanes 0..17 */
-    if (lane < 18) {
+    /* fixed part on lanes 0..17: i, j, their extras (2..9), the own helpers
+     * of i, j (10..13) and of their fourth extras (14..17, read only) */
+    {
         int b = -1;
         if (lane == 0) b = i;
         else if (lane == 1) b = j;
         else if (lane < 6) b = S.er[4 * i + lane - 2];
         else if (lane < 10) b = S.er[4 * j + lane - 6];
-        else {
+        else if (lane < 18) {
             int which = (lane - 10) >> 1;
             int x = which == 0 ? i : which == 1 ? j : which == 2 ? S.er[4 * i + 3] : S.er[4 * j + 3];
             int h1, h2;
             own_helpers(S, x, h1, h2);
             b = (lane & 1) ? h2 : h1;
         }
-        if (lane < 14) visit_w(b);   /* i, j, extras, own helpers */
-        else visit_r(b);             /* the partners' helpers: read only */
+        const bool v = b >= 0;
+        const bool w = v && lane < 14;
         /* queue entries: i, j, the lower extras (0..2) and the helpers */
-        bool q = lane < 2 || (lane >= 2 && lane < 5) || (lane >= 6 && lane < 9) || (lane >= 10 && lane < 14);
-        if (q) visit_q(b);
+        const bool q = v && (lane < 5 || (lane >= 6 && lane < 9) || (lane >= 10 && lane < 14));
+        if (v) atomicMax(&own_r[b], ticket);
+        if (w) atomicMax(&own_w[b], ticket);
+        if (q) atomicMax(&own_q[b], ticket);
+        put(W.rset, RSET_MAX, nr, v, b);
+        put(W.wset, WSET_MAX, nw, w, b);
+        put(W.qset, QSET_MAX, nq, q, b);
     }
-    /* neighbour lists of i and j */
-    int ui = S.upn[i], di = S.dnn[i], uj = S.upn[j], dj = S.dnn[j];
+    /* the neighbour lists of i and j as one range [up i | down i | up j |
+     * down j]: all read, the down lists also queue entries; a down-list
+     * bead whose partner is the list's owner may be fully re-predicted
+     * (cascade) */
+    const int ui = S.upn[i], di = S.dnn[i], uj = S.upn[j], dj = S.dnn[j];
     const int *UI = S.up + (size_t)i * S.cap, *DI = S.dn + (size_t)i * S.cap;
     const int *UJ = S.up + (size_t)j * S.cap, *DJ = S.dn + (size_t)j * S.cap;
-    for (int q = lane; q < ui; q += 32) visit_r(UI[q]);
-    for (int q = lane; q < di; q += 32) visit_q(DI[q]);
-    for (int q = lane; q < uj; q += 32) visit_r(UJ[q]);
-    for (int q = lane; q < dj; q += 32) visit_q(DJ[q]);
-    /* beads that may be fully re-predicted */
+    const int e1 = ui, e2 = ui + di, e3 = ui + di + uj, tot = ui + di + uj + dj;
     int nc = 0;
-    for (int base = 0; base < di + dj; base += 32) {
-        int q = base + lane;
-        int l = -1;
-        if (q < di) { l = DI[q]; if (S.nptnr[l] != i) l = -1; }
-        else if (q < di + dj) { l = DJ[q - di]; if (S.nptnr[l] != j) l = -1; }
-        unsigned m = __ballot_sync(FULL, l >= 0);
-        int pos = nc + __popc(m & ((1u << lane) - 1));
-        if (l >= 0 && pos < CASC_MAX - 10) W.casc[pos] = l;
-        nc += __popc(m);
+    for (int base = 0; base < tot; base += 32) {
+        const int q = base + lane;
+        int l = -1, src = -1;
+        if (q < e1) l = UI[q];
+        else if (q < e2) { l = DI[q - e1]; src = i; }
+        else if (q < e3) l = UJ[q - e2];
+        else if (q < tot) { l = DJ[q - e3]; src = j; }
+        const bool v = l >= 0, down = src >= 0;
+        if (v) atomicMax(&own_r[l], ticket);
+        if (down) atomicMax(&own_q[l], ticket);
+        const bool cas = down && S.nptnr[l] == src;
+        put(W.rset, RSET_MAX, nr, v, l);
+        put(W.qset, QSET_MAX, nq, down, l);
+        put(W.casc, CASC_MAX - 10, nc, cas, l);
     }
-    bool over = nc > CASC_MAX - 10;
+    DMD_SUB(9);
+    const bool over = nc > CASC_MAX - 10;
     nc = min(nc, CASC_MAX - 10);
     if (lane < 10) {
         int b;
@@ -995,21 +1008,31 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
     }
     if (lane == 0) W.cbase[nc] = run;
     __syncwarp();
-    for (int q = lane; q < run; q += 32) {
-        int lo = 0, hi = nc - 1;          /* last cascade bead with cbase <= q */
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (W.cbase[mid] <= q) lo = mid; else hi = mid - 1;
+    DMD_SUB(10);
+    for (int base = 0; base < run; base += 32) {
+        const int q = base + lane;
+        int b = -1;
+        if (q < run) {
+            int lo = 0, hi = nc - 1;          /* last cascade bead with cbase <= q */
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (W.cbase[mid] <= q) lo = mid; else hi = mid - 1;
+            }
+            int l = W.casc[lo];
+            int k = q - W.cbase[lo];
+            int ul = W.cbase[lo + 1] - W.cbase[lo] - 3;
+            b = k < ul ? S.up[(size_t)l * S.cap + k] : S.er[4 * l + (k - ul)];
         }
-        int l = W.casc[lo];
-        int k = q - W.cbase[lo];
-        int ul = W.cbase[lo + 1] - W.cbase[lo] - 3;
-        visit_r(k < ul ? S.up[(size_t)l * S.cap + k] : S.er[4 * l + (k - ul)]);
+        if (b >= 0) atomicMax(&own_r[b], ticket);
+        put(W.rset, RSET_MAX, nr, b >= 0, b);
+    }
+    /* an incomplete list (cascade or set overflow) ends the batch here */
+    if (lane == 0) {
+        W.nrset = nr; W.nwset = nw; W.nqset = nq;
+        W.casc_over = over || nr > RSET_MAX || nw > WSET_MAX || nq > QSET_MAX;
     }
     __syncwarp();
-    /* an incomplete list (cascade or set overflow) ends the batch here */
-    if (lane == 0) W.casc_over = over || W.nrset > RSET_MAX || W.nwset > WSET_MAX || W.nqset > QSET_MAX;
-    __syncwarp();
+    DMD_SUB(11);
 }
 __device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, int N, unsigned ticket) {
     int lane = threadIdx.x & 31;
@@ -1232,22 +1255,64 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
             }
             __syncthreads();
-            /* every pooled prediction task of this CTA's events, all warps */
+            /* every pooled prediction task of this CTA's events, all warps:
+             * first the pair codes, settling in single precision the tasks
+             * that certainly have no event; then the double-precision
+             * predictions of the rest, packed so that their warp
+             * instructions (64 cycles each on the FP64 unit whatever the
+             * active lanes) have all lanes busy */
             {
                 const int ntot = min(TP.n, PTASK_MAX);
-                for (int q = threadIdx.x; q < ntot; q += blockDim.x) {
-                    int pa = TP.a[q];
-                    if (pa < 0) { TP.ok[q] = 0; continue; }
-                    int owner = TP.flag[q] >> 1;
+                if (threadIdx.x == 0) TP.nlive = 0;
+                __syncthreads();
+                DMD_PHASE(12);
+                for (int base = 0; base < ntot; base += NTHREADS) {
+                    const int q = base + threadIdx.x;
+                    bool live = false;
+                    if (q < ntot) {
+                        const int pa = TP.a[q];
+                        if (pa < 0) {
+                            TP.ok[q] = 0;
+                        } else {
+                            const int pbb = TP.b[q];
+                            const bool is_op = (TP.flag[q] & 1) != 0;
+                            const WarpArea &O = warea[TP.flag[q] >> 1];
+                            const int code = rp_code(S, pa, pbb, TP.st[q], is_op, hbonds);
+                            if (f32_no_event(S, pa, pbb, code, d_hi(&O.tf))) {
+                                TP.t[q] = is_op ? O.big_tf : DMD_BIG;
+                                TP.ty[q] = 0;
+                                TP.ok[q] = 1;
+#ifdef DMD_PHASE_TIMERS
+                                atomicAdd((unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 2][3], 1ull);
+#endif
+                            } else {
+                                TP.st[q] = (int8_t)code;
+                                live = true;
+                            }
+                        }
+                    }
+                    const unsigned lm = __ballot_sync(FULL, live);
+                    int pos = 0;
+                    if (lane == 0 && lm) pos = atomicAdd(&TP.nlive, __popc(lm));
+                    pos = __shfl_sync(FULL, pos, 0) + __popc(lm & ((1u << lane) - 1));
+                    if (live) TP.live[pos] = (int16_t)q;
+                }
+                __syncthreads();
+                DMD_PHASE(13);
+                const int nlive = TP.nlive;
+                for (int k = threadIdx.x; k < nlive; k += blockDim.x) {
+                    const int q = TP.live[k];
+                    const int owner = TP.flag[q] >> 1;
                     WarpArea &O = warea[owner];
                     Err EO{&O.err, &O.err_info};
                     double tt;
                     int ty;
-                    bool ok = rp_predict(S, EO, pa, TP.b[q], TP.st[q], (TP.flag[q] & 1) != 0, O.tf, hbonds, tt, ty);
+                    bool ok = rp_predict_code(S, EO, TP.a[q], TP.b[q], TP.st[q], (TP.flag[q] & 1) != 0, O.tf, tt, ty);
                     TP.t[q] = tt; TP.ty[q] = (int8_t)ty; TP.ok[q] = ok;
                 }
             }
             __syncthreads();
+            DMD_PHASE(14);
             if (gw < P) {
                 const int i = W.i, j = W.j;
                 const double tf = W.tf;
@@ -1265,6 +1330,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                         int bp = W.fs.tg_p[t];
                         double braw = W.fs.tg_raw[t];
                         int by = W.fs.tg_y[t];
+#pragma unroll 4
                         for (int x = base + nop + W.fs.tg_base[t]; x < base + nop + W.fs.tg_base[t + 1]; ++x) {
                             if (!TP.ok[x]) continue;
                             long long k = okey(TP.t[x]);
@@ -1278,6 +1344,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 } else {
                     warp_repredict(S, E, W, i, j, tf, imax, hbonds);
                 }
+#ifdef DMD_PHASE_TIMERS
+                if (lane == 0) atomicAdd((unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 2][W.pooled ? 5 : 4], 1ull);
+#endif
                 DMD_SUB(8);
                 if (lane == 0 && W.xpulse) {
                     if (S.ident[i] < S.ident[j]) repuls_del_b(S, i, j); else repuls_del_b(S, j, i);
