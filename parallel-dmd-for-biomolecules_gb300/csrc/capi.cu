@@ -203,7 +203,10 @@ void nbor_setup(HostSys &H, const dmd_tables *T, int hbonds) {
     for (int i = 1; i <= 50; ++i) {
         H.tab.rlsq[i] = 0.0;
         if (H.sig_max[i] != 0.0) { double r = (rl_const - 1) * H.sig_max_all + H.sig_max[i]; H.tab.rlsq[i] = r * r; }
+        H.tab.rlsq_f[i] = (float)H.tab.rlsq[i];
     }
+    H.tab.rlsq_max_f = 0.0f;
+    for (int i = 1; i <= 50; ++i) H.tab.rlsq_max_f = std::max(H.tab.rlsq_max_f, H.tab.rlsq_f[i]);
     double rl = rl_const * H.sig_max_all;
     double h = 0.4 * (rl - H.sig_max_all);
     H.tab.hdelr = h * h;

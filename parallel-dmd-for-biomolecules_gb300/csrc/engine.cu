@@ -373,16 +373,44 @@ __device__ __forceinline__ int cell_coord(double p, int nc) {
     return k < nc ? k : nc - 1;
 }
 
-__device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
+/* Working arrays of a rebuild: single-precision positions, each bead's
+ * cell, the cell-sorted beads and the cell counts and starts.  Staged in
+ * shared memory (scr) when they fit - data the rebuild writes and reads
+ * back at once - else the positions and the grid use the system's global
+ * arrays. */
+struct ListStage {
+    const float *xf, *yf, *zf;
+    int *cell_of, *cell_count, *cell_start, *cell_beads;
+};
+__device__ ListStage list_stage(const DSys &S, char *scr, int scr_bytes) {
+    const int N = S.N, nc = S.ncell;
+    const size_t nc3 = (size_t)nc * nc * nc;
+    ListStage L{S.xf, S.yf, S.zf, nullptr, S.cell_count, S.cell_start, S.cell_beads};
+    if (scr == nullptr || (size_t)20 * N > (size_t)scr_bytes) return L;
+    float *f = reinterpret_cast<float *>(scr);
+    L.xf = f; L.yf = f + N; L.zf = f + 2 * N;
+    L.cell_of = reinterpret_cast<int *>(f + 3 * N);
+    L.cell_beads = L.cell_of + N;
+    if ((size_t)20 * N + 4 * (2 * nc3 + 1) <= (size_t)scr_bytes) {
+        L.cell_count = L.cell_beads + N;
+        L.cell_start = L.cell_count + nc3;
+    }
+    return L;
+}
+
+__device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, const ListStage &L) {
     const int N = S.N, nc = S.ncell;
     const int ncell3 = nc * nc * nc;
     const DTab &T = *S.tab;
+    int *const cell_count = L.cell_count, *const cell_start = L.cell_start, *const cell_beads = L.cell_beads;
     if (nc >= 3) {
-        for (int c = threadIdx.x; c < ncell3; c += blockDim.x) S.cell_count[c] = 0;
+        for (int c = threadIdx.x; c < ncell3; c += blockDim.x) cell_count[c] = 0;
         __syncthreads();
         for (int b = threadIdx.x; b < N; b += blockDim.x) {
-            int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc);
-            atomicAdd(&S.cell_count[(cz * nc + cy) * nc + cx], 1);
+            int c;
+            if (L.cell_of) c = L.cell_of[b];
+            else { int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc); c = (cz * nc + cy) * nc + cx; }
+            atomicAdd(&cell_count[c], 1);
         }
         __syncthreads();
         DMD_ISUB(11);
@@ -390,7 +418,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             int per = (ncell3 + blockDim.x - 1) / blockDim.x;
             int lo = threadIdx.x * per, hi = min(lo + per, ncell3);
             int s = 0;
-            for (int c = lo; c < hi; ++c) s += S.cell_count[c];
+            for (int c = lo; c < hi; ++c) s += cell_count[c];
             int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
             int incl = s;
             for (int o = 1; o < 32; o <<= 1) { int v = __shfl_up_sync(FULL, incl, o); if (lane >= o) incl += v; }
@@ -400,51 +428,62 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             int woff = 0;
             for (int k = 0; k < w; ++k) woff += sh.red_i[k];
             int run = woff + incl - s;
-            for (int c = lo; c < hi; ++c) { int v = S.cell_count[c]; S.cell_start[c] = run; run += v; }
+            for (int c = lo; c < hi; ++c) { int v = cell_count[c]; cell_start[c] = run; run += v; }
             __syncthreads();
-            for (int c = lo; c < hi; ++c) S.cell_count[c] = 0;
-            if (threadIdx.x == 0) S.cell_start[ncell3] = N;
+            for (int c = lo; c < hi; ++c) cell_count[c] = 0;
+            if (threadIdx.x == 0) cell_start[ncell3] = N;
             __syncthreads();
         }
         DMD_ISUB(12);
         for (int b = threadIdx.x; b < N; b += blockDim.x) {
-            int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc);
-            int c = (cz * nc + cy) * nc + cx;
-            int slot = atomicAdd(&S.cell_count[c], 1);
-            S.cell_beads[S.cell_start[c] + slot] = b;
+            int c;
+            if (L.cell_of) c = L.cell_of[b];
+            else { int cx = cell_coord(S.x[b], nc), cy = cell_coord(S.y[b], nc), cz = cell_coord(S.z[b], nc); c = (cz * nc + cy) * nc + cx; }
+            int slot = atomicAdd(&cell_count[c], 1);
+            cell_beads[cell_start[c] + slot] = b;
         }
         __syncthreads();
         DMD_ISUB(13);
     }
     int mdn = 0;
+    const float far_f = T.rlsq_max_f + (4e-7f + 4e-7f * T.rlsq_max_f);   /* above every cut + margin */
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
         int nu = 0, nd = 0;
         int *up = S.up + (size_t)b * S.cap, *dn = S.dn + (size_t)b * S.cap;
         int8_t *upc = S.upc + (size_t)b * S.cap;
         const BeadInfo ib = S.info[b];
-        double xb = S.x[b], yb = S.y[b], zb = S.z[b];
-        const float xbf = S.xf[b], ybf = S.yf[b], zbf = S.zf[b];
+        const float xbf = L.xf[b], ybf = L.yf[b], zbf = L.zf[b];
         auto consider = [&](int c) {
             if (c == b) return;
-            int st = static_code(S.info[c], ib, hbonds);
+            /* Single-precision prefilter.  Positions lie in [-0.5, 0.5] at a
+             * rebuild, so each wrapped single-precision component is within
+             * 1e-7 of the double one and r2 within 4e-7 + 4e-7 * r2; only
+             * pairs that close to the cutoff are decided in double
+             * precision, as the reference does. */
+            float fx = xbf - L.xf[c], fy = ybf - L.yf[c], fz = zbf - L.zf[c];
+            fx = fx - rintf(fx); fy = fy - rintf(fy); fz = fz - rintf(fz);
+            const float r2f = fx * fx + fy * fy + fz * fz;
+            const BeadInfo ic = S.info[c];
+            /* Beyond every pair type's cutoff: listed only as a bond pair
+             * (same chain, residues at most 2 apart) or through an override */
+            if (r2f > far_f) {
+                const int dres = ic.res - ib.res;
+                if (ic.chain != ib.chain || dres < -2 || dres > 2) {
+                    const int *op = S.ovp + 4 * c;
+                    if (op[0] != b && op[1] != b && op[2] != b && op[3] != b) return;
+                }
+            }
+            int st = static_code(ic, ib, hbonds);
             int code = pair_code_st(S, c, b, st);
             bool take;
             if ((code >= 4 && code <= 12) || (code >= 17 && code < 27)) take = true;
             else {
-                /* Single-precision prefilter.  Positions lie in [-0.5, 0.5]
-                 * at a rebuild, so each wrapped single-precision component
-                 * is within 1e-7 of the double one and r2 within
-                 * 4e-7 + 4e-7 * r2; only pairs that close to the cutoff are
-                 * decided in double precision, as the reference does. */
-                float fx = xbf - S.xf[c], fy = ybf - S.yf[c], fz = zbf - S.zf[c];
-                fx = fx - rintf(fx); fy = fy - rintf(fy); fz = fz - rintf(fz);
-                float r2f = fx * fx + fy * fy + fz * fz;
-                float cut = (float)T.rlsq[code];
+                float cut = T.rlsq_f[code];
                 float margin = 4e-7f + 4e-7f * cut;
                 if (r2f > cut + margin) take = false;
                 else if (r2f < cut - margin) take = true;
                 else {
-                    double rx = xb - S.x[c], ry = yb - S.y[c], rz = zb - S.z[c];
+                    double rx = S.x[b] - S.x[c], ry = S.y[b] - S.y[c], rz = S.z[b] - S.z[c];
                     rx = rx - d_nint(rx); ry = ry - d_nint(ry); rz = rz - d_nint(rz);
                     double r2 = rx * rx + ry * ry + rz * rz;
                     take = r2 <= T.rlsq[code];
@@ -463,19 +502,40 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
             }
         };
         if (nc >= 3) {
-            int cx = cell_coord(xb, nc), cy = cell_coord(yb, nc), cz = cell_coord(zb, nc);
-            /* the 27 cell ranges are loaded before the first one is walked */
-            int lo[27], hi[27];
+            int cx, cy, cz;
+            if (L.cell_of) { const int cb = L.cell_of[b]; cx = cb % nc; cy = (cb / nc) % nc; cz = cb / (nc * nc); }
+            else { cx = cell_coord(S.x[b], nc); cy = cell_coord(S.y[b], nc); cz = cell_coord(S.z[b], nc); }
+            /* The 27 cells as bead ranges of the cell-sorted array: a row of
+             * three cells along x is one range, or two where it wraps around
+             * the box.  The ranges are loaded first; then the walk runs over
+             * all of them as one sequence, so that the lanes of a warp (one
+             * bead each) stay together for as many steps as their longest
+             * sequence instead of their longest cell of every one of 27. */
+            int rlo[18], rhi[18];
+            const int xl = cx == 0 ? nc - 1 : cx - 1, xh = cx == nc - 1 ? 0 : cx + 1;
+            const bool wrapx = xl > xh;
 #pragma unroll
-            for (int s27 = 0; s27 < 27; ++s27) {
-                int dx = s27 % 3 - 1, dy = (s27 / 3) % 3 - 1, dz = s27 / 9 - 1;
-                int gx = (cx + dx + nc) % nc, gy = (cy + dy + nc) % nc, gz = (cz + dz + nc) % nc;
-                int c0 = (gz * nc + gy) * nc + gx;
-                lo[s27] = S.cell_start[c0];
-                hi[s27] = S.cell_start[c0 + 1];
+            for (int row = 0; row < 9; ++row) {
+                int gy = cy + row % 3 - 1, gz = cz + row / 3 - 1;
+                gy = gy < 0 ? gy + nc : (gy >= nc ? gy - nc : gy);
+                gz = gz < 0 ? gz + nc : (gz >= nc ? gz - nc : gz);
+                const int base = (gz * nc + gy) * nc;
+                rlo[2 * row] = cell_start[base + xl];
+                rhi[2 * row] = cell_start[base + (wrapx ? nc : xh + 1)];
+                rlo[2 * row + 1] = wrapx ? cell_start[base] : 0;
+                rhi[2 * row + 1] = wrapx ? cell_start[base + xh + 1] : 0;
             }
-            for (int s27 = 0; s27 < 27; ++s27)
-                for (int q = lo[s27]; q < hi[s27]; ++q) consider(S.cell_beads[q]);
+            int sr = 0, q = rlo[0], e = rhi[0];
+            while (q >= e && ++sr < 18) { q = rlo[sr]; e = rhi[sr]; }
+            int c = sr < 18 ? cell_beads[q] : -1;
+            while (sr < 18) {
+                /* the next candidate's index is loaded before this one is tested */
+                ++q;
+                while (q >= e && ++sr < 18) { q = rlo[sr]; e = rhi[sr]; }
+                const int cn = sr < 18 ? cell_beads[q] : -1;
+                consider(c);
+                c = cn;
+            }
         } else {
             for (int c = 0; c < N; ++c) consider(c);
         }
@@ -496,6 +556,17 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds) {
         sh.sc.max_dn = m;
     }
     __syncthreads();
+}
+
+/* position of the n-th (0-based) set bit of m; n < popc(m) */
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1) {
+        const int c = __popc((m >> pos) & ((1u << w) - 1u));
+        if (n >= c) { n -= c; pos += w; }
+    }
+    return pos;
 }
 
 /* events() for beads b0 .. b0+nb-1 (nb <= TG_MAX) on one warp: every
@@ -533,6 +604,42 @@ __device__ void warp_predict_beads(const DSys &S, Err E, FullScratch &F, int b0,
             for (int q = F.tg_base[t]; q < F.tg_base[t + 1]; ++q) F.tmap[q] = (int8_t)t;
         __syncwarp();
     }
+    /* The tasks are decoded 32 at a time and screened in single precision;
+     * the ones that may have an event queue up in two register slots per
+     * lane (in task order, so a bead's tasks stay contiguous) and run in
+     * double precision 32 at a time. */
+    int qa_t = -1, qa_a = -1, qa_b = -1, qa_c = 0;   /* slot A: target, bead, partner, code */
+    int qb_t = -1, qb_a = -1, qb_b = -1, qb_c = 0;   /* slot B */
+    int pend = 0;
+    auto predict32 = [&](int tgt, int pa, int pbb, int code) {
+        double tij = 0.0;
+        int ty = 0;
+        bool ok = false;
+        if (pa >= 0) {
+            ok = d_predict_c(S, pa, pbb, code, 0.0, tij, ty);
+            if (!ok) set_err(E, DMD_E_INPUT, pa);
+            else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
+        }
+        long long k = (tgt >= 0 && ok) ? okey(tij) : DMD_KEY_INF;
+        int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
+        double rt = tij;
+        int y = ty;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long k2 = __shfl_down_sync(FULL, k, o);
+            int p2 = __shfl_down_sync(FULL, p, o);
+            double r2 = __shfl_down_sync(FULL, rt, o);
+            int y2 = __shfl_down_sync(FULL, y, o);
+            int g2 = __shfl_down_sync(FULL, tgt, o);
+            if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
+        }
+        int gprev = __shfl_up_sync(FULL, tgt, 1);
+        bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
+        if (head && key_less(k, p, F.tg_k[tgt], F.tg_p[tgt])) {
+            F.tg_k[tgt] = k; F.tg_p[tgt] = p; F.tg_raw[tgt] = rt; F.tg_y[tgt] = (int8_t)y;
+        }
+        __syncwarp();
+    };
     for (int base = 0; base < run; base += 32) {
         int q = base + lane;
         int tgt = -1, pa = -1, pbb = -1, st = -1;
@@ -563,34 +670,38 @@ __device__ void warp_predict_beads(const DSys &S, Err E, FullScratch &F, int b0,
             }
             if (m > b) { pa = b; pbb = m; }
         }
-        double tij = 0.0;
-        int ty = 0;
-        bool ok = false;
+        int code = 0;
+        bool live = false;
         if (pa >= 0) {
-            int code = st >= 0 ? pair_code_st(S, pbb, pa, st) : pair_code(S, pbb, pa, hbonds);
-            ok = d_predict_c(S, pa, pbb, code, 0.0, tij, ty);
-            if (!ok) set_err(E, DMD_E_INPUT, pa);
-            else if (okey(tij) < okey(-1.0e-10)) set_err(E, DMD_E_NEG_TIME, pa);
+            code = st >= 0 ? pair_code_st(S, pbb, pa, st) : pair_code(S, pbb, pa, hbonds);
+            /* no event for certain: it cannot win against the horizon */
+            live = !f32_no_event(S, pa, pbb, code, 0u);
         }
-        long long k = (tgt >= 0 && ok) ? okey(tij) : DMD_KEY_INF;
-        int p = (tgt >= 0 && ok) ? pbb : INT_MAX;
-        double rt = tij;
-        int y = ty;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            long long k2 = __shfl_down_sync(FULL, k, o);
-            int p2 = __shfl_down_sync(FULL, p, o);
-            double r2 = __shfl_down_sync(FULL, rt, o);
-            int y2 = __shfl_down_sync(FULL, y, o);
-            int g2 = __shfl_down_sync(FULL, tgt, o);
-            if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
+        const unsigned m = __ballot_sync(FULL, live);
+        const int cnt = __popc(m);
+        /* lane d of slot A takes the (d - pend)-th live task, of slot B the (d + 32 - pend)-th */
+        {
+            const int na = lane - pend, nb2 = lane + 32 - pend;
+            const int sa = (na >= 0 && na < cnt) ? nth_set_bit(m, na) : 0;
+            const int sb = (nb2 < cnt) ? nth_set_bit(m, nb2) : 0;
+            const int ta = __shfl_sync(FULL, tgt, sa), aa = __shfl_sync(FULL, pa, sa);
+            const int ba = __shfl_sync(FULL, pbb, sa), ca = __shfl_sync(FULL, code, sa);
+            const int tb = __shfl_sync(FULL, tgt, sb), ab = __shfl_sync(FULL, pa, sb);
+            const int bb = __shfl_sync(FULL, pbb, sb), cb = __shfl_sync(FULL, code, sb);
+            if (na >= 0 && na < cnt) { qa_t = ta; qa_a = aa; qa_b = ba; qa_c = ca; }
+            if (nb2 < cnt) { qb_t = tb; qb_a = ab; qb_b = bb; qb_c = cb; }
         }
-        int gprev = __shfl_up_sync(FULL, tgt, 1);
-        bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
-        if (head && key_less(k, p, F.tg_k[tgt], F.tg_p[tgt])) {
-            F.tg_k[tgt] = k; F.tg_p[tgt] = p; F.tg_raw[tgt] = rt; F.tg_y[tgt] = (int8_t)y;
+        pend += cnt;
+        if (pend >= 32) {
+            predict32(qa_t, qa_a, qa_b, qa_c);
+            qa_t = qb_t; qa_a = qb_a; qa_b = qb_b; qa_c = qb_c;
+            qb_t = -1; qb_a = -1; qb_b = -1; qb_c = 0;
+            pend -= 32;
         }
-        __syncwarp();
+    }
+    if (pend > 0) {
+        if (lane >= pend) { qa_t = -1; qa_a = -1; }
+        predict32(qa_t, qa_a, qa_b, qa_c);
     }
     for (int t = lane; t < nb; t += 32)
         set_pred(S, b0 + t, F.tg_raw[t], F.tg_p[t], F.tg_y[t], F.tg_k[t] < imax_key);
@@ -616,18 +727,29 @@ __device__ void cta_predict_all(const DSys &S, SharedState &sh, ScratchRef fr, d
     __syncthreads();
 }
 
-__device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int hbonds) {
+/* rebuild: wrap the positions into the box, cell lists, neighbour lists,
+ * full prediction, tournament.  scr (scr_bytes, may be null): shared memory
+ * free for the list build. */
+__device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int hbonds, char *scr, int scr_bytes) {
     DMD_SUB(-1);
+    const ListStage L = list_stage(S, scr, scr_bytes);
+    const int nc = S.ncell;
     for (int b = threadIdx.x; b < S.N; b += blockDim.x) {
         double px = S.x[b], py = S.y[b], pz = S.z[b];
         px = px - d_nint(px); py = py - d_nint(py); pz = pz - d_nint(pz);
         S.x[b] = px; S.y[b] = py; S.z[b] = pz;
         S.ox[b] = px; S.oy[b] = py; S.oz[b] = pz;
-        S.xf[b] = (float)px; S.yf[b] = (float)py; S.zf[b] = (float)pz;
+        const float fx = (float)px, fy = (float)py, fz = (float)pz;
+        S.xf[b] = fx; S.yf[b] = fy; S.zf[b] = fz;
+        if (L.cell_of) {
+            float *sx = const_cast<float *>(L.xf);
+            sx[b] = fx; sx[b + S.N] = fy; sx[b + 2 * S.N] = fz;
+            if (nc >= 3) L.cell_of[b] = (cell_coord(pz, nc) * nc + cell_coord(py, nc)) * nc + cell_coord(px, nc);
+        }
     }
     __syncthreads();
     DMD_ISUB(7);
-    cta_build_lists(S, sh, hbonds);
+    cta_build_lists(S, sh, hbonds, L);
     DMD_ISUB(8);
     cta_predict_all(S, sh, fr, sh.sc.interval_max, hbonds);
     DMD_ISUB(9);
@@ -641,7 +763,7 @@ __device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int h
  * displacement and decides on a rebuild, which it does alone.  sh.tf_iv
  * holds tfalse of the event on every CTA. */
 __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L, int rank, int C, ScratchRef fr,
-                                 int hbonds) {
+                                 int hbonds, char *scr, int scr_bytes) {
     const int N = S.N;
     const double tf = sh.tf_iv;
     const DTab &T = *S.tab;
@@ -739,7 +861,7 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
         if (sh.rebuild) {
             for (int k = threadIdx.x; k < N; k += blockDim.x) set_pred(S, k, sh.sc.interval_max + DMD_LTSTEP, -1, -1, false);
             __syncthreads();
-            cta_rebuild(S, sh, fr, hbonds);
+            cta_rebuild(S, sh, fr, hbonds, scr, scr_bytes);
             DMD_ISUB(3);
         }
         if (threadIdx.x == 0) set_pred(S, N + 1, sh.sc.interval * 0.999, -2, -2, true);
@@ -950,7 +1072,10 @@ __device__ void log_event(const DSys &S, long long slot, long long coll, double 
     L->i = i + 1; L->j = j + 1; L->type = type; L->evcode = evcode;
 }
 
+/* shared memory of k_init beyond its static part: the list build's staging */
+#define KINIT_DYN_SMEM (96 * 1024)
 __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, int hbonds_mask) {
+    extern __shared__ __align__(16) unsigned char kinit_dyn[];
     __shared__ SharedState sh;
     __shared__ DSys S_sh;
     int r = blockIdx.x;
@@ -962,7 +1087,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, i
     if (threadIdx.x == 0) { sh.sc = *S.sc; }
     __syncthreads();
     __shared__ FullScratch fs[NWARPS];
-    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds);
+    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds, (char *)kinit_dyn, KINIT_DYN_SMEM);
     if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
@@ -1032,7 +1157,20 @@ static size_t run_smem(int compact, int own_cap) {
 static int own_smem_max(int compact) { return compact ? OWN_SMEM_COMPACT : OWN_SMEM_FULL; }
 
 cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t st) {
-    k_init<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
+    static std::mutex mu;
+    static bool done[256];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (dev >= 0 && dev < 256 && !done[dev]) {
+            e = cudaFuncSetAttribute(k_init, cudaFuncAttributeMaxDynamicSharedMemorySize, KINIT_DYN_SMEM);
+            if (e != cudaSuccess) return e;
+            done[dev] = true;
+        }
+    }
+    k_init<<<nsys, NTHREADS, KINIT_DYN_SMEM, st>>>(d_systems, nsys, hbonds);
     return cudaGetLastError();
 }
 static cudaError_t k_run_attributes() {
@@ -1131,7 +1269,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_predict_noalloc(DSys S_in, int 
     if (threadIdx.x == 0) { S_sh = S_in; sh.sc = *S_in.sc; }
     __syncthreads();
     const DSys &S = S_sh;
-    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds);
+    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds, nullptr, 0);
     for (int b = threadIdx.x; b < S.N; b += blockDim.x) {
         tim_out[b] = S.tim[b];
         int p = S.nptnr[b];

@@ -46,6 +46,8 @@ struct DTab {
     double sqz610[6][DMD_NT];
     double evp1[DMD_NC], evp2[DMD_NC], evp3[DMD_NC];
     double rlsq[DMD_NC];
+    float rlsq_f[DMD_NC];         /* the same rounded to single precision (list-build prefilter) */
+    float rlsq_max_f;             /* their maximum */
     double shd1, shd2, shd3, shd4;
     double eps1;       /* epsilon(1): H-bond depth */
     double setemp, avegtime, hdelr, rl;

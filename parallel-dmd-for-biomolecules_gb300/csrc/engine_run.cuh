@@ -1436,7 +1436,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             ph_kind = 7;
             /* ---- interval: all CTAs ---- */
             double t_before = sh.tnow, tf = sh.tf_iv;
-            bool rb = cluster_interval(S, sh, L, rank, C, ScratchRef{(char *)&warea[0].fs, sizeof(WarpArea)}, hbonds);
+            /* the warp areas are free during an interval: the rebuild's scratch */
+            bool rb = cluster_interval(S, sh, L, rank, C, ScratchRef{(char *)&warea[0].fs, sizeof(WarpArea)}, hbonds,
+                                       (char *)warea, (int)(NWARPS * sizeof(WarpArea)));
             if (leader && threadIdx.x == 0) {
                 sh.sc.n_interval += 1;
                 log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
