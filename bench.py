@@ -276,14 +276,12 @@ def run_ours(args):
 
     # end to end through the public API with host buffers
     e2e_times, h2d, d2h = [], 0, 0
-    for s in specs:
-        n = s.n_beads
-        d2h += 6 * 8 * n + 3 * 4 * n + 4 * 4 * n + 24
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         b2 = Batch(specs)
-        h2d = int(b2.lib.dmd_batch_device_bytes(b2.h))   # the pools' host image, one copy
+        h2d = int(b2.lib.dmd_batch_upload_bytes(b2.h))   # the pools' heads from the pinned host image
+        d2h = int(b2.lib.dmd_batch_readback_bytes(b2.h))  # one state block per replica
         b2.run(E)
         states = [b2.state(r) for r in range(len(specs))]
         torch.cuda.synchronize()

@@ -241,9 +241,16 @@ int dmd_batch_set_cluster(dmd_batch *b, int32_t ctas);
 int dmd_set_cluster(dmd_handle *h, int32_t ctas);
 /* the cluster size the last run used */
 int32_t dmd_batch_cluster(dmd_batch *b);
-/* device bytes of the batch's system pools (what dmd_batch_create copies
- * from host memory in one transfer) */
+/* device bytes of the batch's system pools */
 int64_t dmd_batch_device_bytes(dmd_batch *b);
+/* host-to-device bytes dmd_batch_create copied: each pool's head (tables,
+ * scalars, bead state), one copy per system from a pinned host image; the
+ * rest of a pool (lists, grid, tournament) is written on the device */
+int64_t dmd_batch_upload_bytes(dmd_batch *b);
+/* device-to-host bytes of reading every system's state after a run
+ * (dmd_batch_get_state): one block per system - positions, velocities,
+ * identities, H-bond partners, extra_repuls - plus its scalars */
+int64_t dmd_batch_readback_bytes(dmd_batch *b);
 /* Rebuild grid: cells per side of the finest grid (cells as wide as the
  * list cutoff) divided by div (1..8, at least 3 cells per side).  Lists
  * and results do not depend on it. */

@@ -410,8 +410,10 @@ struct Pool {
 };
 
 /* for_run: the arrays only the event loop uses (down-list codes, claim
- * tables); the allocation-free prediction pass leaves them out */
-size_t layout(const HostSys &H, DSys &d, char *base, bool for_run = true) {
+ * tables); the allocation-free prediction pass leaves them out.  head:
+ * bytes of the pool's head, the arrays filled from host data (those before
+ * the neighbour lists). */
+size_t layout(const HostSys &H, DSys &d, char *base, bool for_run = true, size_t *head = nullptr) {
     Pool P{base, 0};
     size_t N = H.N, NE = H.N + 3, cap = H.cap;
     size_t nc3 = (size_t)H.ncell * H.ncell * H.ncell;
@@ -431,6 +433,7 @@ size_t layout(const HostSys &H, DSys &d, char *base, bool for_run = true) {
     d.ovp = P.take<int>(4 * N);
     d.ovc = P.take<int8_t>(4 * N);
     d.tim = P.take<double>(NE); d.nptnr = P.take<int>(NE); d.colt = P.take<int8_t>(NE); d.queued = P.take<uint8_t>(NE);
+    if (head) *head = P.off;
     d.up = P.take<int>(N * cap); d.dn = P.take<int>(N * cap); d.upc = P.take<int8_t>(N * cap);
     d.dnc = for_run ? P.take<int8_t>(N * cap) : nullptr;
     d.upn = P.take<int>(N); d.dnn = P.take<int>(N);
@@ -467,6 +470,9 @@ struct dmd_batch {
     void *pool_all = nullptr;           /* the pools of all systems, one allocation */
     std::vector<dmd_diag> diag_cache;   /* diagnostics of all systems, valid until the next run */
     bool diag_valid = false;
+    std::vector<char> state_cache;     /* every system's bead state, read back in one copy each */
+    std::vector<size_t> state_off;
+    bool state_valid = false;          /* until the next run */
     int cluster = 0;        /* CTAs per system: 1, 2, 4, 8, or 0 = chosen at run time */
     int last_cluster = 0;   /* what the last run used */
     int cell_div = 1;       /* rebuild grid: the finest grid's cells per side divided by this */
@@ -474,6 +480,7 @@ struct dmd_batch {
     long long graph_events = 0;
     int graph_launches = 0, graph_cluster = 0, graph_compact = -1;
     long long *d_targets = nullptr;    /* per-system event targets of a follow-up launch */
+    long long upload_bytes = 0;        /* host-to-device bytes of the creation */
     int compact_dn = DMD_COMPACT_DN;   /* down-list limit of the compact variant, 0: never */
 };
 struct dmd_handle { dmd_batch b; };
@@ -576,6 +583,12 @@ int upload_system(HostSys &H, DevSys &D, cudaStream_t st, std::string &err) {
     return DMD_OK;
 }
 
+/* Pinned host staging for batch creation, kept between creations (grown
+ * on demand; pinning host memory costs far more than copying into it). */
+std::mutex g_stage_mu;
+char *g_stage = nullptr;
+size_t g_stage_cap = 0;
+
 int upload(dmd_batch &B) {
     std::string &err = B.err;
     int n = (int)B.hs.size();
@@ -583,19 +596,31 @@ int upload(dmd_batch &B) {
     CK(cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking));
     CK(cudaEventCreate(&B.ev0));
     CK(cudaEventCreate(&B.ev1));
-    /* all systems' pools in one allocation, filled from one pinned host
-     * image by one copy */
-    std::vector<size_t> off(n + 1, 0);
+    /* All systems' pools in one allocation.  Each pool's head - tables,
+     * scalars and bead arrays that start from host data - is filled from
+     * one pinned host image, one copy per system; the neighbour lists,
+     * cell grid, tournament and claim tables behind it are written on the
+     * device by the list build. */
+    std::vector<size_t> off(n + 1, 0), head(n, 0), soff(n + 1, 0);
     for (int r = 0; r < n; ++r) {
         DSys tmp{};
-        size_t bytes = (layout(B.hs[r], tmp, nullptr) + 255) & ~(size_t)255;
+        size_t bytes = (layout(B.hs[r], tmp, nullptr, true, &head[r]) + 255) & ~(size_t)255;
         B.ds[r].bytes = bytes;
         off[r + 1] = off[r] + bytes;
+        soff[r + 1] = soff[r] + ((head[r] + 255) & ~(size_t)255);
     }
     size_t total = off[n];
     CK(cudaMalloc(&B.pool_all, total));
-    char *stage = nullptr;
-    CK(cudaMallocHost((void **)&stage, total));
+    std::lock_guard<std::mutex> stage_lock(g_stage_mu);
+    if (g_stage_cap < soff[n]) {
+        if (g_stage) cudaFreeHost(g_stage);
+        g_stage = nullptr;
+        g_stage_cap = 0;
+        CK(cudaMallocHost((void **)&g_stage, soff[n]));
+        g_stage_cap = soff[n];
+    }
+    char *stage = g_stage;
+    B.upload_bytes = 0;
     std::vector<DSys> hd(n);
     std::vector<int> cstart, clen, coff;
     for (int r = 0; r < n; ++r) {
@@ -607,15 +632,16 @@ int upload(dmd_batch &B) {
         PoolTemps keep;
         std::vector<PoolCopy> cps;
         pool_copies(H, D.d, keep, cps);
+        char *base = (char *)B.pool_all + off[r];
         for (const PoolCopy &c : cps)
-            std::memcpy(stage + ((char *)c.dst - (char *)B.pool_all), c.src, c.n);
+            std::memcpy(stage + soff[r] + ((char *)c.dst - base), c.src, c.n);
+        CK(cudaMemcpyAsync(base, stage + soff[r], head[r], cudaMemcpyHostToDevice, B.st));
+        B.upload_bytes += (long long)head[r];
         hd[r] = D.d;
         coff.push_back((int)cstart.size());
         for (int c = 0; c < H.nchains; ++c) { cstart.push_back(H.chain_start[c]); clen.push_back(H.chain_len[c]); }
     }
-    cudaError_t ce = cudaMemcpy(B.pool_all, stage, total, cudaMemcpyHostToDevice);
-    cudaFreeHost(stage);
-    CK(ce);
+    CK(cudaStreamSynchronize(B.st));   /* the stage is free for the next creation */
     CK(cudaMalloc(&B.d_sys, n * sizeof(DSys)));
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
     CK(cudaMalloc(&B.d_cstart, cstart.size() * 4));
@@ -690,6 +716,7 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     std::string &err = B.err;
     if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
     B.diag_valid = false;
+    B.state_valid = false;
     int n = (int)B.hs.size();
     /* event logs: one device ring per system for this call */
     std::vector<DSys> hd(n);
@@ -756,32 +783,48 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     return rc;
 }
 
+/* the bytes of a system's bead state block in its pool: positions and
+ * velocities through the extra_repuls array (one contiguous range) */
+size_t state_block(const DSys &d) { return (size_t)((const char *)(d.er + 4 * (size_t)d.N) - (const char *)d.x); }
+
 int get_state(dmd_batch &B, int r, double *x, double *y, double *z, double *vx, double *vy, double *vz,
               int32_t *bptnr, int32_t *identity, int32_t *er_out, double *t, double *tfalse, int64_t *coll) {
     std::string &err = B.err;
     if (r < 0 || r >= (int)B.hs.size()) { err = "replica index out of range"; return DMD_E_INPUT; }
+    const int n = (int)B.hs.size();
+    if (!B.state_valid) {
+        /* every system's state block and scalars, one copy each */
+        B.state_off.assign(n + 1, 0);
+        for (int q = 0; q < n; ++q) B.state_off[q + 1] = B.state_off[q] + state_block(B.ds[q].d);
+        B.state_cache.resize(B.state_off[n]);
+        CK(cudaStreamSynchronize(B.st));
+        for (int q = 0; q < n; ++q)
+            CK(cudaMemcpyAsync(B.state_cache.data() + B.state_off[q], B.ds[q].d.x, state_block(B.ds[q].d),
+                               cudaMemcpyDeviceToHost, B.st));
+        for (int q = 0; q < n; ++q)
+            CK(cudaMemcpyAsync(&B.hs[q].sc, B.ds[q].d.sc, sizeof(DScal), cudaMemcpyDeviceToHost, B.st));
+        CK(cudaStreamSynchronize(B.st));
+        B.state_valid = true;
+    }
     const DSys &d = B.ds[r].d;
-    size_t N = d.N;
-    CK(cudaStreamSynchronize(B.st));
-    if (x) { CK(cudaMemcpy(x, d.x, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(y, d.y, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(z, d.z, N * 8, cudaMemcpyDeviceToHost)); }
-    if (vx) { CK(cudaMemcpy(vx, d.vx, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(vy, d.vy, N * 8, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(vz, d.vz, N * 8, cudaMemcpyDeviceToHost)); }
+    const size_t N = d.N;
+    const char *blk = B.state_cache.data() + B.state_off[r];
+    auto at = [&](const void *p) { return blk + ((const char *)p - (const char *)d.x); };
+    if (x) { std::memcpy(x, at(d.x), N * 8); std::memcpy(y, at(d.y), N * 8); std::memcpy(z, at(d.z), N * 8); }
+    if (vx) { std::memcpy(vx, at(d.vx), N * 8); std::memcpy(vy, at(d.vy), N * 8); std::memcpy(vz, at(d.vz), N * 8); }
     if (bptnr) {
-        std::vector<int> b(N);
-        CK(cudaMemcpy(b.data(), d.bptnr, N * 4, cudaMemcpyDeviceToHost));
+        const int *b = (const int *)at(d.bptnr);
         for (size_t k = 0; k < N; ++k) bptnr[k] = b[k] + 1;
     }
     if (identity) {
-        std::vector<int8_t> b(N);
-        CK(cudaMemcpy(b.data(), d.ident, N, cudaMemcpyDeviceToHost));
+        const int8_t *b = (const int8_t *)at(d.ident);
         for (size_t k = 0; k < N; ++k) identity[k] = b[k];
     }
     if (er_out) {
-        std::vector<int> b(4 * N);
-        CK(cudaMemcpy(b.data(), d.er, 4 * N * 4, cudaMemcpyDeviceToHost));
+        const int *b = (const int *)at(d.er);
         for (size_t k = 0; k < 4 * N; ++k) er_out[k] = b[k] + 1;
     }
-    DScal sc;
-    CK(cudaMemcpy(&sc, d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+    const DScal &sc = B.hs[r].sc;
     if (t) *t = sc.t;
     if (tfalse) *tfalse = sc.tfalse;
     if (coll) *coll = sc.coll;
@@ -812,6 +855,7 @@ int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
     if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
     if (n_launches <= 0 || n_events < 0) { err = "bad launch count"; return DMD_E_INPUT; }
     B.diag_valid = false;
+    B.state_valid = false;
     int n = (int)B.hs.size();
     int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
     int probe = 0;
@@ -1231,6 +1275,13 @@ int64_t dmd_batch_device_bytes(dmd_batch *b) {
     for (const DevSys &D : b->ds) s += (int64_t)D.bytes;
     return s;
 }
+int64_t dmd_batch_upload_bytes(dmd_batch *b) { return b ? (int64_t)b->upload_bytes : 0; }
+int64_t dmd_batch_readback_bytes(dmd_batch *b) {
+    if (!b) return 0;
+    int64_t s = 0;
+    for (const DevSys &D : b->ds) s += (int64_t)(state_block(D.d) + sizeof(DScal));
+    return s;
+}
 int dmd_batch_run_graph(dmd_batch *b, int64_t n_events, int32_t n_launches) {
     if (!b) return DMD_E_INPUT;
     return batch_run_graph(*b, n_events, n_launches);
@@ -1611,6 +1662,7 @@ int dmd_load_state(dmd_handle *h, const void *buf, int64_t n) {
     CK(cudaMemcpy(&sc, D.d.sc, sizeof sc, cudaMemcpyDeviceToHost));
     B.hs[0].sc = sc;
     B.diag_valid = false;
+    B.state_valid = false;
     return DMD_OK;
 }
 

@@ -245,24 +245,6 @@ __device__ void cta_tree_rebuild(const DSys &S) {
     for (int h = threadIdx.x; h < S.nl2; h += blockDim.x) l2_update(S, h);
     __syncthreads();
 }
-__device__ int warp_tree_root(const DSys &S, long long &kroot) {
-    int lane = threadIdx.x & 31;
-    long long bk = DMD_KEY_INF;
-    int best = INT_MAX;
-    for (int h = lane; h < S.nl2; h += 32) {
-        int e = S.l2i[h];
-        long long k = S.l2k[h];
-        if (key_less(k, e, bk, best)) { bk = k; best = e; }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        long long k2 = __shfl_xor_sync(FULL, bk, o);
-        int b2 = __shfl_xor_sync(FULL, best, o);
-        if (key_less(k2, b2, bk, best)) { bk = k2; best = b2; }
-    }
-    kroot = bk;
-    return bk == DMD_KEY_INF ? -1 : best;
-}
 /* warp: refresh the level-1 groups of the given entries */
 __device__ void warp_l1_refresh(const DSys &S, const int *entries, int n) {
     int lane = threadIdx.x & 31;
@@ -992,72 +974,121 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
 /* The bead events below the cut, sorted in (key, index) order into
  * sh.sort_*; returns how many there are (1 when the window could not be
  * made small enough: the root alone). */
-__device__ int cta_candidates(const DSys &S, SharedState &sh, int root, long long kroot, int slots) {
+/* warp: the earliest queue entry (index, key), or -1 when the queue is
+ * empty: the argmin over the level-1 groups, through level 2 for large
+ * systems */
+__device__ int warp_root(const DSys &S, long long &kroot) {
+    const int lane = threadIdx.x & 31;
+    long long bk = DMD_KEY_INF;
+    int best = INT_MAX;
+    if (S.nl1 <= 256) {
+        for (int g = lane; g < S.nl1; g += 32) {
+            const long long k = S.l1k[g];
+            const int e = S.l1i[g];
+            if (key_less(k, e, bk, best)) { bk = k; best = e; }
+        }
+    } else {
+        for (int h = lane; h < S.nl2; h += 32) l2_update(S, h);
+        __syncwarp();
+        for (int h = lane; h < S.nl2; h += 32) {
+            const long long k = S.l2k[h];
+            const int e = S.l2i[h];
+            if (key_less(k, e, bk, best)) { bk = k; best = e; }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long k2 = __shfl_xor_sync(FULL, bk, o);
+        int b2 = __shfl_xor_sync(FULL, best, o);
+        if (key_less(k2, b2, bk, best)) { bk = k2; best = b2; }
+    }
+    kroot = bk;
+    return bk == DMD_KEY_INF ? -1 : best;
+}
+
+/* The batch candidates: every bead entry whose key lies below a cut (and
+ * below every pseudo event), sorted in (key, index) order into
+ * sh.sort_key/sort_idx; the first is the root.  The cut is the root's time
+ * plus a window sh.delta that adapts to aim at one to four candidates per
+ * warp slot.  Every warp scans the level-1 minima against the cut and takes
+ * every NWARPS-th group below it; warp 0 sorts.  sh.ncand must be 0 on
+ * entry.  Returns their number (1 if the window cannot be made small
+ * enough). */
+__device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, long long kroot, int slots) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const int N = S.N;
-    long long kp = min(min(S.key[N], S.key[N + 1]), S.key[N + 2]);
+    const long long kp = min(min(S.key[N], S.key[N + 1]), S.key[N + 2]);
+    int nc = 0;
     bool ok = false;
     for (int attempt = 0; attempt < 8; ++attempt) {
-        if (threadIdx.x == 0) {
-            double tr = S.tim[root];
-            long long kc = okey(tr + sh.delta);
+        long long kc = 0;
+        if (lane == 0) {
+            kc = okey(S.tim[root] + sh.delta);
             if (kc <= kroot) kc = kroot + 1;
             if (kc > kp) kc = kp;
-            sh.kcut = kc;
-            sh.ncand = 0;
-            sh.ngroups = 0;
         }
-        __syncthreads();
-        long long kc = sh.kcut;
-        /* groups whose minimum lies below the cut */
-        for (int g = threadIdx.x; g < S.nl1; g += blockDim.x) {
-            if (S.l1k[g] < kc) {
-                int s = atomicAdd(&sh.ngroups, 1);
-                if (s < 256) sh.groups[s] = g;
+        kc = __shfl_sync(FULL, kc, 0);
+        int ord = 0;   /* ordinal of the next group below the cut */
+        for (int gb = 0; gb < S.nl1; gb += 32) {
+            const int g = gb + lane;
+            unsigned gm = __ballot_sync(FULL, g < S.nl1 && S.l1k[g] < kc);
+            /* this warp's groups: ordinals warp, warp + NWARPS, ... */
+            while (gm) {
+                const int gg = gb + __ffs(gm) - 1;
+                gm &= gm - 1;
+                if (ord++ % NWARPS != warp) continue;
+                const int e = gg * 32 + lane;
+                const long long k = e < N ? S.key[e] : DMD_KEY_INF;
+                const bool c = k < kc;
+                const unsigned cm = __ballot_sync(FULL, c);
+                int pos = 0;
+                if (lane == 0 && cm) pos = atomicAdd(&sh.ncand, __popc(cm));
+                pos = __shfl_sync(FULL, pos, 0) + __popc(cm & lt);
+                if (c && pos < CAND_MAX) { sh.cand_key[pos] = k; sh.cand_idx[pos] = e; }
             }
         }
         __syncthreads();
-        int ng = sh.ngroups;
-        if (ng <= 256) {
-            int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-            for (int gi = warp; gi < ng; gi += NWARPS) {
-                int e = sh.groups[gi] * 32 + lane;
-                long long k = (e < N) ? S.key[e] : DMD_KEY_INF;
-                if (k < kc) {
-                    int s = atomicAdd(&sh.ncand, 1);
-                    if (s < CAND_MAX) { sh.cand_key[s] = k; sh.cand_idx[s] = e; }
-                }
-            }
-        }
-        __syncthreads();
-        if (ng <= 256 && sh.ncand <= CAND_MAX) { ok = true; break; }
+        nc = sh.ncand;
+        ok = nc <= CAND_MAX;
+        if (ok) break;
+        __syncthreads();                   /* every thread has read ncand */
         if (threadIdx.x == 0) {
+            sh.ncand = 0;
             sh.delta = sh.delta * 0.25;
             if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
         }
         __syncthreads();
     }
-    int nc = sh.ncand;
     if (!ok || nc < 1) {
         if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = root; }
-        __syncthreads();
         return 1;
     }
-    if ((int)threadIdx.x < nc) {
-        long long k = sh.cand_key[threadIdx.x];
-        int e = sh.cand_idx[threadIdx.x];
-        int rank = 0;
-        for (int u = 0; u < nc; ++u)
-            if (key_less(sh.cand_key[u], sh.cand_idx[u], k, e)) ++rank;
-        sh.sort_key[rank] = k;
-        sh.sort_idx[rank] = e;
+    if (warp == 0) {
+        /* rank sort: each candidate counts the candidates before it */
+        long long kk[2];
+        int ee[2], rk[2] = {0, 0};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = lane + 32 * h;
+            kk[h] = c < nc ? sh.cand_key[c] : DMD_KEY_INF;
+            ee[h] = c < nc ? sh.cand_idx[c] : INT_MAX;
+        }
+        for (int u = 0; u < nc; ++u) {
+            const long long ku = sh.cand_key[u];
+            const int eu = sh.cand_idx[u];
+            rk[0] += key_less(ku, eu, kk[0], ee[0]);
+            rk[1] += key_less(ku, eu, kk[1], ee[1]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (lane + 32 * h < nc) { sh.sort_key[rk[h]] = kk[h]; sh.sort_idx[rk[h]] = ee[h]; }
+        if (lane == 0) {
+            if (nc < slots) sh.delta = sh.delta * 2.0;
+            else if (nc > 4 * slots) sh.delta = sh.delta * 0.5;
+            if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
+        }
     }
-    if (threadIdx.x == 0) {
-        /* aim at about one to four candidates per warp */
-        if (nc < slots) sh.delta = sh.delta * 2.0;
-        else if (nc > 4 * slots) sh.delta = sh.delta * 0.5;
-        if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
-    }
-    __syncthreads();
     return nc;
 }
 

@@ -1100,39 +1100,46 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     while (true) {
         /* ---- the leader selects the next event (and a batch) ---- */
         if (leader) {
-            for (int h = threadIdx.x; h < S.nl2; h += blockDim.x) l2_update(S, h);
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                bool ex = sh.sc.done >= target || sh.sc.err || sh.sc.stop;
-                /* lists longer than this variant takes: the host goes on
-                 * with the full variant from here */
-                if (!ex && sh.sc.max_dn > dn_limit) { sh.sc.need_full = 1; ex = true; }
-                if (!ex && ++iter > max_iter) { set_err(sh, DMD_E_DEVICE_TIMEOUT, 0); ex = true; }
-                sh.exitf = ex;
-            }
-            __syncthreads();
-            if (!sh.exitf && warp == 0) {
-                long long kroot;
-                int e = warp_tree_root(S, kroot);
+            if (warp == 0) {
+                /* warp 0: the exit test and the root */
+                int ex = 0;
                 if (lane == 0) {
+                    bool x = sh.sc.done >= target || sh.sc.err || sh.sc.stop;
+                    /* lists longer than this variant takes: the host goes
+                     * on with the full variant from here */
+                    if (!x && sh.sc.max_dn > dn_limit) { sh.sc.need_full = 1; x = true; }
+                    if (!x && ++iter > max_iter) { set_err(sh, DMD_E_DEVICE_TIMEOUT, 0); x = true; }
+                    ex = x;
+                }
+                ex = __shfl_sync(FULL, ex, 0);
+                long long kroot = 0;
+                const int e = ex ? -1 : warp_root(S, kroot);
+                if (!ex && e < 0 && lane == 0) set_err(sh, DMD_E_STATE, 0);
+                ex = ex || e < 0;
+                if (lane == 0) {
+                    sh.exitf = ex;
                     sh.ev = e;
                     sh.kcut = kroot;
-                    if (e < 0) { set_err(sh, DMD_E_STATE, 0); sh.exitf = 1; }
+                    sh.ncand = 0;
+                    if (!ex && e >= N) {
+                        /* a pseudo event: its counter and time */
+                        sh.sc.coll += 1;
+                        sh.tf_iv = S.tim[e];
+                        if (e != N) sh.sc.tfalse = sh.tf_iv;
+                    }
                 }
             }
             __syncthreads();
             DMD_PHASE(0);
             if (!sh.exitf && sh.ev < N) {
-                int e = sh.ev;
-                long long kroot = sh.kcut;
-                long long left = target - sh.sc.done;
-                int m;
+                const int e = sh.ev;
+                const long long kroot = sh.kcut;
+                const long long left = target - sh.sc.done;
+                int m = 1;
                 if (serial || left <= 1) {
                     if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = e; }
-                    __syncthreads();
-                    m = 1;
                 } else {
-                    m = cta_candidates(S, sh, e, kroot, slots);
+                    m = cta_gather_candidates(S, sh, e, kroot, slots);
                     if (m > slots) m = slots;
                     if (m > left) m = (int)left;
                 }
@@ -1142,11 +1149,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     sh.c_simple[0] = 0;    /* set by the footprint test when m > 1 */
                 }
                 DMD_PHASE(1);
-            } else if (!sh.exitf && threadIdx.x == 0) {
-                /* a pseudo event: its counter and time */
-                sh.sc.coll += 1;
-                sh.tf_iv = S.tim[sh.ev];
-                if (sh.ev != N) sh.sc.tfalse = sh.tf_iv;
             }
             if (threadIdx.x == 0) {
                 sh.coll0 = sh.sc.coll; sh.log0 = sh.sc.log_count; sh.imax = sh.sc.interval_max; sh.tnow = sh.sc.t;

@@ -104,7 +104,7 @@ ENGINE_SYMBOLS = [
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
     "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster", "dmd_batch_set_cell_div",
     "dmd_batch_set_compact_limit", "dmd_set_compact_limit",
-    "dmd_batch_run_graph", "dmd_batch_autotune", "dmd_batch_device_bytes", "dmd_state_bytes", "dmd_save_state", "dmd_load_state",
+    "dmd_batch_run_graph", "dmd_batch_autotune", "dmd_batch_device_bytes", "dmd_batch_upload_bytes", "dmd_batch_readback_bytes", "dmd_state_bytes", "dmd_save_state", "dmd_load_state",
     "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
     "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
 ]
@@ -175,6 +175,10 @@ def _declare(lib) -> None:
         getattr(lib, fn).restype = C.c_int
     lib.dmd_batch_device_bytes.argtypes = [C.c_void_p]
     lib.dmd_batch_device_bytes.restype = C.c_int64
+    lib.dmd_batch_upload_bytes.argtypes = [C.c_void_p]
+    lib.dmd_batch_upload_bytes.restype = C.c_int64
+    lib.dmd_batch_readback_bytes.argtypes = [C.c_void_p]
+    lib.dmd_batch_readback_bytes.restype = C.c_int64
     lib.dmd_batch_run_graph.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
     lib.dmd_batch_run_graph.restype = C.c_int
     lib.dmd_batch_autotune.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dbl_p]
