@@ -333,6 +333,23 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
             H.tab.rmass[a][b] = (bmi + bmj) != 0.0 ? 2 * bmi * bmj / (bmi + bmj) : 0.0;
         }
     for (int a = 0; a < DMD_NT; ++a) H.tab.rbm[a] = bmass[a] != 0.0 ? 1.0 / bmass[a] : 0.0;
+    {
+        DTab &D = H.tab;
+        auto rcp = [](double v) { return v != 0.0 ? 1.0 / v : 0.0; };
+        for (int c = 0; c < 14; ++c)
+            for (int a = 0; a < DMD_NT; ++a)
+                for (int b = 0; b < DMD_NT; ++b) D.rcore_sq[c][a][b] = rcp(D.core_sq[c][a][b]);
+        for (int a = 0; a < DMD_NT; ++a)
+            for (int b = 0; b < DMD_NT; ++b) {
+                D.rcore15_sq[a][b] = rcp(D.core15_sq[a][b]);
+                D.rsigma_sq[a][b] = rcp(D.sigma_sq[a][b]);
+                D.rwell_sq[a][b] = rcp(D.welldia_sq[a][b]);
+                D.r2well_sq[a][b] = rcp(2.0 * D.welldia_sq[a][b]);
+                D.rshld_sq[a][b] = rcp(D.shlddia_sq[a][b]);
+                D.r2shld_sq[a][b] = rcp(2.0 * D.shlddia_sq[a][b]);
+                D.rrmass[a][b] = rcp(D.rmass[a][b]);
+            }
+    }
     H.tab.setemp = cfg->tstar * 12.0;
     H.tab.avegtime = 0.00005 / std::sqrt(H.tab.setemp);
 

@@ -64,6 +64,14 @@ struct DTab {
     double rbm[DMD_NT];                  /* 1/mass, rounded to nearest (for div_by) */
     double revp2_sq[DMD_NC], revp3_sq[DMD_NC];   /* 1/evp2_sq, 1/evp3_sq */
     double evp2_sq[DMD_NC], evp3_sq[DMD_NC];
+    /* reciprocals rounded to nearest of the divisors of eventdyn.f, for
+     * div_by(): the core diameters, the wells and shoulders (and twice
+     * them), the reduced masses */
+    double rcore_sq[14][DMD_NT][DMD_NT];
+    double rcore15_sq[DMD_NT][DMD_NT], rsigma_sq[DMD_NT][DMD_NT];
+    double rwell_sq[DMD_NT][DMD_NT], r2well_sq[DMD_NT][DMD_NT];
+    double rshld_sq[DMD_NT][DMD_NT], r2shld_sq[DMD_NT][DMD_NT];
+    double rrmass[DMD_NT][DMD_NT];
 };
 __host__ __device__ __forceinline__ int core_slot(int code) { return code <= 3 ? code : code - 13; }
 

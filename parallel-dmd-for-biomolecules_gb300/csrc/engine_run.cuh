@@ -84,8 +84,12 @@ __device__ WRel warp_rel(const DSys &S, int i, int j, double tf) {
     double b0 = __shfl_sync(FULL, pb, 0), b1 = __shfl_sync(FULL, pb, 1), b2 = __shfl_sync(FULL, pb, 2);
     double r0 = __shfl_sync(FULL, pr, 0), r1 = __shfl_sync(FULL, pr, 1), r2 = __shfl_sync(FULL, pr, 2);
     double v0 = __shfl_sync(FULL, pv, 0), v1 = __shfl_sync(FULL, pv, 1), v2 = __shfl_sync(FULL, pv, 2);
-    /* three independent sums on three lanes, then broadcast */
-    double s = lane == 0 ? b0 + b1 + b2 : (lane == 1 ? r0 + r1 + r2 : v0 + v1 + v2);
+    /* three independent sums on three lanes (operands selected first, so
+     * that the warp issues two additions, not six), then broadcast */
+    const double s0 = lane == 0 ? b0 : (lane == 1 ? r0 : v0);
+    const double s1 = lane == 0 ? b1 : (lane == 1 ? r1 : v1);
+    const double s2 = lane == 0 ? b2 : (lane == 1 ? r2 : v2);
+    double s = s0 + s1 + s2;
     w.bij = __shfl_sync(FULL, s, 0);
     w.rijsq = __shfl_sync(FULL, s, 1);
     w.vijsq = __shfl_sync(FULL, s, 2);
@@ -178,56 +182,63 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
             double rhi = side ? S.rblmax_sq[i] : T.revp3_sq[evcode];
             ratio = div_by(rmass * bij, hi, rhi);
         } else if (ct == 1) {
-            double sigsq;
-            if (evcode == 15) sigsq = S.bptnr[i] == j ? T.core15_sq[a][b] : T.sigma_sq[a][b];
-            else sigsq = T.core_sq[core_slot(evcode)][a][b];
-            ratio = rmass * bij / sigsq;
+            if (evcode == 15) {
+                const bool hb = S.bptnr[i] == j;
+                ratio = div_by(rmass * bij, hb ? T.core15_sq[a][b] : T.sigma_sq[a][b],
+                               hb ? T.rcore15_sq[a][b] : T.rsigma_sq[a][b]);
+            } else if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {
+                const int sl = core_slot(evcode);
+                ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
+            } else {
+                ratio = rmass * bij / T.core_sq[core_slot(evcode)][a][b];
+            }
         } else if (ct == 4) {
             double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
-            double del_pe = 4.0 * wellsq * epsave / rmass;
+            double del_pe = div_by(4.0 * wellsq * epsave, rmass, T.rrmass[a][b]);
             bd = DMD_SMDIST * sqrt(wellsq);
             if (bij * bij + del_pe > 0.0) {
-                ratio = rmass * (sqrt((4.0 * wellsq * epsave / rmass) + bij * bij) + bij) / (2.0 * wellsq);
+                /* the reference recomputes del_pe here: the same value */
+                ratio = div_by(rmass * (sqrt(del_pe + bij * bij) + bij), 2.0 * wellsq, T.r2well_sq[a][b]);
                 ct = 20; bump = -1;
             } else {
-                ratio = rmass * bij / wellsq;
+                ratio = div_by(rmass * bij, wellsq, T.rwell_sq[a][b]);
                 ct = 22; bump = 1;
             }
         } else if (ct == 8) {
             double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
-            double del_pe = 4.0 * wellsq * epsave / rmass;
+            double del_pe = div_by(4.0 * wellsq * epsave, rmass, T.rrmass[a][b]);
             bd = DMD_SMDIST * sqrt(wellsq);
             if (bij * bij > del_pe) {
-                ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
+                ratio = div_by(rmass * (-sqrt(-del_pe + bij * bij) + bij), 2.0 * wellsq, T.r2well_sq[a][b]);
                 ct = 21; bump = 1;
             } else {
-                ratio = rmass * bij / wellsq;
+                ratio = div_by(rmass * bij, wellsq, T.rwell_sq[a][b]);
                 ct = 22; bump = -1;
             }
         } else if (ct == 9) {
             double wellsq = T.welldia_sq[a][b];
-            ratio = rmass * bij / wellsq;
+            ratio = div_by(rmass * bij, wellsq, T.rwell_sq[a][b]);
             ct = 23; bump = 1; bd = DMD_SMDIST * sqrt(wellsq);
         } else if (ct == 5) {
             double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
-            double del_pe = 4.0 * wellsq * epsave / rmass;
+            double del_pe = div_by(4.0 * wellsq * epsave, rmass, T.rrmass[a][b]);
             bd = DMD_SMDIST * sqrt(wellsq);
-            ratio = rmass * (-sqrt(-del_pe + bij * bij) + bij) / (2.0 * wellsq);
+            ratio = div_by(rmass * (-sqrt(-del_pe + bij * bij) + bij), 2.0 * wellsq, T.r2shld_sq[a][b]);
             ct = 24; bump = 1;
         } else if (ct == 6) {
             double wellsq = T.shlddia_sq[a][b], epsave = -T.eps1;
-            double del_pe = 4.0 * wellsq * epsave / rmass;
+            double del_pe = div_by(4.0 * wellsq * epsave, rmass, T.rrmass[a][b]);
             bd = DMD_SMDIST * sqrt(wellsq);
             if (bij * bij > -del_pe) {
-                ratio = rmass * (sqrt(del_pe + bij * bij) + bij) / (2.0 * wellsq);
+                ratio = div_by(rmass * (sqrt(del_pe + bij * bij) + bij), 2.0 * wellsq, T.r2shld_sq[a][b]);
                 ct = 25; bump = -1;
             } else {
-                ratio = rmass * bij / wellsq;
+                ratio = div_by(rmass * bij, wellsq, T.rshld_sq[a][b]);
                 ct = 26; bump = 1;
             }
         } else if (ct == 13) {
             double wellsq = T.shlddia_sq[a][b];
-            ratio = rmass * bij / wellsq;
+            ratio = div_by(rmass * bij, wellsq, T.rshld_sq[a][b]);
             ct = 27; bump = 1; bd = DMD_SMDIST * sqrt(wellsq);
         }
     }
@@ -430,22 +441,22 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
     sh.sc.n_ghost += 1;
     S.x[i] = S.x[i] + S.vx[i] * tfalse; S.y[i] = S.y[i] + S.vy[i] * tfalse; S.z[i] = S.z[i] + S.vz[i] * tfalse;
     double v1, v2, r;
-    double bmi = S.bm[i];
+    double bmi = S.bm[i], rbmi = T.rbm[S.ident[i]];   /* bm(i) = mass(identity(i)) */
     do {
         v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         r = v1 * v1 + v2 * v2;
     } while (((r == 0.0) || (r >= 1.0)) && k < 4096);
     double fact = sqrt(-2.0 * T.setemp * bmi * dmd_log(r) / r);
-    S.vx[i] = v1 * fact / bmi;
-    S.vy[i] = v2 * fact / bmi;
+    S.vx[i] = div_by(v1 * fact, bmi, rbmi);
+    S.vy[i] = div_by(v2 * fact, bmi, rbmi);
     do {
         v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++) - 1.0;
         r = v1 * v1 + v2 * v2;
     } while (((r == 0.0) || (r >= 1.0)) && k < 8192);
     fact = sqrt(-2.0 * T.setemp * bmi * dmd_log(r) / r);
-    S.vz[i] = v1 * fact / bmi;
+    S.vz[i] = div_by(v1 * fact, bmi, rbmi);
     S.x[i] = S.x[i] - S.vx[i] * tfalse; S.y[i] = S.y[i] - S.vy[i] * tfalse; S.z[i] = S.z[i] - S.vz[i] * tfalse;
     double tgho = 0.0;
     while (((tgho < 1e-18) || (tgho == 1.0)) && k < 12288) tgho = dmd_uniform(S.seed, DMD_STREAM_GHOST, (uint64_t)g, k++);
@@ -1225,9 +1236,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             /* speculative commit of each event on its warp */
             const long long coll0 = sh.coll0;
             const double imax = sh.imax;
-            /* this CTA's events are warps 0 .. nloc-1 */
+            /* this CTA's events are warps 0 .. nloc-1; the free warps
+             * nloc .. NWARPS-1 take over the task preparation of up to two
+             * events each when that covers every event */
             const int nloc = P > rank ? (P - rank + C - 1) / C : 0;
-            const bool split = nloc <= NWARPS / 2;
+            const int nfree = NWARPS - nloc;
+            const bool split = nfree > 0 && 2 * nfree >= nloc;
             if (gw < P) {
                 int i = sh.sort_idx[gw];
                 int j = S.nptnr[i];
@@ -1245,16 +1259,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 /* the re-prediction's lists and tasks; the tasks go to the
                  * CTA's pool when they fit (one round of full
                  * re-predictions), else this warp runs them after the pool.
-                 * In a batch of at most NWARPS/2 events, a second warp
-                 * prepares them while this one computes the collision,
-                 * when the collision cannot change the H-bond state they
-                 * read (coltype 1-3). */
+                 * A free warp prepares them while this one computes the
+                 * collision, when the collision cannot change the H-bond
+                 * state they read (coltype 1-3). */
                 if (!(split && sh.c_simple[gw])) warp_rp_prepare(S, W, TP, warp, i, j, tf, imax);
-            } else if (split && warp >= NWARPS / 2 && warp - NWARPS / 2 < nloc &&
-                       sh.c_simple[(warp - NWARPS / 2) * C + rank]) {
-                const int k = warp - NWARPS / 2;
-                const int i = sh.sort_idx[k * C + rank];
-                warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
+            } else if (split) {
+                for (int k = warp - nloc; k < nloc; k += nfree) {
+                    const int ge = k * C + rank;
+                    if (!sh.c_simple[ge]) continue;
+                    const int i = sh.sort_idx[ge];
+                    warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
+                }
             }
             __syncthreads();
             /* every pooled prediction task of this CTA's events, all warps:
