@@ -283,13 +283,24 @@ __device__ __forceinline__ double d_wrap(double x) {
     if ((b & 0x7fffffffffffffffLL) < 0x3fe0000000000000LL && b != (long long)0x8000000000000000ULL) return x;
     return x - round(x);
 }
+/* x - round(x) (round half away from zero) as one subtraction where
+ * |x| < 1.5: round(x) is then +-0 (with the sign of x) or +-1, read from
+ * the bits, so a warp of pairs issues one FP64 instruction per component
+ * whether or not some lane wraps (neighbours are never a box and a half
+ * apart; larger |x| and NaN take the rounding) */
+__device__ __forceinline__ double d_wrap1(double x) {
+    const long long b = dbits(x), a = b & 0x7fffffffffffffffLL;
+    if (a >= 0x3ff8000000000000LL) return x - round(x);
+    const long long s = (a >= 0x3fe0000000000000LL ? 0x3ff0000000000000LL : 0LL) | (b & (long long)0x8000000000000000ULL);
+    return x - __longlong_as_double(s);
+}
 __device__ __forceinline__ Rel d_rel_c(const DSys &S, int i, int j, double tfalse) {
     Rel r;
     r.vx = S.vx[i] - S.vx[j]; r.vy = S.vy[i] - S.vy[j]; r.vz = S.vz[i] - S.vz[j];
     r.rx = S.x[i] - S.x[j] + r.vx * tfalse;
     r.ry = S.y[i] - S.y[j] + r.vy * tfalse;
     r.rz = S.z[i] - S.z[j] + r.vz * tfalse;
-    r.rx = d_wrap(r.rx); r.ry = d_wrap(r.ry); r.rz = d_wrap(r.rz);
+    r.rx = d_wrap1(r.rx); r.ry = d_wrap1(r.ry); r.rz = d_wrap1(r.rz);
     r.bij = r.rx * r.vx + r.ry * r.vy + r.rz * r.vz;
     r.rijsq = r.rx * r.rx + r.ry * r.ry + r.rz * r.rz;
     r.vijsq = r.vx * r.vx + r.vy * r.vy + r.vz * r.vz;

@@ -1210,27 +1210,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 }
                 csync(C);
                 DMD_PHASE(11);
-                if (leader && threadIdx.x == 0) {
-                    sh.bseq = sh.tick_reset ? 1 : sh.bseq + 1;
-                    /* the longest conflict-free prefix; an incomplete footprint
-                     * (cascade list overflow) ends the batch after its event */
+                /* every warp: the longest conflict-free prefix (candidate k
+                 * >= 1 whose footprint meets an earlier one ends it before
+                 * k); an incomplete footprint (cascade list overflow) ends
+                 * it after its event */
+                {
                     int p = m;
-                    for (int k = 0; k < m; ++k) {
-                        if (k > 0 && sh.c_conflict[k]) { p = k; break; }
-                        if (sh.c_over[k]) { p = k > 0 ? k : 1; break; }
+#pragma unroll
+                    for (int h = 0; h < CAND_MAX / 32; ++h) {
+                        const int k = lane + 32 * h;
+                        const unsigned cf = __ballot_sync(FULL, k > 0 && k < m && L->c_conflict[k]);
+                        const unsigned ov = __ballot_sync(FULL, k < m && L->c_over[k]);
+                        if (cf) p = min(p, 32 * h + __ffs(cf) - 1);
+                        if (ov) p = min(p, max(32 * h + __ffs(ov) - 1, 1));
                     }
-                    sh.P = p;
+                    P = p;
                 }
-                csync(C);
-                if (!leader) {
-                    if (threadIdx.x == 0) sh.P = L->P;
-                    if (threadIdx.x < NWARPS) {
-                        int k = threadIdx.x * C + rank;
-                        if (k < m) sh.c_simple[k] = L->c_simple[k];
-                    }
-                }
-                __syncthreads();
-                P = sh.P;
+                if (leader && threadIdx.x == 0) sh.bseq = sh.tick_reset ? 1 : sh.bseq + 1;
                 DMD_PHASE(2);
             }
             /* speculative commit of each event on its warp */
@@ -1262,11 +1258,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                  * A free warp prepares them while this one computes the
                  * collision, when the collision cannot change the H-bond
                  * state they read (coltype 1-3). */
-                if (!(split && sh.c_simple[gw])) warp_rp_prepare(S, W, TP, warp, i, j, tf, imax);
+                if (!(split && L->c_simple[gw])) warp_rp_prepare(S, W, TP, warp, i, j, tf, imax);
             } else if (split) {
                 for (int k = warp - nloc; k < nloc; k += nfree) {
                     const int ge = k * C + rank;
-                    if (!sh.c_simple[ge]) continue;
+                    if (!L->c_simple[ge]) continue;
                     const int i = sh.sort_idx[ge];
                     warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
                 }
