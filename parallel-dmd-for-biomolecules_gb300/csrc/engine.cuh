@@ -294,17 +294,27 @@ __device__ __forceinline__ double d_wrap1(double x) {
     const long long s = (a >= 0x3fe0000000000000LL ? 0x3ff0000000000000LL : 0LL) | (b & (long long)0x8000000000000000ULL);
     return x - __longlong_as_double(s);
 }
-__device__ __forceinline__ Rel d_rel_c(const DSys &S, int i, int j, double tfalse) {
+/* si, sj: the bead's position and velocity (x, y, z, vx, vy, vz) where they
+ * are not the current state (a snapshot), else null */
+__device__ __forceinline__ Rel d_rel_cv(const DSys &S, int i, int j, double tfalse, const double *si,
+                                        const double *sj) {
     Rel r;
-    r.vx = S.vx[i] - S.vx[j]; r.vy = S.vy[i] - S.vy[j]; r.vz = S.vz[i] - S.vz[j];
-    r.rx = S.x[i] - S.x[j] + r.vx * tfalse;
-    r.ry = S.y[i] - S.y[j] + r.vy * tfalse;
-    r.rz = S.z[i] - S.z[j] + r.vz * tfalse;
+    const double vxi = si ? si[3] : S.vx[i], vyi = si ? si[4] : S.vy[i], vzi = si ? si[5] : S.vz[i];
+    const double vxj = sj ? sj[3] : S.vx[j], vyj = sj ? sj[4] : S.vy[j], vzj = sj ? sj[5] : S.vz[j];
+    const double xi = si ? si[0] : S.x[i], yi = si ? si[1] : S.y[i], zi = si ? si[2] : S.z[i];
+    const double xj = sj ? sj[0] : S.x[j], yj = sj ? sj[1] : S.y[j], zj = sj ? sj[2] : S.z[j];
+    r.vx = vxi - vxj; r.vy = vyi - vyj; r.vz = vzi - vzj;
+    r.rx = xi - xj + r.vx * tfalse;
+    r.ry = yi - yj + r.vy * tfalse;
+    r.rz = zi - zj + r.vz * tfalse;
     r.rx = d_wrap1(r.rx); r.ry = d_wrap1(r.ry); r.rz = d_wrap1(r.rz);
     r.bij = r.rx * r.vx + r.ry * r.vy + r.rz * r.vz;
     r.rijsq = r.rx * r.rx + r.ry * r.ry + r.rz * r.rz;
     r.vijsq = r.vx * r.vx + r.vy * r.vy + r.vz * r.vz;
     return r;
+}
+__device__ __forceinline__ Rel d_rel_c(const DSys &S, int i, int j, double tfalse) {
+    return d_rel_cv(S, i, j, tfalse, nullptr, nullptr);
 }
 
 /* ------------------------------------------------------------------ */
@@ -332,12 +342,17 @@ __device__ __forceinline__ unsigned d_hi(const double *p) { return reinterpret_c
  * normal float range (zeros) decide nothing.  Bond pairs (always an
  * event), bonded H-bond pairs and invalid codes are not screened.  tf_hi
  * is the high word of tfalse. */
-__device__ __forceinline__ bool f32_no_event(const DSys &S, int i, int j, int evcode, unsigned tf_hi) {
-    /* every load first: positions and velocities, identities, H-bond partner */
+__device__ __forceinline__ bool f32_no_event(const DSys &S, int i, int j, int evcode, unsigned tf_hi,
+                                             const double *si = nullptr, const double *sj = nullptr) {
+    /* every load first: positions and velocities (or the snapshots si, sj,
+     * as in d_rel_cv), identities, H-bond partner */
     unsigned h[12];
     const double *P[6] = {S.x, S.y, S.z, S.vx, S.vy, S.vz};
 #pragma unroll
-    for (int k = 0; k < 6; ++k) { h[2 * k] = d_hi(P[k] + i); h[2 * k + 1] = d_hi(P[k] + j); }
+    for (int k = 0; k < 6; ++k) {
+        h[2 * k] = si ? d_hi(si + k) : d_hi(P[k] + i);
+        h[2 * k + 1] = sj ? d_hi(sj + k) : d_hi(P[k] + j);
+    }
     const int a = S.ident[i], b = S.ident[j];
     const bool core = evcode <= 3 || (evcode >= 17 && evcode <= 26);
     const bool well = evcode == 15 || evcode == 16 || evcode >= 40;
@@ -404,9 +419,10 @@ __device__ __forceinline__ bool f32_no_event(const DSys &S, int i, int j, int ev
 #define PK_STAGE2 4
 
 __device__ __forceinline__ bool d_predict_c(const DSys &S, int i, int j, int evcode, double tfalse,
-                                            double &tij, int &type) {
+                                            double &tij, int &type, const double *si = nullptr,
+                                            const double *sj = nullptr) {
     const DTab &T = *S.tab;
-    Rel r = d_rel_c(S, i, j, tfalse);
+    Rel r = d_rel_cv(S, i, j, tfalse, si, sj);
     int a = S.ident[i], b = S.ident[j];
     bool neg = d_lt0(r.bij);
     bool valid = true;

@@ -698,11 +698,38 @@ __device__ __forceinline__ void rp_task(const DSys &S, const WarpArea &W, int q,
 /* one prediction task: ev_code(l, source) for a down operation, ev_code(m, b)
  * for a full one; the time is tij + tfalse for a down operation and tij for
  * a full one (tfalse is added after its minimum; x + (-0.0) == x) */
+/* Reads of a light batch.  In a batch whose events are all bond or core
+ * events (coltype 1-3), an event writes only the positions and velocities
+ * of its own two beads, during its collision, before any re-prediction
+ * runs.  A re-prediction of event e that reads a bead written by an earlier
+ * event of the batch then sees its new state, as in the serial order; one
+ * that reads a bead written by a later event must see its state before the
+ * batch - the later event's snapshot.  So those reads are no conflict, and
+ * the footprints of light batches hold only the written beads and the
+ * queue entries.  The writer of a bead is the earliest claimer of it in
+ * the write table (two writers of one bead conflict). */
+struct Ver {
+    const unsigned *own_w;   /* write table of the batch, or null: current state */
+    const WarpArea *wa;      /* the events' areas (C = 1: slot = warp) */
+    unsigned tseq;           /* ticket sequence of the batch */
+    int e, P;                /* the reading event's slot, the batch size */
+};
+__device__ __forceinline__ const double *ver_of(const Ver &V, int b) {
+    if (!V.own_w || b < 0) return nullptr;
+    const unsigned t = V.own_w[b];
+    if ((t >> 6) != V.tseq) return nullptr;
+    const int g = 63 - (int)(t & 63u);
+    if (g <= V.e || g >= V.P) return nullptr;
+    const WarpArea &G = V.wa[g];
+    return G.sij + (G.i == b ? 0 : 6);
+}
+
 __device__ __forceinline__ bool rp_predict_code(const DSys &S, Err E, int pa, int pbb, int code, bool is_op,
-                                                double tf, double &tt, int &ty) {
+                                                double tf, double &tt, int &ty, const double *si = nullptr,
+                                                const double *sj = nullptr) {
     double tij = 0.0;
     ty = 0;
-    bool ok = d_predict_c(S, pa, pbb, code, tf, tij, ty);
+    bool ok = d_predict_c(S, pa, pbb, code, tf, tij, ty, si, sj);
 #ifdef DMD_PHASE_TIMERS
     {   /* double-precision predictions: all, no event while separating, no event while approaching */
         unsigned long long *cnt = (unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 2][0];
@@ -720,8 +747,10 @@ __device__ __forceinline__ int rp_code(const DSys &S, int pa, int pbb, int st, b
     return st >= 0 ? pair_code_st(S, a1, a2, st) : pair_code(S, a1, a2, hbonds);
 }
 __device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb, int st, bool is_op, double tf,
-                                           int hbonds, double &tt, int &ty) {
-    if (pa >= 0) return rp_predict_code(S, E, pa, pbb, rp_code(S, pa, pbb, st, is_op, hbonds), is_op, tf, tt, ty);
+                                           int hbonds, double &tt, int &ty, const Ver &V) {
+    if (pa >= 0)
+        return rp_predict_code(S, E, pa, pbb, rp_code(S, pa, pbb, st, is_op, hbonds), is_op, tf, tt, ty,
+                               ver_of(V, pa), ver_of(V, pbb));
     ty = 0;
     tt = 0.0 + (is_op ? tf : -0.0);
     return false;
@@ -754,7 +783,7 @@ __device__ void warp_rp_prepare(const DSys &S, WarpArea &W, TaskPool &TP, int ow
 }
 
 /* 4: the tasks of the round on this warp, 32 per pass */
-__device__ void warp_rp_tasks(const DSys &S, Err E, WarpArea &W, int rd, double tf, int hbonds) {
+__device__ void warp_rp_tasks(const DSys &S, Err E, WarpArea &W, int rd, double tf, int hbonds, const Ver &V) {
     int lane = threadIdx.x & 31;
     const int nop = rd == 0 ? W.nops : 0;
     const int ntask = W.ntask;
@@ -764,7 +793,7 @@ __device__ void warp_rp_tasks(const DSys &S, Err E, WarpArea &W, int rd, double 
         if (q < ntask) rp_task(S, W, q, nop, pa, pbb, st, tgt);
         double tt;
         int ty;
-        bool ok = rp_predict(S, E, pa, pbb, st, q < nop, tf, hbonds, tt, ty);
+        bool ok = rp_predict(S, E, pa, pbb, st, q < nop, tf, hbonds, tt, ty, V);
         if (q < nop) { W.op_t[q] = tt; W.op_y[q] = ok ? (int8_t)ty : (int8_t)-128; }
         /* segmented minimum of the full tasks, segment = target */
         long long k = (tgt >= 0 && ok) ? okey(tt) : DMD_KEY_INF;
@@ -873,7 +902,7 @@ __device__ void warp_rp_tnew(WarpArea &W) {
 }
 
 __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, double tf, double imax,
-                               int hbonds) {
+                               int hbonds, const Ver &V) {
     warp_rp_lists(S, W, i, j);
     DMD_SUB(3);
     const double Hraw = imax + DMD_LTSTEP - tf;   /* eventredo_up's starting time */
@@ -884,7 +913,7 @@ __device__ void warp_repredict(const DSys &S, Err E, WarpArea &W, int i, int j, 
     for (int rd = 0; rd < rounds; ++rd) {
         warp_rp_targets(S, W, i, j, rd, Hraw, Hkey);
         DMD_SUB(4);
-        warp_rp_tasks(S, E, W, rd, tf, hbonds);
+        warp_rp_tasks(S, E, W, rd, tf, hbonds, V);
         DMD_SUB(5);
         warp_rp_finish(S, E, W, i, j, rd, tf, imax);
     }
@@ -1045,6 +1074,57 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
     __syncwarp();
     DMD_SUB(11);
 }
+/* The footprint of an event of a light batch (every event of coltype 1-3):
+ * R = W = {i, j}, the beads its collision reads and writes (its
+ * re-prediction reads others through Ver); Q as in the full footprint -
+ * i, j, the lower extras, the own helpers and both down lists. */
+__device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int N = S.N;
+    unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
+    int nq = 0;
+    auto put = [&](int *arr, int cap, int &n, bool pred, int b) {
+        unsigned m = __ballot_sync(FULL, pred);
+        int pos = n + __popc(m & lt);
+        if (pred && pos < cap) arr[pos] = b;
+        n += __popc(m);
+    };
+    if (lane < 2) {
+        const int b = lane == 0 ? i : j;
+        atomicMax(&own_r[b], ticket);
+        atomicMax(&own_w[b], ticket);
+        W.rset[lane] = b;
+        W.wset[lane] = b;
+    }
+    {
+        int b = -1;
+        if (lane < 2) b = lane == 0 ? i : j;
+        else if (lane < 5) b = S.er[4 * i + lane - 2];
+        else if (lane >= 6 && lane < 9) b = S.er[4 * j + lane - 6];
+        else if (lane >= 10 && lane < 14) {
+            int x = lane < 12 ? i : j, h1, h2;
+            own_helpers(S, x, h1, h2);
+            b = (lane & 1) ? h2 : h1;
+        }
+        const bool q = b >= 0;
+        if (q) atomicMax(&own_q[b], ticket);
+        put(W.qset, QSET_MAX, nq, q, b);
+    }
+    const int di = S.dnn[i], dj = S.dnn[j];
+    const int *DI = S.dn + (size_t)i * S.cap, *DJ = S.dn + (size_t)j * S.cap;
+    for (int base = 0; base < di + dj; base += 32) {
+        const int q = base + lane;
+        const int l = q < di ? DI[q] : (q < di + dj ? DJ[q - di] : -1);
+        if (l >= 0) atomicMax(&own_q[l], ticket);
+        put(W.qset, QSET_MAX, nq, l >= 0, l);
+    }
+    if (lane == 0) {
+        W.nrset = 2; W.nwset = 2; W.nqset = nq;
+        W.casc_over = nq > QSET_MAX;
+    }
+    __syncwarp();
+}
 __device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, int N, unsigned ticket) {
     int lane = threadIdx.x & 31;
     const volatile unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
@@ -1186,6 +1266,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             /* ---- a batch of pair events ---- */
             const int m = sh.m;
             int P = 1;
+            bool light = false;       /* reads of later events' beads go to their snapshots */
+            unsigned tseq = 0;
             if (m > 1) {
                 if (sh.tick_reset) {   /* tickets exhausted: clear the table */
                     for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
@@ -1194,9 +1276,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     __syncthreads();
                 }
                 unsigned ticket = ((unsigned)(sh.bseq + 1) << 6) | (unsigned)(63 - gw);
+                tseq = ticket >> 6;
+                /* a light batch: one CTA, every candidate of coltype 1-3 */
+                {
+                    bool heavy = false;
+                    for (int k = lane; k < m; k += 32) {
+                        const int ct0 = S.colt[sh.sort_idx[k]];
+                        heavy |= ct0 < 1 || ct0 > 3;
+                    }
+                    light = C == 1 && !__any_sync(FULL, heavy);
+                }
                 if (gw < m) {
                     int i = sh.sort_idx[gw];
-                    warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
+                    if (light) warp_footprint_claim_light(S, W, own, ticket, i, S.nptnr[i]);
+                    else warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
                 }
                 csync(C);
                 DMD_PHASE(10);
@@ -1289,9 +1382,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                         } else {
                             const int pbb = TP.b[q];
                             const bool is_op = (TP.flag[q] & 1) != 0;
-                            const WarpArea &O = warea[TP.flag[q] >> 1];
+                            const int owner = TP.flag[q] >> 1;
+                            const WarpArea &O = warea[owner];
                             const int code = rp_code(S, pa, pbb, TP.st[q], is_op, hbonds);
-                            if (f32_no_event(S, pa, pbb, code, d_hi(&O.tf))) {
+                            const Ver V{light ? own + N : nullptr, warea, tseq, owner, P};
+                            if (f32_no_event(S, pa, pbb, code, d_hi(&O.tf), ver_of(V, pa), ver_of(V, pbb))) {
                                 TP.t[q] = is_op ? O.big_tf : DMD_BIG;
                                 TP.ty[q] = 0;
                                 TP.ok[q] = 1;
@@ -1320,7 +1415,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     Err EO{&O.err, &O.err_info};
                     double tt;
                     int ty;
-                    bool ok = rp_predict_code(S, EO, TP.a[q], TP.b[q], TP.st[q], (TP.flag[q] & 1) != 0, O.tf, tt, ty);
+                    const Ver V{light ? own + N : nullptr, warea, tseq, owner, P};
+                    bool ok = rp_predict_code(S, EO, TP.a[q], TP.b[q], TP.st[q], (TP.flag[q] & 1) != 0, O.tf, tt, ty,
+                                              ver_of(V, TP.a[q]), ver_of(V, TP.b[q]));
                     TP.t[q] = tt; TP.ty[q] = (int8_t)ty; TP.ok[q] = ok;
                 }
             }
@@ -1355,7 +1452,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     warp_rp_finish(S, E, W, i, j, 0, tf, imax);
                     warp_rp_tnew(W);
                 } else {
-                    warp_repredict(S, E, W, i, j, tf, imax, hbonds);
+                    warp_repredict(S, E, W, i, j, tf, imax, hbonds, Ver{light ? own + N : nullptr, warea, tseq, warp, P});
                 }
 #ifdef DMD_PHASE_TIMERS
                 if (lane == 0) atomicAdd((unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 2][W.pooled ? 5 : 4], 1ull);
@@ -1432,7 +1529,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 int i = W.i;
                 tf = W.tf;
                 DMD_SUB(-1);
-                warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds);
+                warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds, Ver{nullptr, warea, 0u, 0, 0});
                 warp_commit_preds(S, W);
                 if (lane == 0) {
                     W.pb[W.npred] = N;   /* the ghost entry itself */
