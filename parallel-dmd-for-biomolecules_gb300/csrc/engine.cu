@@ -157,6 +157,7 @@ struct SharedState {
     double imax, tnow, tf_iv;
     int c_conflict[CAND_MAX], c_over[CAND_MAX];
     int8_t c_simple[CAND_MAX];    /* the event's collision cannot change H-bond state (coltype 1-3) */
+    int8_t c_qbad[CAND_MAX];      /* light batch: the event read a queue entry an earlier one changed */
     long long c_tnew_key[CAND_MAX];
     int c_tnew_idx[CAND_MAX], c_err[CAND_MAX], c_err_info[CAND_MAX], c_ct[CAND_MAX];
     double c_tf[CAND_MAX];

@@ -887,7 +887,7 @@ __device__ void warp_rp_tnew(WarpArea &W) {
     int bb = INT_MAX;
     for (int q = lane; q < W.npred; q += 32) {
         int b = W.pb[q];
-        if (b < 0 || !W.pq[q]) continue;
+        if (b < 0 || (W.pq[q] & 3) != 1) continue;   /* queued and changed */
         long long kk = okey(W.pt[q]);
         if (key_less(kk, b, bk, bb)) { bk = kk; bb = b; }
     }
@@ -926,7 +926,8 @@ __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
     for (int q = lane; q < W.npred; q += 32) {
         int b = W.pb[q];
         if (b < 0) continue;
-        set_pred(S, b, W.pt[q], W.pn[q], W.pc[q], W.pq[q] != 0);
+        if (W.pq[q] & 2) continue;   /* unchanged (light batches) */
+        set_pred(S, b, W.pt[q], W.pn[q], W.pc[q], (W.pq[q] & 1) != 0);
     }
     __syncwarp();
 }
@@ -1075,14 +1076,18 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
     DMD_SUB(11);
 }
 /* The footprint of an event of a light batch (every event of coltype 1-3):
- * R = W = {i, j}, the beads its collision reads and writes (its
- * re-prediction reads others through Ver); Q as in the full footprint -
- * i, j, the lower extras, the own helpers and both down lists. */
+ * R = W = {i, j}, the beads its collision reads and writes; its
+ * re-prediction reads other beads through Ver.  Its bead pair i, j is also
+ * claimed in the queue table, and Q lists the queue entries it reads (i,
+ * j, the lower extras, both down lists): a later event that reads an
+ * earlier one's i or j ends the batch before it (those entries always
+ * change).  Other entries it reads are checked after the fact
+ * (warp_mark_queue, warp_check_queue): an event that read an entry an
+ * earlier event of the batch changed is rolled back. */
 __device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int N = S.N;
-    unsigned *own_r = own, *own_w = own + N, *own_q = own + 2 * N;
     int nq = 0;
     auto put = [&](int *arr, int cap, int &n, bool pred, int b) {
         unsigned m = __ballot_sync(FULL, pred);
@@ -1092,31 +1097,24 @@ __device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned 
     };
     if (lane < 2) {
         const int b = lane == 0 ? i : j;
-        atomicMax(&own_r[b], ticket);
-        atomicMax(&own_w[b], ticket);
+        atomicMax(&own[b], ticket);
+        atomicMax(&own[N + b], ticket);
+        atomicMax(&own[2 * N + b], ticket);
         W.rset[lane] = b;
         W.wset[lane] = b;
     }
     {
         int b = -1;
         if (lane < 2) b = lane == 0 ? i : j;
-        else if (lane < 5) b = S.er[4 * i + lane - 2];
-        else if (lane >= 6 && lane < 9) b = S.er[4 * j + lane - 6];
-        else if (lane >= 10 && lane < 14) {
-            int x = lane < 12 ? i : j, h1, h2;
-            own_helpers(S, x, h1, h2);
-            b = (lane & 1) ? h2 : h1;
-        }
-        const bool q = b >= 0;
-        if (q) atomicMax(&own_q[b], ticket);
-        put(W.qset, QSET_MAX, nq, q, b);
+        else if (lane < 5) { b = S.er[4 * i + lane - 2]; if (b >= i) b = -1; }
+        else if (lane >= 6 && lane < 9) { b = S.er[4 * j + lane - 6]; if (b >= j) b = -1; }
+        put(W.qset, QSET_MAX, nq, b >= 0, b);
     }
     const int di = S.dnn[i], dj = S.dnn[j];
     const int *DI = S.dn + (size_t)i * S.cap, *DJ = S.dn + (size_t)j * S.cap;
     for (int base = 0; base < di + dj; base += 32) {
         const int q = base + lane;
         const int l = q < di ? DI[q] : (q < di + dj ? DJ[q - di] : -1);
-        if (l >= 0) atomicMax(&own_q[l], ticket);
         put(W.qset, QSET_MAX, nq, l >= 0, l);
     }
     if (lane == 0) {
@@ -1124,6 +1122,33 @@ __device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned 
         W.casc_over = nq > QSET_MAX;
     }
     __syncwarp();
+}
+/* light batches, after the re-predictions: the queue entries this event
+ * changes (i and j always; the others where the new entry differs from the
+ * current one) are marked with its ticket in own_q; the others are flagged
+ * in W.pq (bit 1) and not written at the commit */
+__device__ void warp_mark_queue(const DSys &S, WarpArea &W, unsigned *own_q, unsigned ticket) {
+    const int lane = threadIdx.x & 31;
+    for (int q = lane; q < W.npred; q += 32) {
+        const int b = W.pb[q];
+        if (b < 0) continue;
+        const bool changed = q < 2 || dbits(W.pt[q]) != dbits(S.tim[b]) || W.pn[q] != S.nptnr[b] ||
+                             W.pc[q] != S.colt[b] || (W.pq[q] & 1) != (S.queued[b] != 0 ? 1 : 0);
+        if (changed) atomicMax(&own_q[b], ticket);
+        else W.pq[q] |= 2;
+    }
+    __syncwarp();
+}
+/* ... and, once every event has marked: whether an earlier event of the
+ * batch changed an entry this one read */
+__device__ bool warp_check_queue(const WarpArea &W, const volatile unsigned *own_q, unsigned ticket) {
+    const int lane = threadIdx.x & 31;
+    bool bad = false;
+    for (int q = lane; q < W.npred; q += 32) {
+        const int b = W.pb[q];
+        if (b >= 0) bad |= own_q[b] > ticket;
+    }
+    return __any_sync(FULL, bad);
 }
 __device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *own, int N, unsigned ticket) {
     int lane = threadIdx.x & 31;
@@ -1267,7 +1292,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             const int m = sh.m;
             int P = 1;
             bool light = false;       /* reads of later events' beads go to their snapshots */
-            unsigned tseq = 0;
+            unsigned tseq = 0, my_ticket = 0;
             if (m > 1) {
                 if (sh.tick_reset) {   /* tickets exhausted: clear the table */
                     for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
@@ -1277,6 +1302,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 }
                 unsigned ticket = ((unsigned)(sh.bseq + 1) << 6) | (unsigned)(63 - gw);
                 tseq = ticket >> 6;
+                my_ticket = ticket;
                 /* a light batch: one CTA, every candidate of coltype 1-3 */
                 {
                     bool heavy = false;
@@ -1462,6 +1488,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     if (S.ident[i] < S.ident[j]) repuls_del_b(S, i, j); else repuls_del_b(S, j, i);
                 }
                 __syncwarp();
+                if (light) {
+                    /* the changed entries only are new: the earliest of them */
+                    warp_mark_queue(S, W, own + 2 * N, my_ticket);
+                    warp_rp_tnew(W);
+                }
                 if (lane == 0) {
                     L->c_tnew_key[gw] = W.tnew_key; L->c_tnew_idx[gw] = W.tnew_idx;
                     L->c_err[gw] = W.err; L->c_err_info[gw] = W.err_info;
@@ -1470,6 +1501,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             }
             if (threadIdx.x == 0) TP.n = 0;   /* the pool is free until the next batch */
             csync(C);
+            if (light) {
+                if (gw < P) {
+                    const bool bad = warp_check_queue(W, own + 2 * N, my_ticket);
+                    if (lane == 0) L->c_qbad[gw] = bad;
+                }
+                csync(C);
+            }
             DMD_PHASE(3);
             /* validation: event k stands if it precedes every new entry of
              * events 0..k-1; the leader also books the committed events */
@@ -1479,6 +1517,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 int bb = INT_MAX;
                 for (int k = 0; k < P; ++k) {
                     if (k > 0 && !key_less(sh.sort_key[k], sh.sort_idx[k], bk, bb)) { v = k; break; }
+                    /* light batches: it read a queue entry an earlier event changed */
+                    if (k > 0 && light && sh.c_qbad[k]) { v = k; break; }
                     if (sh.c_err[k]) {   /* the run stops after the first event in error */
                         set_err(sh, sh.c_err[k], sh.c_err_info[k]);
                         v = k + 1;
@@ -1506,7 +1546,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             __syncthreads();
             DMD_PHASE(4);
             const int V = sh.V;
-            if (gw < P) {
+            if (light) {
+                /* a rolled-back event restores its bead i's coltype, which a
+                 * standing earlier event may rewrite: restores land first */
+                if (gw < P && gw >= V) warp_restore(S, W);
+                csync(C);
+                if (gw < V) {
+                    warp_commit_preds(S, W);
+                    if (lane == 0) log_event(S, sh.log0 + gw, W.coll, sh.tnow, W.tf, W.i, W.j, W.ct, W.evcode);
+                }
+            } else if (gw < P) {
                 if (gw < V) {
                     warp_commit_preds(S, W);
                     if (lane == 0) log_event(S, sh.log0 + gw, W.coll, sh.tnow, W.tf, W.i, W.j, W.ct, W.evcode);
