@@ -1075,6 +1075,7 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
             kk[h] = c < nc ? sh.cand_key[c] : DMD_KEY_INF;
             ee[h] = c < nc ? sh.cand_idx[c] : INT_MAX;
         }
+#pragma unroll 4
         for (int u = 0; u < nc; ++u) {
             const long long ku = sh.cand_key[u];
             const int eu = sh.cand_idx[u];

@@ -470,6 +470,84 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
 /* ------------------------------------------------------------------ */
 /* re-prediction into the warp's buffer (code/partial_events.f)         */
 /* ------------------------------------------------------------------ */
+/* The ghost collision of lane_ghost() on a warp, with the same draws and
+ * arithmetic: the lanes draw the counter-based uniforms of the bead choice,
+ * of the two accept/reject pairs and of the next ghost time in parallel
+ * and ballots find the first accepted of each; the two square roots and
+ * the three logarithms run on three lanes, the three velocity components
+ * on three lanes.  If 32 draws do not settle a choice (never in practice),
+ * lane 0 runs lane_ghost() itself. */
+__device__ int warp_ghost(const DSys &S, SharedState &sh, double &tfalse) {
+    const int lane = threadIdx.x & 31;
+    const DTab &T = *S.tab;
+    const int N = S.N;
+    const uint64_t g = (uint64_t)sh.sc.ghost_index;
+    /* the bead: the first draw k with (int)(u * N) + 1 != N + 1 */
+    const int iv = (int)(dmd_uniform(S.seed, DMD_STREAM_GHOST, g, (uint32_t)lane) * N) + 1;
+    const unsigned mi = __ballot_sync(FULL, iv != N + 1);
+    bool fallback = mi == 0;
+    int i = 0, k = 0;
+    if (!fallback) { const int k0 = __ffs(mi) - 1; i = __shfl_sync(FULL, iv, k0); k = k0 + 1; }
+    /* two accepted pairs (v1, v2) from draws k, k+1, ... */
+    double v1a = 0, v2a = 0, ra = 0, v1b = 0, rb = 0;
+    for (int pair = 0; pair < 2 && !fallback; ++pair) {
+        const double v1 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, g, (uint32_t)(k + 2 * lane)) - 1.0;
+        const double v2 = 2.0 * dmd_uniform(S.seed, DMD_STREAM_GHOST, g, (uint32_t)(k + 2 * lane + 1)) - 1.0;
+        const double r = v1 * v1 + v2 * v2;
+        const unsigned ma = __ballot_sync(FULL, !((r == 0.0) || (r >= 1.0)));
+        if (ma == 0) { fallback = true; break; }
+        const int p = __ffs(ma) - 1;
+        const double w1 = __shfl_sync(FULL, v1, p), w2 = __shfl_sync(FULL, v2, p), wr = __shfl_sync(FULL, r, p);
+        if (pair == 0) { v1a = w1; v2a = w2; ra = wr; } else { v1b = w1; rb = wr; }
+        k += 2 * (p + 1);
+    }
+    /* the next ghost time: the first draw not below 1e-18 and not 1 */
+    double tg = 0.0;
+    if (!fallback) {
+        const double u = dmd_uniform(S.seed, DMD_STREAM_GHOST, g, (uint32_t)(k + lane));
+        const unsigned mt = __ballot_sync(FULL, !((u < 1e-18) || (u == 1.0)));
+        if (mt == 0) fallback = true;
+        else tg = __shfl_sync(FULL, u, __ffs(mt) - 1);
+    }
+    if (fallback) {
+        int ii = 0;
+        double tf = tfalse;
+        if (lane == 0) ii = lane_ghost(S, sh, tf);
+        __syncwarp();
+        tfalse = __shfl_sync(FULL, tf, 0);
+        return __shfl_sync(FULL, ii, 0);
+    }
+    if (i > N) i = N;
+    i -= 1;
+    const double bmi = S.bm[i], rbmi = T.rbm[S.ident[i]];   /* bm(i) = mass(identity(i)) */
+    /* lanes 0, 1: the two factors; lane 2: the next ghost time */
+    const double lx = lane == 0 ? ra : (lane == 1 ? rb : tg);
+    const double L = dmd_log(lx);
+    double fact = 0.0, tn = 0.0;
+    if (lane < 2) fact = sqrt(-2.0 * T.setemp * bmi * L / lx);
+    else if (lane == 2) tn = -1.0 * L * T.avegtime + tfalse;
+    const double fa = __shfl_sync(FULL, fact, 0), fb = __shfl_sync(FULL, fact, 1);
+    tn = __shfl_sync(FULL, tn, 2);
+    /* lanes 0..2: one component each, in the reference's order */
+    if (lane < 3) {
+        double *P = lane == 0 ? S.x : (lane == 1 ? S.y : S.z);
+        double *V = lane == 0 ? S.vx : (lane == 1 ? S.vy : S.vz);
+        double x = P[i] + V[i] * tfalse;
+        const double num = lane == 0 ? v1a * fa : (lane == 1 ? v2a * fa : v1b * fb);
+        const double v = div_by(num, bmi, rbmi);
+        V[i] = v;
+        P[i] = x - v * tfalse;
+    }
+    if (lane == 0) {
+        sh.sc.ghost_index += 1;
+        sh.sc.n_ghost += 1;
+        set_pred(S, N, tn, -2, -2, tn < sh.sc.interval_max);
+    }
+    __syncwarp();
+    if (tfalse < sh.sc.old_tfalse) tfalse = sh.sc.old_tfalse;
+    return i;
+}
+
 __device__ __forceinline__ bool check_tij(Err E, double tij, int i) {
     /* reference debug check: negative time beyond 1e-10 (code/eventredo_up.f:58-74) */
     if (tij < 0.0 && fabs(tij) > 1.0e-10) { set_err(E, DMD_E_NEG_TIME, i); return false; }
@@ -856,6 +934,9 @@ __device__ void warp_rp_finish(const DSys &S, Err E, WarpArea &W, int i, int j, 
         bool qq;
         if (l == i) { t = W.fs.tg_raw[0]; p = W.fs.tg_p[0]; y = W.fs.tg_y[0]; qq = okey(t) < imax_key; }
         else { t = S.tim[l]; p = S.nptnr[l]; y = S.colt[l]; qq = S.queued[l] != 0; }
+        const long long t0 = dbits(t);
+        const int p0 = p, y0 = y;
+        const bool q0 = qq;
         for (int pp = W.lead_q[ld]; pp < n; ++pp) {
             if (W.ops_l[pp] != l) continue;
             int src = W.ops_s[pp];
@@ -873,8 +954,10 @@ __device__ void warp_rp_finish(const DSys &S, Err E, WarpArea &W, int i, int j, 
             W.pb[slot] = -1;
             W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq;
         } else {
+            /* bit 1 of pq: the entry is unchanged (not new, not written) */
+            const bool same = dbits(t) == t0 && p == p0 && y == y0 && qq == q0;
             W.pb[slot] = l;
-            W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = qq;
+            W.pt[slot] = t; W.pn[slot] = p; W.pc[slot] = (int8_t)y; W.pq[slot] = (uint8_t)(qq | (same ? 2 : 0));
         }
     }
     __syncwarp();
@@ -926,7 +1009,7 @@ __device__ void warp_commit_preds(const DSys &S, const WarpArea &W) {
     for (int q = lane; q < W.npred; q += 32) {
         int b = W.pb[q];
         if (b < 0) continue;
-        if (W.pq[q] & 2) continue;   /* unchanged (light batches) */
+        if (W.pq[q] & 2) continue;   /* unchanged */
         set_pred(S, b, W.pt[q], W.pn[q], W.pc[q], (W.pq[q] & 1) != 0);
     }
     __syncwarp();
@@ -1124,18 +1207,14 @@ __device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned 
     __syncwarp();
 }
 /* light batches, after the re-predictions: the queue entries this event
- * changes (i and j always; the others where the new entry differs from the
- * current one) are marked with its ticket in own_q; the others are flagged
- * in W.pq (bit 1) and not written at the commit */
-__device__ void warp_mark_queue(const DSys &S, WarpArea &W, unsigned *own_q, unsigned ticket) {
+ * changes (i and j always; the others where the replay's result differs
+ * from the entry it started from, W.pq bit 1 clear) are marked with its
+ * ticket in own_q */
+__device__ void warp_mark_queue(const WarpArea &W, unsigned *own_q, unsigned ticket) {
     const int lane = threadIdx.x & 31;
     for (int q = lane; q < W.npred; q += 32) {
         const int b = W.pb[q];
-        if (b < 0) continue;
-        const bool changed = q < 2 || dbits(W.pt[q]) != dbits(S.tim[b]) || W.pn[q] != S.nptnr[b] ||
-                             W.pc[q] != S.colt[b] || (W.pq[q] & 1) != (S.queued[b] != 0 ? 1 : 0);
-        if (changed) atomicMax(&own_q[b], ticket);
-        else W.pq[q] |= 2;
+        if (b >= 0 && !(W.pq[q] & 2)) atomicMax(&own_q[b], ticket);
     }
     __syncwarp();
 }
@@ -1476,7 +1555,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     }
                     __syncwarp();
                     warp_rp_finish(S, E, W, i, j, 0, tf, imax);
-                    warp_rp_tnew(W);
+                    if (!light) warp_rp_tnew(W);   /* light: after the marks below */
                 } else {
                     warp_repredict(S, E, W, i, j, tf, imax, hbonds, Ver{light ? own + N : nullptr, warea, tseq, warp, P});
                 }
@@ -1490,7 +1569,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 __syncwarp();
                 if (light) {
                     /* the changed entries only are new: the earliest of them */
-                    warp_mark_queue(S, W, own + 2 * N, my_ticket);
+                    warp_mark_queue(W, own + 2 * N, my_ticket);
                     warp_rp_tnew(W);
                 }
                 if (lane == 0) {
@@ -1570,13 +1649,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             /* ---- ghost collision: leader warp 0 ---- */
             if (leader && warp == 0) {
                 double tf = sh.tf_iv;
-                if (lane == 0) {
-                    int i = lane_ghost(S, sh, tf);
-                    W.i = i; W.tf = tf;
-                }
+                const int i = warp_ghost(S, sh, tf);
+                if (lane == 0) { W.i = i; W.tf = tf; }
                 __syncwarp();
-                int i = W.i;
-                tf = W.tf;
                 DMD_SUB(-1);
                 warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds, Ver{nullptr, warea, 0u, 0, 0});
                 warp_commit_preds(S, W);
