@@ -212,15 +212,18 @@ __device__ __forceinline__ void set_pred(const DSys &S, int b, double t, int p, 
 __device__ void l1_update(const DSys &S, int g, int NE) {
     int lo = g * 32, n = min(32, NE - lo);
     long long k[32];
+    int ix[32];
 #pragma unroll
-    for (int q = 0; q < 32; ++q) k[q] = q < n ? S.key[lo + q] : DMD_KEY_INF;
-    int best = 0;
-    long long bk = k[0];
+    for (int q = 0; q < 32; ++q) { k[q] = q < n ? S.key[lo + q] : DMD_KEY_INF; ix[q] = q; }
+    /* pairwise tree, the left entry winning ties: the first minimum, as a
+     * left-to-right scan finds it, in five levels instead of 31 steps */
 #pragma unroll
-    for (int q = 1; q < 32; ++q)
-        if (k[q] < bk) { bk = k[q]; best = q; }
-    S.l1i[g] = lo + best;
-    S.l1k[g] = bk;
+    for (int w = 1; w < 32; w <<= 1)
+#pragma unroll
+        for (int q = 0; q + w < 32; q += 2 * w)
+            if (k[q + w] < k[q]) { k[q] = k[q + w]; ix[q] = ix[q + w]; }
+    S.l1i[g] = lo + ix[0];
+    S.l1k[g] = k[0];
 }
 __device__ void l2_update(const DSys &S, int h) {
     int lo = h * 32, n = min(32, S.nl1 - lo);

@@ -1590,20 +1590,49 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             DMD_PHASE(3);
             /* validation: event k stands if it precedes every new entry of
              * events 0..k-1; the leader also books the committed events */
+            int Vw = P;
+            const bool vwarp = C == 1 && P <= 32;
+            if (vwarp) {
+                /* every warp: a prefix minimum of the events' new entries by
+                 * a scan, then the first event that fails */
+                const bool in = lane < P;
+                long long bk = in ? sh.c_tnew_key[lane] : DMD_KEY_INF;
+                int bb = in ? sh.c_tnew_idx[lane] : INT_MAX;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long k2 = __shfl_up_sync(FULL, bk, o);
+                    const int b2 = __shfl_up_sync(FULL, bb, o);
+                    if (lane >= o && key_less(k2, b2, bk, bb)) { bk = k2; bb = b2; }
+                }
+                long long ek = __shfl_up_sync(FULL, bk, 1);
+                int eb = __shfl_up_sync(FULL, bb, 1);
+                int cand = P;
+                if (in && lane > 0 &&
+                    (!key_less(sh.sort_key[lane], sh.sort_idx[lane], ek, eb) || (light && sh.c_qbad[lane])))
+                    cand = lane;
+                else if (in && sh.c_err[lane])
+                    cand = lane + 1;   /* the run stops after the first event in error */
+                Vw = __reduce_min_sync(FULL, cand);
+            }
             if (leader && threadIdx.x == 0) {
                 int v = P;
-                long long bk = DMD_KEY_INF;
-                int bb = INT_MAX;
-                for (int k = 0; k < P; ++k) {
-                    if (k > 0 && !key_less(sh.sort_key[k], sh.sort_idx[k], bk, bb)) { v = k; break; }
-                    /* light batches: it read a queue entry an earlier event changed */
-                    if (k > 0 && light && sh.c_qbad[k]) { v = k; break; }
-                    if (sh.c_err[k]) {   /* the run stops after the first event in error */
-                        set_err(sh, sh.c_err[k], sh.c_err_info[k]);
-                        v = k + 1;
-                        break;
+                if (vwarp) {
+                    v = Vw;
+                    if (sh.c_err[v - 1]) set_err(sh, sh.c_err[v - 1], sh.c_err_info[v - 1]);
+                } else {
+                    long long bk = DMD_KEY_INF;
+                    int bb = INT_MAX;
+                    for (int k = 0; k < P; ++k) {
+                        if (k > 0 && !key_less(sh.sort_key[k], sh.sort_idx[k], bk, bb)) { v = k; break; }
+                        /* light batches: it read a queue entry an earlier event changed */
+                        if (k > 0 && light && sh.c_qbad[k]) { v = k; break; }
+                        if (sh.c_err[k]) {   /* the run stops after the first event in error */
+                            set_err(sh, sh.c_err[k], sh.c_err_info[k]);
+                            v = k + 1;
+                            break;
+                        }
+                        if (key_less(sh.c_tnew_key[k], sh.c_tnew_idx[k], bk, bb)) { bk = sh.c_tnew_key[k]; bb = sh.c_tnew_idx[k]; }
                     }
-                    if (key_less(sh.c_tnew_key[k], sh.c_tnew_idx[k], bk, bb)) { bk = sh.c_tnew_key[k]; bb = sh.c_tnew_idx[k]; }
                 }
                 sh.V = v;
                 for (int k = 0; k < v; ++k) {
@@ -1620,11 +1649,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 sh.sc.old_tfalse = sh.c_tf[v - 1];
                 if (S.log && S.log_cap > 0) sh.sc.log_count += v;
             }
-            csync(C);
-            if (!leader && threadIdx.x == 0) sh.V = L->V;
-            __syncthreads();
+            if (!vwarp) {
+                csync(C);
+                if (!leader && threadIdx.x == 0) sh.V = L->V;
+                __syncthreads();
+            }
             DMD_PHASE(4);
-            const int V = sh.V;
+            const int V = vwarp ? Vw : sh.V;
             if (light) {
                 /* a rolled-back event restores its bead i's coltype, which a
                  * standing earlier event may rewrite: restores land first */
