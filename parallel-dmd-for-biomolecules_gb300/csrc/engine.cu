@@ -1033,15 +1033,18 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
             if (kc > kp) kc = kp;
         }
         kc = __shfl_sync(FULL, kc, 0);
-        int ord = 0;   /* ordinal of the next group below the cut */
-        for (int gb = 0; gb < S.nl1; gb += 32) {
+        /* few groups: every warp scans them all and takes the groups below
+         * the cut with ordinals warp, warp + NWARPS, ...; many: each warp
+         * scans blocks of 32 groups in turn and takes their groups */
+        const bool few = S.nl1 <= 32 * (NWARPS / 2);
+        int ord = 0;
+        for (int gb = few ? 0 : 32 * warp; gb < S.nl1; gb += few ? 32 : 32 * NWARPS) {
             const int g = gb + lane;
             unsigned gm = __ballot_sync(FULL, g < S.nl1 && S.l1k[g] < kc);
-            /* this warp's groups: ordinals warp, warp + NWARPS, ... */
             while (gm) {
                 const int gg = gb + __ffs(gm) - 1;
                 gm &= gm - 1;
-                if (ord++ % NWARPS != warp) continue;
+                if (few && ord++ % NWARPS != warp) continue;
                 const int e = gg * 32 + lane;
                 const long long k = e < N ? S.key[e] : DMD_KEY_INF;
                 const bool c = k < kc;

@@ -1412,17 +1412,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                  * >= 1 whose footprint meets an earlier one ends it before
                  * k); an incomplete footprint (cascade list overflow) ends
                  * it after its event */
-                {
+                if (C == 1) {
                     int p = m;
 #pragma unroll
                     for (int h = 0; h < CAND_MAX / 32; ++h) {
                         const int k = lane + 32 * h;
-                        const unsigned cf = __ballot_sync(FULL, k > 0 && k < m && L->c_conflict[k]);
-                        const unsigned ov = __ballot_sync(FULL, k < m && L->c_over[k]);
+                        const unsigned cf = __ballot_sync(FULL, k > 0 && k < m && sh.c_conflict[k]);
+                        const unsigned ov = __ballot_sync(FULL, k < m && sh.c_over[k]);
                         if (cf) p = min(p, 32 * h + __ffs(cf) - 1);
                         if (ov) p = min(p, max(32 * h + __ffs(ov) - 1, 1));
                     }
                     P = p;
+                } else {
+                    /* clusters: the leader decides, the others copy */
+                    if (leader && threadIdx.x == 0) {
+                        int p = m;
+                        for (int k = 0; k < m; ++k) {
+                            if (k > 0 && sh.c_conflict[k]) { p = k; break; }
+                            if (sh.c_over[k]) { p = k > 0 ? k : 1; break; }
+                        }
+                        sh.P = p;
+                    }
+                    csync(C);
+                    if (!leader && threadIdx.x == 0) sh.P = L->P;
+                    __syncthreads();
+                    P = sh.P;
                 }
                 if (leader && threadIdx.x == 0) sh.bseq = sh.tick_reset ? 1 : sh.bseq + 1;
                 DMD_PHASE(2);
