@@ -470,6 +470,94 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
 /* ------------------------------------------------------------------ */
 /* re-prediction into the warp's buffer (code/partial_events.f)         */
 /* ------------------------------------------------------------------ */
+/* The collision of an event of a light batch (coltype 1-3: core bounce,
+ * inner or outer bond wall) on one half of a warp, the other half taking
+ * another event (or none: has = false, no writes): every FP64 warp
+ * instruction serves two events.  The same arithmetic as warp_snapshot,
+ * warp_collision, warp_eventdyn, warp_rel and warp_impulse for those
+ * coltypes: components on lanes 0..2 (0..5) of the half, the impulse ratio
+ * on its lane 0. */
+__device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, int j, double tf, int hbonds) {
+    const int lane = threadIdx.x & 31, hl = lane & 15;
+    const DTab &T = *S.tab;
+    const int ct = S.colt[i];
+    const int evcode = pair_code(S, i, j, hbonds);
+    /* snapshot of what the collision writes */
+    if (has && hl < 12) {
+        const int b = hl < 6 ? i : j, f = hl % 6;
+        const double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
+        W.sij[hl] = A[b];
+    }
+    if (has && hl == 0) { W.nmeta = 0; W.colt_i = (int8_t)ct; }
+    /* relative position and velocity (warp_rel), lanes 0..2 of the half */
+    const int d = hl % 3;
+    const double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+    const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+    const double v = V[i] - V[j];
+    double r = P[i] - P[j] + v * tf;
+    r = d_wrap(r);
+    const double pb = r * v, pr = r * r, pv = v * v;
+    const double rx = __shfl_sync(FULL, r, 0, 16), ry = __shfl_sync(FULL, r, 1, 16), rz = __shfl_sync(FULL, r, 2, 16);
+    const double b0 = __shfl_sync(FULL, pb, 0, 16), b1 = __shfl_sync(FULL, pb, 1, 16), b2 = __shfl_sync(FULL, pb, 2, 16);
+    const double r0 = __shfl_sync(FULL, pr, 0, 16), r1 = __shfl_sync(FULL, pr, 1, 16), r2 = __shfl_sync(FULL, pr, 2, 16);
+    const double v0 = __shfl_sync(FULL, pv, 0, 16), v1 = __shfl_sync(FULL, pv, 1, 16), v2 = __shfl_sync(FULL, pv, 2, 16);
+    const double s0 = hl == 0 ? b0 : (hl == 1 ? r0 : v0);
+    const double s1 = hl == 0 ? b1 : (hl == 1 ? r1 : v1);
+    const double s2 = hl == 0 ? b2 : (hl == 1 ? r2 : v2);
+    const double sum = s0 + s1 + s2;
+    const double bij = __shfl_sync(FULL, sum, 0, 16);
+    /* the impulse ratio (warp_eventdyn, coltypes 1-3) on lane 0 of the half */
+    double ratio = 0.0;
+    if (hl == 0) {
+        const int a = S.ident[i], b = S.ident[j];
+        const double rmass = T.rmass[a][b];
+        const bool side = evcode >= 10 && evcode <= 12;
+        if (ct == 2) {
+            const double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];
+            const double rlo = side ? S.rblmin_sq[i] : T.revp2_sq[evcode];
+            ratio = div_by(rmass * bij, lo, rlo);
+        } else if (ct == 3) {
+            const double hi = side ? S.blmax_sq[i] : T.evp3_sq[evcode];
+            const double rhi = side ? S.rblmax_sq[i] : T.revp3_sq[evcode];
+            ratio = div_by(rmass * bij, hi, rhi);
+        } else if (ct == 1) {
+            if (evcode == 15) {
+                const bool hb = S.bptnr[i] == j;
+                ratio = div_by(rmass * bij, hb ? T.core15_sq[a][b] : T.sigma_sq[a][b],
+                               hb ? T.rcore15_sq[a][b] : T.rsigma_sq[a][b]);
+            } else if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {
+                const int sl = core_slot(evcode);
+                ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
+            } else {
+                ratio = rmass * bij / T.core_sq[core_slot(evcode)][a][b];
+            }
+        }
+    }
+    ratio = __shfl_sync(FULL, ratio, 0, 16);
+    /* the impulse (warp_impulse without a bump), lanes 0..5 of the half */
+    if (has && hl < 6) {
+        const int dd = hl % 3;
+        const bool isj = hl >= 3;
+        const int b = isj ? j : i;
+        double *PP = dd == 0 ? S.x : (dd == 1 ? S.y : S.z);
+        double *VV = dd == 0 ? S.vx : (dd == 1 ? S.vy : S.vz);
+        const double rr = dd == 0 ? rx : (dd == 1 ? ry : rz);
+        double p = PP[b];
+        const double bmb = S.bm[b], rbmb = T.rbm[S.ident[b]];   /* bm(b) = mass(identity(b)) */
+        const double delv = ratio * rr;
+        const double dv = div_by(delv, bmb, rbmb);
+        const double dp = div_by(delv * tf, bmb, rbmb);
+        VV[b] = isj ? VV[b] + dv : VV[b] - dv;
+        p = isj ? p - dp : p + dp;
+        PP[b] = p;
+    }
+    if (has && hl == 0) {
+        S.colt[i] = (int8_t)ct;
+        W.ct = ct; W.evcode = evcode; W.xpulse = 0;
+    }
+    __syncwarp();
+}
+
 /* The ghost collision of lane_ghost() on a warp, with the same draws and
  * arithmetic: the lanes draw the counter-based uniforms of the bead choice,
  * of the two accept/reject pairs and of the next ghost time in parallel
@@ -1450,7 +1538,30 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             const int nloc = P > rank ? (P - rank + C - 1) / C : 0;
             const int nfree = NWARPS - nloc;
             const bool split = nfree > 0 && 2 * nfree >= nloc;
-            if (gw < P) {
+            if (light) {
+                /* light batch (one CTA): two events per collision warp, one
+                 * on each half; the other warps prepare the events' tasks
+                 * meanwhile (the collisions cannot change what they read) */
+                const int ncw = (P + 1) / 2;
+                if (warp < ncw) {
+                    const int k = 2 * warp + (lane >> 4);
+                    const bool has = k < P;
+                    const int kk = has ? k : 2 * warp;
+                    WarpArea &WE = warea[kk];
+                    const int i = sh.sort_idx[kk];
+                    const int j = S.nptnr[i];
+                    const double tf = S.tim[i];
+                    if (has && (lane & 15) == 0) {
+                        WE.i = i; WE.j = j; WE.tf = tf; WE.coll = coll0 + k + 1; WE.err = 0; WE.err_info = 0;
+                    }
+                    hw_collision_light(S, WE, has, i, j, tf, hbonds);
+                } else {
+                    for (int k = warp - ncw; k < P; k += NWARPS - ncw) {
+                        const int i = sh.sort_idx[k];
+                        warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
+                    }
+                }
+            } else if (gw < P) {
                 int i = sh.sort_idx[gw];
                 int j = S.nptnr[i];
                 double tf = S.tim[i];
