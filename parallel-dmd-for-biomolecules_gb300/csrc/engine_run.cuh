@@ -1248,11 +1248,10 @@ __device__ void warp_footprint_claim(const DSys &S, WarpArea &W, unsigned *own, 
 }
 /* The footprint of an event of a light batch (every event of coltype 1-3):
  * R = W = {i, j}, the beads its collision reads and writes; its
- * re-prediction reads other beads through Ver.  Its bead pair i, j is also
- * claimed in the queue table, and Q lists the queue entries it reads (i,
- * j, the lower extras, both down lists): a later event that reads an
- * earlier one's i or j ends the batch before it (those entries always
- * change).  Other entries it reads are checked after the fact
+ * re-prediction reads other beads through Ver.  Q lists the queue entries
+ * it reads (i, j, the lower extras, both down lists): a later event that
+ * reads an earlier one's i or j ends the batch before it (those entries
+ * always change; k_run compares Q with the earlier candidates' pairs).  Other entries it reads are checked after the fact
  * (warp_mark_queue, warp_check_queue): an event that read an entry an
  * earlier event of the batch changed is rolled back. */
 __device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned *own, unsigned ticket, int i, int j) {
@@ -1269,8 +1268,7 @@ __device__ void warp_footprint_claim_light(const DSys &S, WarpArea &W, unsigned 
     if (lane < 2) {
         const int b = lane == 0 ? i : j;
         atomicMax(&own[b], ticket);
-        atomicMax(&own[N + b], ticket);
-        atomicMax(&own[2 * N + b], ticket);
+        atomicMax(&own[N + b], ticket);   /* the write table: who writes b (Ver) */
         W.rset[lane] = b;
         W.wset[lane] = b;
     }
@@ -1479,22 +1477,47 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     }
                     light = C == 1 && !__any_sync(FULL, heavy);
                 }
-                if (gw < m) {
-                    int i = sh.sort_idx[gw];
-                    if (light) warp_footprint_claim_light(S, W, own, ticket, i, S.nptnr[i]);
-                    else warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
-                }
-                csync(C);
-                DMD_PHASE(10);
-                if (gw < m) {
-                    bool c = warp_footprint_test(W, own, N, ticket);
-                    if (lane == 0) {
-                        int ct0 = S.colt[sh.sort_idx[gw]];
-                        L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over;
-                        L->c_simple[gw] = ct0 >= 1 && ct0 <= 3;
+                if (light) {
+                    /* light batch (one CTA): the earlier events' bead pairs
+                     * are known from the candidate list, so each event tests
+                     * its queue reads against them directly - one barrier */
+                    if (gw < m) {
+                        const int i = sh.sort_idx[gw];
+                        warp_footprint_claim_light(S, W, own, ticket, i, S.nptnr[i]);
+                        int pi = -1, pj = -1;
+                        if (lane < gw) { pi = sh.sort_idx[lane]; pj = S.nptnr[pi]; }
+                        bool c = false;
+                        const int nq = min(W.nqset, QSET_MAX);
+                        for (int base = 0; base < nq; base += 32) {
+                            const int q = base + lane;
+                            const int b = q < nq ? W.qset[q] : -1;
+                            for (int k = 0; k < gw; ++k) {
+                                const int ik = __shfl_sync(FULL, pi, k), jk = __shfl_sync(FULL, pj, k);
+                                c |= b >= 0 && (b == ik || b == jk);
+                            }
+                        }
+                        c = __any_sync(FULL, c);
+                        if (lane == 0) { L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over; L->c_simple[gw] = 1; }
                     }
+                    __syncthreads();
+                    DMD_PHASE(10);
+                } else {
+                    if (gw < m) {
+                        int i = sh.sort_idx[gw];
+                        warp_footprint_claim(S, W, own, ticket, i, S.nptnr[i]);
+                    }
+                    csync(C);
+                    DMD_PHASE(10);
+                    if (gw < m) {
+                        bool c = warp_footprint_test(W, own, N, ticket);
+                        if (lane == 0) {
+                            int ct0 = S.colt[sh.sort_idx[gw]];
+                            L->c_conflict[gw] = c; L->c_over[gw] = W.casc_over;
+                            L->c_simple[gw] = ct0 >= 1 && ct0 <= 3;
+                        }
+                    }
+                    csync(C);
                 }
-                csync(C);
                 DMD_PHASE(11);
                 /* every warp: the longest conflict-free prefix (candidate k
                  * >= 1 whose footprint meets an earlier one ends it before
