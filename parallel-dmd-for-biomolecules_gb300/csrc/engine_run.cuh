@@ -1370,7 +1370,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
      * it fits, else the system's global array; cleared at every launch */
     TaskPool &TP = *(TaskPool *)(warea + NWARPS);
     unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)((char *)(warea + NWARPS) + sizeof(TaskPool)) : S.owner;
-    if (threadIdx.x == 0) TP.n = 0;
+    if (threadIdx.x == 0) { TP.n = 0; TP.nlive = 0; }
     for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
     csync(C);
     DMD_PHASE_START(leader ? r : -1);
@@ -1621,9 +1621,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
              * instructions (64 cycles each on the FP64 unit whatever the
              * active lanes) have all lanes busy */
             {
-                const int ntot = min(TP.n, PTASK_MAX);
-                if (threadIdx.x == 0) TP.nlive = 0;
-                __syncthreads();
+                const int ntot = min(TP.n, PTASK_MAX);   /* TP.nlive is 0 (reset with TP.n) */
                 DMD_PHASE(12);
                 for (int base = 0; base < ntot; base += NTHREADS) {
                     const int q = base + threadIdx.x;
@@ -1726,7 +1724,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     L->c_ct[gw] = W.ct; L->c_tf[gw] = W.tf;
                 }
             }
-            if (threadIdx.x == 0) TP.n = 0;   /* the pool is free until the next batch */
+            if (threadIdx.x == 0) { TP.n = 0; TP.nlive = 0; }   /* the pool is free until the next batch */
             csync(C);
             if (light) {
                 if (gw < P) {
@@ -1808,7 +1806,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 /* a rolled-back event restores its bead i's coltype, which a
                  * standing earlier event may rewrite: restores land first */
                 if (gw < P && gw >= V) warp_restore(S, W);
-                csync(C);
+                if (V < P) csync(C);
                 if (gw < V) {
                     warp_commit_preds(S, W);
                     if (lane == 0) log_event(S, sh.log0 + gw, W.coll, sh.tnow, W.tf, W.i, W.j, W.ct, W.evcode);
