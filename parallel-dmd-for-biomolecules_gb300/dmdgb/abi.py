@@ -51,11 +51,13 @@ class RunCfg(C.Structure):
 
 
 class System(C.Structure):
+    """dmd_system; the array fields hold addresses (int32 or float64 data as
+    the header declares them) so that filling one is cheap."""
     _fields_ = [
-        ("n_beads", C.c_int32), ("n_chains", C.c_int32), ("chain_len", i32_p), ("residues", i32_p),
-        ("hp", i32_p), ("boxl", C.c_double),
-        ("x", dbl_p), ("y", dbl_p), ("z", dbl_p), ("vx", dbl_p), ("vy", dbl_p), ("vz", dbl_p),
-        ("bptnr", i32_p), ("t0", C.c_double), ("coll0", C.c_int64),
+        ("n_beads", C.c_int32), ("n_chains", C.c_int32), ("chain_len", C.c_void_p), ("residues", C.c_void_p),
+        ("hp", C.c_void_p), ("boxl", C.c_double),
+        ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("vx", C.c_void_p), ("vy", C.c_void_p),
+        ("vz", C.c_void_p), ("bptnr", C.c_void_p), ("t0", C.c_double), ("coll0", C.c_int64),
     ]
 
 
@@ -131,7 +133,7 @@ def _declare(lib) -> None:
     lib.dmd_run.restype = C.c_int
     lib.dmd_predict_all.argtypes = [C.c_void_p, dbl_p, i32_p, i32_p]
     lib.dmd_predict_all.restype = C.c_int
-    lib.dmd_get_state.argtypes = [C.c_void_p] + [dbl_p] * 6 + [i32_p] * 3 + [dbl_p, dbl_p, i64_p]
+    lib.dmd_get_state.argtypes = [C.c_void_p] + [C.c_void_p] * 9 + [dbl_p, dbl_p, i64_p]
     lib.dmd_get_state.restype = C.c_int
     lib.dmd_diagnostics.argtypes = [C.c_void_p, C.POINTER(Diag)]
     lib.dmd_diagnostics.restype = C.c_int
@@ -148,7 +150,7 @@ def _declare(lib) -> None:
     lib.dmd_batch_create.restype = C.c_int
     lib.dmd_batch_run.argtypes = [C.c_void_p, C.c_int64, C.POINTER(EventLog)]
     lib.dmd_batch_run.restype = C.c_int
-    lib.dmd_batch_get_state.argtypes = [C.c_void_p, C.c_int32] + [dbl_p] * 6 + [i32_p] * 3 + [dbl_p, dbl_p, i64_p]
+    lib.dmd_batch_get_state.argtypes = [C.c_void_p, C.c_int32] + [C.c_void_p] * 9 + [dbl_p, dbl_p, i64_p]
     lib.dmd_batch_get_state.restype = C.c_int
     lib.dmd_batch_diagnostics.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Diag)]
     lib.dmd_batch_diagnostics.restype = C.c_int

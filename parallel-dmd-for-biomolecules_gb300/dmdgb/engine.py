@@ -27,6 +27,23 @@ def _check(rc: int, lib, handle, fn="dmd_last_error"):
         raise DMDError(rc, msg.decode() if msg else "")
 
 
+def _state_buffers(n: int):
+    """Output arrays of a state read (views of one float64 and one int32
+    block) and the get_state arguments that point at them."""
+    f = np.empty(6 * n, np.float64)
+    i = np.empty(6 * n, np.int32)
+    fa, ia = f.ctypes.data, i.ctypes.data
+    sc = (C.c_double(), C.c_double(), C.c_int64())
+    out = {k: f[q * n:(q + 1) * n] for q, k in enumerate(("x", "y", "z", "vx", "vy", "vz"))}
+    out.update(bptnr=i[:n], identity=i[n:2 * n], extra_repuls=i[2 * n:].reshape(n, 4))
+    args = [fa + 8 * n * q for q in range(6)] + [ia, ia + 4 * n, ia + 8 * n] + [C.byref(v) for v in sc]
+
+    def fin(o):
+        o.update(t=sc[0].value, tfalse=sc[1].value, coll=sc[2].value)
+        return o
+    return out, args, fin
+
+
 class Engine:
     """One system on the GPU (the plain one-system-per-launch path)."""
 
@@ -105,20 +122,9 @@ class Engine:
         return tim, np_, ct
 
     def state(self) -> dict:
-        n = self.n
-        a = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
-        bp = np.zeros(n, np.int32)
-        ident = np.zeros(n, np.int32)
-        er = np.zeros(4 * n, np.int32)
-        t = C.c_double()
-        tf = C.c_double()
-        coll = C.c_int64()
-        rc = self.lib.dmd_get_state(self.h, *[abi.ptr(a[k], abi.dbl_p) for k in ("x", "y", "z", "vx", "vy", "vz")],
-                                    abi.ptr(bp, abi.i32_p), abi.ptr(ident, abi.i32_p), abi.ptr(er, abi.i32_p),
-                                    C.byref(t), C.byref(tf), C.byref(coll))
-        _check(rc, self.lib, self.h)
-        a.update(bptnr=bp, identity=ident, extra_repuls=er.reshape(n, 4), t=t.value, tfalse=tf.value, coll=coll.value)
-        return a
+        out, args, fin = _state_buffers(self.n)
+        _check(self.lib.dmd_get_state(self.h, *args), self.lib, self.h)
+        return fin(out)
 
     def diagnostics(self) -> dict:
         d = abi.Diag()
@@ -206,20 +212,11 @@ class Batch:
         return None
 
     def state(self, r: int) -> dict:
-        n = self.specs[r].n_beads
-        a = {k: np.zeros(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
-        bp = np.zeros(n, np.int32)
-        ident = np.zeros(n, np.int32)
-        er = np.zeros(4 * n, np.int32)
-        t = C.c_double()
-        tf = C.c_double()
-        coll = C.c_int64()
-        rc = self.lib.dmd_batch_get_state(self.h, r, *[abi.ptr(a[k], abi.dbl_p) for k in ("x", "y", "z", "vx", "vy", "vz")],
-                                          abi.ptr(bp, abi.i32_p), abi.ptr(ident, abi.i32_p), abi.ptr(er, abi.i32_p),
-                                          C.byref(t), C.byref(tf), C.byref(coll))
-        _check(rc, self.lib, self.h, "dmd_batch_last_error")
-        a.update(bptnr=bp, identity=ident, extra_repuls=er.reshape(n, 4), t=t.value, tfalse=tf.value, coll=coll.value)
-        return a
+        if not 0 <= r < len(self.specs):
+            raise DMDError(-1, "replica index out of range")
+        out, args, fin = _state_buffers(self.specs[r].n_beads)
+        _check(self.lib.dmd_batch_get_state(self.h, r, *args), self.lib, self.h, "dmd_batch_last_error")
+        return fin(out)
 
     def diagnostics(self, r: int) -> dict:
         d = abi.Diag()

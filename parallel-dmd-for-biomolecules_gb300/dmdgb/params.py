@@ -180,12 +180,18 @@ def read_tables(parameters_dir: str, ep_file: str) -> Tables:
 _DATA = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "data")
 
 
+_DEFAULT_JSON = None
+
+
 def default_tables() -> Tables:
     """PRIME20 tables shipped with the package (parsed from the reference's
     parameters/ and parametersep/ep19p_ha55a_weakhp.data by
-    data/make_tables.py)."""
-    with open(os.path.join(_DATA, "prime20_tables.json")) as fh:
-        return Tables.from_json(json.load(fh))
+    data/make_tables.py); the file is read once per process."""
+    global _DEFAULT_JSON
+    if _DEFAULT_JSON is None:
+        with open(os.path.join(_DATA, "prime20_tables.json")) as fh:
+            _DEFAULT_JSON = json.load(fh)
+    return Tables.from_json(_DEFAULT_JSON)
 
 
 # ---------------------------------------------------------------- run file

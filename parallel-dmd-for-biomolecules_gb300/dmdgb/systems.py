@@ -29,11 +29,11 @@ def box_for(n_chains: int, conc_mM: float) -> float:
 
 
 def beads_of(chain_len: List[int], residues: List[int]) -> int:
-    n, p = 0, 0
-    for L in chain_len:
-        n += 3 * L + sum(1 for r in residues[p:p + L] if r != 9)
-        p += L
-    return n
+    """Beads of a system: three backbone beads per residue plus one side
+    chain for every residue that is not glycine (code 9)."""
+    total = int(np.sum(np.asarray(chain_len, dtype=np.int64)))
+    res = np.asarray(residues[:total] if isinstance(residues, list) else np.asarray(residues)[:total])
+    return 3 * total + int(np.count_nonzero(res != 9))
 
 
 @dataclass
@@ -81,9 +81,10 @@ class SystemSpec:
         hp = None if self.hp is None else np.ascontiguousarray(self.hp, np.int32)
         bp = None if self.bptnr is None else np.ascontiguousarray(self.bptnr, np.int32)
         self._keep = [cl, res, hp, bp] + arrs
-        return abi.System(self.n_beads, self.n_chains, abi.ptr(cl, abi.i32_p), abi.ptr(res, abi.i32_p),
-                          abi.ptr(hp, abi.i32_p), float(self.boxl), *[abi.ptr(a, abi.dbl_p) for a in arrs],
-                          abi.ptr(bp, abi.i32_p), float(self.t0), int(self.coll0))
+        def addr(a):
+            return None if a is None else a.ctypes.data
+        return abi.System(beads_of(cl, res), len(cl), addr(cl), addr(res), addr(hp), float(self.boxl),
+                          *[addr(a) for a in arrs], addr(bp), float(self.t0), int(self.coll0))
 
 
 def generate(spec: SystemSpec, tables: Optional[Tables] = None, min_sep: float = 5.0) -> SystemSpec:
