@@ -476,7 +476,6 @@ struct dmd_batch {
     DSys *d_sys = nullptr;
     int *d_cstart = nullptr, *d_clen = nullptr, *d_coff = nullptr;
     dmd_diag *d_diag = nullptr;
-    void *d_meta = nullptr;             /* d_sys, chain tables and d_diag: one allocation */
     dmd_event *d_log = nullptr;
     long long log_cap = 0;
     int hbonds = 1;
@@ -607,30 +606,6 @@ std::mutex g_stage_mu;
 char *g_stage = nullptr;
 size_t g_stage_cap = 0;
 
-/* grows the stage to at least `need` bytes; the caller holds g_stage_mu */
-cudaError_t stage_reserve(size_t need) {
-    if (g_stage_cap >= need) return cudaSuccess;
-    if (g_stage) cudaFreeHost(g_stage);
-    g_stage = nullptr;
-    g_stage_cap = 0;
-    cudaError_t e = cudaMallocHost((void **)&g_stage, need);
-    if (e == cudaSuccess) g_stage_cap = need;
-    return e;
-}
-
-/* fn(r) for r in [0, n) on up to one thread per host core */
-template <class F> void parallel_for(int n, F fn) {
-    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)std::max(n, 1));
-    std::atomic<int> next(0);
-    auto work = [&]() {
-        for (int r = next++; r < n; r = next++) fn(r);
-    };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
-    work();
-    for (auto &t : pool) t.join();
-}
-
 int upload(dmd_batch &B) {
     std::string &err = B.err;
     int n = (int)B.hs.size();
@@ -653,62 +628,53 @@ int upload(dmd_batch &B) {
     }
     size_t total = off[n];
     CK(cudaMalloc(&B.pool_all, total));
-    /* behind the heads in the stage: the system table and the chain tables
-     * (one copy into one device allocation that also holds the diagnostics) */
-    size_t nch = 0;
-    for (int r = 0; r < n; ++r) nch += (size_t)B.hs[r].nchains;
-    auto a256 = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    const size_t m_sys = 0, m_cstart = a256(n * sizeof(DSys)), m_clen = m_cstart + a256(nch * 4),
-                 m_coff = m_clen + a256(nch * 4), m_diag = m_coff + a256((size_t)n * 4),
-                 m_host = m_diag, m_total = m_diag + a256((size_t)n * sizeof(dmd_diag));
-    const size_t need = std::max(soff[n] + m_host, (size_t)n * sizeof(DScal));
     std::lock_guard<std::mutex> stage_lock(g_stage_mu);
-    CK(stage_reserve(need));
+    if (g_stage_cap < soff[n]) {
+        if (g_stage) cudaFreeHost(g_stage);
+        g_stage = nullptr;
+        g_stage_cap = 0;
+        CK(cudaMallocHost((void **)&g_stage, soff[n]));
+        g_stage_cap = soff[n];
+    }
     char *stage = g_stage;
     B.upload_bytes = 0;
-    char *meta = stage + soff[n];
-    DSys *hd = (DSys *)(meta + m_sys);
-    int *cstart = (int *)(meta + m_cstart), *clen = (int *)(meta + m_clen), *coff = (int *)(meta + m_coff);
-    /* the heads' host images, one system per thread */
-    parallel_for(n, [&](int r) {
+    std::vector<DSys> hd(n);
+    std::vector<int> cstart, clen, coff;
+    for (int r = 0; r < n; ++r) {
         HostSys &H = B.hs[r];
         DevSys &D = B.ds[r];
         D.pool = nullptr;                      /* part of pool_all */
-        char *base = (char *)B.pool_all + off[r];
-        layout(H, D.d, base);
+        layout(H, D.d, (char *)B.pool_all + off[r]);
         set_scalars(H, D.d);
         PoolTemps keep;
         std::vector<PoolCopy> cps;
         pool_copies(H, D.d, keep, cps);
+        char *base = (char *)B.pool_all + off[r];
         for (const PoolCopy &c : cps)
             std::memcpy(stage + soff[r] + ((char *)c.dst - base), c.src, c.n);
-        hd[r] = D.d;
-    });
-    size_t ci = 0;
-    for (int r = 0; r < n; ++r) {
-        const HostSys &H = B.hs[r];
-        CK(cudaMemcpyAsync((char *)B.pool_all + off[r], stage + soff[r], head[r], cudaMemcpyHostToDevice, B.st));
+        CK(cudaMemcpyAsync(base, stage + soff[r], head[r], cudaMemcpyHostToDevice, B.st));
         B.upload_bytes += (long long)head[r];
-        coff[r] = (int)ci;
-        for (int c = 0; c < H.nchains; ++c, ++ci) { cstart[ci] = H.chain_start[c]; clen[ci] = H.chain_len[c]; }
+        hd[r] = D.d;
+        coff.push_back((int)cstart.size());
+        for (int c = 0; c < H.nchains; ++c) { cstart.push_back(H.chain_start[c]); clen.push_back(H.chain_len[c]); }
     }
-    CK(cudaMalloc(&B.d_meta, m_total));
-    char *dm = (char *)B.d_meta;
-    B.d_sys = (DSys *)(dm + m_sys);
-    B.d_cstart = (int *)(dm + m_cstart);
-    B.d_clen = (int *)(dm + m_clen);
-    B.d_coff = (int *)(dm + m_coff);
-    B.d_diag = (dmd_diag *)(dm + m_diag);
-    CK(cudaMemcpyAsync(dm, meta, m_host, cudaMemcpyHostToDevice, B.st));
-    CK(dmd_launch_init(B.d_sys, n, B.hbonds, B.st));
-    /* the stage's copies are done once the list build has run: its head
-     * holds every system's scalars next */
-    DScal *scs = (DScal *)stage;
-    for (int r = 0; r < n; ++r)
-        CK(cudaMemcpyAsync(&scs[r], B.ds[r].d.sc, sizeof(DScal), cudaMemcpyDeviceToHost, B.st));
     CK(cudaStreamSynchronize(B.st));   /* the stage is free for the next creation */
-    for (int r = 0; r < n; ++r)
-        if (scs[r].err) { err = "device error during list build (code " + std::to_string(scs[r].err) + ")"; return scs[r].err; }
+    CK(cudaMalloc(&B.d_sys, n * sizeof(DSys)));
+    CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&B.d_cstart, cstart.size() * 4));
+    CK(cudaMalloc(&B.d_clen, clen.size() * 4));
+    CK(cudaMalloc(&B.d_coff, coff.size() * 4));
+    CK(cudaMemcpy(B.d_cstart, cstart.data(), cstart.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_clen, clen.data(), clen.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_coff, coff.data(), coff.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&B.d_diag, n * sizeof(dmd_diag)));
+    CK(dmd_launch_init(B.d_sys, n, B.hbonds, B.st));
+    CK(cudaStreamSynchronize(B.st));
+    for (int r = 0; r < n; ++r) {
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        if (sc.err) { err = "device error during list build (code " + std::to_string(sc.err) + ")"; return sc.err; }
+    }
     B.ready = 1;
     return DMD_OK;
 }
@@ -722,7 +688,15 @@ int batch_create(dmd_batch &B, int n, const dmd_run_cfg *cfgs, const dmd_tables 
     /* the host set-up of the systems on parallel threads */
     std::vector<std::string> errs(n);
     std::vector<char> ok(n, 0);
-    parallel_for(n, [&](int r) { ok[r] = setup_host(B.hs[r], &cfgs[r], tables, &systems[r], errs[r]); });
+    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)n);
+    std::atomic<int> next(0);
+    auto work = [&]() {
+        for (int r = next++; r < n; r = next++) ok[r] = setup_host(B.hs[r], &cfgs[r], tables, &systems[r], errs[r]);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
     for (int r = 0; r < n; ++r)
         if (!ok[r]) { B.err = "system " + std::to_string(r) + ": " + errs[r]; return DMD_E_INPUT; }
     return upload(B);
@@ -730,20 +704,11 @@ int batch_create(dmd_batch &B, int n, const dmd_run_cfg *cfgs, const dmd_tables 
 
 int sync_check(dmd_batch &B) {
     std::string &err = B.err;
-    const size_t n = B.ds.size();
-    CK(cudaStreamSynchronize(B.st));   /* the launches end before the stage is taken */
-    {
-        /* every system's scalars through the pinned stage, one sync */
-        std::lock_guard<std::mutex> stage_lock(g_stage_mu);
-        CK(stage_reserve(n * sizeof(DScal)));
-        DScal *scs = (DScal *)g_stage;
-        for (size_t r = 0; r < n; ++r)
-            CK(cudaMemcpyAsync(&scs[r], B.ds[r].d.sc, sizeof(DScal), cudaMemcpyDeviceToHost, B.st));
-        CK(cudaStreamSynchronize(B.st));
-        for (size_t r = 0; r < n; ++r) B.hs[r].sc = scs[r];
-    }
-    for (size_t r = 0; r < n; ++r) {
-        const DScal &sc = B.hs[r].sc;
+    CK(cudaStreamSynchronize(B.st));
+    for (size_t r = 0; r < B.ds.size(); ++r) {
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        B.hs[r].sc = sc;
         if (sc.err) {
             err = "device error " + std::to_string(sc.err) + " in system " + std::to_string(r) + " (info " + std::to_string(sc.err_info) + ")";
             return sc.err;
@@ -849,21 +814,13 @@ int get_state(dmd_batch &B, int r, double *x, double *y, double *z, double *vx, 
         B.state_off.assign(n + 1, 0);
         for (int q = 0; q < n; ++q) B.state_off[q + 1] = B.state_off[q] + state_block(B.ds[q].d);
         B.state_cache.resize(B.state_off[n]);
-        /* through the pinned stage: copies into pageable memory would each
-         * wait for the host */
-        const size_t sc_off = (B.state_off[n] + 255) & ~(size_t)255, need = sc_off + (size_t)n * sizeof(DScal);
         CK(cudaStreamSynchronize(B.st));
-        std::lock_guard<std::mutex> stage_lock(g_stage_mu);
-        CK(stage_reserve(need));
         for (int q = 0; q < n; ++q)
-            CK(cudaMemcpyAsync(g_stage + B.state_off[q], B.ds[q].d.x, state_block(B.ds[q].d),
+            CK(cudaMemcpyAsync(B.state_cache.data() + B.state_off[q], B.ds[q].d.x, state_block(B.ds[q].d),
                                cudaMemcpyDeviceToHost, B.st));
-        DScal *scs = (DScal *)(g_stage + sc_off);
         for (int q = 0; q < n; ++q)
-            CK(cudaMemcpyAsync(&scs[q], B.ds[q].d.sc, sizeof(DScal), cudaMemcpyDeviceToHost, B.st));
+            CK(cudaMemcpyAsync(&B.hs[q].sc, B.ds[q].d.sc, sizeof(DScal), cudaMemcpyDeviceToHost, B.st));
         CK(cudaStreamSynchronize(B.st));
-        std::memcpy(B.state_cache.data(), g_stage, B.state_off[n]);
-        for (int q = 0; q < n; ++q) B.hs[q].sc = scs[q];
         B.state_valid = true;
     }
     const DSys &d = B.ds[r].d;
@@ -1026,11 +983,11 @@ void batch_free(dmd_batch &B) {
     for (auto &D : B.ds) if (D.pool) cudaFree(D.pool);
     if (B.pool_all) cudaFree(B.pool_all);
     B.pool_all = nullptr;
-    if (B.d_meta) cudaFree(B.d_meta);
-    B.d_meta = nullptr;
-    B.d_sys = nullptr;
-    B.d_cstart = B.d_clen = B.d_coff = nullptr;
-    B.d_diag = nullptr;
+    if (B.d_sys) cudaFree(B.d_sys);
+    if (B.d_cstart) cudaFree(B.d_cstart);
+    if (B.d_clen) cudaFree(B.d_clen);
+    if (B.d_coff) cudaFree(B.d_coff);
+    if (B.d_diag) cudaFree(B.d_diag);
     if (B.d_log) cudaFree(B.d_log);
     if (B.d_targets) cudaFree(B.d_targets);
     if (B.ev0) cudaEventDestroy(B.ev0);

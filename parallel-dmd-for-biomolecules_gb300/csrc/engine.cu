@@ -713,10 +713,10 @@ __device__ void cta_predict_all(const DSys &S, SharedState &sh, ScratchRef fr, d
     __syncthreads();
 }
 
-/* the first half of a rebuild: wrap the positions into the box, cell
- * lists, neighbour lists.  scr (scr_bytes, may be null): shared memory free
- * for the list build. */
-__device__ void cta_rebuild_lists(const DSys &S, SharedState &sh, int hbonds, char *scr, int scr_bytes) {
+/* rebuild: wrap the positions into the box, cell lists, neighbour lists,
+ * full prediction, tournament.  scr (scr_bytes, may be null): shared memory
+ * free for the list build. */
+__device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int hbonds, char *scr, int scr_bytes) {
     DMD_SUB(-1);
     const ListStage L = list_stage(S, scr, scr_bytes);
     const int nc = S.ncell;
@@ -737,11 +737,6 @@ __device__ void cta_rebuild_lists(const DSys &S, SharedState &sh, int hbonds, ch
     DMD_ISUB(7);
     cta_build_lists(S, sh, hbonds, L);
     DMD_ISUB(8);
-}
-
-/* rebuild: the lists, the full prediction, the tournament */
-__device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int hbonds, char *scr, int scr_bytes) {
-    cta_rebuild_lists(S, sh, hbonds, scr, scr_bytes);
     cta_predict_all(S, sh, fr, sh.sc.interval_max, hbonds);
     DMD_ISUB(9);
     cta_tree_rebuild(S);
@@ -1116,13 +1111,8 @@ __device__ void log_event(const DSys &S, long long slot, long long coll, double 
     L->i = i + 1; L->j = j + 1; L->type = type; L->evcode = evcode;
 }
 
-/* Creation runs the first rebuild of every system in three launches: the
- * lists (one CTA per system), the full prediction (INIT_SPLIT CTAs per
- * system: the prediction is most of a large system's rebuild, and every
- * bead's is independent of the others'), then the pseudo events and the
- * tournament (one CTA per system).  The result is that of cta_rebuild. */
-#define KINIT_DYN_SMEM (96 * 1024)   /* shared memory of k_init beyond its static part: the list staging */
-#define INIT_SPLIT 4
+/* shared memory of k_init beyond its static part: the list build's staging */
+#define KINIT_DYN_SMEM (96 * 1024)
 __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, int hbonds_mask) {
     extern __shared__ __align__(16) unsigned char kinit_dyn[];
     __shared__ SharedState sh;
@@ -1135,42 +1125,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, i
     int hbonds = hbonds_mask & 1;
     if (threadIdx.x == 0) { sh.sc = *S.sc; }
     __syncthreads();
-    cta_rebuild_lists(S, sh, hbonds, (char *)kinit_dyn, KINIT_DYN_SMEM);
-    if (threadIdx.x == 0) *S.sc = sh.sc;
-}
-/* CTA g of a system takes, on warp w, the groups of TG_MAX beads g * NWARPS
- * + w, stepping by INIT_SPLIT * NWARPS groups; errors go straight to the
- * system's status (the first one stays) */
-__global__ void __launch_bounds__(NTHREADS) k_init_predict(DSys *systems, int nsys, int hbonds_mask) {
-    __shared__ DSys S_sh;
     __shared__ FullScratch fs[NWARPS];
-    const int r = blockIdx.x / INIT_SPLIT, g = blockIdx.x % INIT_SPLIT;
-    if (r >= nsys) return;
-    if (threadIdx.x == 0) S_sh = systems[r];
-    __syncthreads();
-    const DSys &S = S_sh;
-    const int N = S.N, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const double interval_max = S.sc->interval_max;
-    const Err E{&S.sc->err, &S.sc->err_info};
-    for (int q = g * nwarps + warp; q * TG_MAX < N; q += INIT_SPLIT * nwarps)
-        warp_predict_beads(S, E, fs[warp], q * TG_MAX, min(TG_MAX, N - q * TG_MAX), interval_max, hbonds_mask & 1);
-}
-__global__ void __launch_bounds__(NTHREADS) k_init_tree(DSys *systems, int nsys) {
-    __shared__ DSys S_sh;
-    const int r = blockIdx.x;
-    if (r >= nsys) return;
-    if (threadIdx.x == 0) S_sh = systems[r];
-    __syncthreads();
-    const DSys &S = S_sh;
-    if (threadIdx.x < 3) {
-        const int e = S.N + threadIdx.x;
-        const double interval_max = S.sc->interval_max;
-        const bool q = S.tim[e] < interval_max;
-        S.queued[e] = q;
-        S.key[e] = q ? okey(S.tim[e]) : DMD_KEY_INF;
-    }
-    __syncthreads();
-    cta_tree_rebuild(S);
+    cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds, (char *)kinit_dyn, KINIT_DYN_SMEM);
+    if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
 /* k_run and its per-event functions, compiled in two variants that differ
@@ -1253,12 +1210,6 @@ cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t 
         }
     }
     k_init<<<nsys, NTHREADS, KINIT_DYN_SMEM, st>>>(d_systems, nsys, hbonds);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_init_predict<<<nsys * INIT_SPLIT, NTHREADS, 0, st>>>(d_systems, nsys, hbonds);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_init_tree<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys);
     return cudaGetLastError();
 }
 static cudaError_t k_run_attributes() {

@@ -37,6 +37,21 @@ def test_predict_all_initial(built):
     assert np.array_equal(gt, ot)
 
 
+@pytest.mark.parametrize("pick", ["smallest", "largest"])
+def test_predict_all_initial_c3(built, pick):
+    """The first rebuild's predictions of the 32-replica workload's smallest
+    and largest systems (626 and 5,576 beads: the full prediction is shared
+    by several CTAs per system)."""
+    specs = sorted(systems.config_c3(32, seed=1), key=lambda s: s.n_beads)
+    spec = systems.generate(specs[0] if pick == "smallest" else specs[-1])
+    with Engine(spec) as eng:
+        gt, gp, gc = eng.predictions()
+    ot, op, oc = Oracle(spec).predictions()
+    assert np.array_equal(gp, op)
+    assert np.array_equal(gc, oc)
+    assert np.array_equal(gt, ot)
+
+
 def test_c1_event_sequence(built):
     spec = systems.generate(systems.config_c1())
     log = _compare_run(spec, 20000)
