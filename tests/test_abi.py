@@ -39,3 +39,52 @@ def test_errors_are_status_codes(built):
     assert rc == -1
     assert b"empty" in lib.dmd_last_error(h)
     lib.dmd_destroy(h)
+
+
+def test_system_struct_matches_header_layout():
+    """abi.System mirrors struct dmd_system: the array fields hold addresses,
+    and the field offsets are those of the C declaration."""
+    from dmdgb import systems
+    spec = systems.klvffae_system(2, 5.0, 0.2, seed=1)
+    n = spec.n_beads
+    import numpy as np
+    spec.x, spec.y, spec.z, spec.vx, spec.vy, spec.vz = [np.full(n, float(k)) for k in range(6)]
+    s = spec.c_system()
+    assert s.n_beads == n == 2 * (3 * 7 + 7) and s.n_chains == 2   # KLVFFAE: no glycine
+    assert s.x == spec._keep[4].ctypes.data and s.hp is None and s.bptnr is None
+    # sizeof and offsetof of struct dmd_system as gcc lays out include/dmd.h
+    assert C.sizeof(abi.System) == 112
+    assert (abi.System.boxl.offset, abi.System.x.offset, abi.System.t0.offset, abi.System.coll0.offset) == (32, 40, 96, 104)
+
+
+def test_bead_count_rule():
+    """Three backbone beads per residue and a side chain for every residue
+    but glycine (code 9), over the residues the chains use."""
+    from dmdgb.systems import beads_of
+    rng = __import__("numpy").random.default_rng(5)
+    for _ in range(20):
+        cl = [int(v) for v in rng.integers(3, 12, size=rng.integers(1, 6))]
+        res = [int(v) for v in rng.integers(9, 29, size=sum(cl) + int(rng.integers(0, 3)))]
+        want = 0
+        p = 0
+        for L in cl:
+            want += 3 * L + sum(1 for r in res[p:p + L] if r != 9)
+            p += L
+        assert beads_of(cl, res) == want
+        import numpy as np
+        assert beads_of(np.array(cl, np.int32), np.array(res, np.int32)) == want
+
+
+def test_state_buffers_point_at_outputs():
+    """The get_state arguments address the returned arrays: six float64
+    columns, then bptnr, identity and the 4-wide extra_repuls block."""
+    from dmdgb.engine import _state_buffers
+    n = 37
+    out, args, fin = _state_buffers(n)
+    for q, k in enumerate(("x", "y", "z", "vx", "vy", "vz")):
+        assert args[q] == out[k].ctypes.data and out[k].shape == (n,)
+    assert args[6] == out["bptnr"].ctypes.data and args[7] == out["identity"].ctypes.data
+    assert args[8] == out["extra_repuls"].ctypes.data and out["extra_repuls"].shape == (n, 4)
+    assert out["extra_repuls"].ctypes.data + 16 * n == out["bptnr"].ctypes.data + 24 * n
+    d = fin(out)
+    assert d["t"] == 0.0 and d["coll"] == 0
