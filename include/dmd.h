@@ -158,6 +158,19 @@ int dmd_get_state(dmd_handle *h, double *x, double *y, double *z,
                   int32_t *identity, int32_t *extra_repuls,
                   double *t, double *tfalse, int64_t *coll);
 
+/* State write: replaces the system's state by the given positions (box
+ * units, at time t: read back as x + vx * tfalse), velocities, 1-based
+ * H-bond partners (or NULL) and collision count, as the reference's
+ * restart from .config/.bptnr/.lastvel records does (code/main.F90:240-321:
+ * identities and shoulders restored from bptnr, lists, cell grid and event
+ * queue rebuilt, intervals restarted; the ghost random stream starts again
+ * from the seed).  The result is that of dmd_create from the same system
+ * with that state; the cluster, rebuild-grid and compact-variant settings
+ * are kept.  On an error the previous state stays in force. */
+int dmd_set_state(dmd_handle *h, const double *x, const double *y, const double *z,
+                  const double *vx, const double *vy, const double *vz, const int32_t *bptnr,
+                  double t, int64_t coll);
+
 /* Replaces code/energy.f, code/radgyr.f, code/end2end.f at the current time. */
 int dmd_diagnostics(dmd_handle *h, dmd_diag *out);
 

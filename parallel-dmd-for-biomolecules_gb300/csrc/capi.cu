@@ -500,7 +500,16 @@ struct dmd_batch {
     long long upload_bytes = 0;        /* host-to-device bytes of the creation */
     int compact_dn = DMD_COMPACT_DN;   /* down-list limit of the compact variant, 0: never */
 };
-struct dmd_handle { dmd_batch b; };
+/* a single system: its batch of one, and the inputs that define the system
+ * apart from its state (kept for dmd_set_state) */
+struct dmd_handle {
+    dmd_batch b;
+    dmd_run_cfg cfg{};
+    dmd_tables tables{};
+    std::vector<int32_t> chain_len, residues, hp;
+    int32_t n_beads = 0;
+    double boxl = 0.0;
+};
 
 namespace {
 
@@ -1329,8 +1338,51 @@ int dmd_create(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_syste
     if (!out) return DMD_E_INPUT;
     dmd_handle *h = new dmd_handle();
     int rc = batch_create(h->b, 1, cfg, tables, sys);
+    if (rc == DMD_OK) {
+        h->cfg = *cfg;
+        h->tables = *tables;
+        h->n_beads = sys->n_beads;
+        h->boxl = sys->boxl;
+        h->chain_len.assign(sys->chain_len, sys->chain_len + sys->n_chains);
+        size_t nres = 0;
+        for (int c = 0; c < sys->n_chains; ++c) nres += (size_t)sys->chain_len[c];
+        h->residues.assign(sys->residues, sys->residues + nres);
+        if (sys->hp) h->hp.assign(sys->hp, sys->hp + sys->n_beads);
+    }
     *out = h;
     return rc;
+}
+int dmd_set_state(dmd_handle *h, const double *x, const double *y, const double *z, const double *vx,
+                  const double *vy, const double *vz, const int32_t *bptnr, double t, int64_t coll) {
+    if (!h) return DMD_E_INPUT;
+    if (!h->b.ready) { h->b.err = "handle not created"; return DMD_E_STATE; }
+    if (!x || !y || !z || !vx || !vy || !vz) { h->b.err = "positions and velocities are required"; return DMD_E_INPUT; }
+    dmd_system sys{};
+    sys.n_beads = h->n_beads;
+    sys.n_chains = (int32_t)h->chain_len.size();
+    sys.chain_len = h->chain_len.data();
+    sys.residues = h->residues.data();
+    sys.hp = h->hp.empty() ? nullptr : h->hp.data();
+    sys.boxl = h->boxl;
+    sys.x = x; sys.y = y; sys.z = z; sys.vx = vx; sys.vy = vy; sys.vz = vz;
+    sys.bptnr = bptnr;
+    sys.t0 = t;
+    sys.coll0 = coll;
+    /* the new state is set up beside the old one, which stays in force if
+     * that fails */
+    dmd_batch nb;
+    int rc = batch_create(nb, 1, &h->cfg, &h->tables, &sys);
+    if (rc != DMD_OK) {
+        h->b.err = nb.err;
+        batch_free(nb);
+        return rc;
+    }
+    nb.cluster = h->b.cluster;
+    nb.cell_div = h->b.cell_div;
+    nb.compact_dn = h->b.compact_dn;
+    std::swap(h->b, nb);
+    batch_free(nb);
+    return DMD_OK;
 }
 int dmd_run(dmd_handle *h, int64_t n_events, dmd_event_log *log) {
     if (!h) return DMD_E_INPUT;

@@ -100,7 +100,7 @@ class GenSpec(C.Structure):
 
 # the symbols include/dmd.h declares
 ENGINE_SYMBOLS = [
-    "dmd_create", "dmd_run", "dmd_predict_all", "dmd_get_state", "dmd_diagnostics", "dmd_get_evcode",
+    "dmd_create", "dmd_run", "dmd_predict_all", "dmd_get_state", "dmd_set_state", "dmd_diagnostics", "dmd_get_evcode",
     "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
@@ -134,6 +134,8 @@ def _declare(lib) -> None:
     lib.dmd_predict_all.argtypes = [C.c_void_p, dbl_p, i32_p, i32_p]
     lib.dmd_predict_all.restype = C.c_int
     lib.dmd_get_state.argtypes = [C.c_void_p] + [C.c_void_p] * 9 + [dbl_p, dbl_p, i64_p]
+    lib.dmd_set_state.argtypes = [C.c_void_p] + [C.c_void_p] * 7 + [C.c_double, C.c_int64]
+    lib.dmd_set_state.restype = C.c_int
     lib.dmd_get_state.restype = C.c_int
     lib.dmd_diagnostics.argtypes = [C.c_void_p, C.POINTER(Diag)]
     lib.dmd_diagnostics.restype = C.c_int

@@ -126,6 +126,29 @@ class Engine:
         _check(self.lib.dmd_get_state(self.h, *args), self.lib, self.h)
         return fin(out)
 
+    def set_state(self, x, y, z, vx, vy, vz, bptnr=None, t: float = 0.0, coll: int = 0):
+        """Restart this system from the given state (positions in box units
+        at time t, velocities, 1-based H-bond partners or None, collision
+        count), as dmd_create from that state would; the previous state
+        stays if the call fails."""
+        cols = [np.ascontiguousarray(a, np.float64) for a in (x, y, z, vx, vy, vz)]
+        if any(c.shape != (self.n,) for c in cols):
+            raise ValueError(f"positions and velocities need {self.n} entries each")
+        bp = None if bptnr is None else np.ascontiguousarray(bptnr, np.int32)
+        if bp is not None and bp.shape != (self.n,):
+            raise ValueError(f"bptnr needs {self.n} entries")
+        _check(self.lib.dmd_set_state(self.h, *[c.ctypes.data for c in cols], None if bp is None else bp.ctypes.data,
+                                      float(t), int(coll)), self.lib, self.h)
+
+    def state_now(self) -> dict:
+        """The state at the current time, in dmd_set_state's terms: positions
+        advanced by vx * tfalse (code/config.f:15-24; dmd_set_state wraps
+        them into the box), velocities, bptnr, t and coll."""
+        s = self.state()
+        out = {k: s[k] + s[v] * s["tfalse"] for k, v in (("x", "vx"), ("y", "vy"), ("z", "vz"))}
+        out.update(vx=s["vx"], vy=s["vy"], vz=s["vz"], bptnr=s["bptnr"], t=s["t"], coll=s["coll"])
+        return out
+
     def diagnostics(self) -> dict:
         d = abi.Diag()
         _check(self.lib.dmd_diagnostics(self.h, C.byref(d)), self.lib, self.h)

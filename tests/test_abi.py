@@ -39,6 +39,7 @@ def test_errors_are_status_codes(built):
     assert rc == -1
     assert b"empty" in lib.dmd_last_error(h)
     lib.dmd_destroy(h)
+    assert lib.dmd_set_state(None, None, None, None, None, None, None, None, 0.0, 0) == -1
 
 
 def test_system_struct_matches_header_layout():

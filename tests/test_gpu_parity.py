@@ -52,6 +52,51 @@ def test_predict_all_initial_c3(built, pick):
     assert np.array_equal(gt, ot)
 
 
+def test_set_state_restarts(built):
+    """dmd_set_state on a running system equals dmd_create from the same
+    state, and both follow the oracle restarted from it (the reference's
+    restart from its records, code/main.F90:240-321), H-bonds included."""
+    import dataclasses
+    spec = dense_system(n_chains=10, L=10, box=38.0, tstar=0.12, seed=21, rng_seed=5)
+    with Engine(spec) as eng:
+        eng.run(40000)
+        now = eng.state_now()
+    assert (now["bptnr"] > 0).any(), "the restart should carry H-bonds"
+    restart = dataclasses.replace(spec, x=now["x"], y=now["y"], z=now["z"], vx=now["vx"], vy=now["vy"], vz=now["vz"],
+                                  bptnr=now["bptnr"], t0=now["t"], coll0=now["coll"])
+    n = 8000
+    with Engine(spec) as eng:
+        eng.run(500)   # another state first
+        eng.set_state(now["x"], now["y"], now["z"], now["vx"], now["vy"], now["vz"], now["bptnr"], now["t"], now["coll"])
+        slog = eng.run(n, log_capacity=n + 64)
+        sst = eng.state()
+    with Engine(restart) as eng:
+        clog = eng.run(n, log_capacity=n + 64)
+    ora = Oracle(restart)
+    olog = ora.run(n, log_capacity=n + 64)
+    ost = ora.state()
+    assert first_mismatch(slog, clog) < 0
+    k = first_mismatch(slog, olog)
+    assert k < 0, f"restart diverges from the oracle at {k}:\n{describe(slog, olog, k)}"
+    for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity", "extra_repuls"):
+        assert np.array_equal(sst[key], ost[key]), key
+    assert sst["t"] == ost["t"] and sst["coll"] == ost["coll"]
+
+
+def test_set_state_rejects_bad_input_and_keeps_state(built):
+    spec = dense_system(seed=6)
+    with Engine(spec) as eng:
+        eng.run(1000)
+        before = eng.state()
+        bad = np.full(eng.n, np.nan)
+        with pytest.raises(Exception):
+            eng.set_state(bad, bad, bad, bad, bad, bad)
+        after = eng.state()
+        for key in ("x", "vx", "bptnr"):
+            assert np.array_equal(before[key], after[key])
+        eng.run(100)
+
+
 def test_c1_event_sequence(built):
     spec = systems.generate(systems.config_c1())
     log = _compare_run(spec, 20000)
