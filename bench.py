@@ -299,6 +299,10 @@ def run_ours(args):
     if rank == 0 and not args.no_single:
         single = run_single_systems(E)
 
+    sidechain = None
+    if rank == 0 and not args.no_sidechain:
+        sidechain = run_sidechain(with_cpu=not args.no_cpu)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = max(1, min(os.cpu_count() or 1, 64))
@@ -326,6 +330,7 @@ def run_ours(args):
             "clocks": clk.summary(),
             "serving": serving,
             "single_system": single,
+            "sidechain_search": sidechain,
         }
         print(json.dumps(line))
     if world > 1:
@@ -351,6 +356,47 @@ def run_single_systems(E: int) -> dict:
         out[name] = {"events_per_s": E / ms * 1e3, "cluster": t["cluster"], "cell_div": t["cell_div"]}
         b.close()
     return out
+
+
+def run_sidechain(with_cpu: bool) -> dict:
+    """The initial-configuration generator's side-chain placement search on
+    its own 22-residue template (the committed fixture of its inputs and
+    results): 22 x 1,401^3 grid points on the GPU, host-timed through the
+    public call (tables, copies, search, read-back) after a warm-up, checked
+    against the fixture's winners; with with_cpu, the CPU restatement's rate
+    on a bounded sample (one residue, 200^3 points)."""
+    import json
+    import numpy as np
+    from dmdgb import systems
+    from dmdgb.params import default_tables
+
+    with open(os.path.join(REPO, "tests", "golden", "sidechain_template.json")) as fh:
+        d = json.load(fh)
+    t = default_tables()
+    t.rca, t.rnh, t.rco, t.sqz = (np.array(d[k]) for k in ("rca", "rnh", "rco", "sqz"))
+    args = [np.array(d[k]) for k in ("ca", "nh", "co", "side_start")]
+    res = d["residues"]
+    systems.sidechain_search(*args, res, d["move"], d["step"], tables=t)   # warm-up
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        out, rmin, idx = systems.sidechain_search(*args, res, d["move"], d["step"], tables=t)
+        times.append(time.perf_counter() - t0)
+    m = int(systems.abi.load_engine().dmd_sidechain_grid(d["move"], d["step"]))
+    points = len(res) * m ** 3
+    sec = statistics.median(times)
+    out_d = {"workload": f"genconfig template, {len(res)} residues x {m}^3 grid points", "ms": sec * 1e3,
+             "points_per_s": points / sec, "matches_reference_fixture": bool(np.array_equal(idx, d["oracle_index"]))}
+    if with_cpu:
+        from oracle import oracle as ora
+        t0 = time.perf_counter()
+        ora.sidechain_search(*args, res, 0.5, d["step"], tables=t, only=(1, 2))
+        cs = time.perf_counter() - t0
+        cm = len(ora.sidechain_grid(0.5, d["step"]))
+        out_d["cpu_points_per_s"] = cm ** 3 / cs
+        out_d["cpu_sample"] = f"CPU restatement, 1 core: one residue, {cm}^3 points, {cs:.2f} s"
+        out_d["cpu_s_for_workload"] = points / out_d["cpu_points_per_s"]
+    return out_d
 
 
 def run_serving(args, scale: float = None) -> dict:
@@ -392,6 +438,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-single", action="store_true")
+    ap.add_argument("--no-sidechain", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-scale", type=float, default=0.01)
     ap.add_argument("--serve-slots", type=int, default=256)

@@ -336,6 +336,32 @@ int dmd_generate(const dmd_gen_spec *spec, const dmd_tables *tables, int32_t n_b
                  double *x, double *y, double *z, double *vx, double *vy, double *vz,
                  char *err, int32_t errlen);
 
+/* The side-chain placement search of the reference's initial-configuration
+ * generator (genconfig/gen_config_random-SQZ.f90:250-348), on the GPU.  For
+ * each of n_res consecutive residues of one chain (positions [n_res][3] in
+ * angstrom: C-alpha, NH, CO, and the side chain's start), the side chain is
+ * moved over the grid of offsets -move .. move in steps of step on each axis
+ * (the generator's Fortran DO loops over real variables: trip count
+ * INT((2 move + step) / step), values by repeated addition; the reference
+ * uses move 3.5, step 0.005, i.e. 1,401^3 points); the winner is the first
+ * point in the generator's loop order (x outermost) with the smallest
+ * r3 = |rca - r(CA)| + |rnh - r(NH)| + |rco - r(CO)| (tables->rca/rnh/rco of
+ * the residue's identity 9..28) below 100 among the points whose distances
+ * to CO and CA of the previous residue and NH and CA of the next one are
+ * not below tables->sqz (sz6, sz8, sz7, sz9).  side_out gets the moved side
+ * chains, rmin_out each residue's r3, index_out (may be NULL) the winning
+ * point (i1 * m + i2) * m + i3 with m = dmd_sidechain_grid(move, step).  A
+ * residue without an admissible point keeps its start (rmin 100, index -1;
+ * the generator would apply the previous residue's offset).  Results are
+ * exactly those of the generator's expressions in double precision.  Up to
+ * 4,096 grid values per axis and 65,535 residues per call. */
+int dmd_sidechain_search(int32_t n_res, const double *ca, const double *nh, const double *co,
+                         const double *side, const int32_t *residue, const dmd_tables *tables,
+                         double move, double step, double *side_out, double *rmin_out,
+                         int64_t *index_out, char *err, int32_t errlen);
+/* grid values per axis of dmd_sidechain_search, -1 for a bad move or step */
+int64_t dmd_sidechain_grid(double move, double step);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,11 @@ int ora_get_scalars(ora_handle *h, double *out, int n);
 int ora_n_outputs(ora_handle *h);
 int ora_get_output(ora_handle *h, int k, dmd_diag *d);
 void ora_destroy(ora_handle *h);
+/* genconfig's side-chain placement search (sidechain_oracle.cpp) */
+int64_t ora_sidechain_grid(double move, double step, double *values, int64_t cap);
+int64_t ora_sidechain_search(int32_t n, const double *ca, const double *nh, const double *co, const double *side,
+                             const int32_t *residue, const dmd_tables *T, double move, double step, int32_t r0,
+                             int32_t r1, double *side_out, double *rmin_out, int64_t *index_out);
 #ifdef __cplusplus
 }
 #endif

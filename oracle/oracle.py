@@ -47,6 +47,12 @@ def lib():
         L.ora_get_output.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.Diag)]
         L.ora_destroy.argtypes = [C.c_void_p]
         L.ora_destroy.restype = None
+        L.ora_sidechain_grid.restype = C.c_int64
+        L.ora_sidechain_grid.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_int64]
+        L.ora_sidechain_search.restype = C.c_int64
+        L.ora_sidechain_search.argtypes = [C.c_int32] + [C.c_void_p] * 5 + [C.POINTER(abi.Tables), C.c_double,
+                                                                              C.c_double, C.c_int32, C.c_int32] + \
+            [C.c_void_p] * 3
         _lib = L
     return _lib
 
@@ -140,3 +146,32 @@ class Oracle:
             self.L.ora_get_output(self.h, k, C.byref(d))
             out.append(d.as_dict())
         return out
+
+
+def sidechain_grid(move: float, step: float) -> np.ndarray:
+    """The offsets of one axis of genconfig's search grid (a Fortran DO loop
+    over a real variable: repeated addition)."""
+    m = lib().ora_sidechain_grid(float(move), float(step), None, 0)
+    out = np.zeros(max(m, 0))
+    lib().ora_sidechain_grid(float(move), float(step), out.ctypes.data, len(out))
+    return out
+
+
+def sidechain_search(ca, nh, co, side, residues, move: float = 3.5, step: float = 0.005, tables=None, only=None):
+    """genconfig's side-chain placement search on the CPU (positions [n, 3]
+    in angstrom): (moved side chains, r3 minima, winning grid indices).
+    only=(r0, r1) searches residues r0..r1-1 and copies the others."""
+    ca, nh, co, side = [np.ascontiguousarray(a, np.float64).reshape(-1, 3) for a in (ca, nh, co, side)]
+    res = np.ascontiguousarray(residues, np.int32)
+    n = len(res)
+    r0, r1 = only if only is not None else (0, n)
+    t = abi.tables_struct(tables or default_tables())
+    out = np.zeros((n, 3))
+    rmin = np.zeros(n)
+    idx = np.zeros(n, np.int64)
+    m = lib().ora_sidechain_search(n, ca.ctypes.data, nh.ctypes.data, co.ctypes.data, side.ctypes.data, res.ctypes.data,
+                                   C.byref(t), float(move), float(step), int(r0), int(r1), out.ctypes.data,
+                                   rmin.ctypes.data, idx.ctypes.data)
+    if m < 0:
+        raise ValueError("bad side-chain search input")
+    return out, rmin, idx

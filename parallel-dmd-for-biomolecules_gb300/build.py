@@ -22,7 +22,7 @@ LIB = os.path.join(OUT, "libdmd_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
-CU_SOURCES = ["engine.cu", "capi.cu"]
+CU_SOURCES = ["engine.cu", "capi.cu", "sidechain.cu"]
 CPP_SOURCES = ["generate.cpp"]
 
 

@@ -109,6 +109,7 @@ ENGINE_SYMBOLS = [
     "dmd_batch_run_graph", "dmd_batch_autotune", "dmd_batch_device_bytes", "dmd_batch_upload_bytes", "dmd_batch_readback_bytes", "dmd_state_bytes", "dmd_save_state", "dmd_load_state",
     "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
     "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
+    "dmd_sidechain_search", "dmd_sidechain_grid",
 ]
 
 REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -136,6 +137,11 @@ def _declare(lib) -> None:
     lib.dmd_get_state.argtypes = [C.c_void_p] + [C.c_void_p] * 9 + [dbl_p, dbl_p, i64_p]
     lib.dmd_set_state.argtypes = [C.c_void_p] + [C.c_void_p] * 7 + [C.c_double, C.c_int64]
     lib.dmd_set_state.restype = C.c_int
+    lib.dmd_sidechain_search.argtypes = [C.c_int32] + [C.c_void_p] * 5 + [C.POINTER(Tables), C.c_double, C.c_double] + \
+        [C.c_void_p] * 3 + [C.c_char_p, C.c_int32]
+    lib.dmd_sidechain_search.restype = C.c_int
+    lib.dmd_sidechain_grid.argtypes = [C.c_double, C.c_double]
+    lib.dmd_sidechain_grid.restype = C.c_int64
     lib.dmd_get_state.restype = C.c_int
     lib.dmd_diagnostics.argtypes = [C.c_void_p, C.POINTER(Diag)]
     lib.dmd_diagnostics.restype = C.c_int

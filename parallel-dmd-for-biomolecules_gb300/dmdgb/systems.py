@@ -105,6 +105,33 @@ def generate(spec: SystemSpec, tables: Optional[Tables] = None, min_sep: float =
     return spec
 
 
+def sidechain_search(ca, nh, co, side, residues, move: float = 3.5, step: float = 0.005,
+                     tables: Optional[Tables] = None):
+    """The initial-configuration generator's side-chain placement search
+    (genconfig/gen_config_random-SQZ.f90:250-348) on the GPU, for the
+    consecutive residues of one chain: positions [n, 3] in angstrom
+    (C-alpha, NH, CO, side-chain start), identities 9..28.  Returns the moved
+    side chains [n, 3], each residue's r3 and its winning grid point (-1:
+    none admissible, side chain left at its start)."""
+    lib = abi.load_engine()
+    ca, nh, co, side = [np.ascontiguousarray(a, np.float64).reshape(-1, 3) for a in (ca, nh, co, side)]
+    res = np.ascontiguousarray(residues, np.int32)
+    n = len(res)
+    if not (len(ca) == len(nh) == len(co) == len(side) == n):
+        raise ValueError("one C-alpha, NH, CO and side-chain position per residue")
+    t = abi.tables_struct(tables or default_tables())
+    out = np.zeros((n, 3))
+    rmin = np.zeros(n)
+    idx = np.zeros(n, np.int64)
+    err = C.create_string_buffer(256)
+    rc = lib.dmd_sidechain_search(n, ca.ctypes.data, nh.ctypes.data, co.ctypes.data, side.ctypes.data,
+                                  res.ctypes.data, C.byref(t), float(move), float(step), out.ctypes.data,
+                                  rmin.ctypes.data, idx.ctypes.data, err, 256)
+    if rc != 0:
+        raise RuntimeError(f"dmd_sidechain_search failed ({abi.ERRORS.get(rc, rc)}): {err.value.decode()}")
+    return out, rmin, idx
+
+
 def random_sequence(rng: np.random.Generator, length: int) -> List[int]:
     """Residue identities uniform over the 20 PRIME20 types (9..28)."""
     return [int(v) for v in rng.integers(9, 29, size=length)]
