@@ -34,6 +34,17 @@
  * first minimum of its points (it visits them in increasing grid index);
  * the blocks and then the residues' partial results are reduced by
  * (r3, grid index), which gives the reference's first minimum.
+ *
+ * Pruning across threads.  The screen's limit is the smallest of the
+ * thread's own best r3 and the best any thread of the residue has found so
+ * far (a float, atomicMin on its bits), plus MARGIN: a point above it has an
+ * exact r3 above that best and can neither win nor tie.  A whole line is
+ * skipped when sum over CA, NH, CO of max(0, r_xy - bond) exceeds the limit,
+ * r_xy being the distance from the line's (i1, i2) part alone: along the
+ * line the squared distance only grows ((X + Y) + Z >= X + Y exactly, and the
+ * rounded square root is monotone), so every point's exact r3 is at least
+ * that sum, which the float value (distances within 4.2e-6 A) undershoots by
+ * less than MARGIN.
  */
 #include <cuda_runtime.h>
 
@@ -69,7 +80,7 @@ __device__ __forceinline__ bool sc_less(double a, long long ia, double b, long l
 /* tables: [residue][axis][ref][m] doubles (tab64) and floats (tab32) */
 __global__ void __launch_bounds__(SC_THREADS) k_sidechain(const ScResidue *res, const double *tab64,
                                                           const float *tab32, int m, double *part_r3,
-                                                          long long *part_idx) {
+                                                          long long *part_idx, unsigned int *glim) {
     extern __shared__ float zsh[];  /* [SC_REFS][m] */
     const int r = blockIdx.y;
     const ScResidue R = res[r];
@@ -89,6 +100,15 @@ __global__ void __launch_bounds__(SC_THREADS) k_sidechain(const ScResidue *res, 
         float xy[SC_REFS];
 #pragma unroll
         for (int j = 0; j < SC_REFS; ++j) xy[j] = X32[j * m + i1] + Y32[j * m + i2];
+        lim = fminf(lim, __uint_as_float(*(volatile unsigned int *)(glim + r)));
+        {
+            const float b[3] = {R.bdf, R.bnf, R.bcf};
+            float lb = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                if (xy[j] > 0.0f) lb += fmaxf(0.0f, xy[j] * rsqrtf(xy[j]) - b[j]);
+            if (lb > lim) continue;
+        }
         for (int i3 = 0; i3 < m; ++i3) {
             float q[SC_REFS];
 #pragma unroll
@@ -113,6 +133,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_sidechain(const ScResidue *res, 
                 best = r3;
                 bidx = ((long long)i1 * m + i2) * m + i3;
                 lim = (float)(best + (double)SC_MARGIN);
+                atomicMin(glim + r, __float_as_uint(lim));
             }
         }
     }
@@ -253,10 +274,12 @@ extern "C" int dmd_sidechain_search(int32_t n_res, const double *ca, const doubl
     float *d32 = nullptr;
     long long *p_idx = nullptr, *o_idx = nullptr;
     ScResidue *dres = nullptr;
+    unsigned int *dlim = nullptr;
     std::vector<double> h_r3(n_res);
     std::vector<long long> h_idx(n_res);
     auto done = [&](cudaError_t ce) {
         cudaFree(d64); cudaFree(d32); cudaFree(p_r3); cudaFree(p_idx); cudaFree(o_r3); cudaFree(o_idx); cudaFree(dres);
+        cudaFree(dlim);
         return ce;
     };
     e = cudaMalloc(&d64, t64.size() * sizeof(double));
@@ -266,13 +289,22 @@ extern "C" int dmd_sidechain_search(int32_t n_res, const double *ca, const doubl
     if (e == cudaSuccess) e = cudaMalloc(&o_r3, (size_t)n_res * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&o_idx, (size_t)n_res * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&dres, (size_t)n_res * sizeof(ScResidue));
+    if (e == cudaSuccess) e = cudaMalloc(&dlim, (size_t)n_res * sizeof(unsigned int));
+    {
+        /* the residues' shared limits start at 100 + MARGIN, the threads' own */
+        const float l0 = 100.0f + SC_MARGIN;
+        unsigned int bits = 0;
+        std::memcpy(&bits, &l0, sizeof bits);
+        const std::vector<unsigned int> init((size_t)n_res, bits);
+        if (e == cudaSuccess) e = cudaMemcpy(dlim, init.data(), init.size() * sizeof(unsigned int), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(d64, t64.data(), t64.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dres, hres.data(), hres.size() * sizeof(ScResidue), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && smem > 48 * 1024)
         e = cudaFuncSetAttribute(k_sidechain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) {
-        k_sidechain<<<dim3(nb, n_res), SC_THREADS, smem>>>(dres, d64, d32, m, p_r3, p_idx);
+        k_sidechain<<<dim3(nb, n_res), SC_THREADS, smem>>>(dres, d64, d32, m, p_r3, p_idx, dlim);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
