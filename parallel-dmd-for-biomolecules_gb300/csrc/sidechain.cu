@@ -45,6 +45,15 @@
  * rounded square root is monotone), so every point's exact r3 is at least
  * that sum, which the float value (distances within 4.2e-6 A) undershoots by
  * less than MARGIN.
+ *
+ * Seeding.  Before the scan, k_sidechain_seed walks every SC_SEED_STRIDE-th
+ * grid value of each axis in single precision, keeps per thread the point
+ * of smallest r3 estimate among those whose squeeze distances are certainly
+ * clear (float squared distance above L^2 (1 + 1e-5)), evaluates that one
+ * point exactly and, when it is admissible, lowers the residue's shared
+ * limit to its exact r3 + MARGIN.  The seed is a point of the full grid, so
+ * the winner's r3 is at most its r3 and the pruning argument above holds
+ * from the first line of the scan on.
  */
 #include <cuda_runtime.h>
 
@@ -64,11 +73,14 @@ constexpr int SC_THREADS = 256;
 constexpr int SC_MAX_GRID = 4096;   /* grid values per axis (shared memory: 7 x 4 B each) */
 constexpr float SC_MARGIN = 1e-4f;
 constexpr double SC_SQZ_LO = 1.0 - 1e-5;
+constexpr double SC_SQZ_HI = 1.0 + 1e-5;
+constexpr int SC_SEED_STRIDE = 8;
 
 struct ScResidue {
     double bd, bn, bc;              /* bdln, bl_rn, bl_rc */
     double lim[4];                  /* squeeze limits of refs 3..6 (sz6, sz8, sz7, sz9) */
     float lo2[4];                   /* certainly-violated bound of each squared distance */
+    float hi2[4];                   /* certainly-clear bound of each squared distance */
     float bdf, bnf, bcf;
     int present;                    /* bit j: reference j exists */
 };
@@ -159,6 +171,54 @@ __global__ void __launch_bounds__(SC_THREADS) k_sidechain(const ScResidue *res, 
     }
 }
 
+/* the residue's exact r3 at grid point (i1, i2, i3), or a negative value
+ * when a squeeze limit is violated */
+__device__ double sc_exact(const ScResidue &R, const double *X64, const double *Y64, const double *Z64, int m,
+                           int i1, int i2, int i3) {
+    const bool prev = (R.present >> 3) & 1, next = (R.present >> 5) & 1;
+    double d[SC_REFS];
+#pragma unroll
+    for (int j = 0; j < SC_REFS; ++j) d[j] = sqrt(X64[j * m + i1] + Y64[j * m + i2] + Z64[j * m + i3]);
+    bool isz = false;
+    if (prev) isz = d[3] < R.lim[0] || d[4] < R.lim[1];
+    if (next) isz = isz || d[5] < R.lim[2] || d[6] < R.lim[3];
+    return isz ? -1.0 : fabs(R.bd - d[0]) + fabs(R.bn - d[1]) + fabs(R.bc - d[2]);
+}
+
+/* the coarse pre-pass: an admissible upper bound of each residue's winner */
+__global__ void __launch_bounds__(SC_THREADS) k_sidechain_seed(const ScResidue *res, const double *tab64,
+                                                               const float *tab32, int m, unsigned int *glim) {
+    const int r = blockIdx.y;
+    const ScResidue R = res[r];
+    const size_t per_axis = (size_t)SC_REFS * m;
+    const double *X64 = tab64 + (size_t)r * 3 * per_axis, *Y64 = X64 + per_axis, *Z64 = Y64 + per_axis;
+    const float *X32 = tab32 + (size_t)r * 3 * per_axis, *Y32 = X32 + per_axis, *Z32 = Y32 + per_axis;
+    const bool prev = (R.present >> 3) & 1, next = (R.present >> 5) & 1;
+    const int mc = (m + SC_SEED_STRIDE - 1) / SC_SEED_STRIDE;
+    const long long total = (long long)mc * mc * mc;
+    float bestf = 3.0e38f;
+    int b1 = -1, b2 = 0, b3 = 0;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < total;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int i1 = (int)(p / ((long long)mc * mc)) * SC_SEED_STRIDE;
+        const int i2 = (int)((p / mc) % mc) * SC_SEED_STRIDE, i3 = (int)(p % mc) * SC_SEED_STRIDE;
+        float q[SC_REFS];
+#pragma unroll
+        for (int j = 0; j < SC_REFS; ++j) q[j] = X32[j * m + i1] + Y32[j * m + i2] + Z32[j * m + i3];
+        bool clear = true;
+        if (prev) clear = q[3] > R.hi2[0] && q[4] > R.hi2[1];
+        if (next) clear = clear && q[5] > R.hi2[2] && q[6] > R.hi2[3];
+        if (!clear || !(q[0] > 0.0f && q[1] > 0.0f && q[2] > 0.0f)) continue;
+        const float est = fabsf(R.bdf - q[0] * rsqrtf(q[0])) + fabsf(R.bnf - q[1] * rsqrtf(q[1])) +
+                          fabsf(R.bcf - q[2] * rsqrtf(q[2]));
+        if (est < bestf) { bestf = est; b1 = i1; b2 = i2; b3 = i3; }
+    }
+    if (b1 >= 0) {
+        const double r3 = sc_exact(R, X64, Y64, Z64, m, b1, b2, b3);
+        if (r3 >= 0.0 && r3 < 100.0) atomicMin(glim + r, __float_as_uint((float)(r3 + (double)SC_MARGIN)));
+    }
+}
+
 /* one block per residue: the minimum over the blocks' partial results */
 __global__ void __launch_bounds__(SC_THREADS) k_sidechain_reduce(const double *part_r3, const long long *part_idx,
                                                                  int nparts, double *out_r3, long long *out_idx) {
@@ -243,7 +303,10 @@ extern "C" int dmd_sidechain_search(int32_t n_res, const double *ca, const doubl
         R.bdf = (float)R.bd; R.bnf = (float)R.bn; R.bcf = (float)R.bc;
         /* sqz6to10.data columns: sz8, sz6, sz7, sz9 (genconfig's SQZ610(1..4)) */
         R.lim[0] = T->sqz[row][1]; R.lim[1] = T->sqz[row][0]; R.lim[2] = T->sqz[row][2]; R.lim[3] = T->sqz[row][3];
-        for (int q = 0; q < 4; ++q) R.lo2[q] = (float)(R.lim[q] * R.lim[q] * SC_SQZ_LO);
+        for (int q = 0; q < 4; ++q) {
+            R.lo2[q] = (float)(R.lim[q] * R.lim[q] * SC_SQZ_LO);
+            R.hi2[q] = (float)(R.lim[q] * R.lim[q] * SC_SQZ_HI);
+        }
         const bool prev = k >= 1, next = k + 1 < n_res;
         R.present = 7 | (prev ? (8 | 16) : 0) | (next ? (32 | 64) : 0);
         const double *refs[SC_REFS] = {ca + 3 * k, nh + 3 * k, co + 3 * k, prev ? co + 3 * (k - 1) : ca + 3 * k,
@@ -303,6 +366,12 @@ extern "C" int dmd_sidechain_search(int32_t n_res, const double *ca, const doubl
     if (e == cudaSuccess) e = cudaMemcpy(dres, hres.data(), hres.size() * sizeof(ScResidue), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && smem > 48 * 1024)
         e = cudaFuncSetAttribute(k_sidechain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+        long long ws = (long long)sms * 4 / n_res;
+        if (ws < 1) ws = 1;
+        k_sidechain_seed<<<dim3((unsigned)ws, n_res), SC_THREADS>>>(dres, d64, d32, m, dlim);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) {
         k_sidechain<<<dim3(nb, n_res), SC_THREADS, smem>>>(dres, d64, d32, m, p_r3, p_idx, dlim);
         e = cudaGetLastError();
