@@ -1,0 +1,187 @@
+"""The library's host code (capi.cu: set-up, pools, copies, launch
+parameters, state read-back and replacement) on the CPU, linked against a
+stand-in CUDA runtime (tests/host_mock/): device memory is host memory and
+a launch checks what its kernel would be given instead of running it."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+import types
+
+import numpy as np
+import pytest
+
+from dmdgb import abi, systems
+from dmdgb.params import default_tables
+from helpers import dense_system
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+MOCK = os.path.join(HERE, "host_mock")
+CSRC = os.path.join(REPO, "parallel-dmd-for-biomolecules_gb300", "csrc")
+OUT = os.path.join(MOCK, "_build")
+LIB = os.path.join(OUT, "libdmd_hostmock.so")
+
+
+def _build() -> str:
+    srcs = [os.path.join(CSRC, "capi.cu"), os.path.join(CSRC, "generate.cpp"), os.path.join(MOCK, "mock_rt.cpp"),
+            os.path.join(MOCK, "mock_engine.cu")]
+    deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(REPO, "include", "dmd.h")]
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in deps):
+        return LIB
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    os.makedirs(OUT, exist_ok=True)
+    inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC]
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+    objs = []
+    for s in srcs:
+        o = os.path.join(OUT, os.path.basename(s) + ".o")
+        if s.endswith(".cu"):
+            cmd = [nvcc, "-O1", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"] + inc + ["-c", s, "-o", o]
+        else:
+            cmd = ["g++", "-O1", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + cuda_inc] + inc + ["-c", s, "-o", o]
+        subprocess.run(cmd, check=True, capture_output=True)
+        objs.append(o)
+    subprocess.run(["g++", "-shared", "-o", LIB + ".tmp"] + objs + ["-Wl,--no-undefined"], check=True,
+                   capture_output=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class _Tolerant:
+    """abi's declarations, skipping the entry points this library leaves out."""
+    def __init__(self, lib):
+        self._lib = lib
+
+    def __getattr__(self, name):
+        try:
+            return getattr(self._lib, name)
+        except AttributeError:
+            return types.SimpleNamespace()
+
+
+@pytest.fixture(scope="module")
+def mock():
+    lib = C.CDLL(_build())
+    abi._declare(_Tolerant(lib))
+    lib.mock_report.restype = C.c_char_p
+    lib.mock_live_allocations.restype = C.c_size_t
+    lib.mock_counts.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong),
+                                C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    return lib
+
+
+def counts(lib):
+    v = [C.c_int(), C.c_int(), C.c_int(), C.c_longlong(), C.c_int(), C.c_int()]
+    lib.mock_counts(*[C.byref(x) for x in v])
+    return [x.value for x in v]
+
+
+def state_of(lib, h, r, n, batch=True):
+    f = np.zeros((6, n))
+    i = np.zeros((6, n), np.int32)
+    t, tf, coll = C.c_double(), C.c_double(), C.c_int64()
+    args = [f[k].ctypes.data for k in range(6)] + [i[0].ctypes.data, i[1].ctypes.data, i[2].ctypes.data]
+    if batch:
+        rc = lib.dmd_batch_get_state(h, r, *args, C.byref(t), C.byref(tf), C.byref(coll))
+    else:
+        rc = lib.dmd_get_state(h, *args, C.byref(t), C.byref(tf), C.byref(coll))
+    assert rc == 0
+    return f, i, t.value, coll.value
+
+
+def test_layout_checker_flags_an_overlap(mock):
+    assert mock.mock_selftest() == 1
+
+
+def test_batch_pools_launches_and_state(mock):
+    """Five 32-replica-workload systems and three KLVFFAE systems in one
+    batch: every launch's pools are laid out as the kernels index them, the
+    chain tables are right, and the state read back is the input wrapped
+    into the box with no H-bond."""
+    specs = sorted(systems.config_c3(32, seed=1), key=lambda s: s.n_beads)[:4] + [systems.config_c3(32, seed=1)[31]]
+    specs += [systems.klvffae_system(4, 5.0, 0.2 + 0.05 * r, seed=r + 1) for r in range(3)]
+    for s in specs:
+        systems.generate(s)
+    n = len(specs)
+    tabs = abi.tables_struct(default_tables())
+    cfgs = (abi.RunCfg * n)(*[s.run_cfg(0, 0) for s in specs])
+    syss = (abi.System * n)(*[s.c_system() for s in specs])
+    mock.mock_reset()
+    base = mock.mock_live_allocations()
+    h = C.c_void_p()
+    assert mock.dmd_batch_create(n, cfgs, C.byref(tabs), syss, C.byref(h)) == 0, mock.dmd_batch_last_error(h)
+    cap = 64
+    bufs = [np.zeros(cap, abi.EVENT_DTYPE) for _ in range(n)]
+    logs = (abi.EventLog * n)(*[abi.EventLog(b.ctypes.data_as(C.POINTER(abi.Event)), cap, 0) for b in bufs])
+    assert mock.dmd_batch_run(h, 1000, logs) == 0, mock.dmd_batch_last_error(h)
+    d = abi.Diag()
+    assert mock.dmd_batch_diagnostics(h, 2, C.byref(d)) == 0
+    init, run, diag, target, C_, compact = counts(mock)
+    assert (init, diag) == (1, 1) and run >= 1 and target == 1000
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    for r, s in enumerate(specs):
+        f, i, t, coll = state_of(mock, h, r, s.n_beads)
+        for k, a in enumerate((s.x, s.y, s.z)):
+            assert np.array_equal(f[k], a - np.round(a))
+        for k, a in enumerate((s.vx, s.vy, s.vz)):
+            assert np.array_equal(f[3 + k], a)
+        assert (i[0] == 0).all() and (i[2] == 0).all()          # bptnr, extra_repuls: none (1-based 0)
+        assert set(np.unique(i[1]).tolist()) <= set([1, 2, 4] + list(range(10, 29)))
+        assert t == 0.0 and coll == 0
+    mock.dmd_batch_destroy(h)
+    assert mock.mock_live_allocations() <= base + 1          # the pinned stage stays for the next creation
+
+
+def test_set_state_replaces_in_place_and_keeps_state_on_error(mock):
+    spec = systems.generate(dense_system(seed=6))
+    n = spec.n_beads
+    tabs = abi.tables_struct(default_tables())
+    cfg = spec.run_cfg(0, 0)
+    sys_ = spec.c_system()
+    mock.mock_reset()
+    base = mock.mock_live_allocations()
+    h = C.c_void_p()
+    assert mock.dmd_create(C.byref(cfg), C.byref(tabs), C.byref(sys_), C.byref(h)) == 0
+    rng = np.random.default_rng(2)
+    new = [np.ascontiguousarray(a) + rng.normal(0, 1e-3, n) for a in (spec.x, spec.y, spec.z)]
+    newv = [np.ascontiguousarray(a) * 0.5 for a in (spec.vx, spec.vy, spec.vz)]
+    cols = new + newv
+    assert mock.dmd_set_state(h, *[c.ctypes.data for c in cols], None, 2.5, 1234) == 0, mock.dmd_last_error(h)
+    f, i, t, coll = state_of(mock, h, 0, n, batch=False)
+    assert t == 2.5 and coll == 1234
+    for k in range(3):
+        assert np.array_equal(f[k], cols[k] - np.round(cols[k])) and np.array_equal(f[3 + k], cols[3 + k])
+    bad = np.full(n, np.nan)
+    assert mock.dmd_set_state(h, *[bad.ctypes.data] * 6, None, 0.0, 0) == -1
+    assert b"non-finite" in mock.dmd_last_error(h)
+    f2, i2, t2, coll2 = state_of(mock, h, 0, n, batch=False)
+    assert np.array_equal(f2, f) and t2 == 2.5 and coll2 == 1234
+    short = np.zeros(n, np.int32)
+    short[0] = n + 5                                          # a partner beyond the system
+    assert mock.dmd_set_state(h, *[c.ctypes.data for c in cols], short.ctypes.data, 0.0, 0) == -1
+    assert mock.dmd_run(h, 500, None) == 0
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    mock.dmd_destroy(h)
+    assert mock.mock_live_allocations() <= base + 1
+
+
+def test_creation_errors_leave_nothing_behind(mock):
+    """A system that fails its set-up returns DMD_E_INPUT with the
+    replica's index, and destroying the handle frees everything."""
+    good = systems.generate(systems.klvffae_system(2, 5.0, 0.2, seed=1))
+    bad = systems.generate(systems.klvffae_system(2, 5.0, 0.2, seed=2))
+    bad.vx = bad.vx.copy()
+    bad.vx[3] = np.inf
+    specs = [good, bad]
+    tabs = abi.tables_struct(default_tables())
+    cfgs = (abi.RunCfg * 2)(*[s.run_cfg(0, 0) for s in specs])
+    syss = (abi.System * 2)(*[s.c_system() for s in specs])
+    base = mock.mock_live_allocations()
+    h = C.c_void_p()
+    assert mock.dmd_batch_create(2, cfgs, C.byref(tabs), syss, C.byref(h)) == -1
+    assert b"system 1" in mock.dmd_batch_last_error(h)
+    mock.dmd_batch_destroy(h)
+    assert mock.mock_live_allocations() <= base + 1
