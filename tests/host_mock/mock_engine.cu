@@ -104,11 +104,25 @@ cudaError_t dmd_launch_init(DSys *d, int nsys, int, cudaStream_t) {
     check("init", d, nsys, nullptr, nullptr, nullptr);
     return cudaSuccess;
 }
-cudaError_t dmd_launch_run(DSys *d, int nsys, int, int C, int compact, long long target, const long long *, int,
-                           const int *cs, const int *cl, const int *co, dmd_diag *, cudaStream_t) {
+/* the run launch also stands in for the kernel's bookkeeping: every system
+ * counts its target (the per-system one when given) as done, 1,000 cycles
+ * per event, and its collision count advances by as much; positions do not
+ * move */
+cudaError_t dmd_launch_run(DSys *d, int nsys, int, int C, int compact, long long target, const long long *targets,
+                           int, const int *cs, const int *cl, const int *co, dmd_diag *, cudaStream_t) {
     ++g_run;
     g_last_target = target; g_last_C = C; g_last_compact = compact;
     check("run", d, nsys, cs, cl, co);
+    for (int r = 0; r < nsys; ++r) {
+        DScal &sc = *d[r].sc;
+        const long long t = targets ? targets[r] : target;
+        sc.done = t;
+        sc.done_all += t;
+        sc.coll += t;
+        sc.run_cycles = 1000 * t;
+        sc.need_full = 0;
+        sc.stop = 0;
+    }
     return cudaSuccess;
 }
 cudaError_t dmd_max_active_clusters(int, int *n) { *n = 1000; return cudaSuccess; }

@@ -130,7 +130,7 @@ def test_batch_pools_launches_and_state(mock):
             assert np.array_equal(f[3 + k], a)
         assert (i[0] == 0).all() and (i[2] == 0).all()          # bptnr, extra_repuls: none (1-based 0)
         assert set(np.unique(i[1]).tolist()) <= set([1, 2, 4] + list(range(10, 29)))
-        assert t == 0.0 and coll == 0
+        assert t == 0.0 and coll == 1000                          # the stand-in kernel counts its target
     mock.dmd_batch_destroy(h)
     assert mock.mock_live_allocations() <= base + 1          # the pinned stage stays for the next creation
 
@@ -185,3 +185,102 @@ def test_creation_errors_leave_nothing_behind(mock):
     assert b"system 1" in mock.dmd_batch_last_error(h)
     mock.dmd_batch_destroy(h)
     assert mock.mock_live_allocations() <= base + 1
+
+
+def _server(lib, slots, budget, chunk):
+    s = C.c_void_p()
+    assert lib.dmd_server_create(slots, budget, chunk, C.byref(s)) == 0
+    return s
+
+
+def _submit(lib, s, spec, n_events):
+    tabs = abi.tables_struct(default_tables())
+    cfg = spec.run_cfg(0, 0)
+    sys_ = spec.c_system()
+    rid = C.c_int64()
+    rc = lib.dmd_server_submit(s, C.byref(cfg), C.byref(tabs), C.byref(sys_), n_events, C.byref(rid))
+    return rc, rid.value
+
+
+def _status(lib, s, rid):
+    st, done = C.c_int32(), C.c_int64()
+    ts, ta, tf = C.c_double(), C.c_double(), C.c_double()
+    rc = lib.dmd_server_status(s, rid, C.byref(st), C.byref(done), C.byref(ts), C.byref(ta), C.byref(tf))
+    return rc, st.value, done.value, ta.value
+
+
+def _drain(lib, s, ids, limit=200):
+    max_active, steps = 0, 0
+    while True:
+        na, nf = C.c_int32(), C.c_int32()
+        assert lib.dmd_server_step(s, C.byref(na), C.byref(nf)) == 0, lib.dmd_server_last_error(s)
+        max_active = max(max_active, na.value)
+        steps += 1
+        if all(_status(lib, s, i)[1] == 2 for i in ids):
+            return max_active, steps
+        assert steps < limit
+
+
+def test_server_admits_in_order_within_slots_and_chunks(mock):
+    """Requests are admitted first in, first out, never more than the slots
+    at once; each step advances a request by at most its chunk-sized target
+    until its events are done; the result is its own state."""
+    specs = [systems.generate(systems.klvffae_system(2 + r % 3, 5.0, 0.2, seed=r + 1)) for r in range(6)]
+    events = [2500, 1000, 3000, 500, 1000, 1500]
+    mock.mock_reset()
+    s = _server(mock, 2, 0, 1000)
+    ids = []
+    for spec, ev in zip(specs, events):
+        rc, rid = _submit(mock, s, spec, ev)
+        assert rc == 0
+        ids.append(rid)
+    max_active, steps = _drain(mock, s, ids)
+    assert max_active <= 2
+    admits = [_status(mock, s, i)[3] for i in ids]
+    assert admits == sorted(admits)
+    for rid, ev, spec in zip(ids, events, specs):
+        rc, st, done, _ = _status(mock, s, rid)
+        assert (rc, st, done) == (0, 2, ev)
+        n = spec.n_beads
+        f = np.zeros((6, n))
+        i = np.zeros((2, n), np.int32)
+        t, tf, coll = C.c_double(), C.c_double(), C.c_int64()
+        d = abi.Diag()
+        assert mock.dmd_server_result(s, rid, C.byref(d), *[abi.ptr(f[k], abi.dbl_p) for k in range(6)],
+                                      abi.ptr(i[0], abi.i32_p), abi.ptr(i[1], abi.i32_p), C.byref(t), C.byref(tf),
+                                      C.byref(coll)) == 0
+        assert np.array_equal(f[0], spec.x - np.round(spec.x)) and np.array_equal(f[5], spec.vz)
+        assert coll.value == ev
+        assert mock.dmd_server_release(s, rid) == 0
+        assert _status(mock, s, rid)[0] != 0
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    mock.dmd_server_destroy(s)
+
+
+def test_server_respects_the_memory_budget(mock):
+    """A budget that holds one request's pool admits one at a time; a request
+    larger than the budget is refused at submission."""
+    spec = systems.generate(systems.klvffae_system(3, 5.0, 0.2, seed=4))
+    s = _server(mock, 8, 0, 1000)
+    rc, rid = _submit(mock, s, spec, 1000)
+    na, nf = C.c_int32(), C.c_int32()
+    assert rc == 0 and mock.dmd_server_step(s, C.byref(na), C.byref(nf)) == 0
+    steps, events, wait, act, used, budget = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64()
+    ms = C.c_double()
+    assert mock.dmd_server_stats(s, C.byref(steps), C.byref(events), C.byref(ms), C.byref(wait), C.byref(act),
+                                 C.byref(used), C.byref(budget)) == 0
+    need = used.value
+    assert need > 0
+    mock.dmd_server_destroy(s)
+    s = _server(mock, 8, int(need * 1.5), 1000)
+    ids = []
+    for r in range(3):
+        rc, rid = _submit(mock, s, systems.generate(systems.klvffae_system(3, 5.0, 0.2, seed=10 + r)), 2000)
+        assert rc == 0
+        ids.append(rid)
+    max_active, _ = _drain(mock, s, ids)
+    assert max_active == 1
+    big = systems.generate(systems.klvffae_system(12, 5.0, 0.2, seed=20))
+    rc, _ = _submit(mock, s, big, 1000)
+    assert rc == -7 and b"budget" in mock.dmd_server_last_error(s)
+    mock.dmd_server_destroy(s)
