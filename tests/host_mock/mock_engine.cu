@@ -23,6 +23,8 @@ std::string g_report;
 int g_init = 0, g_run = 0, g_diag = 0;
 long long g_last_target = -2;
 int g_last_C = 0, g_last_compact = -1;
+int g_handoff = -1;                  /* system that outgrows the compact variant at its next compact launch */
+std::vector<long long> g_last_targets;
 
 struct Span { const char *name; const void *p; size_t n; };
 
@@ -93,7 +95,11 @@ void check(const char *what, const DSys *d, int nsys, const int *cs, const int *
 
 extern "C" {
 const char *mock_report(void) { return g_report.c_str(); }
-void mock_reset(void) { g_report.clear(); g_init = g_run = g_diag = 0; }
+void mock_reset(void) { g_report.clear(); g_init = g_run = g_diag = 0; g_handoff = -1; g_last_targets.clear(); }
+void mock_set_handoff(int system) { g_handoff = system; }
+long long mock_last_target_of(int system) {
+    return system >= 0 && system < (int)g_last_targets.size() ? g_last_targets[system] : -2;
+}
 void mock_counts(int *init, int *run, int *diag, long long *target, int *C, int *compact) {
     *init = g_init; *run = g_run; *diag = g_diag; *target = g_last_target; *C = g_last_C; *compact = g_last_compact;
 }
@@ -107,20 +113,29 @@ cudaError_t dmd_launch_init(DSys *d, int nsys, int, cudaStream_t) {
 /* the run launch also stands in for the kernel's bookkeeping: every system
  * counts its target (the per-system one when given) as done, 1,000 cycles
  * per event, and its collision count advances by as much; positions do not
- * move */
+ * move.  The system set by mock_set_handoff stops halfway at its next compact
+ * launch with need_full set, as a system whose lists outgrew the compact
+ * variant at a rebuild does. */
 cudaError_t dmd_launch_run(DSys *d, int nsys, int, int C, int compact, long long target, const long long *targets,
                            int, const int *cs, const int *cl, const int *co, dmd_diag *, cudaStream_t) {
     ++g_run;
     g_last_target = target; g_last_C = C; g_last_compact = compact;
     check("run", d, nsys, cs, cl, co);
+    g_last_targets.assign(nsys, 0);
     for (int r = 0; r < nsys; ++r) {
         DScal &sc = *d[r].sc;
-        const long long t = targets ? targets[r] : target;
+        long long t = targets ? targets[r] : target;
+        g_last_targets[r] = t;
+        sc.need_full = 0;
+        if (compact > 0 && r == g_handoff) {
+            t = t / 2;
+            sc.need_full = 1;
+            g_handoff = -1;
+        }
         sc.done = t;
         sc.done_all += t;
         sc.coll += t;
         sc.run_cycles = 1000 * t;
-        sc.need_full = 0;
         sc.stop = 0;
     }
     return cudaSuccess;

@@ -284,3 +284,29 @@ def test_server_respects_the_memory_budget(mock):
     rc, _ = _submit(mock, s, big, 1000)
     assert rc == -7 and b"budget" in mock.dmd_server_last_error(s)
     mock.dmd_server_destroy(s)
+
+
+def test_compact_variant_hands_over_to_the_full_one(mock):
+    """A system whose lists outgrow the compact variant stops with need_full;
+    the host runs the full variant for that system's remaining events only
+    (the others enter with target 0), and every system ends with its target."""
+    mock.mock_set_handoff.argtypes = [C.c_int]
+    mock.mock_last_target_of.restype = C.c_longlong
+    mock.mock_last_target_of.argtypes = [C.c_int]
+    specs = [systems.generate(systems.klvffae_system(3, 5.0, 0.2 + 0.02 * r, seed=30 + r)) for r in range(4)]
+    n = len(specs)
+    tabs = abi.tables_struct(default_tables())
+    cfgs = (abi.RunCfg * n)(*[s.run_cfg(0, 0) for s in specs])
+    syss = (abi.System * n)(*[s.c_system() for s in specs])
+    mock.mock_reset()
+    h = C.c_void_p()
+    assert mock.dmd_batch_create(n, cfgs, C.byref(tabs), syss, C.byref(h)) == 0
+    mock.mock_set_handoff(2)
+    assert mock.dmd_batch_run(h, 3001, None) == 0, mock.dmd_batch_last_error(h)
+    init, run, diag, target, C_, compact = counts(mock)
+    assert run == 2 and compact == 0 and target == 0           # the follow-up: full variant, per-system targets
+    assert [mock.mock_last_target_of(r) for r in range(n)] == [0, 0, 3001 - 1500, 0]
+    for r, s in enumerate(specs):
+        assert state_of(mock, h, r, s.n_beads)[3] == 3001
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    mock.dmd_batch_destroy(h)
