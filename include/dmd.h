@@ -210,16 +210,21 @@ int dmd_static_evcode(const dmd_run_cfg *cfg, const dmd_tables *tables, const dm
  * a serving process that reserves a fixed budget up front), where a
  * cudaMalloc would synchronise the device, fail, or break that accounting.
  * The caller passes the same host inputs as dmd_create and three device
- * buffers of n_beads entries that receive the full prediction pass
- * (code/events.f): times, 1-based partners, event types.  All intermediate
+ * buffers of n_beads entries that receive the full prediction pass: times,
+ * 1-based partners, event types, equal to what dmd_predict_all returns right
+ * after dmd_create from the same inputs.  All intermediate
  * data lives in one static device array of 8 MiB inside the library, which
  * every GPU that loads the library holds until the process exits; systems of
  * at most 8192 beads, neighbour lists of at most 64 entries (list_cap) and a
  * rebuild grid of at most 48 cells per side fit, and larger inputs are
  * rejected with DMD_E_CAPACITY and a message.  The first call on a device
- * looks up the array's address (with that device current); make that first
- * call before any stream capture.  Every call reuses the array: calls whose
- * work overlaps on the GPU (different streams or host threads) race on it.
+ * looks up the array's address there (with that device current) and keeps
+ * it for later calls.  The call copies its inputs from
+ * pageable host memory and waits for the stream, so it may not be called
+ * while any stream is being captured into a CUDA graph; such a call returns
+ * DMD_E_STATE with a message and leaves the capture alone.  Every call
+ * reuses the array: calls whose work overlaps on the GPU (different streams
+ * or host threads) race on it.
  * stream: a cudaStream_t, or NULL for the default stream; the call returns
  * after the stream has finished the pass. */
 int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, const dmd_system *sys,

@@ -1210,38 +1210,71 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
                           nullptr, V.run_st));
         CK(cudaEventRecord(V.e1, V.run_st));
         CK(dmd_launch_diag(V.d_sys, n, V.d_cstart, V.d_clen, V.d_coff, V.d_diag, V.run_st));
+        /* From here on requests change state (admitted, retired, failed):
+         * every exit goes through the bookkeeping below, so that the active
+         * set never names a request whose pool was freed and no admitted
+         * request is dropped.  A request whose read-back fails is failed
+         * alone; the step reports the first such error after the rest are
+         * booked. */
         server_admit(V, n, admitted);          /* overlaps the launch */
-        CK(cudaStreamSynchronize(V.run_st));   /* (the host vectors above outlive the copies) */
+        int first_rc = DMD_OK;
+        std::string first_err;
+        const cudaError_t se = cudaStreamSynchronize(V.run_st);   /* (the host vectors above outlive the copies) */
+        if (se != cudaSuccess) {
+            first_rc = DMD_E_CUDA;
+            first_err = std::string("cudaStreamSynchronize: ") + cudaGetErrorString(se);
+        }
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, V.e0, V.e1) == cudaSuccess) V.kernel_ms += ms;
+        if (se == cudaSuccess && cudaEventElapsedTime(&ms, V.e0, V.e1) == cudaSuccess) V.kernel_ms += ms;
         for (int r = 0; r < n; ++r) {
             ServerReq &R = *act[r];
+            if (se != cudaSuccess) { keep.push_back(&R); continue; }   /* nothing known about this round */
             DScal sc;
-            CK(cudaMemcpy(&sc, R.D.d.sc, sizeof sc, cudaMemcpyDeviceToHost));
-            R.H.sc = sc;
-            R.done += sc.done;
-            V.events += sc.done;
-            if (sc.done > 0 && sc.run_cycles > 0) R.cpe = (double)sc.run_cycles / (double)sc.done;
-            if (sc.err) {
-                R.state = DMD_REQ_FAILED; R.rc = sc.err;
-                R.err = "device error " + std::to_string(sc.err) + " (info " + std::to_string(sc.err_info) + ")";
-            } else if (R.done >= R.total) {
-                rc = server_retire(V, R, r);
-                if (rc != DMD_OK) return rc;
-                R.state = DMD_REQ_DONE;
+            const cudaError_t ce = cudaMemcpy(&sc, R.D.d.sc, sizeof sc, cudaMemcpyDeviceToHost);
+            if (ce != cudaSuccess) {
+                R.state = DMD_REQ_FAILED; R.rc = DMD_E_CUDA;
+                R.err = std::string("state read-back: ") + cudaGetErrorString(ce);
+            } else {
+                R.H.sc = sc;
+                R.done += sc.done;
+                V.events += sc.done;
+                if (sc.done > 0 && sc.run_cycles > 0) R.cpe = (double)sc.run_cycles / (double)sc.done;
+                if (sc.err) {
+                    R.state = DMD_REQ_FAILED; R.rc = sc.err;
+                    R.err = "device error " + std::to_string(sc.err) + " (info " + std::to_string(sc.err_info) + ")";
+                } else if (R.done >= R.total) {
+                    const int rr = server_retire(V, R, r);
+                    if (rr == DMD_OK) {
+                        R.state = DMD_REQ_DONE;
+                    } else {
+                        R.state = DMD_REQ_FAILED; R.rc = rr; R.err = "result read-back: " + V.err;
+                    }
+                }
             }
             if (R.state == DMD_REQ_ACTIVE) { keep.push_back(&R); continue; }
+            if (R.state == DMD_REQ_FAILED && first_rc == DMD_OK) {
+                first_rc = R.rc;
+                first_err = "request " + std::to_string(R.id) + ": " + R.err;
+            }
             R.t_finish = now_s();
-            CK(cudaFreeAsync(R.D.pool, V.copy_st));
+            cudaFreeAsync(R.D.pool, V.copy_st);   /* an error here leaves the pool to the runtime's teardown */
             R.D.pool = nullptr;
             ++finished;
             std::lock_guard<std::mutex> lock(V.mu);
             V.used -= R.need;
         }
         ++V.steps;
-    } else {
-        server_admit(V, 0, admitted);
+        {
+            std::lock_guard<std::mutex> lock(V.mu);
+            V.active = keep;
+            for (ServerReq *R : admitted) V.active.push_back(R);
+            if (n_finished) *n_finished = finished;
+            if (n_active) *n_active = (int)V.active.size();
+        }
+        if (first_rc != DMD_OK) err = first_err;
+        return first_rc;
     }
+    server_admit(V, 0, admitted);
     std::lock_guard<std::mutex> lock(V.mu);
     V.active = keep;
     for (ServerReq *R : admitted) V.active.push_back(R);
@@ -1483,8 +1516,15 @@ int dmd_predict_all_noalloc(const dmd_run_cfg *cfg, const dmd_tables *tables, co
     if (H.ncell > DMD_NOALLOC_MAX_CELLS)
         return fail_msg(DMD_E_CAPACITY, "dmd_predict_all_noalloc: the box needs " + std::to_string(H.ncell) +
                                             " cells per side, at most " + std::to_string(DMD_NOALLOC_MAX_CELLS));
+    /* the copies below come from pageable host memory and the call waits
+     * for the stream: neither is allowed while a stream is captured */
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+    if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+        return fail_msg(DMD_E_STATE, std::string("dmd_predict_all_noalloc may not be called while a stream is being "
+                                                 "captured (") + (ce != cudaSuccess ? cudaGetErrorString(ce) : "capture active") + ")");
     void *base = nullptr;
-    cudaError_t ce = dmd_noalloc_scratch(&base);
+    ce = dmd_noalloc_scratch(&base);
     if (ce != cudaSuccess) return fail_msg(DMD_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce));
     DSys d{};
     size_t bytes = layout(H, d, (char *)base, false);

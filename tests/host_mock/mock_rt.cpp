@@ -48,7 +48,14 @@ cudaError_t cudaFree(void *p) { give(p); return cudaSuccess; }
 cudaError_t cudaFreeAsync(void *p, cudaStream_t) { give(p); return cudaSuccess; }
 cudaError_t cudaMallocHost(void **p, size_t n) { *p = take(n, false); return *p ? cudaSuccess : cudaErrorMemoryAllocation; }
 cudaError_t cudaFreeHost(void *p) { give(p); return cudaSuccess; }
-cudaError_t cudaMemcpy(void *d, const void *s, size_t n, cudaMemcpyKind) { std::memmove(d, s, n); return cudaSuccess; }
+/* failure injection: the k-th device-to-host copy from now fails (0: none) */
+static int g_fail_d2h = 0;
+void mock_fail_d2h(int k) { g_fail_d2h = k; }
+cudaError_t cudaMemcpy(void *d, const void *s, size_t n, cudaMemcpyKind k) {
+    if (k == cudaMemcpyDeviceToHost && g_fail_d2h > 0 && --g_fail_d2h == 0) return cudaErrorUnknown;
+    std::memmove(d, s, n);
+    return cudaSuccess;
+}
 cudaError_t cudaMemcpyAsync(void *d, const void *s, size_t n, cudaMemcpyKind k, cudaStream_t) { return cudaMemcpy(d, s, n, k); }
 cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
 cudaError_t cudaStreamCreateWithFlags(cudaStream_t *s, unsigned int) { *s = (cudaStream_t)take(8, false); return cudaSuccess; }
@@ -62,6 +69,7 @@ cudaError_t cudaGetLastError(void) { return cudaSuccess; }
 const char *cudaGetErrorString(cudaError_t) { return "mock runtime error"; }
 cudaError_t cudaMemGetInfo(size_t *f, size_t *t) { *f = (size_t)100 << 30; *t = (size_t)200 << 30; return cudaSuccess; }
 cudaError_t cudaGetSymbolAddress(void **, const void *) { return cudaErrorInvalidSymbol; }
+cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus *s) { *s = cudaStreamCaptureStatusNone; return cudaSuccess; }
 cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) { return cudaErrorNotSupported; }
 cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t *) { return cudaErrorNotSupported; }
 cudaError_t cudaGraphInstantiate(cudaGraphExec_t *, cudaGraph_t, unsigned long long) { return cudaErrorNotSupported; }

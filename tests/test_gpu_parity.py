@@ -325,3 +325,66 @@ def test_compact_variant_batch_and_graph(built):
                 assert np.array_equal(st[key], want[r][key]), (graph, r, key)
             assert st["coll"] == want[r]["coll"], (graph, r)
         b.close()
+
+
+def _compare_states(st, ost, what):
+    for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity", "extra_repuls"):
+        assert np.array_equal(st[key], ost[key]), f"{what}: final {key} differs"
+    assert st["t"] == ost["t"] and st["coll"] == ost["coll"], what
+
+
+@pytest.mark.parametrize("ctas", [1, 2])
+def test_c2_event_sequence(built, ctas):
+    """48 x KLVFFAE (1,344 beads, 252 A box, T* = 0.18): the single-system
+    workload's first 20,000 events on one CTA and on a 2-CTA cluster."""
+    spec = systems.generate(systems.config_c2())
+    n = 20000
+    with Engine(spec, cluster=ctas) as eng:
+        glog = eng.run(n, log_capacity=n + 64)
+        gst = eng.state()
+    ora = Oracle(spec)
+    olog = ora.run(n, log_capacity=n + 64)
+    k = first_mismatch(glog, olog)
+    assert k < 0, f"C2 (C={ctas}) diverges at {k}:\n{describe(glog, olog, k)}"
+    _compare_states(gst, ora.state(), f"C2 C={ctas}")
+
+
+def test_c4_event_sequence(built):
+    """1,000 random 10-mers (40,000 beads, 10 mM, T* = 0.22): the large
+    single-system workload's first 12,000 events on a 4-CTA cluster (global
+    footprint tables, candidates spread over the cluster's shared memory)
+    and on one CTA, both against one oracle run."""
+    spec = systems.generate(systems.config_c4())
+    n = 12000
+    runs = {}
+    for ctas in (4, 1):
+        with Engine(spec, cluster=ctas) as eng:
+            runs[ctas] = (eng.run(n, log_capacity=n + 64), eng.state())
+    ora = Oracle(spec)
+    olog = ora.run(n, log_capacity=n + 64)
+    ost = ora.state()
+    for ctas, (glog, gst) in runs.items():
+        k = first_mismatch(glog, olog)
+        assert k < 0, f"C4 (C={ctas}) diverges at {k}:\n{describe(glog, olog, k)}"
+        _compare_states(gst, ost, f"C4 C={ctas}")
+
+
+def test_c3_largest_replica_batched(built):
+    """The 32-replica workload's largest system (5,576 beads: footprint
+    tables in global memory) advanced in one launch beside the smallest,
+    20,000 events each, against the oracle."""
+    specs = sorted(systems.config_c3(32, seed=1), key=lambda s: s.n_beads)
+    pick = [specs[-1], specs[0]]
+    for s in pick:
+        systems.generate(s)
+    assert pick[0].n_beads > 5000
+    n = 20000
+    b = Batch(pick)
+    logs = b.run(n, log_capacity=n + 64)
+    for r, s in enumerate(pick):
+        ora = Oracle(s)
+        olog = ora.run(n, log_capacity=n + 64)
+        k = first_mismatch(logs[r], olog)
+        assert k < 0, f"replica of {s.n_beads} beads diverges at {k}:\n{describe(logs[r], olog, k)}"
+        _compare_states(b.state(r), ora.state(), f"{s.n_beads} beads")
+    b.close()

@@ -310,3 +310,62 @@ def test_compact_variant_hands_over_to_the_full_one(mock):
         assert state_of(mock, h, r, s.n_beads)[3] == 3001
     assert mock.mock_report() == b"", mock.mock_report().decode()
     mock.dmd_batch_destroy(h)
+
+
+def test_server_step_books_a_failed_read_back(mock):
+    """A result read-back that fails while a finished request is retired
+    fails that request alone: its pool is freed and it leaves the active
+    set, the step reports the error, and the next steps run the other
+    request to completion without touching the freed pool."""
+    mock.mock_fail_d2h.argtypes = [C.c_int]
+    a = systems.generate(systems.klvffae_system(2, 5.0, 0.2, seed=41))
+    b = systems.generate(systems.klvffae_system(3, 5.0, 0.2, seed=42))
+    mock.mock_reset()
+    base = mock.mock_live_allocations()
+    s = _server(mock, 4, 0, 1000)
+    rc, ida = _submit(mock, s, a, 800)       # finishes in its first running step
+    assert rc == 0
+    rc, idb = _submit(mock, s, b, 3000)
+    assert rc == 0
+    na, nf = C.c_int32(), C.c_int32()
+    assert mock.dmd_server_step(s, C.byref(na), C.byref(nf)) == 0   # admits both
+    assert na.value == 2
+    # next step: copy 1 reads request a's scalars, copy 2 is the first copy of its result
+    mock.mock_fail_d2h(2)
+    rc = mock.dmd_server_step(s, C.byref(na), C.byref(nf))
+    assert rc == -6, rc                                               # DMD_E_CUDA
+    assert b"request" in mock.dmd_server_last_error(s)
+    assert (na.value, nf.value) == (1, 1)
+    rc_a, st_a, _, _ = _status(mock, s, ida)
+    assert rc_a == -6 and st_a == 3                                   # DMD_REQ_FAILED, its status
+    mock.mock_fail_d2h(0)
+    _drain(mock, s, [idb])
+    rc_b, st_b, done_b, _ = _status(mock, s, idb)
+    assert (rc_b, st_b, done_b) == (0, 2, 3000)
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    mock.dmd_server_destroy(s)
+    assert mock.mock_live_allocations() <= base + 1
+
+
+def _noalloc_call(lib, spec, list_cap=0):
+    n = spec.n_beads
+    cfg = spec.run_cfg(0, list_cap)
+    tabs = abi.tables_struct(default_tables())
+    sys_ = spec.c_system()
+    outs = [np.zeros(n), np.zeros(n, np.int32), np.zeros(n, np.int32)]
+    err = C.create_string_buffer(256)
+    rc = lib.dmd_predict_all_noalloc(C.byref(cfg), C.byref(tabs), C.byref(sys_), *[o.ctypes.data for o in outs],
+                                     None, err, 256)
+    return rc, err.value
+
+
+def test_noalloc_rejects_list_cap_and_grid_beyond_its_array(mock):
+    """The allocation-free prediction pass refuses, before any device call,
+    neighbour lists longer than 64 entries and a rebuild grid of more than
+    48 cells per side, each with DMD_E_CAPACITY and a message."""
+    spec = systems.generate(systems.klvffae_system(4, 5.0, 0.2, seed=3))
+    rc, msg = _noalloc_call(mock, spec, list_cap=65)
+    assert rc == -7 and b"list_cap at most 64" in msg, (rc, msg)
+    wide = systems.generate(systems.klvffae_system(4, 0.01, 0.2, seed=3))  # 0.01 mM: a box of ~870 A
+    rc, msg = _noalloc_call(mock, wide)
+    assert rc == -7 and b"cells per side" in msg, (rc, msg)
