@@ -80,6 +80,15 @@ typedef struct dmd_run_cfg {
 #define DMD_FLAG_STOP_AT_OUTPUT 1  /* dmd_run returns after every output (N+3) event */
 #define DMD_FLAG_COUNT_PHYSICAL 2  /* dmd_run counts pair + ghost events only (else the reference's coll) */
 #define DMD_FLAG_SERIAL         4  /* one event per step (no conflict-free batching) */
+/* The overlap check of code/checkover.f:18-131 (a non-bonded pair inside
+ * its core, a bonded pair outside its window) runs on every initial state
+ * (dmd_create, dmd_set_state, batch and server creation) and fails it with
+ * DMD_E_OVERLAP naming the pair; the reference only reports it at start-up
+ * (code/main.F90:347-354).  ALLOW_OVERLAP skips that check. */
+#define DMD_FLAG_ALLOW_OVERLAP  8
+/* The -Ddebugging checks at every output event (code/main.F90:1193-1205):
+ * an overlap or a broken bond stops the run with DMD_E_OVERLAP. */
+#define DMD_FLAG_CHECK_OVERLAP 16
 
 /* One system: chains, sequences, initial state (code/inputinfo.f:5-101,
  * code/main.F90:240-321). */
@@ -130,6 +139,10 @@ typedef struct dmd_diag {
     int64_t n_batches;        /* engine: pair-event batches committed (0 in a serial run) */
     int64_t n_rolled_back;    /* engine: speculative pair events undone and redone later */
     int64_t n_candidates;     /* engine: pair events that entered a batch (before validation) */
+    /* code/check_nc_int.f:9-360: H-bonded pairs whose geometry fails
+     * repuls_check, and unbonded NH-CO pairs inside their well whose
+     * geometry passes it (0 and 0 in a consistent state) */
+    int64_t nc_boundbad, nc_unboundbad;
 } dmd_diag;
 
 typedef struct dmd_handle dmd_handle;

@@ -250,6 +250,14 @@ struct Oracle {
         for (int k = N + 1; k <= N + 3; ++k) { nptnr[k] = -2; coltype[k] = -2; }
         nbor_setup();   /* main.F90:389; evaluated on the make_code table, before the restore's shoulders */
         if (S->bptnr) runr_restore(S->bptnr);
+        if (!(flags & DMD_FLAG_ALLOW_OVERLAP)) {   /* main.F90:347, before the lists and predictions */
+            int bi = 0, bj = 0;
+            if (checkover(bi, bj) > 0) {
+                err = "beads " + std::to_string(bi) + " and " + std::to_string(bj) +
+                      " overlap, or their bond is outside its window";
+                return false;
+            }
+        }
 
         num_cell = (int)(boxl / (sig_max_all * rl_const) * n_wrap) + 2 * n_wrap;
         if (num_cell - 2 * n_wrap < 2 * n_wrap + 1) { err = "box too small for the cell stencil"; return false; }
@@ -271,6 +279,69 @@ struct Oracle {
         events();
         old_tfalse = tfalse;
         return err.empty();
+    }
+
+    /* code/checkover.f:18-131: every pair i < j; a pair of type 1 or >= 15
+     * closer than its core diameter, a bonded pair (4-12) outside its window.
+     * Returns the number of offending pairs; (bi, bj) the first (1-based). */
+    int checkover(int &bi, int &bj) const {
+        int nbad = 0;
+        for (int i = 1; i <= N - 1; ++i)
+            for (int j = i + 1; j <= N; ++j) {
+                int evcode = code(j, i);
+                bool bad = false;
+                if (evcode == 1 || evcode >= 15) {
+                    double p = ev_param[1][evcode];
+                    double sigsq = sigma_sq[identity[i]][identity[j]] * (p * p);
+                    if (evcode >= 22 && evcode <= 26) {
+                        int k = std::max(identity[i], identity[j]);
+                        double s = sqz610[evcode - 21][k];
+                        sigsq = sigsq * (s * s);
+                    }
+                    Rel r = rel(i, j);
+                    double rijsq = r.rijsq * 1.0000000001;
+                    bad = rijsq <= sigsq;
+                } else if (evcode >= 4 && evcode <= 12) {
+                    double blmin, blmax;
+                    bond_limits(i, evcode, blmin, blmax);
+                    blmin = blmin * blmin;
+                    blmax = blmax * blmax;
+                    Rel r = rel(i, j);
+                    double rijsq_min = r.rijsq * 1.0000000001, rijsq_max = r.rijsq * 0.9999999999;
+                    bad = rijsq_max > blmax || rijsq_min < blmin;
+                }
+                if (bad && nbad++ == 0) { bi = i; bj = j; }
+            }
+        return nbad;
+    }
+
+    /* code/check_nc_int.f:9-360: over every bead's up list, the H-bonded
+     * pairs whose geometry fails repuls_check and the unbonded NH-CO pairs
+     * inside their well whose geometry passes it; pairs with an end bead
+     * (local index chnln+1 or 3*chnln) are not rated. */
+    void check_nc_int(int64_t &boundbad, int64_t &unboundbad) const {
+        boundbad = unboundbad = 0;
+        for (int i = 1; i <= N; ++i)
+            for (int k = 0; k < na_npt[i]; ++k) {
+                int j = nb[(size_t)(i - 1) * cap + k];
+                if (code(j, i) != 15) continue;
+                int ci = chain_of[i], cj = chain_of[j];
+                int ii = local_of[i], jj = local_of[j], Li = chain_L[ci], Lj = chain_L[cj];
+                bool rated = ii != Li + 1 && jj != Lj + 1 && ii != 3 * Li && jj != 3 * Lj;
+                if (bptnr[i] == j) {
+                    double rating = 10.0;
+                    if (rated) rating = identity[i] < identity[j] ? repuls_check(i, j) : repuls_check(j, i);
+                    if (rating > 10.0) boundbad += 1;
+                } else {
+                    Rel r = rel(i, j);
+                    double diff = r.rijsq - welldia_sq[identity[i]][identity[j]];
+                    if (diff < 0.0) {
+                        double rating = 11.0;
+                        if (rated) rating = identity[i] < identity[j] ? repuls_check(i, j) : repuls_check(j, i);
+                        if (rating <= 10.0) unboundbad += 1;
+                    }
+                }
+            }
     }
 
     void scale_down() {  /* code/scale_down.f:1-87 */
@@ -1265,6 +1336,14 @@ struct Oracle {
             if (rec) { rec->coll = coll; rec->t = t_before; rec->tfalse = tf; rec->i = i; rec->j = 0; rec->type = type; rec->evcode = 0; }
             return type;
         } else {
+            if (flags & DMD_FLAG_CHECK_OVERLAP) {   /* main.F90:1193-1205 (-Ddebugging) */
+                int bi = 0, bj = 0;
+                if (checkover(bi, bj) > 0) {
+                    err = "overlap at coll " + std::to_string(coll) + ": beads " + std::to_string(bi) + " and " +
+                          std::to_string(bj);
+                    return -1;
+                }
+            }
             output_event();
             type = DMD_EV_OUTPUT;
             n_output += 1;
@@ -1346,6 +1425,7 @@ struct Oracle {
         double nbr = 0.0;
         for (int i = 1; i <= N; ++i) nbr += (double)(na_npt[i] + nnabdn[i]);
         d->nbr_mean = nbr / (double)N;
+        check_nc_int(d->nc_boundbad, d->nc_unboundbad);
     }
 };
 
@@ -1443,5 +1523,34 @@ int ora_get_output(ora_handle *h, int k, dmd_diag *d) {
 }
 
 void ora_destroy(ora_handle *h) { delete h; }
+
+void ora_log_many(const double *x, double *y, int64_t n) {
+    for (int64_t k = 0; k < n; ++k) y[k] = dmd_log(x[k]);
+}
+
+int ora_pair_case(ora_handle *h, int32_t i, int32_t j, int32_t ida, int32_t idb, int32_t evcode, int32_t bonded,
+                  const double *st, int32_t ct_in, double *tij, int32_t *type, double *st_out, int32_t *ct_out,
+                  double *mass) {
+    Oracle &o = h->o;
+    const int a = i + 1, b = j + 1;
+    if (a < 1 || a > o.N || b < 1 || b > o.N || a == b) return -1;
+    if (ida > 0) o.identity[a] = ida;
+    if (idb > 0) o.identity[b] = idb;
+    o.bptnr[a] = bonded ? b : 0;
+    o.bptnr[b] = bonded ? a : 0;
+    o.tfalse = 0.0;
+    o.sx[a] = st[0]; o.sy[a] = st[1]; o.sz[a] = st[2]; o.vx[a] = st[3]; o.vy[a] = st[4]; o.vz[a] = st[5];
+    o.sx[b] = st[6]; o.sy[b] = st[7]; o.sz[b] = st[8]; o.vx[b] = st[9]; o.vy[b] = st[10]; o.vz[b] = st[11];
+    int ty = 0;
+    if (!o.predict(a, b, evcode, *tij, ty)) return -2;
+    *type = ty;
+    *ct_out = ct_in > 0 ? o.eventdyn(a, b, evcode, ct_in) : 0;
+    const double out[12] = {o.sx[a], o.sy[a], o.sz[a], o.vx[a], o.vy[a], o.vz[a],
+                            o.sx[b], o.sy[b], o.sz[b], o.vx[b], o.vy[b], o.vz[b]};
+    for (int k = 0; k < 12; ++k) st_out[k] = out[k];
+    mass[0] = o.bm[a];
+    mass[1] = o.bm[b];
+    return 0;
+}
 
 }  // extern "C"

@@ -23,6 +23,18 @@ int ora_get_scalars(ora_handle *h, double *out, int n);
 int ora_n_outputs(ora_handle *h);
 int ora_get_output(ora_handle *h, int k, dmd_diag *d);
 void ora_destroy(ora_handle *h);
+/* dmd_log (dmd_rng.h, the logarithm of the ghost draws) over n inputs */
+void ora_log_many(const double *x, double *y, int64_t n);
+/* Known-answer hook: beads i and j (0-based; identities ida/idb when > 0,
+ * H-bond partners of each other when bonded) placed at st[0..5] = x, y, z,
+ * vx, vy, vz of i (positions in box units) and st[6..11] for j at tfalse = 0;
+ * returns the pair prediction under evcode (code/eventredo_up.f:28-46:
+ * time, type) and, when ct_in > 0, the impulse of code/eventdyn.f for
+ * collision type ct_in (final type, state after it); mass[0..1] = bm(i),
+ * bm(j).  Overwrites the handle's state of i and j. */
+int ora_pair_case(ora_handle *h, int32_t i, int32_t j, int32_t ida, int32_t idb, int32_t evcode, int32_t bonded,
+                  const double *st, int32_t ct_in, double *tij, int32_t *type, double *st_out, int32_t *ct_out,
+                  double *mass);
 /* genconfig's side-chain placement search (sidechain_oracle.cpp) */
 int64_t ora_sidechain_grid(double move, double step, double *values, int64_t cap);
 int64_t ora_sidechain_search(int32_t n, const double *ca, const double *nh, const double *co, const double *side,

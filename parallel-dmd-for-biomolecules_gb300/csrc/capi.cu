@@ -682,6 +682,13 @@ int upload(dmd_batch &B) {
     for (int r = 0; r < n; ++r) {
         DScal sc;
         CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        if (sc.err == DMD_E_OVERLAP) {
+            err = "system " + std::to_string(r) + ": beads " + std::to_string(sc.err_info + 1) + " and " +
+                  std::to_string(sc.err_info2 + 1) +
+                  " overlap, or their bond is outside its window (code/checkover.f); DMD_FLAG_ALLOW_OVERLAP "
+                  "accepts such a state";
+            return sc.err;
+        }
         if (sc.err) { err = "device error during list build (code " + std::to_string(sc.err) + ")"; return sc.err; }
     }
     B.ready = 1;
@@ -718,6 +725,12 @@ int sync_check(dmd_batch &B) {
         DScal sc;
         CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
         B.hs[r].sc = sc;
+        if (sc.err == DMD_E_OVERLAP) {
+            err = "system " + std::to_string(r) + ", coll " + std::to_string(sc.coll) + ": beads " +
+                  std::to_string(sc.err_info + 1) + " and " + std::to_string(sc.err_info2 + 1) +
+                  " overlap, or their bond is outside its window (output-event check of code/checkover.f)";
+            return sc.err;
+        }
         if (sc.err) {
             err = "device error " + std::to_string(sc.err) + " in system " + std::to_string(r) + " (info " + std::to_string(sc.err_info) + ")";
             return sc.err;
@@ -1114,7 +1127,11 @@ void server_admit(dmd_server &V, int n_running, std::vector<ServerReq *> &admitt
         if (rc == DMD_OK) {
             DScal sc;
             if (cudaMemcpy(&sc, R->D.d.sc, sizeof sc, cudaMemcpyDeviceToHost) != cudaSuccess) { rc = DMD_E_CUDA; e = "read-back"; }
-            else if (sc.err) { rc = sc.err; e = "device error during the list build"; }
+            else if (sc.err == DMD_E_OVERLAP) {
+                rc = sc.err;
+                e = "beads " + std::to_string(sc.err_info + 1) + " and " + std::to_string(sc.err_info2 + 1) +
+                    " overlap, or their bond is outside its window (code/checkover.f)";
+            } else if (sc.err) { rc = sc.err; e = "device error during the list build"; }
         }
         std::lock_guard<std::mutex> lock(V.mu);
         if (rc != DMD_OK) {

@@ -44,6 +44,7 @@
 
 #define NTHREADS 256
 #define NWARPS (NTHREADS / 32)
+#define NWARPS_MAX 16     /* the most warps any kernel here runs per CTA */
 #define CAND_MAX 64
 #define META_MAX 16
 #define TG_MAX 64         /* full re-predictions per round (i, j, marked beads) */
@@ -53,7 +54,13 @@
 /* systems up to this size keep the claim tables in shared memory (full and
  * compact variants of k_run); larger ones use their global array */
 #define OWN_SMEM_FULL 2048
-#define OWN_SMEM_COMPACT 1536
+#define OWN_SMEM_COMPACT 1024
+/* threads of k_run per CTA: one candidate event per warp, so the warps of a
+ * CTA bound a batch; the compact variant's smaller event areas leave room
+ * for twice the warps */
+#define RUN_NT_FULL 256
+#define RUN_NT_COMPACT 512
+#define RUN_CARVEOUT_COMPACT_KB 164
 #define DMD_TICKET_SEQ_MAX ((1 << 25) - 2)
 #define FULL 0xffffffffu
 
@@ -144,8 +151,8 @@ struct SharedState {
     double delta;        /* time window of the candidate cut */
     int groups[256];
     int ngroups;
-    double red_d[NWARPS];
-    int red_i[NWARPS * 4];
+    double red_d[NWARPS_MAX];
+    int red_i[NWARPS_MAX * 4];
     int rebuild;
     int touched[8];
     int bseq;            /* footprint claims of this launch (ticket base) */
@@ -322,7 +329,7 @@ __device__ double cta_max(SharedState &sh, double v) {
     if ((threadIdx.x & 31) == 0) sh.red_d[w] = v;
     __syncthreads();
     double r = sh.red_d[0];
-    for (int k = 1; k < NWARPS; ++k) r = fmax(r, sh.red_d[k]);
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) r = fmax(r, sh.red_d[k]);
     __syncthreads();
     return r;
 }
@@ -333,7 +340,7 @@ __device__ double cta_sum(SharedState &sh, double v) {
     if ((threadIdx.x & 31) == 0) sh.red_d[w] = v;
     __syncthreads();
     double r = 0.0;
-    for (int k = 0; k < NWARPS; ++k) r += sh.red_d[k];
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) r += sh.red_d[k];
     __syncthreads();
     return r;
 }
@@ -344,7 +351,7 @@ __device__ int cta_sum_i(SharedState &sh, int v) {
     if ((threadIdx.x & 31) == 0) sh.red_i[w] = v;
     __syncthreads();
     int r = 0;
-    for (int k = 0; k < NWARPS; ++k) r += sh.red_i[k];
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) r += sh.red_i[k];
     __syncthreads();
     return r;
 }
@@ -538,7 +545,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, cons
     __syncthreads();
     if (threadIdx.x == 0) {
         int m = 0;
-        for (int w = 0; w < NWARPS; ++w) m = max(m, sh.red_i[w]);
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = max(m, sh.red_i[w]);
         sh.sc.max_dn = m;
     }
     __syncthreads();
@@ -811,7 +818,7 @@ __device__ bool cluster_interval(const DSys &S, SharedState &sh, SharedState *L,
     __syncthreads();
     if (threadIdx.x == 0) {
         long long m = 0;
-        for (int w = 0; w < NWARPS; ++w) { long long v = dbits(sh.red_d[w]); if (v > m) m = v; }
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { long long v = dbits(sh.red_d[w]); if (v > m) m = v; }
         L->red_max[rank] = __longlong_as_double(m);
     }
     csync(C);
@@ -873,6 +880,103 @@ __device__ double dist_now(const DSys &S, int a, int b, double tfalse) {
     double d = rx * rx + ry * ry + rz * rz;
     return sqrt(d);
 }
+/* code/checkover.f:18-131 over the neighbour lists (each pair once, from
+ * the lower bead's up list; every pair the reference can flag is listed:
+ * bonded pairs always, the others within their cutoff, which exceeds every
+ * contact diameter).  A pair of type 1 or >= 15 whose squared distance
+ * times 1.0000000001 is at most its squared core diameter overlaps; a
+ * bonded pair (types 4-12) is broken when its squared distance times
+ * 0.9999999999 exceeds the squared outer window or times 1.0000000001 falls
+ * below the inner one.  The first offence found sets DMD_E_OVERLAP with the
+ * pair's beads (0-based) in err_info / err_info2.  Returns the number of
+ * offending pairs. */
+__device__ int cta_checkover(const DSys &S, SharedState &sh) {
+    const int N = S.N;
+    const DTab &T = *S.tab;
+    const double tf = sh.sc.tfalse;
+    int bad_pairs = 0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const int *up = S.up + (size_t)i * S.cap;
+        const int8_t *upc = S.upc + (size_t)i * S.cap;
+        for (int k = 0; k < S.upn[i]; ++k) {
+            const int j = up[k];
+            const int code = pair_code_st(S, i, j, upc[k]);
+            const int a = S.ident[i], b = S.ident[j];
+            bool bad = false;
+            if (code == 1 || code >= 15) {
+                /* sigma_sq * ev_param(1,code)**2 (* sqz610**2 for 22-26):
+                 * the tables hold these products in that order; the factor
+                 * is 1 for 16 and the shoulder codes */
+                const double sigsq = code == 15 ? T.core15_sq[a][b]
+                                     : (code == 1 || (code >= 17 && code <= 26)) ? T.core_sq[core_slot(code)][a][b]
+                                                                                 : T.sigma_sq[a][b];
+                const Rel r = d_rel(S, i, j, tf);
+                bad = r.rijsq * 1.0000000001 <= sigsq;
+            } else if (code >= 4 && code <= 12) {
+                const bool side = code >= 10;
+                const double lo = side ? S.blmin_sq[i] : T.evp2_sq[code];
+                const double hi = side ? S.blmax_sq[i] : T.evp3_sq[code];
+                const Rel r = d_rel(S, i, j, tf);
+                bad = r.rijsq * 0.9999999999 > hi || r.rijsq * 1.0000000001 < lo;
+            }
+            if (bad) {
+                ++bad_pairs;
+                if (atomicCAS(&sh.sc.err, 0, DMD_E_OVERLAP) == 0) { sh.sc.err_info = i; sh.sc.err_info2 = j; }
+            }
+        }
+    }
+    return cta_sum_i(sh, bad_pairs);
+}
+
+/* code/repuls_check.f:1-85 for the H-bond pair (n, c): 10 when the four
+ * helper distances all exceed the shoulder distances, else 11 */
+__device__ double repuls_rating(const DSys &S, int n, int c, double tf) {
+    int ncim1, ncai, ncaj, nnjp1;
+    helpers_of(S, n, c, ncim1, ncai, ncaj, nnjp1);
+    const int pa[4] = {n, n, c, c}, pb[4] = {ncaj, nnjp1, ncai, ncim1};
+    double d[4];
+    for (int q = 0; q < 4; ++q) {
+        const Rel r = d_rel(S, pa[q], pb[q], tf);
+        d[q] = sqrt(r.rijsq);
+    }
+    const DTab &T = *S.tab;
+    return (d[0] > T.shd1 && d[1] > T.shd2 && d[2] > T.shd3 && d[3] > T.shd4) ? 10.0 : 11.0;
+}
+
+/* code/check_nc_int.f:9-360 over the up lists: an H-bonded pair whose
+ * geometry fails repuls_check (boundbad), and an unbonded NH-CO pair inside
+ * its well whose geometry passes it (unboundbad); pairs with an end bead
+ * (NH of residue 1, CO of residue L) are not rated. */
+__device__ void cta_nc_int(const DSys &S, SharedState &sh, int &boundbad, int &unboundbad) {
+    const int N = S.N;
+    const DTab &T = *S.tab;
+    const double tf = sh.sc.tfalse;
+    int bb = 0, ub = 0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const int *up = S.up + (size_t)i * S.cap;
+        const int8_t *upc = S.upc + (size_t)i * S.cap;
+        for (int k = 0; k < S.upn[i]; ++k) {
+            const int j = up[k];
+            if (pair_code_st(S, i, j, upc[k]) != 15) continue;
+            const bool ends = S.info[i].is_end || S.info[j].is_end;
+            const int a = S.ident[i], b = S.ident[j];
+            const int n = a < b ? i : j, c = a < b ? j : i;
+            if (S.bptnr[i] == j) {
+                const double rating = ends ? 10.0 : repuls_rating(S, n, c, tf);
+                if (rating > 10.0) ++bb;
+            } else {
+                const Rel r = d_rel(S, i, j, tf);
+                if (r.rijsq - T.welldia_sq[a][b] < 0.0) {
+                    const double rating = ends ? 11.0 : repuls_rating(S, n, c, tf);
+                    if (rating <= 10.0) ++ub;
+                }
+            }
+        }
+    }
+    boundbad = cta_sum_i(sh, bb);
+    unboundbad = cta_sum_i(sh, ub);
+}
+
 __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start, const int *chain_len,
                          dmd_diag *out) {
     const int N = S.N;
@@ -951,6 +1055,8 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
     e2e = cta_sum(sh, e2e);
     rgsum = cta_sum(sh, rgsum);
     nbb = cta_sum_i(sh, nbb);
+    int boundbad = 0, unboundbad = 0;
+    cta_nc_int(S, sh, boundbad, unboundbad);
     if (threadIdx.x == 0 && out) {
         double sumeps = -((hb_ii + hb_ij) * T.eps_hb + (ehh_ii + ehh_ij));
         out->e_total = 0.5 * sumvel + sumeps;
@@ -968,6 +1074,8 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
         out->n_batches = sh.sc.n_batches; out->n_rolled_back = sh.sc.n_rolled_back;
         out->n_candidates = sh.sc.n_candidates;
         out->max_down = sh.sc.max_dn;
+        out->nc_boundbad = boundbad;
+        out->nc_unboundbad = unboundbad;
     }
     __syncthreads();
 }
@@ -1019,7 +1127,7 @@ __device__ int warp_root(const DSys &S, long long &kroot) {
  * entry.  Returns their number (1 if the window cannot be made small
  * enough). */
 __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, long long kroot, int slots) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     const int N = S.N;
     const long long kp = min(min(S.key[N], S.key[N + 1]), S.key[N + 2]);
@@ -1034,17 +1142,17 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
         }
         kc = __shfl_sync(FULL, kc, 0);
         /* few groups: every warp scans them all and takes the groups below
-         * the cut with ordinals warp, warp + NWARPS, ...; many: each warp
+         * the cut with ordinals warp, warp + nw, ...; many: each warp
          * scans blocks of 32 groups in turn and takes their groups */
-        const bool few = S.nl1 <= 32 * (NWARPS / 2);
+        const bool few = S.nl1 <= 32 * (nw / 2);
         int ord = 0;
-        for (int gb = few ? 0 : 32 * warp; gb < S.nl1; gb += few ? 32 : 32 * NWARPS) {
+        for (int gb = few ? 0 : 32 * warp; gb < S.nl1; gb += few ? 32 : 32 * nw) {
             const int g = gb + lane;
             unsigned gm = __ballot_sync(FULL, g < S.nl1 && S.l1k[g] < kc);
             while (gm) {
                 const int gg = gb + __ffs(gm) - 1;
                 gm &= gm - 1;
-                if (few && ord++ % NWARPS != warp) continue;
+                if (few && ord++ % nw != warp) continue;
                 const int e = gg * 32 + lane;
                 const long long k = e < N ? S.key[e] : DMD_KEY_INF;
                 const bool c = k < kc;
@@ -1127,6 +1235,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, i
     __syncthreads();
     __shared__ FullScratch fs[NWARPS];
     cta_rebuild(S, sh, ScratchRef{(char *)fs, sizeof(FullScratch)}, hbonds, (char *)kinit_dyn, KINIT_DYN_SMEM);
+    /* the start-up overlap check of code/main.F90:347 (an error unless the
+     * caller accepts overlapping states, as the reference does).  The
+     * reference checks before it predicts, so an overlap is reported in
+     * place of what the prediction of an overlapping pair raised; with
+     * lists over capacity the check cannot run. */
+    if (!(S.flags & DMD_FLAG_ALLOW_OVERLAP) && sh.sc.err != DMD_E_CAPACITY) {
+        const int saved = sh.sc.err, saved_info = sh.sc.err_info;
+        __syncthreads();
+        if (threadIdx.x == 0) sh.sc.err = 0;
+        __syncthreads();
+        if (cta_checkover(S, sh) == 0 && threadIdx.x == 0) { sh.sc.err = saved; sh.sc.err_info = saved_info; }
+    }
+    __syncthreads();
     if (threadIdx.x == 0) *S.sc = sh.sc;
 }
 
@@ -1143,6 +1264,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_init(DSys *systems, int nsys, i
 #define DMD_RUN_RSET 384
 #define DMD_RUN_QSET 160
 #define DMD_RUN_DN_LIMIT INT_MAX
+#define DMD_RUN_NT RUN_NT_FULL
 namespace run_full {
 #include "engine_run.cuh"
 }
@@ -1150,10 +1272,12 @@ namespace run_full {
 #undef DMD_RUN_RSET
 #undef DMD_RUN_QSET
 #undef DMD_RUN_DN_LIMIT
+#undef DMD_RUN_NT
 #define DMD_RUN_OPS 72           /* 2 * 32 + 6 extras + slack */
 #define DMD_RUN_RSET 192
 #define DMD_RUN_QSET 96
 #define DMD_RUN_DN_LIMIT DMD_COMPACT_DN
+#define DMD_RUN_NT RUN_NT_COMPACT
 namespace run_compact {
 #include "engine_run.cuh"
 }
@@ -1161,6 +1285,7 @@ namespace run_compact {
 #undef DMD_RUN_RSET
 #undef DMD_RUN_QSET
 #undef DMD_RUN_DN_LIMIT
+#undef DMD_RUN_NT
 
 __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, const int *chain_start, const int *chain_len,
                                                    const int *chain_off, dmd_diag *out) {
@@ -1181,17 +1306,18 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, cons
 /* ------------------------------------------------------------------ */
 /* dynamic shared memory of k_run: the per-warp event areas, the task pool
  * and, for systems of at most own_cap beads, the claim tables */
-template <typename WA> constexpr size_t run_smem_of(int own_cap) {
-    return sizeof(WA) * NWARPS + sizeof(TaskPool) + (size_t)own_cap * 3 * sizeof(unsigned);
+template <typename WA> constexpr size_t run_smem_of(int own_cap, int nwarps) {
+    return sizeof(WA) * nwarps + sizeof(TaskPool) + (size_t)own_cap * 3 * sizeof(unsigned);
 }
-static_assert(run_smem_of<run_full::WarpArea>(OWN_SMEM_FULL) + sizeof(SharedState) + sizeof(DSys) <= 227 * 1024,
+static_assert(run_smem_of<run_full::WarpArea>(OWN_SMEM_FULL, RUN_NT_FULL / 32) + sizeof(SharedState) + sizeof(DSys) <=
+                  227 * 1024,
               "k_run shared memory above the 227 KB a block may use");
-static_assert(run_smem_of<run_compact::WarpArea>(OWN_SMEM_COMPACT) + sizeof(SharedState) + sizeof(DSys) + 1024 <=
-                  100 * 1024,
-              "compact k_run (with the 1 KB the system reserves per block) must fit the 100 KB carve-out, "
-              "leaving 156 KB of the SM's 256 KB to L1");
+static_assert(run_smem_of<run_compact::WarpArea>(OWN_SMEM_COMPACT, RUN_NT_COMPACT / 32) + sizeof(SharedState) +
+                      sizeof(DSys) + 1024 <= RUN_CARVEOUT_COMPACT_KB * 1024,
+              "compact k_run (with the 1 KB the system reserves per block) must fit its shared-memory carve-out");
 static size_t run_smem(int compact, int own_cap) {
-    return compact ? run_smem_of<run_compact::WarpArea>(own_cap) : run_smem_of<run_full::WarpArea>(own_cap);
+    return compact ? run_smem_of<run_compact::WarpArea>(own_cap, RUN_NT_COMPACT / 32)
+                   : run_smem_of<run_full::WarpArea>(own_cap, RUN_NT_FULL / 32);
 }
 static int own_smem_max(int compact) { return compact ? OWN_SMEM_COMPACT : OWN_SMEM_FULL; }
 
@@ -1240,10 +1366,10 @@ static cudaError_t k_run_attributes() {
 }
 
 static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, int nsys, int C, size_t smem,
-                           cudaStream_t st) {
+                           cudaStream_t st, int nthreads) {
     cfg = cudaLaunchConfig_t{};
     cfg.gridDim = dim3((unsigned)(nsys * C), 1, 1);
-    cfg.blockDim = dim3(NTHREADS, 1, 1);
+    cfg.blockDim = dim3((unsigned)nthreads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1265,7 +1391,7 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int 
     int own_cap = C == 1 ? std::min(max_beads, own_smem_max(compact)) : 0;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    cluster_config(cfg, attr, nsys, C, run_smem(compact, own_cap), st);
+    cluster_config(cfg, attr, nsys, C, run_smem(compact, own_cap), st, compact ? RUN_NT_COMPACT : RUN_NT_FULL);
     if (compact)
         return cudaLaunchKernelEx(&cfg, run_compact::k_run, d_systems, nsys, target, targets, hbonds, chain_start,
                                   chain_len, chain_off, outputs, own_cap, C, std::min(compact, (int)DMD_COMPACT_DN));
@@ -1279,7 +1405,7 @@ cudaError_t dmd_max_active_clusters(int C, int *n) {
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    cluster_config(cfg, attr, 1, C, run_smem(0, C == 1 ? OWN_SMEM_FULL : 0), 0);
+    cluster_config(cfg, attr, 1, C, run_smem(0, C == 1 ? OWN_SMEM_FULL : 0), 0, RUN_NT_FULL);
     return cudaOccupancyMaxActiveClusters(n, run_full::k_run, &cfg);
 }
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,

@@ -91,7 +91,7 @@ struct DScal {
     long long run_cycles; /* SM clock cycles of this system's last launch (scheduling hint) */
     long long done_all;   /* events over all launches since the host last cleared it */
     int need_full;        /* 1: a compact launch stopped here; lists need the full variant */
-    int pad;
+    int err_info2;        /* second bead of an overlap error (err_info holds the first) */
 };
 
 /* device view of one system; all arrays in global memory */

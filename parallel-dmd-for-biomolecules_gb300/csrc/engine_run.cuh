@@ -14,6 +14,9 @@ constexpr int OPS_MAX = DMD_RUN_OPS;
 constexpr int RSET_MAX = DMD_RUN_RSET;
 constexpr int QSET_MAX = DMD_RUN_QSET;
 constexpr int DN_LIMIT = DMD_RUN_DN_LIMIT;
+constexpr int RUN_NT = DMD_RUN_NT;          /* threads per CTA of this variant */
+constexpr int RUN_NW = RUN_NT / 32;
+static_assert(RUN_NW <= NWARPS_MAX && RUN_NW <= CAND_MAX, "warps per CTA");
 static_assert(OPS_MAX >= 2 * (DN_LIMIT < 128 ? DN_LIMIT : 128) + 6, "down-list operations of one event must fit");
 
 /* per-warp working area of one event (dynamic shared memory) */
@@ -1330,7 +1333,7 @@ __device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *
  * by one cluster of C CTAs (C = 1: one CTA).  The leader CTA (rank 0)
  * selects events and keeps the counters; a batch's candidates go one per
  * warp over all CTAs of the cluster. */
-__global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, long long target_all,
+__global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long long target_all,
                                                      const long long *targets, int hbonds_mask,
                                                      const int *chain_start, const int *chain_len,
                                                      const int *chain_off, dmd_diag *outputs, int own_cap, int C,
@@ -1357,7 +1360,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
      * CTAs of a cluster, so that a short batch still spreads its events
      * (and their pooled prediction tasks) over all SMs of the cluster */
     const int gw = warp * C + rank;
-    const int slots = min(C * NWARPS, CAND_MAX);
+    const int slots = min(C * RUN_NW, CAND_MAX);
     WarpArea &W = warea[warp];
     SharedState *L = C > 1 ? cg::this_cluster().map_shared_rank(&sh, 0) : &sh;
     if (threadIdx.x == 0) {
@@ -1368,8 +1371,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
     }
     /* footprint claim table: shared memory when one CTA holds the system and
      * it fits, else the system's global array; cleared at every launch */
-    TaskPool &TP = *(TaskPool *)(warea + NWARPS);
-    unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)((char *)(warea + NWARPS) + sizeof(TaskPool)) : S.owner;
+    TaskPool &TP = *(TaskPool *)(warea + RUN_NW);
+    unsigned *own = (C == 1 && N <= own_cap) ? (unsigned *)((char *)(warea + RUN_NW) + sizeof(TaskPool)) : S.owner;
     if (threadIdx.x == 0) { TP.n = 0; TP.nlive = 0; }
     for (int b = rank * blockDim.x + threadIdx.x; b < 3 * N; b += C * blockDim.x) own[b] = 0u;
     csync(C);
@@ -1442,7 +1445,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                 sh.exitf = L->exitf; sh.ev = L->ev; sh.m = L->m; sh.tick_reset = L->tick_reset; sh.bseq = L->bseq;
                 sh.coll0 = L->coll0; sh.log0 = L->log0; sh.imax = L->imax; sh.tnow = L->tnow; sh.tf_iv = L->tf_iv;
             }
-            if (threadIdx.x < NWARPS) {
+            if (threadIdx.x < RUN_NW) {
                 int k = threadIdx.x * C + rank;
                 if (k < CAND_MAX) { sh.sort_idx[k] = L->sort_idx[k]; sh.sort_key[k] = L->sort_key[k]; }
             }
@@ -1556,10 +1559,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             const long long coll0 = sh.coll0;
             const double imax = sh.imax;
             /* this CTA's events are warps 0 .. nloc-1; the free warps
-             * nloc .. NWARPS-1 take over the task preparation of up to two
+             * nloc .. RUN_NW-1 take over the task preparation of up to two
              * events each when that covers every event */
             const int nloc = P > rank ? (P - rank + C - 1) / C : 0;
-            const int nfree = NWARPS - nloc;
+            const int nfree = RUN_NW - nloc;
             const bool split = nfree > 0 && 2 * nfree >= nloc;
             if (light) {
                 /* light batch (one CTA): two events per collision warp, one
@@ -1579,7 +1582,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
                     }
                     hw_collision_light(S, WE, has, i, j, tf, hbonds);
                 } else {
-                    for (int k = warp - ncw; k < P; k += NWARPS - ncw) {
+                    for (int k = warp - ncw; k < P; k += RUN_NW - ncw) {
                         const int i = sh.sort_idx[k];
                         warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
                     }
@@ -1623,7 +1626,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             {
                 const int ntot = min(TP.n, PTASK_MAX);   /* TP.nlive is 0 (reset with TP.n) */
                 DMD_PHASE(12);
-                for (int base = 0; base < ntot; base += NTHREADS) {
+                for (int base = 0; base < ntot; base += RUN_NT) {
                     const int q = base + threadIdx.x;
                     bool live = false;
                     if (q < ntot) {
@@ -1849,7 +1852,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             double t_before = sh.tnow, tf = sh.tf_iv;
             /* the warp areas are free during an interval: the rebuild's scratch */
             bool rb = cluster_interval(S, sh, L, rank, C, ScratchRef{(char *)&warea[0].fs, sizeof(WarpArea)}, hbonds,
-                                       (char *)warea, (int)(NWARPS * sizeof(WarpArea)));
+                                       (char *)warea, (int)(RUN_NW * sizeof(WarpArea)));
             if (leader && threadIdx.x == 0) {
                 sh.sc.n_interval += 1;
                 log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
@@ -1861,6 +1864,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_run(DSys *systems, int nsys, lo
             ph_kind = 8;
             /* ---- output: the leader CTA ---- */
             if (leader) {
+                /* the -Ddebugging check of code/main.F90:1193-1205: stop on an
+                 * overlap or a broken bond */
+                if (S.flags & DMD_FLAG_CHECK_OVERLAP) cta_checkover(S, sh);
                 cta_diag(S, sh, cs, cl, outputs ? outputs + r : nullptr);
                 if (threadIdx.x == 0) {
                     sh.sc.n_output += 1;

@@ -23,6 +23,8 @@ ERRORS = {
 FLAG_STOP_AT_OUTPUT = 1
 FLAG_COUNT_PHYSICAL = 2
 FLAG_SERIAL = 4
+FLAG_ALLOW_OVERLAP = 8
+FLAG_CHECK_OVERLAP = 16
 EV_GHOST, EV_INTERVAL, EV_REBUILD, EV_OUTPUT = 100, 101, 102, 103
 
 dbl_p = C.POINTER(C.c_double)
@@ -85,6 +87,7 @@ class Diag(C.Structure):
         ("n_output", C.c_int64), ("n_updates", C.c_int64), ("n_forced_updates", C.c_int64),
         ("t", C.c_double), ("tfalse", C.c_double), ("nbr_mean", C.c_double),
         ("n_batches", C.c_int64), ("n_rolled_back", C.c_int64), ("n_candidates", C.c_int64),
+        ("nc_boundbad", C.c_int64), ("nc_unboundbad", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
