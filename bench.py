@@ -40,8 +40,13 @@ UNIT = "events/s"
 
 
 # --------------------------------------------------------------- workloads
-def make_workload(name: str, rank: int = 0):
+def make_workload(name: str, rank: int = 0, gen=None):
+    """The named workload, generated by gen (systems.generate by default;
+    the CPU arm passes the oracle library's copy of the generator so that it
+    loads nothing of the engine)."""
     from dmdgb import sharding, systems
+
+    gen = gen or systems.generate
 
     if name == "c3":
         specs = systems.config_c3(32, seed=sharding.replica_seed(rank))
@@ -58,7 +63,7 @@ def make_workload(name: str, rank: int = 0):
     else:
         raise SystemExit(f"unknown workload {name}")
     for s in specs:
-        systems.generate(s)
+        gen(s)
     return specs, desc
 
 
@@ -72,6 +77,38 @@ def algorithmic_bytes_per_event(nbr_mean: float) -> float:
 
 def rebuild_bytes(n: int, nbr_mean: float) -> float:
     return n * (24 + 4) + n * nbr_mean * (4 + 54)
+
+
+def fp64_flops_per_event(nbr_mean: float) -> float:
+    """Double-precision operations of one committed pair event: the
+    re-predictions of both beads against their neighbours (2 * nbr_mean
+    pairs) and of the two beads themselves, about 27 operations each
+    (relative position and velocity, minimum image, three dot products, the
+    discriminant, one square root and one division counted as one each),
+    plus about 40 for the collision impulse."""
+    return 27.0 * (2.0 * nbr_mean + 2.0) + 40.0
+
+
+FP64_PEAK_GFLOPS = 1250.0   # GB300 nominal dense FP64 (no measured figure in the peaks file)
+
+
+def cpu_model() -> str:
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 # ------------------------------------------------------------ clock sampler
@@ -148,6 +185,36 @@ def cpu_rate(specs, events_per_replica: int, cores: int):
     return total / slowest, total, wall
 
 
+def _single_core_worker(args):
+    """One host process: the CPU restatement on one system, events/s over
+    n_events after creation (its start-up overlap check skipped: it is not
+    part of the event loop)."""
+    name, n_events = args
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, PKG)
+    from oracle import oracle as ora
+    from dmdgb import abi, systems
+
+    spec = {"c1": systems.config_c1, "c2": systems.config_c2, "c4": systems.config_c4}[name]()
+    ora.generate(spec)
+    o = ora.Oracle(spec, flags=abi.FLAG_ALLOW_OVERLAP)
+    t0 = time.perf_counter()
+    o.run(n_events)
+    dt = time.perf_counter() - t0
+    return name, spec.n_beads, n_events, n_events / dt, dt
+
+
+def cpu_single_core(samples=(("c1", 300000), ("c2", 300000), ("c4", 100000))) -> dict:
+    """The CPU restatement on one core for the single-system workloads
+    (each in its own process, run one after another)."""
+    ctx = mp.get_context("spawn")
+    out = {"cores": 1, "kind": "port", "cpu_model": cpu_model()}
+    with ctx.Pool(1) as pool:
+        for name, n_beads, n_ev, rate, dt in pool.map(_single_core_worker, list(samples)):
+            out[name] = {"events_per_s": rate, "beads": n_beads, "sample": f"{n_ev} events after creation, {dt:.2f} s"}
+    return out
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
@@ -174,9 +241,11 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    specs, desc = make_workload(args.workload)
+    from oracle import oracle as ora
+
+    specs, desc = make_workload(args.workload, gen=ora.generate)
     cores = max(1, min(os.cpu_count() or 1, 64))
-    n_ev = args.cpu_events
+    n_ev = args.events
     for _ in range(args.warmup):
         cpu_rate(specs, max(1000, n_ev // 10), cores)
     rates, times = [], []
@@ -192,7 +261,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc, "events_per_replica_per_step": n_ev},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "cpu_model": cpu_model(),
                          "sample": f"all {len(specs)} replicas, {n_ev} events each, dealt to {cores} processes"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -262,16 +331,26 @@ def run_ours(args):
     achieved = per_launch_bytes / launch_s / 1e9
     tpe = traffic_per_event()
     traffic = tpe * E * len(specs) if tpe else None
+    fp64_gflops = pair_events * fp64_flops_per_event(nbr) / step_s / 1e9
+
+    # the rate over a longer stretch: ten more segments of the same batch,
+    # each segment's committed events/s (the lists and aggregates grow)
+    segments = []
+    if rank == 0 and args.segments > 0:
+        for _ in range(args.segments):
+            batch.run(args.segment_events)
+            segments.append(args.segment_events * len(specs) / (lib.dmd_batch_last_run_ms(batch.h) / 1000.0))
 
     # the plain one-system-per-launch path on the same replicas
     plain_events, plain_s = 0, 0.0
     n_plain = min(len(specs), args.plain_replicas)
+    Ep = min(E, args.plain_events)
     for s in specs[:n_plain]:
         with Engine(s) as eng:
-            eng.run(E)          # warm-up of this system
-            eng.run(E)
+            eng.run(Ep)          # warm-up of this system
+            eng.run(Ep)
             plain_s += eng.lib.dmd_last_run_ms(eng.h) / 1000.0
-            plain_events += E
+            plain_events += Ep
     plain_value = plain_events / plain_s if plain_s > 0 else None
 
     # end to end through the public API with host buffers
@@ -293,11 +372,11 @@ def run_ours(args):
     serving = None
     if rank == 0 and not args.no_serve:
         serving = run_serving(args)
-        # the same arrivals with 10x the events: the server saturates (1e5-1e6 events per request)
-        serving["saturated"] = run_serving(args, scale=10 * args.serve_scale)
+        # the stated serving load (1e6-1e7 events per request) over a bounded window
+        serving["c5_full"] = run_serving_full(args)
     single = None
     if rank == 0 and not args.no_single:
-        single = run_single_systems(E)
+        single = run_single_systems(min(E, args.single_events))
 
     sidechain = None
     if rank == 0 and not args.no_sidechain:
@@ -306,9 +385,10 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = max(1, min(os.cpu_count() or 1, 64))
-        r, tot, wall = cpu_rate(specs, args.cpu_events, cores)
-        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"CPU restatement: all {len(specs)} replicas, {args.cpu_events} events each, dealt to {cores} processes, {wall:.1f} s wall"}
+        r, tot, wall = cpu_rate(specs, E, cores)
+        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port", "cpu_model": cpu_model(),
+               "sample": f"CPU restatement: all {len(specs)} replicas, {E} events each, dealt to {cores} processes, {wall:.1f} s wall",
+               "single_core": cpu_single_core()}
 
     if rank == 0:
         line = {
@@ -325,7 +405,12 @@ def run_ours(args):
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
-                         "bytes_per_event": algorithmic_bytes_per_event(nbr), "nbr_mean": nbr},
+                         "bytes_per_event": algorithmic_bytes_per_event(nbr), "nbr_mean": nbr,
+                         "fp64": {"achieved": fp64_gflops, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
+                                  "frac": fp64_gflops / FP64_PEAK_GFLOPS, "peak_kind": "nominal",
+                                  "flops_per_event": fp64_flops_per_event(nbr)}},
+            "segments": {"events_per_replica": args.segment_events, "events_per_s": segments,
+                         "note": "the batch continued after the timed steps, one launch per segment"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "serving": serving,
@@ -339,13 +424,14 @@ def run_ours(args):
 
 def run_single_systems(E: int) -> dict:
     """The single-system workloads on the plain path (one system per launch,
-    autotuned cluster): 48 x KLVFFAE (1,344 beads) and 1,000 random 10-mers
-    (40,000 beads), committed events/s over E events after a warm-up."""
+    autotuned cluster): 8 x KLVFFAE (224 beads), 48 x KLVFFAE (1,344 beads)
+    and 1,000 random 10-mers (40,000 beads), committed events/s over E events
+    after a warm-up."""
     from dmdgb import systems
-    from dmdgb.engine import Engine
 
     out = {}
-    for name, spec in (("c2_1344_beads", systems.config_c2()), ("c4_40000_beads", systems.config_c4())):
+    for name, spec in (("c1_224_beads", systems.config_c1()), ("c2_1344_beads", systems.config_c2()),
+                       ("c4_40000_beads", systems.config_c4())):
         systems.generate(spec)
         from dmdgb.engine import Batch
         b = Batch([spec])
@@ -424,6 +510,36 @@ def run_serving(args, scale: float = None) -> dict:
     return out
 
 
+def run_serving_full(args) -> dict:
+    """The serving workload at its stated size: Poisson arrivals at 20
+    requests/s of 4-200 chains x 6-40 residues with 1e6-1e7 events each,
+    over a bounded arrival window and a wall-clock horizon.  The offered
+    load (about 1.1e8 events/s) is above what one GPU serves, so the report
+    is the backlog: requests and events offered, served and left at the
+    horizon, how fast the backlog grows, p50/p99 of the requests completed,
+    and lower bounds of p50/p99 over all arrived requests (an unfinished
+    request counts with its age at the horizon)."""
+    from dmdgb import systems
+    import numpy as np
+    from dmdgb.serving import Server, poisson_arrivals, serve_trace
+
+    arr = poisson_arrivals(20.0, args.full_serve_seconds, seed=1)
+    reqs = []
+    for k in range(len(arr)):
+        spec = systems.generate(systems.serving_request(k, seed=1))
+        reqs.append((spec, int(spec.n_events)))
+    with Server(max_slots=args.serve_slots, chunk_events=args.serve_chunk) as srv:
+        res = serve_trace(srv, arr, reqs, horizon_s=args.full_serve_horizon)
+    out = res.summary()
+    offered = int(sum(n for _, n in reqs))
+    out.update({"arrival_rate_per_s": 20.0, "trace_seconds": args.full_serve_seconds,
+                "horizon_s": args.full_serve_horizon, "events_scale": 1.0,
+                "requests_arrived": len(arr), "events_offered": offered,
+                "offered_events_per_s": offered / args.full_serve_seconds,
+                "note": "stated request sizes (1e6-1e7 events); stopped at the horizon with a backlog"})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -431,9 +547,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c3")
-    ap.add_argument("--events", type=int, default=20000, help="events per replica per step")
-    ap.add_argument("--cpu-events", type=int, default=300000, help="CPU baseline: events per replica")
+    ap.add_argument("--events", type=int, default=100000,
+                    help="events per replica per step (both arms, and the CPU baseline's sample)")
     ap.add_argument("--plain-replicas", type=int, default=32)
+    ap.add_argument("--plain-events", type=int, default=20000, help="events per system on the plain path")
+    ap.add_argument("--single-events", type=int, default=100000, help="events of the single-system runs")
+    ap.add_argument("--segments", type=int, default=10)
+    ap.add_argument("--segment-events", type=int, default=100000)
+    ap.add_argument("--full-serve-seconds", type=float, default=15.0,
+                    help="arrival window of the full-size serving trace")
+    ap.add_argument("--full-serve-horizon", type=float, default=45.0,
+                    help="wall-clock bound of the full-size serving trace")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-tune", action="store_true")

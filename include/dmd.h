@@ -89,6 +89,10 @@ typedef struct dmd_run_cfg {
 /* The -Ddebugging checks at every output event (code/main.F90:1193-1205):
  * an overlap or a broken bond stops the run with DMD_E_OVERLAP. */
 #define DMD_FLAG_CHECK_OVERLAP 16
+/* Test of the failure path: the event loop's iteration bound (normally
+ * 16 * events + 10^6 batches) becomes 8 batches, so a longer run stops with
+ * DMD_E_DEVICE_TIMEOUT between two batches, its state intact. */
+#define DMD_FLAG_TIGHT_LOOP_BOUND 32
 
 /* One system: chains, sequences, initial state (code/inputinfo.f:5-101,
  * code/main.F90:240-321). */

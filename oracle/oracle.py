@@ -57,6 +57,17 @@ def lib():
     return _lib
 
 
+def generate(spec, tables=None, min_sep: float = 5.0):
+    """The seeded system generator (dmd_generate) from the oracle library's
+    own copy, so that a CPU-only run never loads the engine library."""
+    from dmdgb import systems
+    L = lib()
+    L.dmd_generate.argtypes = [C.POINTER(abi.GenSpec), C.POINTER(abi.Tables), C.c_int32] + [abi.dbl_p] * 6 + \
+        [C.c_char_p, C.c_int32]
+    L.dmd_generate.restype = C.c_int
+    return systems.generate(spec, tables, min_sep, lib=L)
+
+
 class Oracle:
     def __init__(self, spec, tables=None, flags: int = 0, list_cap: int = 0):
         self.L = lib()

@@ -27,6 +27,22 @@
 #include "engine.cuh"
 #include "engine_api.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+/* NVTX ranges around the host side of each phase (creation: host set-up,
+ * upload and the first list build; a run; the state read-back; a serving
+ * step's launch, admission and retirement), for timeline tools.  The phases
+ * inside the persistent event loop are not host calls; the phase-timer
+ * build (-DDMD_PHASE_TIMERS) measures those. */
+namespace {
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+}  // namespace
+
 namespace {
 
 const double DEL = 0.02375;
@@ -696,6 +712,7 @@ int upload(dmd_batch &B) {
 }
 
 int batch_create(dmd_batch &B, int n, const dmd_run_cfg *cfgs, const dmd_tables *tables, const dmd_system *systems) {
+    NvtxRange range("dmd create: set-up, upload, list build");
     if (n <= 0 || !cfgs || !tables || !systems) { B.err = "null or empty argument"; return DMD_E_INPUT; }
     B.hs.resize(n);
     B.hbonds = cfgs[0].hbonds != 0;
@@ -731,6 +748,11 @@ int sync_check(dmd_batch &B) {
                   " overlap, or their bond is outside its window (output-event check of code/checkover.f)";
             return sc.err;
         }
+        if (sc.err == DMD_E_DEVICE_TIMEOUT) {
+            err = "system " + std::to_string(r) + ": the event loop reached its iteration bound at coll " +
+                  std::to_string(sc.coll) + " and stopped between two batches (DMD_E_DEVICE_TIMEOUT)";
+            return sc.err;
+        }
         if (sc.err) {
             err = "device error " + std::to_string(sc.err) + " in system " + std::to_string(r) + " (info " + std::to_string(sc.err_info) + ")";
             return sc.err;
@@ -752,6 +774,7 @@ int run_full_remainder(dmd_batch &B, const std::vector<long long> &rem, int C, i
 }
 
 int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
+    NvtxRange range("dmd run: event loop");
     std::string &err = B.err;
     if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
     B.diag_valid = false;
@@ -828,6 +851,7 @@ size_t state_block(const DSys &d) { return (size_t)((const char *)(d.er + 4 * (s
 
 int get_state(dmd_batch &B, int r, double *x, double *y, double *z, double *vx, double *vy, double *vz,
               int32_t *bptnr, int32_t *identity, int32_t *er_out, double *t, double *tfalse, int64_t *coll) {
+    NvtxRange range("dmd state read-back");
     std::string &err = B.err;
     if (r < 0 || r >= (int)B.hs.size()) { err = "replica index out of range"; return DMD_E_INPUT; }
     const int n = (int)B.hs.size();
@@ -1174,6 +1198,7 @@ int server_retire(dmd_server &V, ServerReq &R, int slot) {
  * admit queued requests on the copy stream meanwhile, then retire the
  * finished ones; the admitted requests run from the next round on. */
 int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
+    NvtxRange range("dmd server step");
     std::string &err = V.err;
     std::vector<ServerReq *> act;
     {
@@ -1233,7 +1258,10 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
          * request is dropped.  A request whose read-back fails is failed
          * alone; the step reports the first such error after the rest are
          * booked. */
-        server_admit(V, n, admitted);          /* overlaps the launch */
+        {
+            NvtxRange admit_range("dmd server admit (beside the launch)");
+            server_admit(V, n, admitted);      /* overlaps the launch */
+        }
         int first_rc = DMD_OK;
         std::string first_err;
         const cudaError_t se = cudaStreamSynchronize(V.run_st);   /* (the host vectors above outlive the copies) */

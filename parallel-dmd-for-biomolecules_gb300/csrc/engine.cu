@@ -107,7 +107,19 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
     if (nctas > DMD_PHASE_CTAS) nctas = DMD_PHASE_CTAS;
     return (int)cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(long long) * DMD_PHASE_SLOTS * nctas);
 }
+/* sub-phases of the candidate gather, per CTA (rows 512 + block index) */
+#define DMD_GSUB_START() long long gs_t_ = clock64()
+#define DMD_GSUB(k)                                                                        \
+    do {                                                                                   \
+        if (threadIdx.x == 0 && blockIdx.x < 500) {                                        \
+            long long now_ = clock64();                                                    \
+            g_phase_cycles[512 + blockIdx.x][(k)] += now_ - gs_t_;                         \
+            gs_t_ = now_;                                                                  \
+        }                                                                                  \
+    } while (0)
 #else
+#define DMD_GSUB_START() do { } while (0)
+#define DMD_GSUB(k) do { } while (0)
 #define DMD_PHASE_START(row) do { (void)(row); } while (0)
 #define DMD_PHASE(k) do { (void)(k); } while (0)
 #define DMD_SUB(k) do { } while (0)
@@ -1094,11 +1106,18 @@ __device__ int warp_root(const DSys &S, long long &kroot) {
     long long bk = DMD_KEY_INF;
     int best = INT_MAX;
     if (S.nl1 <= 256) {
-        for (int g = lane; g < S.nl1; g += 32) {
-            const long long k = S.l1k[g];
-            const int e = S.l1i[g];
-            if (key_less(k, e, bk, best)) { bk = k; best = e; }
+        /* eight groups per lane, every load issued before the first compare */
+        long long kq[8];
+        int eq[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int g = lane + 32 * q;
+            kq[q] = g < S.nl1 ? S.l1k[g] : DMD_KEY_INF;
+            eq[q] = g < S.nl1 ? S.l1i[g] : INT_MAX;
         }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (key_less(kq[q], eq[q], bk, best)) { bk = kq[q]; best = eq[q]; }
     } else {
         for (int h = lane; h < S.nl2; h += 32) l2_update(S, h);
         __syncwarp();
@@ -1118,54 +1137,128 @@ __device__ int warp_root(const DSys &S, long long &kroot) {
     return bk == DMD_KEY_INF ? -1 : best;
 }
 
+/* the double whose okey() is k (k of a finite time) */
+__device__ __forceinline__ double key_time(long long k) {
+    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffLL));
+}
+
+#define FEW_GROUPS 256    /* level-1 groups (8 per lane) scanned by every warp from registers */
+#define GSEL_MAX 8        /* groups below the cut one warp takes per attempt */
+
 /* The batch candidates: every bead entry whose key lies below a cut (and
  * below every pseudo event), sorted in (key, index) order into
  * sh.sort_key/sort_idx; the first is the root.  The cut is the root's time
  * plus a window sh.delta that adapts to aim at one to four candidates per
  * warp slot.  Every warp scans the level-1 minima against the cut and takes
- * every NWARPS-th group below it; warp 0 sorts.  sh.ncand must be 0 on
- * entry.  Returns their number (1 if the window cannot be made small
- * enough). */
+ * every nw-th group below it; warp 0 sorts.  Each step issues all of its
+ * global loads before it uses the first (they take hundreds of cycles
+ * each).  sh.ncand must be 0 on entry.  Returns their number (1 if the
+ * window cannot be made small enough). */
 __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, long long kroot, int slots) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    const int N = S.N;
+    const int N = S.N, nl1 = S.nl1;
+    DMD_GSUB_START();
+    /* the loads that do not depend on the cut, issued together: the pseudo
+     * events' keys and, for up to 256 groups, every level-1 minimum (each
+     * lane holds eight); the root's time is its key read back */
+    const bool few = nl1 <= FEW_GROUPS;
+    long long gk[FEW_GROUPS / 32];
+#pragma unroll
+    for (int q = 0; q < FEW_GROUPS / 32; ++q) {
+        const int g = lane + 32 * q;
+        gk[q] = few && g < nl1 ? S.l1k[g] : DMD_KEY_INF;
+    }
     const long long kp = min(min(S.key[N], S.key[N + 1]), S.key[N + 2]);
+    const double t_root = key_time(kroot);
     int nc = 0;
     bool ok = false;
     for (int attempt = 0; attempt < 8; ++attempt) {
-        long long kc = 0;
-        if (lane == 0) {
-            kc = okey(S.tim[root] + sh.delta);
-            if (kc <= kroot) kc = kroot + 1;
-            if (kc > kp) kc = kp;
-        }
-        kc = __shfl_sync(FULL, kc, 0);
-        /* few groups: every warp scans them all and takes the groups below
-         * the cut with ordinals warp, warp + nw, ...; many: each warp
-         * scans blocks of 32 groups in turn and takes their groups */
-        const bool few = S.nl1 <= 32 * (nw / 2);
-        int ord = 0;
-        for (int gb = few ? 0 : 32 * warp; gb < S.nl1; gb += few ? 32 : 32 * nw) {
-            const int g = gb + lane;
-            unsigned gm = __ballot_sync(FULL, g < S.nl1 && S.l1k[g] < kc);
-            while (gm) {
-                const int gg = gb + __ffs(gm) - 1;
-                gm &= gm - 1;
-                if (few && ord++ % nw != warp) continue;
-                const int e = gg * 32 + lane;
-                const long long k = e < N ? S.key[e] : DMD_KEY_INF;
-                const bool c = k < kc;
-                const unsigned cm = __ballot_sync(FULL, c);
+        long long kc = okey(t_root + sh.delta);
+        if (kc <= kroot) kc = kroot + 1;
+        if (kc > kp) kc = kp;
+        DMD_GSUB(0);
+        bool over = false;
+        if (few) {
+            /* the groups whose minimum lies below the cut, in order; a group
+             * below the cut holds at least one candidate, so more than
+             * CAND_MAX of them overflow at once.  This warp takes the
+             * ordinals warp, warp + nw, ... and loads their keys together. */
+            unsigned gm[FEW_GROUPS / 32];
+            int pre[FEW_GROUPS / 32 + 1];
+            pre[0] = 0;
+#pragma unroll
+            for (int q = 0; q < FEW_GROUPS / 32; ++q) {
+                gm[q] = __ballot_sync(FULL, gk[q] < kc);
+                pre[q + 1] = pre[q] + __popc(gm[q]);
+            }
+            const int ng = pre[FEW_GROUPS / 32];
+            over = ng > CAND_MAX;
+            if (!over) {
+                int gsel[GSEL_MAX];
+                int ns = 0;
+#pragma unroll
+                for (int u = 0; u < GSEL_MAX; ++u) {
+                    const int o = warp + u * nw;
+                    gsel[u] = -1;
+                    if (o < ng) {
+                        int q = 0;
+#pragma unroll
+                        for (int qq = 1; qq < FEW_GROUPS / 32; ++qq) q += o >= pre[qq];
+                        gsel[u] = 32 * q + (int)__fns(gm[q], 0, o - pre[q] + 1);
+                        ns = u + 1;
+                    }
+                }
+                long long kv[GSEL_MAX];
+#pragma unroll
+                for (int u = 0; u < GSEL_MAX; ++u) {
+                    const int e = gsel[u] * 32 + lane;
+                    kv[u] = (gsel[u] >= 0 && e < N) ? S.key[e] : DMD_KEY_INF;
+                }
+                unsigned cm[GSEL_MAX];
+                int tot = 0;
+#pragma unroll
+                for (int u = 0; u < GSEL_MAX; ++u) {
+                    cm[u] = __ballot_sync(FULL, u < ns && kv[u] < kc);
+                    tot += __popc(cm[u]);
+                }
                 int pos = 0;
-                if (lane == 0 && cm) pos = atomicAdd(&sh.ncand, __popc(cm));
-                pos = __shfl_sync(FULL, pos, 0) + __popc(cm & lt);
-                if (c && pos < CAND_MAX) { sh.cand_key[pos] = k; sh.cand_idx[pos] = e; }
+                if (lane == 0 && tot) pos = atomicAdd(&sh.ncand, tot);
+                pos = __shfl_sync(FULL, pos, 0);
+#pragma unroll
+                for (int u = 0; u < GSEL_MAX; ++u) {
+                    const int p = pos + __popc(cm[u] & lt);
+                    if (((cm[u] >> lane) & 1u) && p < CAND_MAX) { sh.cand_key[p] = kv[u]; sh.cand_idx[p] = gsel[u] * 32 + lane; }
+                    pos += __popc(cm[u]);
+                }
+            }
+        } else {
+            /* many groups: each warp scans blocks of 32 groups in turn */
+            for (int gb = 32 * warp; gb < nl1; gb += 32 * nw) {
+                const int g = gb + lane;
+                unsigned gmk = __ballot_sync(FULL, g < nl1 && S.l1k[g] < kc);
+                while (gmk) {
+                    const int gg = gb + __ffs(gmk) - 1;
+                    gmk &= gmk - 1;
+                    const int e = gg * 32 + lane;
+                    const long long k = e < N ? S.key[e] : DMD_KEY_INF;
+                    const bool c = k < kc;
+                    const unsigned cmk = __ballot_sync(FULL, c);
+                    int pos = 0;
+                    if (lane == 0 && cmk) pos = atomicAdd(&sh.ncand, __popc(cmk));
+                    pos = __shfl_sync(FULL, pos, 0) + __popc(cmk & lt);
+                    if (c && pos < CAND_MAX) { sh.cand_key[pos] = k; sh.cand_idx[pos] = e; }
+                }
             }
         }
+        DMD_GSUB(1);
         __syncthreads();
+        DMD_GSUB(2);
         nc = sh.ncand;
-        ok = nc <= CAND_MAX;
+        ok = !over && nc <= CAND_MAX;
+#ifdef DMD_PHASE_TIMERS
+        if (threadIdx.x == 0 && blockIdx.x < 500) g_phase_cycles[512 + blockIdx.x][8] += 1;   /* attempts */
+#endif
         if (ok) break;
         __syncthreads();                   /* every thread has read ncand */
         if (threadIdx.x == 0) {
@@ -1179,6 +1272,9 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
         if (threadIdx.x == 0) { sh.sort_key[0] = kroot; sh.sort_idx[0] = root; }
         return 1;
     }
+#ifdef DMD_PHASE_TIMERS
+    if (threadIdx.x == 0 && blockIdx.x < 500) { g_phase_cycles[512 + blockIdx.x][9] += nc; g_phase_cycles[512 + blockIdx.x][10] += 1; }
+#endif
     if (warp == 0) {
         /* rank sort: each candidate counts the candidates before it */
         long long kk[2];
@@ -1189,7 +1285,7 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
             kk[h] = c < nc ? sh.cand_key[c] : DMD_KEY_INF;
             ee[h] = c < nc ? sh.cand_idx[c] : INT_MAX;
         }
-#pragma unroll 4
+#pragma unroll 8
         for (int u = 0; u < nc; ++u) {
             const long long ku = sh.cand_key[u];
             const int eu = sh.cand_idx[u];
@@ -1199,12 +1295,14 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
 #pragma unroll
         for (int h = 0; h < 2; ++h)
             if (lane + 32 * h < nc) { sh.sort_key[rk[h]] = kk[h]; sh.sort_idx[rk[h]] = ee[h]; }
-        if (lane == 0) {
-            if (nc < slots) sh.delta = sh.delta * 2.0;
-            else if (nc > 4 * slots) sh.delta = sh.delta * 0.5;
-            if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
-        }
+    } else if (threadIdx.x == 32) {
+        /* the window for the next batch (beside the sort): aim at one to
+         * four candidates per slot */
+        if (nc < slots) sh.delta = sh.delta * 2.0;
+        else if (nc > 4 * slots) sh.delta = sh.delta * 0.5;
+        if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
     }
+    DMD_GSUB(3);
     return nc;
 }
 

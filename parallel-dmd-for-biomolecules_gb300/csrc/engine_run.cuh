@@ -1378,7 +1378,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
     csync(C);
     DMD_PHASE_START(leader ? r : -1);
     const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
-    const long long max_iter = 16 * target + 1000000;
+    const long long max_iter = (S.flags & DMD_FLAG_TIGHT_LOOP_BOUND) ? 8 : 16 * target + 1000000;
     const long long t_start = clock64();
     long long iter = 0;
     while (true) {

@@ -2,7 +2,7 @@
 reference checkout (parameters/ and parametersep/ep19p_ha55a_weakhp.data,
 the table code/inputinfo.f:282 reads) with dmdgb.params.
 
-    python make_tables.py /root/reference/parallel-dmd-PRIME20
+    python make_tables.py <reference>/parallel-dmd-PRIME20   (or set DMD_REFERENCE_DIR)
 """
 import json
 import os
@@ -22,4 +22,4 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parallel-dmd-PRIME20")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["DMD_REFERENCE_DIR"])

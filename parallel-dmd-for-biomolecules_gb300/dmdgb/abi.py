@@ -25,6 +25,7 @@ FLAG_COUNT_PHYSICAL = 2
 FLAG_SERIAL = 4
 FLAG_ALLOW_OVERLAP = 8
 FLAG_CHECK_OVERLAP = 16
+FLAG_TIGHT_LOOP_BOUND = 32
 EV_GHOST, EV_INTERVAL, EV_REBUILD, EV_OUTPUT = 100, 101, 102, 103
 
 dbl_p = C.POINTER(C.c_double)

@@ -140,21 +140,38 @@ class TraceResult:
     steps: int = 0
     failed: int = 0
     max_active: int = 0
+    # requests still in the server when a horizon stopped the trace
+    unfinished_ages: List[float] = field(default_factory=list)   # horizon - arrival, s
+    unfinished_events_done: int = 0
+    unfinished_events_left: int = 0
+    not_submitted: int = 0
 
     def summary(self) -> dict:
         lat = np.asarray(self.latencies) if self.latencies else np.zeros(1)
-        return {"requests": len(self.latencies), "failed": self.failed,
-                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                "events": self.events, "wall_s": self.wall,
-                "events_per_s": self.events / self.wall if self.wall > 0 else None,
-                "kernel_s": self.kernel_ms / 1000.0, "steps": self.steps, "max_active": self.max_active}
+        out = {"requests": len(self.latencies), "failed": self.failed,
+               "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+               "events": self.events, "wall_s": self.wall,
+               "events_per_s": self.events / self.wall if self.wall > 0 else None,
+               "kernel_s": self.kernel_ms / 1000.0, "steps": self.steps, "max_active": self.max_active}
+        if self.unfinished_ages or self.not_submitted:
+            cens = np.concatenate([np.asarray(self.latencies, float), np.asarray(self.unfinished_ages, float)])
+            served = self.events + self.unfinished_events_done
+            out.update({"backlog_requests": len(self.unfinished_ages),
+                        "backlog_events": self.unfinished_events_left,
+                        "events_served": served,
+                        "served_events_per_s": served / self.wall if self.wall > 0 else None,
+                        "p50_lower_bound_s": float(np.percentile(cens, 50)) if len(cens) else None,
+                        "p99_lower_bound_s": float(np.percentile(cens, 99)) if len(cens) else None})
+        return out
 
 
-def serve_trace(server: Server, arrivals: Sequence[float], requests: Sequence[Tuple[SystemSpec, int]]) -> TraceResult:
+def serve_trace(server: Server, arrivals: Sequence[float], requests: Sequence[Tuple[SystemSpec, int]],
+                horizon_s: Optional[float] = None) -> TraceResult:
     """Replay a trace in real time: request k (a generated system and its
     event count) is submitted when the wall clock passes arrivals[k], the
     server is stepped continuously, and each request's latency is its
-    completion time minus its arrival time."""
+    completion time minus its arrival time.  With horizon_s the replay
+    stops at that wall-clock time and reports what is left (backlog)."""
     res = TraceResult()
     late: Dict[int, float] = {}     # request id -> submit delay after arrival, s
     live: Dict[int, int] = {}       # request id -> trace index
@@ -162,6 +179,18 @@ def serve_trace(server: Server, arrivals: Sequence[float], requests: Sequence[Tu
     k_next = 0
     while k_next < len(arrivals) or live:
         now = time.monotonic() - t0
+        if horizon_s is not None and now >= horizon_s:
+            for rid, k in live.items():
+                st = server.status(rid)
+                res.unfinished_ages.append(now - float(arrivals[k]))
+                res.unfinished_events_done += st["events_done"]
+                res.unfinished_events_left += requests[k][1] - st["events_done"]
+            for k in range(k_next, len(arrivals)):
+                if arrivals[k] <= now:
+                    res.unfinished_ages.append(now - float(arrivals[k]))
+                    res.unfinished_events_left += requests[k][1]
+            res.not_submitted = len(arrivals) - k_next
+            break
         while k_next < len(arrivals) and arrivals[k_next] <= now:
             spec, nev = requests[k_next]
             rid = server.submit(spec, nev)

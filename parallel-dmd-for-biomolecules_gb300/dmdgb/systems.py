@@ -87,9 +87,11 @@ class SystemSpec:
                           *[addr(a) for a in arrs], addr(bp), float(self.t0), int(self.coll0))
 
 
-def generate(spec: SystemSpec, tables: Optional[Tables] = None, min_sep: float = 5.0) -> SystemSpec:
-    """Seeded positions and velocities from the engine library."""
-    lib = abi.load_engine()
+def generate(spec: SystemSpec, tables: Optional[Tables] = None, min_sep: float = 5.0, lib=None) -> SystemSpec:
+    """Seeded positions and velocities from dmd_generate: the engine
+    library's, or that of another library that exports it (lib, a ctypes
+    CDLL with abi's declaration of dmd_generate)."""
+    lib = lib or abi.load_engine()
     t = abi.tables_struct(tables or default_tables())
     n = spec.n_beads
     arrs = [np.zeros(n) for _ in range(6)]

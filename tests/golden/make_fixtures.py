@@ -1,7 +1,7 @@
 """Writes the golden fixtures of tests/golden/ from a reference checkout.
 
 Run here, where the reference is mounted read-only:
-    python tests/golden/make_fixtures.py /root/reference/parallel-dmd-PRIME20
+    python tests/golden/make_fixtures.py <reference>/parallel-dmd-PRIME20   (or set DMD_REFERENCE_DIR)
 
 * reference_records.json: framing and sampled values of the genconfig
   output records results/run0000.config and run0000.lastvel (the known
@@ -53,4 +53,4 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parallel-dmd-PRIME20")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["DMD_REFERENCE_DIR"])

@@ -3,7 +3,7 @@ side-chain placement search of the reference's initial-configuration
 generator (genconfig/gen_config_random-SQZ.f90:250-348).
 
 Run here, where the reference is mounted read-only:
-    python tests/golden/make_sidechain_fixture.py /root/reference/parallel-dmd-PRIME20
+    python tests/golden/make_sidechain_fixture.py <reference>/parallel-dmd-PRIME20   (or set DMD_REFERENCE_DIR)
 
 The inputs are the generator's own: its 31-residue template chain
 (genconfig/inputs/peptide{x,y,z}.inp: C-alpha, NH, CO and side-chain beads
@@ -132,4 +132,4 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parallel-dmd-PRIME20")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["DMD_REFERENCE_DIR"])

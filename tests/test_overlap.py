@@ -70,7 +70,8 @@ def test_create_rejects_overlap_and_broken_bond(built):
         with pytest.raises(DMDError) as ei:
             Engine(bad)
         assert ei.value.rc == -2, str(ei.value)
-        assert f"beads {pair[0]} and {pair[1]}" in str(ei.value)
+        named = [int(w) for w in str(ei.value).split("beads ")[1].split(" overlap")[0].split(" and ")]
+        assert pair[1] in named, str(ei.value)      # the moved bead (the device reports the pair it met first)
         try:                                  # no overlap check: at most the negative-time stop
             Engine(bad, flags=abi.FLAG_ALLOW_OVERLAP).close()
         except DMDError as e:
@@ -101,8 +102,8 @@ def test_output_event_check_and_nc_counters(built):
     """With the output-event check on, an H-bond-rich run stays clean and
     commits the same events as the oracle with the same check; the
     check_nc_int counters agree with the oracle's."""
-    spec = dense_system(n_chains=10, L=10, box=38.0, tstar=0.12, seed=21, rng_seed=5)
-    n = 60000
+    spec = dense_system(n_chains=4, L=10, box=30.0, tstar=0.12, seed=21, rng_seed=5)
+    n = 1450000                               # the first output event comes at about 1.42e6
     flags = abi.FLAG_CHECK_OVERLAP
     with Engine(spec, flags=flags) as eng:
         glog = eng.run(n, log_capacity=n + 64)
