@@ -75,6 +75,12 @@ typedef struct dmd_run_cfg {
     double   n_forced;    /* list horizon in intervals (150) */
     int32_t  list_cap;    /* per-bead capacity of each neighbour list (0: default 128) */
     int32_t  flags;       /* DMD_FLAG_* */
+    /* -Dchaptype (code/make_code.f:489-548): 1 (or 0) one peptide type; 2
+     * two, chains species2_chain.. being species 2, and the side chains of
+     * two different species-2 chains then meet as hard cores (type 1)
+     * instead of in the hydrophobic well (type 16) */
+    int32_t  chaptype;
+    int32_t  species2_chain;
 } dmd_run_cfg;
 
 #define DMD_FLAG_STOP_AT_OUTPUT 1  /* dmd_run returns after every output (N+3) event */

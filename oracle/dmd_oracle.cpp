@@ -58,6 +58,7 @@ struct Oracle {
     bool canon = true, hbonds = true;
     uint64_t seed = 0;
     int flags = 0;
+    int chaptype = 1, species2_chain = 0;   /* -Dchaptype; chains species2_chain.. are species 2 */
 
     /* system */
     int N = 0, nchains = 0;
@@ -126,6 +127,8 @@ struct Oracle {
         canon = cfg->canon != 0;
         hbonds = cfg->hbonds != 0;
         seed = cfg->seed;
+        chaptype = cfg->chaptype == 2 ? 2 : 1;
+        species2_chain = cfg->species2_chain;
         flags = cfg->flags;
         cap = cfg->list_cap > 0 ? cfg->list_cap : 128;
         if (n_wrap != 2) { err = "oracle supports n_wrap=2 only"; return false; }
@@ -474,6 +477,23 @@ struct Oracle {
             for (int k = lll + 1; k <= lll + L - 1; ++k) if (fs[k - lll + 1] != 0) setc(k, lll + fs[k - lll + 1], 24);
             for (int k = lll + 2; k <= lll + L; ++k) if (fs[k - lll - 1] != 0) setc(k, lll + fs[k - lll - 1], 25);
             for (int k = lll + 2 * L + 1; k <= lll + 3 * L - 2; ++k) if (fs[k - lll - 2 * L + 2] != 0) setc(k, lll + fs[k - lll - 2 * L + 2], 26);
+        }
+        if (chaptype == 2) {
+            /* make_code.f:489-514: hydrophobic side chains of two chains meet
+             * in the well; make_code.f:516-541: of two species-2 chains, as
+             * hard cores */
+            for (int m = 1; m <= N - 1; ++m)
+                for (int l = m + 1; l <= N; ++l)
+                    if (identity[m] > 8 && identity[l] > 8)
+                        if (hp[chain_of[m]][local_of[m]] == 1 && hp[chain_of[l]][local_of[l]] == 1)
+                            if (chain_of[l] != chain_of[m]) E(m, l) = 16;
+            for (int m = 1; m <= N - 1; ++m) {
+                if (chain_of[m] < species2_chain) continue;
+                for (int l = m + 1; l <= N; ++l)
+                    if (identity[m] > 8 && identity[l] > 8)
+                        if (hp[chain_of[m]][local_of[m]] == 1 && hp[chain_of[l]][local_of[l]] == 1)
+                            if (chain_of[l] != chain_of[m]) E(m, l) = 1;
+            }
         }
         for (int i = 1; i <= N - 1; ++i)       /* make_code.f:560-566 */
             for (int j = i + 1; j <= N; ++j) E(j, i) = E(i, j);

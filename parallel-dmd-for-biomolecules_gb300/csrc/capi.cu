@@ -188,7 +188,7 @@ void nbor_setup(HostSys &H, const dmd_tables *T, int hbonds) {
     std::map<std::vector<int>, std::set<int>> sig_chains;
     for (int b = 0; b < H.N; ++b) {
         const BeadInfo &I = H.info[b];
-        std::vector<int> k = {H.ident[b], I.hp, I.kind, I.pro_nh};
+        std::vector<int> k = {H.ident[b], I.hp, I.kind, I.pro_nh, I.sp2};
         auto &st = sig_chains[k];
         if (st.size() < 2) st.insert(I.chain);
     }
@@ -199,7 +199,9 @@ void nbor_setup(HostSys &H, const dmd_tables *T, int hbonds) {
             if (!meet) continue;
             BeadInfo A{}, Bq{};
             A.kind = (int8_t)p.first[2]; A.hp = (int8_t)p.first[1]; A.pro_nh = (int8_t)p.first[3];
+            A.sp2 = (int8_t)p.first[4];
             Bq.kind = (int8_t)q.first[2]; Bq.hp = (int8_t)q.first[1]; Bq.pro_nh = (int8_t)q.first[3];
+            Bq.sp2 = (int8_t)q.first[4];
             for (int order = 0; order < 2; ++order) {
                 A.chain = order; Bq.chain = 1 - order;
                 visit(static_code(Bq, A, hbonds), p.first[0], q.first[0]);
@@ -330,6 +332,13 @@ bool setup_host(HostSys &H, const dmd_run_cfg *cfg, const dmd_tables *T, const d
         rpos += L;
     }
     if (pos != H.N) return fail(err, "n_beads larger than the chains need");
+    /* -Dchaptype=2: chains from species2_chain on are species 2 */
+    if (cfg->chaptype != 0 && cfg->chaptype != 1 && cfg->chaptype != 2) return fail(err, "chaptype must be 1 or 2");
+    if (cfg->chaptype == 2) {
+        if (cfg->species2_chain < 0 || cfg->species2_chain > H.nchains)
+            return fail(err, "species2_chain outside 0..n_chains");
+        for (int b = 0; b < H.N; ++b) H.info[b].sp2 = (int8_t)(H.info[b].chain >= cfg->species2_chain);
+    }
     H.bm.assign(H.N, 0.0);
     for (int b = 0; b < H.N; ++b) H.bm[b] = bmass[H.ident[b]];
     H.blmin_sq.assign(H.N, 0.0);

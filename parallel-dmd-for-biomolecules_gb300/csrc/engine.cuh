@@ -35,6 +35,7 @@ struct BeadInfo {
     int8_t hp;         /* hydrophobic flag */
     int8_t pro_nh;     /* NH whose index equals a proline side chain minus 2L */
     int8_t is_end;     /* NH of residue 1 or CO of residue L */
+    int8_t sp2;        /* on a species-2 chain of a two-species run (chaptype 2) */
 };
 
 /* box-scaled tables (code/scale_down.f, code/make_code.f:15-60, code/nbor_setup.f) */
@@ -187,7 +188,9 @@ __host__ __device__ __forceinline__ int static_code(const BeadInfo &A, const Bea
             return dr >= 4 ? 15 : 1;
         return 1;
     }
-    if (A.kind == BK_R && B.kind == BK_R) return (A.hp == 1 && B.hp == 1) ? 16 : 1;
+    /* side chains of two chains; two species-2 chains meet as hard cores
+     * (code/make_code.f:515-541) */
+    if (A.kind == BK_R && B.kind == BK_R) return (A.hp == 1 && B.hp == 1 && !(A.sp2 && B.sp2)) ? 16 : 1;
     if (hbonds) {
         if (A.kind == BK_NH && B.kind == BK_CO) return (A.pro_nh && B.chain > A.chain) ? 1 : 15;
         if (A.kind == BK_CO && B.kind == BK_NH) return (B.pro_nh && A.chain > B.chain) ? 1 : 15;

@@ -50,6 +50,7 @@ class RunCfg(C.Structure):
         ("tstar", C.c_double), ("seed", C.c_uint64), ("canon", C.c_int32), ("hbonds", C.c_int32),
         ("numbin", C.c_int32), ("n_wrap", C.c_int32), ("rl_const", C.c_double), ("t_fact", C.c_double),
         ("n_forced", C.c_double), ("list_cap", C.c_int32), ("flags", C.c_int32),
+        ("chaptype", C.c_int32), ("species2_chain", C.c_int32),
     ]
 
 

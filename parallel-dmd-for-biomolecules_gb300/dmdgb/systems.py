@@ -57,6 +57,8 @@ class SystemSpec:
     hp: Optional[np.ndarray] = None
     t0: float = 0.0
     coll0: int = 0
+    chaptype: int = 1          # 2: two peptide species, chains species2_chain.. of the second
+    species2_chain: int = 0
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -69,7 +71,8 @@ class SystemSpec:
 
     def run_cfg(self, flags: int = 0, list_cap: int = 0) -> abi.RunCfg:
         return abi.RunCfg(float(self.tstar), int(self.seed), int(bool(self.canon)), int(bool(self.hbonds)),
-                          2000, 2, 1.2, 5e-5, 150.0, int(list_cap), int(flags))
+                          2000, 2, 1.2, 5e-5, 150.0, int(list_cap), int(flags), int(self.chaptype),
+                          int(self.species2_chain))
 
     def c_system(self) -> abi.System:
         """C view of this system; the arrays stay referenced by the spec."""

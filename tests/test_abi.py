@@ -32,7 +32,7 @@ def test_errors_are_status_codes(built):
     """Bad input returns a negative status and a message; nothing exits."""
     lib = abi.load_engine()
     h = C.c_void_p()
-    cfg = abi.RunCfg(0.2, 1, 1, 1, 2000, 2, 1.2, 5e-5, 150.0, 0, 0)
+    cfg = abi.RunCfg(0.2, 1, 1, 1, 2000, 2, 1.2, 5e-5, 150.0, 0, 0, 1, 0)
     t = abi.Tables()
     s = abi.System()  # empty system
     rc = lib.dmd_create(C.byref(cfg), C.byref(t), C.byref(s), C.byref(h))
@@ -56,6 +56,13 @@ def test_system_struct_matches_header_layout():
     # sizeof and offsetof of struct dmd_system as gcc lays out include/dmd.h
     assert C.sizeof(abi.System) == 112
     assert (abi.System.boxl.offset, abi.System.x.offset, abi.System.t0.offset, abi.System.coll0.offset) == (32, 40, 96, 104)
+
+
+def test_run_cfg_struct_matches_header_layout():
+    """abi.RunCfg mirrors struct dmd_run_cfg (gcc layout of include/dmd.h)."""
+    assert C.sizeof(abi.RunCfg) == 72
+    assert (abi.RunCfg.rl_const.offset, abi.RunCfg.list_cap.offset, abi.RunCfg.flags.offset,
+            abi.RunCfg.chaptype.offset, abi.RunCfg.species2_chain.offset) == (32, 56, 60, 64, 68)
 
 
 def test_bead_count_rule():

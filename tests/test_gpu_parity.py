@@ -388,3 +388,21 @@ def test_c3_largest_replica_batched(built):
         assert k < 0, f"replica of {s.n_beads} beads diverges at {k}:\n{describe(logs[r], olog, k)}"
         _compare_states(b.state(r), ora.state(), f"{s.n_beads} beads")
     b.close()
+
+
+def test_two_species_event_sequence(built):
+    """-Dchaptype=2 (code/make_code.f:489-548): two peptide species whose
+    species-2 side chains meet as hard cores across chains; the events of a
+    crowded mixed system against the oracle with the same rule."""
+    spec = dense_system(n_chains=8, L=10, box=42.0, tstar=0.2, seed=31, rng_seed=9)
+    spec.chaptype = 2
+    spec.species2_chain = 4
+    n = 40000
+    with Engine(spec) as eng:
+        glog = eng.run(n, log_capacity=n + 64)
+        gst = eng.state()
+    ora = Oracle(spec)
+    olog = ora.run(n, log_capacity=n + 64)
+    k = first_mismatch(glog, olog)
+    assert k < 0, f"two-species run diverges at {k}:\n{describe(glog, olog, k)}"
+    _compare_states(gst, ora.state(), "two species")

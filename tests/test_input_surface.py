@@ -36,13 +36,45 @@ def test_shipped_table_values():
     assert t.rca[0] == 0.654 and t.rco[19] == 2.959 and t.sqz[0][0] == 4.064
 
 
+def test_shipped_tables_against_values_typed_from_the_files():
+    """Entries typed by hand from the reference's parameter files (row and
+    column as the files state them), so that the parse is checked against
+    values it did not produce: parameters/beadwell_ha55a.data (pair
+    diameter, well diameter), parametersep/ep19p_ha55a_weakhp.data (raw
+    value), parameters/rcarnrco.data (CA-R, NH-R, CO-R and the three
+    window fractions), parameters/sqz6to10.data (sz8, sz6, sz7, sz9, sz10)
+    and parameters/mass.data."""
+    t = params.default_tables()
+    i = lambda ident: ident - 9        # residue identity 9..28 -> row 0..19
+    # beadwell: "G  9  G  9   3.100   3.100", "G  9  R 10   3.200   3.200",
+    # "S 18  V 28   2.800   6.158", "V 28  Y 27   3.000   6.521", "V 28  V 28   3.300   6.306"
+    for a, b, bd, wl in ((9, 9, 3.1, 3.1), (9, 10, 3.2, 3.2), (18, 28, 2.8, 6.158), (28, 27, 3.0, 6.521),
+                         (28, 28, 3.3, 6.306)):
+        assert (t.bds[i(a), i(b)], t.wel[i(a), i(b)]) == (bd, wl), (a, b)
+    # ep19p_ha55a_weakhp: "G  9  G  9     0.000", "T 19  L 23     0.015", "T 19  M 24    -0.116"
+    assert t.ep[i(9), i(9)] == 0.0 and t.ep[i(19), i(23)] == 0.015 and t.ep[i(19), i(24)] == -0.116
+    # rcarnrco: G " 0.654   1.908   1.967   0.023   0.023   0.023", R " 4.700   5.100   5.900 ...",
+    # V " 2.002   2.775   2.959 ..."
+    assert (t.rca[0], t.rnh[0], t.rco[0]) == (0.654, 1.908, 1.967)
+    assert (t.rca[1], t.rnh[1], t.rco[1]) == (4.7, 5.1, 5.9)
+    assert (t.rca[19], t.rnh[19], t.rco[19]) == (2.002, 2.775, 2.959)
+    assert t.del_rca[0] == t.del_rnh[0] == t.del_rco[19] == 0.023
+    # sqz6to10: G " 4.064   2.600   2.601   4.013   4.904", R " 5.703   4.827 ...", L (row 15)
+    assert list(t.sqz[0]) == [4.064, 2.6, 2.601, 4.013, 4.904]
+    assert list(t.sqz[1]) == [5.703, 4.827, 4.651, 5.535, 4.978]
+    assert list(t.sqz[i(23)]) == [4.936, 3.918, 3.724, 4.863, 5.001]
+    # mass.data: "CA   2     0.866", "NH   1     0.999", "CO   4     1.863", " G   9     0.067", " R  10     6.728"
+    assert (t.mass[2], t.mass[1], t.mass[4], t.mass[9], t.mass[10]) == (0.866, 0.999, 1.863, 0.067, 6.728)
+
+
 @pytest.mark.skipif(not has_reference(), reason="reference checkout not mounted")
 def test_parse_reference_tables():
+    """The parser on the reference files (when mounted) gives the shipped tables."""
     t = params.read_tables(os.path.join(REFERENCE, "parameters"),
                            os.path.join(REFERENCE, "parametersep", "ep19p_ha55a_weakhp.data"))
-    want = json.load(open(os.path.join(GOLD, "tables_digest.json")))
-    for k, h in want.items():
-        assert _digest(getattr(t, k)) == h, k
+    shipped = params.default_tables()
+    for k in shipped.__dict__:
+        assert np.array_equal(getattr(t, k), getattr(shipped, k)), k
 
 
 @pytest.mark.skipif(not has_reference(), reason="reference checkout not mounted")

@@ -87,3 +87,59 @@ def test_setup_values_match(maker):
     o = Oracle(spec).scalars()
     for k in ("interval", "interval_max", "sig_max_all", "hdelr", "rlsq1", "rlsq15", "rlsq16", "rlsq40", "evp1_15"):
         assert e[k] == o[k], k
+
+
+def _two_species(seed, split=3):
+    """A mixed system run with -Dchaptype=2: chains split.. are species 2."""
+    spec = _mixed(seed, n_chains=6, lens=(8, 10, 12))
+    spec.chaptype = 2
+    spec.species2_chain = split
+    return spec
+
+
+def _chain_of_beads(spec):
+    out, p = [], 0
+    for c, L in enumerate(spec.chain_len):
+        res = spec.residues[p:p + L]
+        out += [c] * (3 * L + sum(1 for r in res if r != 9))
+        p += L
+    return np.asarray(out)
+
+
+@pytest.mark.parametrize("seed,split", [(11, 3), (12, 0), (13, 6)])
+def test_rule_two_species_equals_literal_make_code(seed, split):
+    """code/make_code.f:489-548: side chains of two different species-2
+    chains meet as hard cores; species 1 and mixed pairs keep the well."""
+    import dataclasses
+    spec = _two_species(seed, split)
+    ev = _engine_static(spec)
+    assert np.array_equal(ev, Oracle(spec).evcode())
+    ev1 = _engine_static(dataclasses.replace(spec, chaptype=1))
+    chain = _chain_of_beads(spec)
+    diff = np.argwhere(ev != ev1)
+    for a, b in diff:                        # every change: 16 -> 1 between two species-2 chains
+        assert (ev1[a, b], ev[a, b]) == (16, 1)
+        assert chain[a] != chain[b] and chain[a] >= split and chain[b] >= split
+    if split <= 4:
+        assert len(diff) > 0
+
+
+def test_setup_values_two_species():
+    spec = _two_species(14, 2)
+    e = _engine_inspect(spec)
+    o = Oracle(spec).scalars()
+    for k in ("interval", "interval_max", "sig_max_all", "hdelr", "rlsq1", "rlsq15", "rlsq16", "rlsq40", "evp1_15"):
+        assert e[k] == o[k], k
+
+
+def test_chaptype_is_checked():
+    spec = _two_species(15, 2)
+    spec.species2_chain = 99
+    lib = abi.load_engine()
+    t = abi.tables_struct(default_tables())
+    cfg = spec.run_cfg()
+    s = spec.c_system()
+    out = np.zeros((spec.n_beads, spec.n_beads), np.int8)
+    err = C.create_string_buffer(256)
+    assert lib.dmd_static_evcode(C.byref(cfg), C.byref(t), C.byref(s), out.ctypes.data_as(abi.i8_p), err, 256) == -1
+    assert b"species2_chain" in err.value
