@@ -107,6 +107,16 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
     if (nctas > DMD_PHASE_CTAS) nctas = DMD_PHASE_CTAS;
     return (int)cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(long long) * DMD_PHASE_SLOTS * nctas);
 }
+/* sub-phases of a light batch on warp 0 of CTA g_sub_cta (row DMD_PHASE_CTAS - 5) */
+__device__ long long g_lsub_last;
+#define DMD_LSUB(k)                                                                        \
+    do {                                                                                   \
+        if (blockIdx.x == g_sub_cta && threadIdx.x == 0) {                                 \
+            long long now_ = clock64();                                                    \
+            if ((k) >= 0) g_phase_cycles[DMD_PHASE_CTAS - 5][(k)] += now_ - g_lsub_last;   \
+            g_lsub_last = now_;                                                            \
+        }                                                                                  \
+    } while (0)
 /* sub-phases of the candidate gather, per CTA (rows 512 + block index) */
 #define DMD_GSUB_START() long long gs_t_ = clock64()
 #define DMD_GSUB(k)                                                                        \
@@ -119,6 +129,7 @@ extern "C" int dmd_debug_phase_cycles(long long *out, int nctas) {
     } while (0)
 #else
 #define DMD_GSUB_START() do { } while (0)
+#define DMD_LSUB(k) do { } while (0)
 #define DMD_GSUB(k) do { } while (0)
 #define DMD_PHASE_START(row) do { (void)(row); } while (0)
 #define DMD_PHASE(k) do { (void)(k); } while (0)

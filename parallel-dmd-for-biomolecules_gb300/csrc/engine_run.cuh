@@ -482,22 +482,25 @@ __device__ int lane_ghost(const DSys &S, SharedState &sh, double &tfalse) {
  * on its lane 0. */
 __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, int j, double tf, int hbonds) {
     const int lane = threadIdx.x & 31, hl = lane & 15;
+    const unsigned hbase = lane & 16;          /* first lane of this half */
     const DTab &T = *S.tab;
+    /* every load that needs only i and j, issued together: lanes 0..11 of
+     * the half hold the positions and velocities of i (0..5) and j (6..11),
+     * which are also the snapshot of what the collision writes */
+    const int fb = hl < 6 ? i : j, ff = hl % 6;
+    const double *A = ff == 0 ? S.x : ff == 1 ? S.y : ff == 2 ? S.z : ff == 3 ? S.vx : ff == 4 ? S.vy : S.vz;
+    const double mine = hl < 12 ? A[fb] : 0.0;
     const int ct = S.colt[i];
+    const int a = S.ident[i], b = S.ident[j];
     const int evcode = pair_code(S, i, j, hbonds);
-    /* snapshot of what the collision writes */
-    if (has && hl < 12) {
-        const int b = hl < 6 ? i : j, f = hl % 6;
-        const double *A = f == 0 ? S.x : f == 1 ? S.y : f == 2 ? S.z : f == 3 ? S.vx : f == 4 ? S.vy : S.vz;
-        W.sij[hl] = A[b];
-    }
+    if (has && hl < 12) W.sij[hl] = mine;
     if (has && hl == 0) { W.nmeta = 0; W.colt_i = (int8_t)ct; }
     /* relative position and velocity (warp_rel), lanes 0..2 of the half */
     const int d = hl % 3;
-    const double *P = d == 0 ? S.x : (d == 1 ? S.y : S.z);
-    const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
-    const double v = V[i] - V[j];
-    double r = P[i] - P[j] + v * tf;
+    const double xi = __shfl_sync(FULL, mine, hbase + d), vi = __shfl_sync(FULL, mine, hbase + 3 + d);
+    const double xj = __shfl_sync(FULL, mine, hbase + 6 + d), vj = __shfl_sync(FULL, mine, hbase + 9 + d);
+    const double v = vi - vj;
+    double r = xi - xj + v * tf;
     r = d_wrap(r);
     const double pb = r * v, pr = r * r, pv = v * v;
     const double rx = __shfl_sync(FULL, r, 0, 16), ry = __shfl_sync(FULL, r, 1, 16), rz = __shfl_sync(FULL, r, 2, 16);
@@ -512,7 +515,6 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
     /* the impulse ratio (warp_eventdyn, coltypes 1-3) on lane 0 of the half */
     double ratio = 0.0;
     if (hl == 0) {
-        const int a = S.ident[i], b = S.ident[j];
         const double rmass = T.rmass[a][b];
         const bool side = evcode >= 10 && evcode <= 12;
         if (ct == 2) {
@@ -537,22 +539,26 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
         }
     }
     ratio = __shfl_sync(FULL, ratio, 0, 16);
-    /* the impulse (warp_impulse without a bump), lanes 0..5 of the half */
+    /* the impulse (warp_impulse without a bump), lanes 0..5 of the half;
+     * the position and velocity are the values held above (lanes 0..5:
+     * position of component dd, lanes 3..5 of i hold velocities, so the
+     * component's position of b comes from lane (isj ? 6 : 0) + dd and its
+     * velocity from lane (isj ? 9 : 3) + dd) */
+    const int dd = hl % 3;
+    const bool isj = hl >= 3;
+    const double pcur = __shfl_sync(FULL, mine, hbase + (isj ? 6 : 0) + dd);
+    const double vcur = __shfl_sync(FULL, mine, hbase + (isj ? 9 : 3) + dd);
     if (has && hl < 6) {
-        const int dd = hl % 3;
-        const bool isj = hl >= 3;
-        const int b = isj ? j : i;
+        const int bb = isj ? j : i;
         double *PP = dd == 0 ? S.x : (dd == 1 ? S.y : S.z);
         double *VV = dd == 0 ? S.vx : (dd == 1 ? S.vy : S.vz);
         const double rr = dd == 0 ? rx : (dd == 1 ? ry : rz);
-        double p = PP[b];
-        const double bmb = S.bm[b], rbmb = T.rbm[S.ident[b]];   /* bm(b) = mass(identity(b)) */
+        const double bmb = S.bm[bb], rbmb = T.rbm[isj ? b : a];   /* bm(b) = mass(identity(b)) */
         const double delv = ratio * rr;
         const double dv = div_by(delv, bmb, rbmb);
         const double dp = div_by(delv * tf, bmb, rbmb);
-        VV[b] = isj ? VV[b] + dv : VV[b] - dv;
-        p = isj ? p - dp : p + dp;
-        PP[b] = p;
+        VV[bb] = isj ? vcur + dv : vcur - dv;
+        PP[bb] = isj ? pcur - dp : pcur + dp;
     }
     if (has && hl == 0) {
         S.colt[i] = (int8_t)ct;
@@ -928,14 +934,23 @@ __device__ __forceinline__ bool rp_predict(const DSys &S, Err E, int pa, int pbb
  * must fit one round and the pool), else W.pooled = 0 and the owner warp
  * runs warp_repredict() after the pool */
 __device__ void warp_rp_prepare(const DSys &S, WarpArea &W, TaskPool &TP, int owner, int i, int j, double tf,
-                                double imax) {
+                                double imax, bool timed = false) {
     int lane = threadIdx.x & 31;
+#ifdef DMD_PHASE_TIMERS
+    long long pt0 = clock64();
+#endif
     warp_rp_lists(S, W, i, j);
+#ifdef DMD_PHASE_TIMERS
+    if (timed && lane == 0) { long long t = clock64(); g_phase_cycles[DMD_PHASE_CTAS - 6][0] += t - pt0; pt0 = t; }
+#endif
     bool pooled = W.nmarked <= TG_MAX - 2;
     int base = 0;
     if (pooled) {
         const double Hraw = imax + DMD_LTSTEP - tf;
         warp_rp_targets(S, W, i, j, 0, Hraw, okey(Hraw));
+#ifdef DMD_PHASE_TIMERS
+        if (timed && lane == 0) { long long t = clock64(); g_phase_cycles[DMD_PHASE_CTAS - 6][1] += t - pt0; pt0 = t; }
+#endif
         int nt = W.ntask, nop = W.nops;
         if (lane == 0) base = atomicAdd(&TP.n, nt);
         base = __shfl_sync(FULL, base, 0);
@@ -946,6 +961,16 @@ __device__ void warp_rp_prepare(const DSys &S, WarpArea &W, TaskPool &TP, int ow
             TP.a[base + q] = pa; TP.b[base + q] = pbb; TP.st[base + q] = (int8_t)st;
             TP.flag[base + q] = (int8_t)((q < nop ? 1 : 0) | (owner << 1));
         }
+#ifdef DMD_PHASE_TIMERS
+        if (timed && lane == 0) {
+            long long t = clock64();
+            g_phase_cycles[DMD_PHASE_CTAS - 6][2] += t - pt0;
+            g_phase_cycles[DMD_PHASE_CTAS - 6][3] += 1;
+            g_phase_cycles[DMD_PHASE_CTAS - 6][4] += nt;
+            g_phase_cycles[DMD_PHASE_CTAS - 6][5] += W.nops;
+            g_phase_cycles[DMD_PHASE_CTAS - 6][6] += W.nmarked;
+        }
+#endif
     }
     if (lane == 0) { W.pooled = pooled; W.pool_base = base; W.big_tf = DMD_BIG + tf; }
     __syncwarp();
@@ -1564,6 +1589,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
             const int nloc = P > rank ? (P - rank + C - 1) / C : 0;
             const int nfree = RUN_NW - nloc;
             const bool split = nfree > 0 && 2 * nfree >= nloc;
+            if (light) DMD_LSUB(-1);
             if (light) {
                 /* light batch (one CTA): two events per collision warp, one
                  * on each half; the other warps prepare the events' tasks
@@ -1581,10 +1607,16 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                         WE.i = i; WE.j = j; WE.tf = tf; WE.coll = coll0 + k + 1; WE.err = 0; WE.err_info = 0;
                     }
                     hw_collision_light(S, WE, has, i, j, tf, hbonds);
+                    DMD_LSUB(1);
                 } else {
                     for (int k = warp - ncw; k < P; k += RUN_NW - ncw) {
                         const int i = sh.sort_idx[k];
-                        warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax);
+#ifdef DMD_PHASE_TIMERS
+                        const bool timed = blockIdx.x == g_sub_cta && warp == ncw;
+#else
+                        const bool timed = false;
+#endif
+                        warp_rp_prepare(S, warea[k], TP, k, i, S.nptnr[i], S.tim[i], imax, timed);
                     }
                 }
             } else if (gw < P) {
@@ -1617,6 +1649,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                 }
             }
             __syncthreads();
+            if (light) DMD_LSUB(2);
             /* every pooled prediction task of this CTA's events, all warps:
              * first the pair codes, settling in single precision the tasks
              * that certainly have no event; then the double-precision
@@ -1661,6 +1694,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                 }
                 __syncthreads();
                 DMD_PHASE(13);
+                if (light) DMD_LSUB(3);
                 const int nlive = TP.nlive;
                 for (int k = threadIdx.x; k < nlive; k += blockDim.x) {
                     const int q = TP.live[k];
@@ -1677,6 +1711,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
             }
             __syncthreads();
             DMD_PHASE(14);
+            if (light) DMD_LSUB(4);
             if (gw < P) {
                 const int i = W.i, j = W.j;
                 const double tf = W.tf;
@@ -1689,21 +1724,48 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                         W.op_t[q] = TP.t[base + q];
                         W.op_y[q] = TP.ok[base + q] ? TP.ty[base + q] : (int8_t)-128;
                     }
-                    for (int t = lane; t < ntg; t += 32) {
-                        long long bk = W.fs.tg_k[t];
-                        int bp = W.fs.tg_p[t];
-                        double braw = W.fs.tg_raw[t];
-                        int by = W.fs.tg_y[t];
-#pragma unroll 4
-                        for (int x = base + nop + W.fs.tg_base[t]; x < base + nop + W.fs.tg_base[t + 1]; ++x) {
-                            if (!TP.ok[x]) continue;
-                            long long k = okey(TP.t[x]);
-                            if (key_less(k, TP.b[x], bk, bp)) { bk = k; bp = TP.b[x]; braw = TP.t[x]; by = TP.ty[x]; }
+                    /* the full tasks, 32 at a time: a segmented (key, partner)
+                     * minimum over each target's run of tasks by shuffles, the
+                     * run's head lane merging it into the target's minimum */
+                    const int f0 = base + nop, nf = W.fs.tg_base[ntg];
+                    for (int c = 0; c < nf; c += 32) {
+                        const int x = c + lane;
+                        int tgt = -1;
+                        long long k = DMD_KEY_INF;
+                        int p = INT_MAX, y = 0;
+                        double rt = 0.0;
+                        if (x < nf) {
+                            if (nf <= TMAP_MAX) tgt = W.fs.tmap[x];
+                            else {
+                                int lo = 0, hi = ntg - 1;   /* last target with tg_base <= x */
+                                while (lo < hi) {
+                                    const int mid = (lo + hi + 1) >> 1;
+                                    if (W.fs.tg_base[mid] <= x) lo = mid; else hi = mid - 1;
+                                }
+                                tgt = lo;
+                            }
+                            if (TP.ok[f0 + x]) { rt = TP.t[f0 + x]; k = okey(rt); p = TP.b[f0 + x]; y = TP.ty[f0 + x]; }
                         }
-                        W.fs.tg_k[t] = bk; W.fs.tg_p[t] = bp; W.fs.tg_raw[t] = braw; W.fs.tg_y[t] = (int8_t)by;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const long long k2 = __shfl_down_sync(FULL, k, o);
+                            const int p2 = __shfl_down_sync(FULL, p, o);
+                            const double r2 = __shfl_down_sync(FULL, rt, o);
+                            const int y2 = __shfl_down_sync(FULL, y, o);
+                            const int g2 = __shfl_down_sync(FULL, tgt, o);
+                            if (lane + o < 32 && g2 == tgt && key_less(k2, p2, k, p)) { k = k2; p = p2; rt = r2; y = y2; }
+                        }
+                        const int gprev = __shfl_up_sync(FULL, tgt, 1);
+                        const bool head = tgt >= 0 && (lane == 0 || gprev != tgt);
+                        if (head && key_less(k, p, W.fs.tg_k[tgt], W.fs.tg_p[tgt])) {
+                            W.fs.tg_k[tgt] = k; W.fs.tg_p[tgt] = p; W.fs.tg_raw[tgt] = rt; W.fs.tg_y[tgt] = (int8_t)y;
+                        }
+                        __syncwarp();
                     }
                     __syncwarp();
+                    if (light) DMD_LSUB(5);
                     warp_rp_finish(S, E, W, i, j, 0, tf, imax);
+                    if (light) DMD_LSUB(6);
                     if (!light) warp_rp_tnew(W);   /* light: after the marks below */
                 } else {
                     warp_repredict(S, E, W, i, j, tf, imax, hbonds, Ver{light ? own + N : nullptr, warea, tseq, warp, P});
@@ -1726,15 +1788,18 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                     L->c_err[gw] = W.err; L->c_err_info[gw] = W.err_info;
                     L->c_ct[gw] = W.ct; L->c_tf[gw] = W.tf;
                 }
+                if (light) DMD_LSUB(7);
             }
             if (threadIdx.x == 0) { TP.n = 0; TP.nlive = 0; }   /* the pool is free until the next batch */
             csync(C);
+            if (light) DMD_LSUB(8);
             if (light) {
                 if (gw < P) {
                     const bool bad = warp_check_queue(W, own + 2 * N, my_ticket);
                     if (lane == 0) L->c_qbad[gw] = bad;
                 }
                 csync(C);
+                DMD_LSUB(9);
             }
             DMD_PHASE(3);
             /* validation: event k stands if it precedes every new entry of
@@ -1763,7 +1828,10 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                     cand = lane + 1;   /* the run stops after the first event in error */
                 Vw = __reduce_min_sync(FULL, cand);
             }
-            if (leader && threadIdx.x == 0) {
+            /* the booking thread: lane 0 of a warp without an event when there
+             * is one (so that no event's commit waits for it), else thread 0 */
+            const int book_thread = (vwarp && P < RUN_NW) ? 32 * (RUN_NW - 1) : 0;
+            if (leader && threadIdx.x == book_thread) {
                 int v = P;
                 if (vwarp) {
                     v = Vw;
@@ -1804,6 +1872,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                 __syncthreads();
             }
             DMD_PHASE(4);
+            if (light) DMD_LSUB(10);
             const int V = vwarp ? Vw : sh.V;
             if (light) {
                 /* a rolled-back event restores its bead i's coltype, which a
@@ -1823,7 +1892,12 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                 }
             }
             csync(C);   /* every commit lands before any level-1 group is recomputed */
+            if (light) DMD_LSUB(11);
             if (gw < V) warp_l1_refresh(S, W.pb, W.npred);
+            if (light) DMD_LSUB(12);
+#ifdef DMD_PHASE_TIMERS
+            if (light && blockIdx.x == g_sub_cta && threadIdx.x == 0) g_phase_cycles[DMD_PHASE_CTAS - 5][15] += 1;
+#endif
         } else if (e == N) {
             ph_kind = 6;
             /* ---- ghost collision: leader warp 0 ---- */
