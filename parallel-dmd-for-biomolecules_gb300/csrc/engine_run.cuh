@@ -688,39 +688,53 @@ __device__ __forceinline__ bool check_tij(Err E, double tij, int i) {
  * beads among them (leaders) with their first operation and mark */
 __device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
     int lane = threadIdx.x & 31;
-    /* 1. the down-list operations in the reference's order */
+    /* 1. the down-list operations in the reference's order: i's down list,
+     * i's lower extras, j's down list without i, j's lower extras.  Every
+     * load that needs only i and j is issued first (list lengths, extras),
+     * then both lists together, 32 entries of each per pass. */
     int n = 0;
     {
-        int cnt = S.dnn[i];
+        const int cnt = S.dnn[i];
+        const int cj = j >= 0 ? S.dnn[j] : 0;
+        const int eri = lane < 3 ? S.er[4 * i + lane] : -1;
+        const int erj = (j >= 0 && lane < 3) ? S.er[4 * j + lane] : -1;
         const int *dn = S.dn + (size_t)i * S.cap;
         const int8_t *dc = S.dnc ? S.dnc + (size_t)i * S.cap : nullptr;
-        for (int q = lane; q < cnt; q += 32) { W.ops_l[q] = dn[q]; W.ops_s[q] = i; W.ops_c[q] = dc ? dc[q] : (int8_t)-1; }
-        n = cnt;
-        if (lane == 0)
-            for (int k = 0; k < 3; ++k) {
-                int l = S.er[4 * i + k];
-                if (l >= 0 && l < i) { W.ops_l[n] = l; W.ops_s[n] = i; W.ops_c[n] = -1; ++n; }
-            }
-        n = __shfl_sync(FULL, n, 0);
+        const int *dj = j >= 0 ? S.dn + (size_t)j * S.cap : nullptr;
+        const int8_t *dcj = (j >= 0 && S.dnc) ? S.dnc + (size_t)j * S.cap : nullptr;
+        const int passes = (max(cnt, cj) + 31) >> 5;
+        /* i's list goes to ops[0, cnt); j's kept entries are counted per pass
+         * and placed after i's extras once their number is known */
+        int nj = 0;
+        const bool ei_keep = lane < 3 && eri >= 0 && eri < i;
+        const unsigned mei = __ballot_sync(FULL, ei_keep);
+        const int base_j = cnt + __popc(mei);
+        for (int ps = 0; ps < passes; ++ps) {
+            const int q = 32 * ps + lane;
+            const int li = q < cnt ? dn[q] : -1;
+            const int8_t ci = (q < cnt && dc) ? dc[q] : (int8_t)-1;
+            const int lj = q < cj ? dj[q] : -1;
+            const int8_t cjv = (q < cj && dcj) ? dcj[q] : (int8_t)-1;
+            if (q < cnt) { W.ops_l[q] = li; W.ops_s[q] = i; W.ops_c[q] = ci; }
+            const bool keep = q < cj && lj != i;
+            const unsigned m = __ballot_sync(FULL, keep);
+            const int pos = base_j + nj + __popc(m & ((1u << lane) - 1));
+            if (keep) { W.ops_l[pos] = lj; W.ops_s[pos] = j; W.ops_c[pos] = cjv; }
+            nj += __popc(m);
+        }
+        if (ei_keep) {
+            const int pos = cnt + __popc(mei & ((1u << lane) - 1));
+            W.ops_l[pos] = eri; W.ops_s[pos] = i; W.ops_c[pos] = -1;
+        }
+        n = base_j + nj;
         if (j >= 0) {
-            int cj = S.dnn[j];
-            const int *dj = S.dn + (size_t)j * S.cap;
-            const int8_t *dcj = S.dnc ? S.dnc + (size_t)j * S.cap : nullptr;
-            for (int base = 0; base < cj; base += 32) {
-                int q = base + lane;
-                int l = q < cj ? dj[q] : -1;
-                bool keep = q < cj && l != i;
-                unsigned m = __ballot_sync(FULL, keep);
-                int pos = n + __popc(m & ((1u << lane) - 1));
-                if (keep) { W.ops_l[pos] = l; W.ops_s[pos] = j; W.ops_c[pos] = dcj ? dcj[q] : (int8_t)-1; }
-                n += __popc(m);
+            const bool ej_keep = lane < 3 && erj >= 0 && erj < j;
+            const unsigned mej = __ballot_sync(FULL, ej_keep);
+            if (ej_keep) {
+                const int pos = n + __popc(mej & ((1u << lane) - 1));
+                W.ops_l[pos] = erj; W.ops_s[pos] = j; W.ops_c[pos] = -1;
             }
-            if (lane == 0)
-                for (int k = 0; k < 3; ++k) {
-                    int l = S.er[4 * j + k];
-                    if (l >= 0 && l < j) { W.ops_l[n] = l; W.ops_s[n] = j; W.ops_c[n] = -1; ++n; }
-                }
-            n = __shfl_sync(FULL, n, 0);
+            n += __popc(mej);
         }
     }
     __syncwarp();
