@@ -493,6 +493,13 @@ __device__ __forceinline__ bool d_predict_c(const DSys &S, int i, int j, int evc
         double den = bond ? s1 : r.vijsq;
         tij = num / den;
         type = y;
+        /* A bonded H-bond pair that rounding left just outside its well
+         * takes the square root of a negative discriminant (the reference's
+         * nc_sqwel.f:69-93 does not test it): a NaN time, which no
+         * comparison of the reference ever selects and its negative-time
+         * check never flags.  Its integer key would depend on the NaN's sign
+         * bit, so it becomes "no event", which is selected just as rarely. */
+        if ((dbits(tij) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) { tij = DMD_BIG; type = 0; }
     }
     return valid;
 }

@@ -193,7 +193,11 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
                 const int sl = core_slot(evcode);
                 ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
             } else {
-                ratio = rmass * bij / T.core_sq[core_slot(evcode)][a][b];
+                /* the other codes with a core (16: inside a hydrophobic well;
+                 * 40/50: under a shoulder): eventdyn.f's sigma_sq *
+                 * ev_param(1,code)**2 with ev_param(1,code) = 1, which is
+                 * sigma_sq */
+                ratio = div_by(rmass * bij, T.sigma_sq[a][b], T.rsigma_sq[a][b]);
             }
         } else if (ct == 4) {
             double wellsq = T.welldia_sq[a][b], epsave = T.ep_sqrt[a][b];
@@ -534,7 +538,11 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
                 const int sl = core_slot(evcode);
                 ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
             } else {
-                ratio = rmass * bij / T.core_sq[core_slot(evcode)][a][b];
+                /* the other codes with a core (16: inside a hydrophobic well;
+                 * 40/50: under a shoulder): eventdyn.f's sigma_sq *
+                 * ev_param(1,code)**2 with ev_param(1,code) = 1, which is
+                 * sigma_sq */
+                ratio = div_by(rmass * bij, T.sigma_sq[a][b], T.rsigma_sq[a][b]);
             }
         }
     }

@@ -406,3 +406,21 @@ def test_two_species_event_sequence(built):
     k = first_mismatch(glog, olog)
     assert k < 0, f"two-species run diverges at {k}:\n{describe(glog, olog, k)}"
     _compare_states(gst, ora.state(), "two species")
+
+
+def test_c3_replica_long_run(built):
+    """Replica 29 of the 32-replica workload (1,260 beads, T* = 0.48) over
+    2.2 million events, chunk by chunk against the oracle: past 1.75 million
+    events a bonded H-bond pair sits just outside its well, where the
+    reference's root is a NaN that nothing selects (nc_sqwel.f:69-93)."""
+    s = systems.generate(systems.config_c3(32, seed=1)[29])
+    b = Batch([s])
+    ora = Oracle(s)
+    chunk = 200000
+    for c in range(11):
+        glog = b.run(chunk, log_capacity=chunk + 64)[0]
+        olog = ora.run(chunk, log_capacity=chunk + 64)
+        k = first_mismatch(glog, olog)
+        assert k < 0, f"chunk {c}: logs diverge at {k}:\n{describe(glog, olog, k)}"
+    _compare_states(b.state(0), ora.state(), "replica 29 after 2.2e6 events")
+    b.close()

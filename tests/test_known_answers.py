@@ -18,8 +18,9 @@ its constants (code/def.h, code/scale_down.f:32-35, code/make_code.f).
 
 The CPU test pins the oracle (the CPU restatement used as the checker) to
 these answers; the GPU test runs the same cases through the engine's own
-device predictor and impulse (tests/gpu_src/known_answers.cu) and requires
-the closed forms and bit equality with the oracle."""
+device predictor and impulse (tests/gpu_src/known_answers.cu), and the
+core and bond cases also through the light batches' half-warp collision,
+and requires the closed forms and bit equality with the oracle."""
 import ctypes as C
 import os
 import shutil
@@ -191,10 +192,24 @@ def _cases(boxl, masses):
                 add("step off the shoulder", r, v, None, None, ct_in=5, dke=eps)
                 r, v = wall(Rw, 0.9, -1.0)
                 add("shoulder closed (a hard wall)", r, v, None, None, ct_in=13, dke=0.0)
+                r, v = wall(Rc, 0.9, -1.0)
+                add("core under the shoulder", r, v, None, None, ct_in=1, dke=0.0)
+            elif kind == "hbwell":
+                r, v = wall(Rc, 0.9, -1.0)
+                add("core inside the well", r, v, None, None, ct_in=1, dke=0.0)
         elif kind == "hbbond":
             mid = 0.5 * (Rc + Rw)
             r, v, t = approach(mid, Rc, 0.6)
             add("core", r, v, 1, t)
+            # rounding can leave a bonded pair just outside its well; moving
+            # mostly sideways, its discriminant is negative and the
+            # reference's root (nc_sqwel.f:69-93) is a NaN that nothing
+            # selects: no event
+            n = _unit(rng)
+            tvec = _unit(rng)
+            tvec = tvec - tvec.dot(n) * n
+            tvec /= np.linalg.norm(tvec)
+            add("just outside, moving sideways", 1.02 * Rw * n, 0.1 * n + 1.0 * tvec, 0, None)
             r, v, t = leave(mid, Rw, 0.6)
             add("exit", r, v, 8, t)
             r, v = wall(Rw, HIGH_E, 1.0)
@@ -217,9 +232,12 @@ def _check_case(case, tij, ty, valid, st_out, ct_out, masses):
     name, i, j, ida, idb, ev, bonded, Rc, Rw, eps, kind = row
     assert valid, label
     if ct_in == 0:
+        if np.isnan(tij):                     # the reference's NaN root: never selected, no event
+            assert ty_exp == 0 and t_exp is None, label
+            return
         assert ty == ty_exp, f"{label}: type {ty}, expected {ty_exp}"
         if t_exp is None:
-            assert tij == 1e9, f"{label}: time {tij} for no event"
+            assert tij == 1e9 or np.isnan(tij), f"{label}: time {tij} for no event"
         else:
             assert tij == pytest.approx(t_exp, rel=1e-12), label
         return
@@ -314,17 +332,22 @@ def test_device_known_answers(built):
     ct = np.ascontiguousarray([c[3] or 0 for c in cases], np.int32)
     tij, ty, valid, cto = np.zeros(n), np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
     out = np.zeros(12 * n)
+    light = np.zeros(12 * n)
     t = abi.tables_struct(default_tables())
     cfg = spec.run_cfg()
     sys_ = spec.c_system()
     err = C.create_string_buffer(256)
     rc = L.ka_pair_cases(C.byref(cfg), C.byref(t), C.byref(sys_), n, *[a.ctypes.data for a in (i, j, ida, idb, ev, bond)],
                          st.ctypes.data, ct.ctypes.data, tij.ctypes.data, ty.ctypes.data, valid.ctypes.data,
-                         out.ctypes.data, cto.ctypes.data, err, 256)
+                         out.ctypes.data, cto.ctypes.data, light.ctypes.data, err, 256)
     assert rc == 0, err.value.decode()
     ora = _run_oracle(spec, cases)
     for q, case in enumerate(cases):
         _check_case(case, tij[q], int(ty[q]), bool(valid[q]), out[12 * q:12 * q + 12], int(cto[q]), masses)
         otij, oty, _, oout, octo, _ = ora[q]
+        if np.isnan(otij):                    # the reference's NaN root: no event on the device
+            otij, oty = 1e9, 0
         assert (tij[q], int(ty[q]), int(cto[q])) == (otij, oty, octo), case[0]
         assert np.array_equal(out[12 * q:12 * q + 12], oout), case[0]
+        if case[3] in (1, 2, 3):   # the light batches' half-warp collision gives the same bits
+            assert np.array_equal(light[12 * q:12 * q + 12], oout), case[0] + " (half-warp collision)"
