@@ -218,6 +218,13 @@ int dmd_load_state(dmd_handle *h, const void *buf, int64_t n);
 
 void dmd_destroy(dmd_handle *h);
 
+/* Checked build only (compiled with -DDMD_BOUNDS; no reference
+ * counterpart): the first out-of-range index any device array access met
+ * since the last call, recorded instead of faulting (the access used index
+ * 0), then cleared.  Returns 1 with *rec = site << 40 | extent << 20 |
+ * index, 0 if none, -1 in a build without the checks. */
+int dmd_debug_bounds(long long *rec);
+
 const char *dmd_last_error(dmd_handle *h);
 const char *dmd_version(void);
 

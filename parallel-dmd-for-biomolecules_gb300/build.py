@@ -16,7 +16,10 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
-OUT = os.path.join(PKG, "_build")
+# DMD_CHECKED=1: the checked build (-DDMD_BOUNDS: device index checks that
+# record the first out-of-range index instead of faulting), kept apart
+CHECKED = os.environ.get("DMD_CHECKED", "") == "1"
+OUT = os.path.join(PKG, "_build_checked" if CHECKED else "_build")
 LIB = os.path.join(OUT, "libdmd_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -42,6 +45,12 @@ def _run(cmd):
 
 def build(verbose: bool = False, extra: list | None = None) -> str:
     os.makedirs(OUT, exist_ok=True)
+    if CHECKED:
+        extra = list(extra or []) + ["-DDMD_BOUNDS"]
+        stamp = os.path.join(OUT, "checked.stamp")
+        newest_src = max(os.path.getmtime(os.path.join(CSRC, f)) for f in os.listdir(CSRC))
+        if os.path.exists(LIB) and os.path.exists(stamp) and os.path.getmtime(stamp) >= newest_src:
+            return LIB
     nv = nvcc()
     srcs = CU_SOURCES + CPP_SOURCES
     newest = max(os.path.getmtime(os.path.join(CSRC, f)) for f in os.listdir(CSRC))
@@ -65,6 +74,8 @@ def build(verbose: bool = False, extra: list | None = None) -> str:
     tmp = LIB + ".tmp"
     _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
     os.replace(tmp, LIB)
+    if CHECKED:
+        open(os.path.join(OUT, "checked.stamp"), "w").close()
     return LIB
 
 

@@ -227,6 +227,7 @@ __device__ __forceinline__ void warp_keymin(long long &k, int &p, double &t, int
 }
 
 __device__ __forceinline__ void set_pred(const DSys &S, int b, double t, int p, int ty, bool q) {
+    b = DMD_CHK(b, S.N + 3, 10);
     S.tim[b] = t;
     S.nptnr[b] = p;
     S.colt[b] = (int8_t)ty;
@@ -931,7 +932,7 @@ __device__ int cta_checkover(const DSys &S, SharedState &sh) {
                  * the tables hold these products in that order; the factor
                  * is 1 for 16 and the shoulder codes */
                 const double sigsq = code == 15 ? T.core15_sq[a][b]
-                                     : (code == 1 || (code >= 17 && code <= 26)) ? T.core_sq[core_slot(code)][a][b]
+                                     : (code == 1 || (code >= 17 && code <= 26)) ? T.core_sq[core_slot_d(code)][a][b]
                                                                                  : T.sigma_sq[a][b];
                 const Rel r = d_rel(S, i, j, tf);
                 bad = r.rijsq * 1.0000000001 <= sigsq;
@@ -1521,6 +1522,22 @@ cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, c
                             const int *chain_off, dmd_diag *out, cudaStream_t st) {
     k_diag<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, chain_start, chain_len, chain_off, out);
     return cudaGetLastError();
+}
+
+/* the first out-of-range index of a checked build (-DDMD_BOUNDS), then
+ * cleared: 1 and *rec set (site << 40 | extent << 20 | index) if one was
+ * recorded, 0 if none, -1 in a build without the checks */
+extern "C" int dmd_debug_bounds(long long *rec) {
+#ifdef DMD_BOUNDS
+    unsigned long long v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_dmd_bounds, sizeof v) != cudaSuccess) return -2;
+    if (cudaMemcpyToSymbol(g_dmd_bounds, &zero, sizeof zero) != cudaSuccess) return -2;
+    if (rec) *rec = (long long)v;
+    return v ? 1 : 0;
+#else
+    if (rec) *rec = 0;
+    return -1;
+#endif
 }
 
 /* ------------------------------------------------------------------ */

@@ -74,7 +74,28 @@ struct DTab {
     double rshld_sq[DMD_NT][DMD_NT], r2shld_sq[DMD_NT][DMD_NT];
     double rrmass[DMD_NT][DMD_NT];
 };
+/* Checked build (-DDMD_BOUNDS): every index DMD_CHK guards is tested
+ * against its array's extent; the first one outside it is recorded in
+ * g_dmd_bounds (site << 40 | extent << 20 | index, 20 bits each, plus one in
+ * bit 62) and replaced by 0, so that the kernel carries on without a fault
+ * and the host reports it (dmd_debug_bounds).  Other builds: no check. */
+#ifdef DMD_BOUNDS
+__device__ unsigned long long g_dmd_bounds;
+__device__ __forceinline__ int dmd_chk(int i, int n, int site) {
+    if ((unsigned)i < (unsigned)n) return i;
+    const unsigned long long rec = (1ull << 62) | ((unsigned long long)(site & 0x3fffff) << 40) |
+                                   ((unsigned long long)(n & 0xfffff) << 20) | (unsigned long long)(i & 0xfffff);
+    atomicCAS(&g_dmd_bounds, 0ull, rec);
+    return 0;
+}
+#define DMD_CHK(i, n, site) dmd_chk((i), (n), (site))
+#else
+#define DMD_CHK(i, n, site) (i)
+#endif
+
 __host__ __device__ __forceinline__ int core_slot(int code) { return code <= 3 ? code : code - 13; }
+/* slot of a squeezed or plain core code (1-3, 17-26) in DTab::core_sq */
+__device__ __forceinline__ int core_slot_d(int code) { return DMD_CHK(core_slot(code), 14, 1); }
 
 /* per-system scalars kept between launches */
 struct DScal {
@@ -302,6 +323,8 @@ __device__ __forceinline__ double d_wrap1(double x) {
 __device__ __forceinline__ Rel d_rel_cv(const DSys &S, int i, int j, double tfalse, const double *si,
                                         const double *sj) {
     Rel r;
+    i = DMD_CHK(i, S.N, 2);
+    j = DMD_CHK(j, S.N, 3);
     const double vxi = si ? si[3] : S.vx[i], vyi = si ? si[4] : S.vy[i], vzi = si ? si[5] : S.vz[i];
     const double vxj = sj ? sj[3] : S.vx[j], vyj = sj ? sj[4] : S.vy[j], vzj = sj ? sj[5] : S.vz[j];
     const double xi = si ? si[0] : S.x[i], yi = si ? si[1] : S.y[i], zi = si ? si[2] : S.z[i];
@@ -362,7 +385,7 @@ __device__ __forceinline__ bool f32_no_event(const DSys &S, int i, int j, int ev
     if (!core && !well) return false;
     if (evcode == 15 && a + b != 5 && S.bptnr[i] == j) return false;
     const DTab &T = *S.tab;
-    const double *Rp = core ? &T.core_sq[core_slot(evcode)][a][b]
+    const double *Rp = core ? &T.core_sq[core_slot_d(evcode)][a][b]
                             : evcode >= 40 ? &T.shlddia_sq[a][b] : &T.welldia_sq[a][b];
     const bool need_out = well && (evcode != 15 || a + b == 5);
     const unsigned Rh = d_hi(Rp);
@@ -426,7 +449,8 @@ __device__ __forceinline__ bool d_predict_c(const DSys &S, int i, int j, int evc
                                             const double *sj = nullptr) {
     const DTab &T = *S.tab;
     Rel r = d_rel_cv(S, i, j, tfalse, si, sj);
-    int a = S.ident[i], b = S.ident[j];
+    int a = DMD_CHK(S.ident[DMD_CHK(i, S.N, 2)], DMD_NT, 4), b = DMD_CHK(S.ident[DMD_CHK(j, S.N, 3)], DMD_NT, 4);
+    evcode = DMD_CHK(evcode, DMD_NC, 5);
     bool neg = d_lt0(r.bij);
     bool valid = true;
     /* stage 1: diameter R1; outcome if D1 > 0 (k1p, y1p) or not (k1n, y1n);
@@ -434,7 +458,7 @@ __device__ __forceinline__ bool d_predict_c(const DSys &S, int i, int j, int evc
     double R1 = 0.0, R2 = 0.0;
     int k1p = PK_NONE, y1p = 0, k1n = PK_NONE, y1n = 0, k2p = PK_NONE, y2p = 0, k2n = PK_NONE, y2n = 0;
     if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {                 /* core.f:3-44 */
-        if (neg) { R1 = T.core_sq[core_slot(evcode)][a][b]; k1p = PK_MINUS; y1p = 1; }
+        if (neg) { R1 = T.core_sq[core_slot_d(evcode)][a][b]; k1p = PK_MINUS; y1p = 1; }
     } else if (evcode >= 4 && evcode <= 12) {                           /* bond.f:4-121 */
         bool side = evcode >= 10;
         double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];

@@ -190,7 +190,7 @@ __device__ int warp_eventdyn(const DSys &S, int i, int j, int evcode, int ct, do
                 ratio = div_by(rmass * bij, hb ? T.core15_sq[a][b] : T.sigma_sq[a][b],
                                hb ? T.rcore15_sq[a][b] : T.rsigma_sq[a][b]);
             } else if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {
-                const int sl = core_slot(evcode);
+                const int sl = core_slot_d(evcode);
                 ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
             } else {
                 /* the other codes with a core (16: inside a hydrophobic well;
@@ -535,7 +535,7 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
                 ratio = div_by(rmass * bij, hb ? T.core15_sq[a][b] : T.sigma_sq[a][b],
                                hb ? T.rcore15_sq[a][b] : T.rsigma_sq[a][b]);
             } else if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {
-                const int sl = core_slot(evcode);
+                const int sl = core_slot_d(evcode);
                 ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
             } else {
                 /* the other codes with a core (16: inside a hydrophobic well;
@@ -723,15 +723,15 @@ __device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
             const int8_t ci = (q < cnt && dc) ? dc[q] : (int8_t)-1;
             const int lj = q < cj ? dj[q] : -1;
             const int8_t cjv = (q < cj && dcj) ? dcj[q] : (int8_t)-1;
-            if (q < cnt) { W.ops_l[q] = li; W.ops_s[q] = i; W.ops_c[q] = ci; }
+            if (q < cnt) { const int qq = DMD_CHK(q, OPS_MAX, 20); W.ops_l[qq] = li; W.ops_s[qq] = i; W.ops_c[qq] = ci; }
             const bool keep = q < cj && lj != i;
             const unsigned m = __ballot_sync(FULL, keep);
-            const int pos = base_j + nj + __popc(m & ((1u << lane) - 1));
+            const int pos = DMD_CHK(base_j + nj + __popc(m & ((1u << lane) - 1)), OPS_MAX, 21);
             if (keep) { W.ops_l[pos] = lj; W.ops_s[pos] = j; W.ops_c[pos] = cjv; }
             nj += __popc(m);
         }
         if (ei_keep) {
-            const int pos = cnt + __popc(mei & ((1u << lane) - 1));
+            const int pos = DMD_CHK(cnt + __popc(mei & ((1u << lane) - 1)), OPS_MAX, 22);
             W.ops_l[pos] = eri; W.ops_s[pos] = i; W.ops_c[pos] = -1;
         }
         n = base_j + nj;
@@ -739,7 +739,7 @@ __device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
             const bool ej_keep = lane < 3 && erj >= 0 && erj < j;
             const unsigned mej = __ballot_sync(FULL, ej_keep);
             if (ej_keep) {
-                const int pos = n + __popc(mej & ((1u << lane) - 1));
+                const int pos = DMD_CHK(n + __popc(mej & ((1u << lane) - 1)), OPS_MAX, 23);
                 W.ops_l[pos] = erj; W.ops_s[pos] = j; W.ops_c[pos] = -1;
             }
             n += __popc(mej);
@@ -766,8 +766,8 @@ __device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
         int pos = __popc(m & ((1u << lane) - 1));
         unsigned mm = __ballot_sync(FULL, mark);
         int mpos = __popc(mm & ((1u << lane) - 1));
-        if (lead) { W.lead_l[pos] = l; W.lead_q[pos] = (int16_t)q; W.lead_m[pos] = mark; }
-        if (mark) W.mk[mpos] = (int16_t)pos;
+        if (lead) { const int pp = DMD_CHK(pos, OPS_MAX, 24); W.lead_l[pp] = l; W.lead_q[pp] = (int16_t)q; W.lead_m[pp] = mark; }
+        if (mark) W.mk[DMD_CHK(mpos, OPS_MAX, 25)] = (int16_t)pos;
         nl = __popc(m);
         nm = __popc(mm);
     }
@@ -794,8 +794,8 @@ __device__ void warp_rp_lists(const DSys &S, WarpArea &W, int i, int j) {
         int pos = nl + __popc(m & ((1u << lane) - 1));
         unsigned mm = __ballot_sync(FULL, lead && mark);
         int mpos = nm + __popc(mm & ((1u << lane) - 1));
-        if (lead) { W.lead_l[pos] = l; W.lead_q[pos] = (int16_t)q; W.lead_m[pos] = mark; }
-        if (lead && mark) W.mk[mpos] = (int16_t)pos;
+        if (lead) { const int pp = DMD_CHK(pos, OPS_MAX, 26); W.lead_l[pp] = l; W.lead_q[pp] = (int16_t)q; W.lead_m[pp] = mark; }
+        if (lead && mark) W.mk[DMD_CHK(mpos, OPS_MAX, 27)] = (int16_t)pos;
         nl += __popc(m);
         nm += __popc(mm);
     }
@@ -820,7 +820,7 @@ __device__ void warp_rp_targets(const DSys &S, WarpArea &W, int i, int j, int rd
         int b;
         if (t == 0) b = rd == 0 ? i : -1;
         else if (t == 1) b = rd == 0 ? j : -1;
-        else b = W.lead_l[W.mk[m0 + t - 2]];
+        else b = W.lead_l[DMD_CHK(W.mk[DMD_CHK(m0 + t - 2, OPS_MAX, 29)], OPS_MAX, 30)];
         W.fs.tg_b[t] = b;
         W.fs.tg_k[t] = Hkey; W.fs.tg_p[t] = -1; W.fs.tg_raw[t] = Hraw; W.fs.tg_y[t] = -1;
     }
@@ -1087,7 +1087,7 @@ __device__ void warp_rp_finish(const DSys &S, Err E, WarpArea &W, int i, int j, 
                 if (key_less(kn, src, okey(t), p)) { t = tn; p = src; y = W.op_y[pp]; qq = kn < imax_key; }
             }
         }
-        int slot = 2 + ld;
+        int slot = DMD_CHK(2 + ld, OPS_MAX + 2, 28);
         if (l == i) {
             W.pb[slot] = -1;
             W.pt[0] = t; W.pn[0] = p; W.pc[0] = (int8_t)y; W.pq[0] = qq;

@@ -13,7 +13,9 @@ import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REPO_DIR = os.path.dirname(PKG_DIR)
-ENGINE_SO = os.path.join(PKG_DIR, "_build", "libdmd_gb300.so")
+# DMD_CHECKED=1 selects the checked build (device index checks, build.py)
+ENGINE_SO = os.path.join(PKG_DIR, "_build_checked" if os.environ.get("DMD_CHECKED", "") == "1" else "_build",
+                         "libdmd_gb300.so")
 
 DMD_OK = 0
 ERRORS = {
@@ -106,7 +108,7 @@ class GenSpec(C.Structure):
 # the symbols include/dmd.h declares
 ENGINE_SYMBOLS = [
     "dmd_create", "dmd_run", "dmd_predict_all", "dmd_get_state", "dmd_set_state", "dmd_diagnostics", "dmd_get_evcode",
-    "dmd_destroy", "dmd_last_error", "dmd_version", "dmd_batch_create", "dmd_batch_run",
+    "dmd_destroy", "dmd_last_error", "dmd_debug_bounds", "dmd_version", "dmd_batch_create", "dmd_batch_run",
     "dmd_batch_get_state", "dmd_batch_diagnostics", "dmd_batch_destroy", "dmd_batch_last_error",
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
     "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster", "dmd_batch_set_cell_div",
@@ -135,6 +137,8 @@ def ptr(a, typ):
 def _declare(lib) -> None:
     lib.dmd_create.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System), C.POINTER(C.c_void_p)]
     lib.dmd_create.restype = C.c_int
+    lib.dmd_debug_bounds.argtypes = [C.POINTER(C.c_longlong)]
+    lib.dmd_debug_bounds.restype = C.c_int
     lib.dmd_run.argtypes = [C.c_void_p, C.c_int64, C.POINTER(EventLog)]
     lib.dmd_run.restype = C.c_int
     lib.dmd_predict_all.argtypes = [C.c_void_p, dbl_p, i32_p, i32_p]

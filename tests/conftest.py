@@ -28,3 +28,18 @@ def built():
 
 def has_reference() -> bool:
     return os.path.isdir(REFERENCE)
+
+
+@pytest.fixture(autouse=True)
+def _checked_build_bounds(request):
+    """In the checked build (DMD_CHECKED=1), every GPU test must also leave
+    no out-of-range device index behind."""
+    yield
+    if os.environ.get("DMD_CHECKED", "") != "1" or request.node.get_closest_marker("gpu") is None:
+        return
+    import ctypes as C
+    from dmdgb import abi
+    rec = C.c_longlong()
+    rc = abi.load_engine().dmd_debug_bounds(C.byref(rec))
+    assert rc == 0, (f"out-of-range device index: site {(rec.value >> 40) & 0x3fffff}, "
+                     f"extent {(rec.value >> 20) & 0xfffff}, index {rec.value & 0xfffff}")
