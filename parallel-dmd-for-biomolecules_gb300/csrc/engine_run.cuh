@@ -1411,6 +1411,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
     WarpArea &W = warea[warp];
     SharedState *L = C > 1 ? cg::this_cluster().map_shared_rank(&sh, 0) : &sh;
     if (threadIdx.x == 0) {
+        sh.ncand = 0;
         sh.sc = *S.sc; sh.sc.done = 0; sh.sc.stop = 0; sh.sc.need_full = 0;
         sh.delta = sh.sc.interval * 0.05;
         sh.bseq = 0;
@@ -1430,7 +1431,35 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
     long long iter = 0;
     while (true) {
         /* ---- the leader selects the next event (and a batch) ---- */
-        if (leader) {
+        ++iter;   /* on every thread, so that each can take the test below */
+        /* One CTA with at most 256 level-1 groups: every warp finds the root
+         * itself from the level-1 minima and, when it is a bead's event of a
+         * batch, goes straight into the candidate gather without a barrier;
+         * otherwise (exit, pseudo event, last event, clusters) warp 0 decides
+         * and the others wait for it. */
+        bool fast = false;
+        int fe = -1;
+        long long fk = 0;
+        if (C == 1 && !serial && S.nl1 <= 256 && !(sh.sc.done >= target || sh.sc.err || sh.sc.stop) &&
+            !(sh.sc.max_dn > dn_limit) && !(iter > max_iter) && target - sh.sc.done > 1) {
+            fe = warp_root(S, fk);
+            fast = fe >= 0 && fe < N;
+        }
+        if (fast) {
+            if (threadIdx.x == 0) { sh.exitf = 0; sh.ev = fe; sh.kcut = fk; }
+            DMD_PHASE(0);
+            int m = cta_gather_candidates(S, sh, fe, fk, slots);
+            if (m > slots) m = slots;
+            const long long left = target - sh.sc.done;
+            if (m > left) m = (int)left;
+            if (threadIdx.x == 0) {
+                sh.m = m;
+                sh.tick_reset = m > 1 && sh.bseq >= DMD_TICKET_SEQ_MAX;
+                sh.c_simple[0] = 0;
+                sh.coll0 = sh.sc.coll; sh.log0 = sh.sc.log_count; sh.imax = sh.sc.interval_max; sh.tnow = sh.sc.t;
+            }
+            DMD_PHASE(1);
+        } else if (leader) {
             if (warp == 0) {
                 /* warp 0: the exit test and the root */
                 int ex = 0;
@@ -1439,7 +1468,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                     /* lists longer than this variant takes: the host goes
                      * on with the full variant from here */
                     if (!x && sh.sc.max_dn > dn_limit) { sh.sc.need_full = 1; x = true; }
-                    if (!x && ++iter > max_iter) { set_err(sh, DMD_E_DEVICE_TIMEOUT, 0); x = true; }
+                    if (!x && iter > max_iter) { set_err(sh, DMD_E_DEVICE_TIMEOUT, 0); x = true; }
                     ex = x;
                 }
                 ex = __shfl_sync(FULL, ex, 0);
@@ -1979,6 +2008,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                 if (warp == 0) warp_l1_refresh(S, sh.touched, 1);
             }
         }
+        if (threadIdx.x == 0) sh.ncand = 0;   /* the next gather may start without a barrier */
         csync(C);
         DMD_PHASE(ph_kind);
     }
