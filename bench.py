@@ -292,7 +292,7 @@ def run_ours(args):
     E = args.events
     batch = Batch(specs)
     lib = batch.lib
-    tuned = batch.autotune(max(2000, E // 4)) if not args.no_tune else None
+    tuned = batch.autotune(max(2000, E // 4), cache=args.tune_cache) if not args.no_tune else None
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -340,6 +340,21 @@ def run_ours(args):
         for _ in range(args.segments):
             batch.run(args.segment_events)
             segments.append(args.segment_events * len(specs) / (lib.dmd_batch_last_run_ms(batch.h) / 1000.0))
+
+    # rebuild cycles replayed from a captured CUDA graph: every launch ends
+    # each replica at its next list rebuild (the host regains control every
+    # launches_per_graph cycles); the same events as the persistent launch
+    cycles = None
+    if rank == 0 and not args.no_cycles:
+        per_graph = 8
+        batch.run_cycles(max(1000, E // 4), per_graph)      # capture and warm-up
+        flush.fill_(3.0)
+        torch.cuda.synchronize()
+        k = batch.run_cycles(E, per_graph)
+        cyc_s = lib.dmd_batch_last_run_ms(batch.h) / 1000.0
+        cycles = {"value": E * len(specs) / cyc_s, "unit": UNIT, "events_per_replica": E, "launches": k,
+                  "launches_per_graph": per_graph,
+                  "note": "same batch continued; each launch runs every replica to its next neighbour-list rebuild"}
 
     # the plain one-system-per-launch path on the same replicas
     plain_events, plain_s = 0, 0.0
@@ -409,6 +424,7 @@ def run_ours(args):
                          "fp64": {"achieved": fp64_gflops, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
                                   "frac": fp64_gflops / FP64_PEAK_GFLOPS, "peak_kind": "nominal",
                                   "flops_per_event": fp64_flops_per_event(nbr)}},
+            "rebuild_cycle_graph": cycles,
             "segments": {"events_per_replica": args.segment_events, "events_per_s": segments,
                          "note": "the batch continued after the timed steps, one launch per segment"},
             "cpu_baseline": cpu,
@@ -563,6 +579,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-single", action="store_true")
     ap.add_argument("--no-sidechain", action="store_true")
+    ap.add_argument("--no-cycles", action="store_true")
+    ap.add_argument("--tune-cache", default=None, help="JSON file keeping the autotuner's choices")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-scale", type=float, default=0.01)
     ap.add_argument("--serve-slots", type=int, default=256)

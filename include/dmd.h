@@ -315,12 +315,33 @@ int dmd_set_compact_limit(dmd_handle *h, int32_t max_down);
  * first call (and again when the sizes or the cluster size change) and
  * replayed; the same result as dmd_batch_run with n_events * n_launches. */
 int dmd_batch_run_graph(dmd_batch *b, int64_t n_events, int32_t n_launches);
+/* Rebuild cycles from a CUDA graph (the loop of code/main.F90:1126-1187,
+ * one list rebuild per launch): launches_per_graph launches are captured
+ * into a graph on the first call (and again when the cluster size or the
+ * event-loop variant changes); each launch runs every system up to and
+ * including its next neighbour-list rebuild, or to the end of its events,
+ * and keeps the events it still has to run on the device.  The graph is
+ * replayed until every system has run n_events; n_launches (may be NULL)
+ * receives the launches replayed.  The same result as dmd_batch_run with
+ * n_events.  The host regains control at each replay, every
+ * launches_per_graph rebuild cycles. */
+int dmd_batch_run_cycles(dmd_batch *b, int64_t n_events, int32_t launches_per_graph, int64_t *n_launches);
 /* Autotuner: trial runs of a copy of the batch (from its create-time inputs)
  * for each cluster size that fits and rebuild grids with div 1 and 2; keeps
  * the fastest for this batch and reports it (best_ms: device time of its
  * trial).  The batch's own state is not advanced. */
 int dmd_batch_autotune(dmd_batch *b, int64_t trial_events, int32_t *cluster, int32_t *cell_div,
                        double *best_ms);
+/* The autotuner with its choices kept in a JSON file (created if absent):
+ * a batch whose systems have the same bead counts, chain counts, list
+ * capacities and grids, on a device of the same compute capability and SM
+ * count, with the same library version, compact limit, H-bond flag and
+ * trial_events, takes the stored cluster size and rebuild grid without
+ * trial runs (*from_cache = 1); otherwise the trials run and their result
+ * is added to the file (*from_cache = 0).  A file that is not such a cache
+ * is left untouched and DMD_E_INPUT returned.  Output pointers may be NULL. */
+int dmd_batch_autotune_cached(dmd_batch *b, int64_t trial_events, const char *cache_path, int32_t *cluster,
+                              int32_t *cell_div, double *best_ms, int32_t *from_cache);
 void dmd_batch_destroy(dmd_batch *b);
 const char *dmd_batch_last_error(dmd_batch *b);
 

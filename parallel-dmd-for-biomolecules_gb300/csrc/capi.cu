@@ -522,6 +522,8 @@ struct dmd_batch {
     long long graph_events = 0;
     int graph_launches = 0, graph_cluster = 0, graph_compact = -1;
     long long *d_targets = nullptr;    /* per-system event targets of a follow-up launch */
+    cudaGraphExec_t cyc_graph = nullptr;   /* captured rebuild-cycle launches of dmd_batch_run_cycles */
+    int cyc_launches = 0, cyc_cluster = 0, cyc_compact = -1;
     long long upload_bytes = 0;        /* host-to-device bytes of the creation */
     int compact_dn = DMD_COMPACT_DN;   /* down-list limit of the compact variant, 0: never */
 };
@@ -991,6 +993,87 @@ int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
     return rc;
 }
 
+/* Rebuild cycles from a CUDA graph: per_graph launches captured once, each
+ * of which runs every system up to and including its next list rebuild
+ * (the nbor/events block of code/main.F90:1144-1166) or to the end of its
+ * events.  The events each system still has to run stay on the device
+ * (d_targets): a launch reads them and writes them back, so a replay needs
+ * nothing from the host.  The graph is replayed until every system has run
+ * n_events; between replays the host reads the remaining counts and the
+ * systems' scalars (errors, the compact variant's overflow).  The committed
+ * events equal those of batch_run with n_events. */
+int batch_run_cycles(dmd_batch &B, int64_t n_events, int per_graph, int64_t *launches_out) {
+    NvtxRange range("dmd run: rebuild-cycle graph");
+    std::string &err = B.err;
+    if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    if (n_events < 0 || per_graph <= 0 || per_graph > 4096) { err = "bad event or launch count"; return DMD_E_INPUT; }
+    B.diag_valid = false;
+    B.state_valid = false;
+    int n = (int)B.hs.size();
+    int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
+    int probe = 0;
+    CK(dmd_max_active_clusters(C, &probe));   /* kernel attributes are set outside the capture */
+    std::vector<DSys> hd(n);
+    int compact = B.compact_dn;
+    for (int r = 0; r < n; ++r) {
+        hd[r] = B.ds[r].d;
+        hd[r].ncell = coarse_cells(B.hs[r].ncell, B.cell_div);
+        hd[r].log = nullptr; hd[r].log_cap = 0;
+        DScal sc;
+        CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
+        if (sc.max_dn > B.compact_dn) compact = 0;
+    }
+    int max_beads = 0;
+    for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
+    CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
+    if (!B.d_targets) CK(cudaMalloc(&B.d_targets, (size_t)n * sizeof(long long)));
+    std::vector<long long> rem(n, (long long)n_events);
+    CK(cudaMemcpyAsync(B.d_targets, rem.data(), (size_t)n * sizeof(long long), cudaMemcpyHostToDevice, B.st));
+    B.last_cluster = C;
+    CK(cudaEventRecord(B.ev0, B.st));
+    long long launches = 0;
+    int rc = DMD_OK;
+    while (true) {
+        if (!B.cyc_graph || B.cyc_launches != per_graph || B.cyc_cluster != C || B.cyc_compact != compact) {
+            if (B.cyc_graph) cudaGraphExecDestroy(B.cyc_graph);
+            B.cyc_graph = nullptr;
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal));
+            cudaError_t ce = cudaSuccess;
+            for (int k = 0; k < per_graph && ce == cudaSuccess; ++k)
+                ce = dmd_launch_run(B.d_sys, n, max_beads, C, compact, 0, B.d_targets, B.hbonds, B.d_cstart, B.d_clen,
+                                    B.d_coff, nullptr, B.st, 1);
+            cudaError_t ce2 = cudaStreamEndCapture(B.st, &g);
+            if (ce != cudaSuccess) { err = cudaGetErrorString(ce); if (ce2 == cudaSuccess) cudaGraphDestroy(g); return DMD_E_CUDA; }
+            CK(ce2);
+            cudaError_t ce3 = cudaGraphInstantiate(&B.cyc_graph, g, 0);
+            cudaGraphDestroy(g);
+            CK(ce3);
+            B.cyc_launches = per_graph; B.cyc_cluster = C; B.cyc_compact = compact;
+        }
+        CK(cudaGraphLaunch(B.cyc_graph, B.st));
+        launches += per_graph;
+        CK(cudaMemcpyAsync(rem.data(), B.d_targets, (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost, B.st));
+        rc = sync_check(B);
+        if (rc != DMD_OK) break;
+        bool left = false, full = false;
+        for (int r = 0; r < n; ++r) {
+            left = left || rem[r] > 0;
+            full = full || B.hs[r].sc.need_full;
+        }
+        if (!left) break;
+        /* a system whose lists outgrew the compact variant: the rest of the
+         * cycles run on the full one */
+        if (full) compact = 0;
+    }
+    CK(cudaEventRecord(B.ev1, B.st));
+    CK(cudaEventSynchronize(B.ev1));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) B.last_ms = ms;
+    if (launches_out) *launches_out = launches;
+    return rc;
+}
+
 void batch_free(dmd_batch &B);
 
 /* Autotuner: times trial runs of a copy of the batch (made from its
@@ -1032,9 +1115,184 @@ int batch_autotune(dmd_batch &B, int64_t trial_events, int32_t *best_cluster, in
     return DMD_OK;
 }
 
+/* ---- the autotuner's results kept in a JSON file ----
+ * {"format": "dmd-autotune-1", "entries": {"<key>": {"cluster": C,
+ * "cell_div": D, "trial_ms": T, "trial_events": E, "systems": n,
+ * "beads": b}, ...}}.  The key names the device (compute capability and SM
+ * count), the library version, the event-loop variant limit, the H-bond
+ * flag, the trial length and a 64-bit FNV-1a hash of every system's bead
+ * count, chain count, list capacity and finest grid; a batch of the same
+ * shapes on the same device takes the stored choice without trial runs. */
+struct TuneEntry { int cluster = 1, cell_div = 1; double trial_ms = 0; long long trial_events = 0, systems = 0, beads = 0; };
+
+/* a reader for the file's own subset of JSON: objects, strings without
+ * escapes other than \\ and \", and numbers */
+struct JsonIn {
+    const std::string &s;
+    size_t p = 0;
+    bool ok = true;
+    explicit JsonIn(const std::string &t) : s(t) {}
+    void ws() { while (p < s.size() && (s[p] == ' ' || s[p] == '\n' || s[p] == '\r' || s[p] == '\t')) ++p; }
+    bool eat(char c) { ws(); if (p < s.size() && s[p] == c) { ++p; return true; } return false; }
+    std::string str() {
+        std::string o;
+        if (!eat('"')) { ok = false; return o; }
+        while (p < s.size() && s[p] != '"') {
+            if (s[p] == '\\' && p + 1 < s.size()) ++p;
+            o += s[p++];
+        }
+        if (p >= s.size()) { ok = false; return o; }
+        ++p;
+        return o;
+    }
+    double num() {
+        ws();
+        const char *b = s.c_str() + p;
+        char *e = nullptr;
+        double v = std::strtod(b, &e);
+        if (e == b) { ok = false; return 0; }
+        p += (size_t)(e - b);
+        return v;
+    }
+};
+
+bool tune_read(const std::string &path, std::map<std::string, TuneEntry> &out, std::string &err) {
+    out.clear();
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) return true;                      /* no file yet: an empty cache */
+    std::string t;
+    char buf[4096];
+    size_t k;
+    while ((k = std::fread(buf, 1, sizeof buf, f)) > 0) t.append(buf, k);
+    std::fclose(f);
+    JsonIn J(t);
+    bool fmt = false;
+    if (!J.eat('{')) { err = "autotune cache " + path + ": not a JSON object"; return false; }
+    while (J.ok && !J.eat('}')) {
+        std::string key = J.str();
+        if (!J.ok || !J.eat(':')) break;
+        if (key == "format") { fmt = J.str() == "dmd-autotune-1"; }
+        else if (key == "entries") {
+            if (!J.eat('{')) { J.ok = false; break; }
+            while (J.ok && !J.eat('}')) {
+                std::string ek = J.str();
+                if (!J.ok || !J.eat(':') || !J.eat('{')) { J.ok = false; break; }
+                TuneEntry e;
+                while (J.ok && !J.eat('}')) {
+                    std::string f2 = J.str();
+                    if (!J.ok || !J.eat(':')) { J.ok = false; break; }
+                    double v = J.num();
+                    if (f2 == "cluster") e.cluster = (int)v;
+                    else if (f2 == "cell_div") e.cell_div = (int)v;
+                    else if (f2 == "trial_ms") e.trial_ms = v;
+                    else if (f2 == "trial_events") e.trial_events = (long long)v;
+                    else if (f2 == "systems") e.systems = (long long)v;
+                    else if (f2 == "beads") e.beads = (long long)v;
+                    J.eat(',');
+                }
+                if (J.ok) out[ek] = e;
+                J.eat(',');
+            }
+        } else { J.ok = false; break; }
+        J.eat(',');
+    }
+    if (!J.ok || !fmt) { err = "autotune cache " + path + ": not a dmd-autotune-1 file"; out.clear(); return false; }
+    for (auto &kv : out)
+        if ((kv.second.cluster != 1 && kv.second.cluster != 2 && kv.second.cluster != 4 && kv.second.cluster != 8) ||
+            kv.second.cell_div < 1 || kv.second.cell_div > 8) {
+            err = "autotune cache " + path + ": entry out of range";
+            out.clear();
+            return false;
+        }
+    return true;
+}
+
+bool tune_write(const std::string &path, const std::map<std::string, TuneEntry> &m, std::string &err) {
+    std::string tmp = path + ".tmp" + std::to_string((long long)std::chrono::steady_clock::now().time_since_epoch().count());
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) { err = "autotune cache " + path + ": cannot write"; return false; }
+    std::fprintf(f, "{\n  \"format\": \"dmd-autotune-1\",\n  \"entries\": {");
+    bool first = true;
+    for (auto &kv : m) {
+        const TuneEntry &e = kv.second;
+        std::fprintf(f, "%s\n    \"%s\": {\"cluster\": %d, \"cell_div\": %d, \"trial_ms\": %.6g, \"trial_events\": %lld, "
+                        "\"systems\": %lld, \"beads\": %lld}",
+                     first ? "" : ",", kv.first.c_str(), e.cluster, e.cell_div, e.trial_ms, e.trial_events, e.systems, e.beads);
+        first = false;
+    }
+    std::fprintf(f, "\n  }\n}\n");
+    bool ok = std::fclose(f) == 0;
+    if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) {
+        std::remove(tmp.c_str());
+        err = "autotune cache " + path + ": cannot write";
+        return false;
+    }
+    return true;
+}
+
+std::string tune_key(const dmd_batch &B, int64_t trial_events, long long *beads) {
+    int dev = 0, major = 0, minor = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t h = 1469598103934665603ULL;
+    auto mix = [&](long long v) {
+        for (int b = 0; b < 8; ++b) { h ^= (uint64_t)((v >> (8 * b)) & 0xff); h *= 1099511628211ULL; }
+    };
+    *beads = 0;
+    for (const HostSys &H : B.hs) { mix(H.N); mix(H.nchains); mix(H.cap); mix(H.ncell); *beads += H.N; }
+    char k[256];
+    std::snprintf(k, sizeof k, "cc%d.%d/sm%d/%s/compact%d/hb%d/trial%lld/n%zu/%016llx", major, minor, sms,
+                  dmd_version(), B.compact_dn, B.hbonds, (long long)trial_events, B.hs.size(), (unsigned long long)h);
+    for (char *c = k; *c; ++c) if (*c == '"' || *c == '\\' || *c == ' ') *c = '_';
+    return k;
+}
+
+/* the autotuner with its results kept in the file at path */
+int batch_autotune_cached(dmd_batch &B, int64_t trial_events, const char *path, int32_t *cluster, int32_t *cell_div,
+                          double *best_ms, int32_t *from_cache) {
+    std::string &err = B.err;
+    if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    if (!path || !*path) { err = "no autotune cache path"; return DMD_E_INPUT; }
+    if (trial_events <= 0) { err = "trial_events must be positive"; return DMD_E_INPUT; }
+    std::map<std::string, TuneEntry> m;
+    if (!tune_read(path, m, err)) return DMD_E_INPUT;
+    long long beads = 0;
+    const std::string key = tune_key(B, trial_events, &beads);
+    auto it = m.find(key);
+    if (it != m.end()) {
+        B.cluster = it->second.cluster;
+        B.cell_div = it->second.cell_div;
+        if (cluster) *cluster = B.cluster;
+        if (cell_div) *cell_div = B.cell_div;
+        if (best_ms) *best_ms = it->second.trial_ms;
+        if (from_cache) *from_cache = 1;
+        return DMD_OK;
+    }
+    int32_t c = 1, d = 1;
+    double ms = 0;
+    int rc = batch_autotune(B, trial_events, &c, &d, &ms);
+    if (rc != DMD_OK) return rc;
+    TuneEntry e;
+    e.cluster = c; e.cell_div = d; e.trial_ms = ms; e.trial_events = trial_events;
+    e.systems = (long long)B.hs.size(); e.beads = beads;
+    m[key] = e;
+    if (!tune_read(path, m, err)) return DMD_E_INPUT;   /* entries another process added meanwhile */
+    m[key] = e;
+    if (!tune_write(path, m, err)) return DMD_E_INPUT;
+    if (cluster) *cluster = c;
+    if (cell_div) *cell_div = d;
+    if (best_ms) *best_ms = ms;
+    if (from_cache) *from_cache = 0;
+    return DMD_OK;
+}
+
 void batch_free(dmd_batch &B) {
     if (B.graph) cudaGraphExecDestroy(B.graph);
     B.graph = nullptr;
+    if (B.cyc_graph) cudaGraphExecDestroy(B.cyc_graph);
+    B.cyc_graph = nullptr;
     for (auto &D : B.ds) if (D.pool) cudaFree(D.pool);
     if (B.pool_all) cudaFree(B.pool_all);
     B.pool_all = nullptr;
@@ -1399,9 +1657,18 @@ int dmd_batch_run_graph(dmd_batch *b, int64_t n_events, int32_t n_launches) {
     if (!b) return DMD_E_INPUT;
     return batch_run_graph(*b, n_events, n_launches);
 }
+int dmd_batch_run_cycles(dmd_batch *b, int64_t n_events, int32_t launches_per_graph, int64_t *n_launches) {
+    if (!b) return DMD_E_INPUT;
+    return batch_run_cycles(*b, n_events, launches_per_graph, n_launches);
+}
 int dmd_batch_autotune(dmd_batch *b, int64_t trial_events, int32_t *cluster, int32_t *cell_div, double *best_ms) {
     if (!b) return DMD_E_INPUT;
     return batch_autotune(*b, trial_events, cluster, cell_div, best_ms);
+}
+int dmd_batch_autotune_cached(dmd_batch *b, int64_t trial_events, const char *cache_path, int32_t *cluster,
+                              int32_t *cell_div, double *best_ms, int32_t *from_cache) {
+    if (!b) return DMD_E_INPUT;
+    return batch_autotune_cached(*b, trial_events, cache_path, cluster, cell_div, best_ms, from_cache);
 }
 int dmd_batch_set_cell_div(dmd_batch *b, int32_t div) {
     if (!b) return DMD_E_INPUT;

@@ -1492,8 +1492,8 @@ static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, i
 
 /* k_run with one cluster of C CTAs per system (C = 1, 2, 4 or 8) */
 cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int compact, long long target,
-                           const long long *targets, int hbonds, const int *chain_start, const int *chain_len,
-                           const int *chain_off, dmd_diag *outputs, cudaStream_t st) {
+                           long long *targets, int hbonds, const int *chain_start, const int *chain_len,
+                           const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles) {
     if (C != 1 && C != 2 && C != 4 && C != 8) return cudaErrorInvalidValue;
     cudaError_t e = k_run_attributes();
     if (e != cudaSuccess) return e;
@@ -1504,9 +1504,9 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int 
     cluster_config(cfg, attr, nsys, C, run_smem(compact, own_cap), st, compact ? RUN_NT_COMPACT : RUN_NT_FULL);
     if (compact)
         return cudaLaunchKernelEx(&cfg, run_compact::k_run, d_systems, nsys, target, targets, hbonds, chain_start,
-                                  chain_len, chain_off, outputs, own_cap, C, std::min(compact, (int)DMD_COMPACT_DN));
+                                  chain_len, chain_off, outputs, own_cap, C, std::min(compact, (int)DMD_COMPACT_DN), cycles);
     return cudaLaunchKernelEx(&cfg, run_full::k_run, d_systems, nsys, target, targets, hbonds, chain_start, chain_len,
-                              chain_off, outputs, own_cap, C, INT_MAX);
+                              chain_off, outputs, own_cap, C, INT_MAX, cycles);
 }
 
 /* how many clusters of C CTAs of k_run can be resident at once */

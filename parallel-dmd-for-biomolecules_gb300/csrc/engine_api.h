@@ -15,10 +15,12 @@ cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t 
  * variant, which takes any list.  compact: 0 = the full variant, k > 0 =
  * the compact one with the down-list limit min(k, DMD_COMPACT_DN). */
 #define DMD_COMPACT_DN 32
-/* targets: per-system event counts (device array), or NULL for target */
+/* targets: per-system event counts (device array), or NULL for target.
+ * cycles != 0: each system also stops after its next list rebuild and
+ * writes the events it still has to run back into targets[r]. */
 cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int compact, long long target,
-                           const long long *targets, int hbonds, const int *chain_start, const int *chain_len,
-                           const int *chain_off, dmd_diag *outputs, cudaStream_t st);
+                           long long *targets, int hbonds, const int *chain_start, const int *chain_len,
+                           const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles = 0);
 cudaError_t dmd_max_active_clusters(int C, int *n);
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st);

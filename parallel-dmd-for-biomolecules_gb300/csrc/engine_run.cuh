@@ -1381,10 +1381,10 @@ __device__ bool warp_footprint_test(const WarpArea &W, const volatile unsigned *
  * selects events and keeps the counters; a batch's candidates go one per
  * warp over all CTAs of the cluster. */
 __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long long target_all,
-                                                     const long long *targets, int hbonds_mask,
+                                                     long long *targets, int hbonds_mask,
                                                      const int *chain_start, const int *chain_len,
                                                      const int *chain_off, dmd_diag *outputs, int own_cap, int C,
-                                                     int dn_limit) {
+                                                     int dn_limit, int cycles) {
     extern __shared__ __align__(16) unsigned char dsmem[];
     WarpArea *warea = reinterpret_cast<WarpArea *>(dsmem);
     __shared__ SharedState sh;
@@ -1981,6 +1981,9 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
             if (leader && threadIdx.x == 0) {
                 sh.sc.n_interval += 1;
                 log_event(S, sh.sc.log_count, sh.sc.coll, t_before, tf, N + 1, -1, rb ? DMD_EV_REBUILD : DMD_EV_INTERVAL, 0);
+                /* rebuild-cycle launches end each system at its list rebuild
+                 * (the nbor/events call of code/main.F90:1151-1166) */
+                if (cycles && rb) sh.sc.stop = 1;
                 if (S.log && S.log_cap > 0) sh.sc.log_count += 1;
                 sh.sc.old_tfalse = sh.sc.tfalse;
                 if (!phys) sh.sc.done += 1;
@@ -2018,6 +2021,8 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
             sh.sc.run_cycles = clock64() - t_start;
             sh.sc.done_all += sh.sc.done;
             *S.sc = sh.sc;
+            /* a rebuild-cycle launch leaves the events still to run */
+            if (cycles && targets) targets[r] = target > sh.sc.done ? target - sh.sc.done : 0;
         }
     }
     if (C > 1) cg::this_cluster().sync();   /* no CTA leaves while others may read its shared memory */

@@ -113,7 +113,7 @@ ENGINE_SYMBOLS = [
     "dmd_generate", "dmd_static_evcode", "dmd_inspect", "dmd_last_run_ms", "dmd_batch_last_run_ms", "dmd_predict_all_noalloc",
     "dmd_batch_set_cluster", "dmd_set_cluster", "dmd_batch_cluster", "dmd_batch_set_cell_div",
     "dmd_batch_set_compact_limit", "dmd_set_compact_limit",
-    "dmd_batch_run_graph", "dmd_batch_autotune", "dmd_batch_device_bytes", "dmd_batch_upload_bytes", "dmd_batch_readback_bytes", "dmd_state_bytes", "dmd_save_state", "dmd_load_state",
+    "dmd_batch_run_graph", "dmd_batch_run_cycles", "dmd_batch_autotune", "dmd_batch_autotune_cached", "dmd_batch_device_bytes", "dmd_batch_upload_bytes", "dmd_batch_readback_bytes", "dmd_state_bytes", "dmd_save_state", "dmd_load_state",
     "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
     "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
     "dmd_sidechain_search", "dmd_sidechain_grid",
@@ -200,8 +200,13 @@ def _declare(lib) -> None:
     lib.dmd_batch_readback_bytes.restype = C.c_int64
     lib.dmd_batch_run_graph.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
     lib.dmd_batch_run_graph.restype = C.c_int
+    lib.dmd_batch_run_cycles.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_int64)]
+    lib.dmd_batch_run_cycles.restype = C.c_int
     lib.dmd_batch_autotune.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dbl_p]
     lib.dmd_batch_autotune.restype = C.c_int
+    lib.dmd_batch_autotune_cached.argtypes = [C.c_void_p, C.c_int64, C.c_char_p, C.POINTER(C.c_int32),
+                                              C.POINTER(C.c_int32), dbl_p, C.POINTER(C.c_int32)]
+    lib.dmd_batch_autotune_cached.restype = C.c_int
     lib.dmd_predict_all_noalloc.argtypes = [C.POINTER(RunCfg), C.POINTER(Tables), C.POINTER(System),
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int32]
     lib.dmd_predict_all_noalloc.restype = C.c_int

@@ -6,6 +6,7 @@ engine and raises if the library or the GPU is unavailable.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -205,13 +206,35 @@ class Batch:
         _check(self.lib.dmd_batch_run_graph(self.h, int(n_events), int(n_launches)), self.lib, self.h,
                "dmd_batch_last_error")
 
-    def autotune(self, trial_events: int = 5000) -> dict:
-        """Pick the cluster size and rebuild grid by timing trial runs on a copy."""
+    def run_cycles(self, n_events: int, launches_per_graph: int = 8) -> int:
+        """n_events per system as rebuild cycles (one neighbour-list rebuild
+        per launch) replayed from a captured CUDA graph; returns the launches."""
+        k = C.c_int64()
+        _check(self.lib.dmd_batch_run_cycles(self.h, int(n_events), int(launches_per_graph), C.byref(k)), self.lib,
+               self.h, "dmd_batch_last_error")
+        return int(k.value)
+
+    def autotune(self, trial_events: int = 5000, cache: str = None) -> dict:
+        """Pick the cluster size and rebuild grid by timing trial runs on a copy;
+        with cache (a JSON file path) a stored choice for the same shapes and
+        device is taken without trials, and a new one is stored."""
         c, d = C.c_int32(), C.c_int32()
         ms = C.c_double()
-        _check(self.lib.dmd_batch_autotune(self.h, int(trial_events), C.byref(c), C.byref(d), C.byref(ms)), self.lib,
-               self.h, "dmd_batch_last_error")
-        return {"cluster": c.value, "cell_div": d.value, "trial_ms": ms.value}
+        if cache is None:
+            _check(self.lib.dmd_batch_autotune(self.h, int(trial_events), C.byref(c), C.byref(d), C.byref(ms)),
+                   self.lib, self.h, "dmd_batch_last_error")
+            return {"cluster": c.value, "cell_div": d.value, "trial_ms": ms.value}
+        hit = C.c_int32()
+        _check(self.lib.dmd_batch_autotune_cached(self.h, int(trial_events), os.fsencode(cache), C.byref(c),
+                                                  C.byref(d), C.byref(ms), C.byref(hit)),
+               self.lib, self.h, "dmd_batch_last_error")
+        return {"cluster": c.value, "cell_div": d.value, "trial_ms": ms.value, "cached": bool(hit.value)}
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def close(self):
         if getattr(self, "h", None):

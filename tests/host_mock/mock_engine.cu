@@ -11,12 +11,14 @@
  */
 #include <algorithm>
 #include <cstdio>
+#include <functional>
 #include <string>
 #include <vector>
 
 #include "engine_api.h"
 
 bool mock_alloc_of(const void *p, const char **base, size_t *n);
+bool mock_capture_push(std::function<void()> f);
 
 namespace {
 std::string g_report;
@@ -24,6 +26,7 @@ int g_init = 0, g_run = 0, g_diag = 0;
 long long g_last_target = -2;
 int g_last_C = 0, g_last_compact = -1;
 int g_handoff = -1;                  /* system that outgrows the compact variant at its next compact launch */
+int g_outgrown = -1;                 /* the system that has outgrown it */
 std::vector<long long> g_last_targets;
 
 struct Span { const char *name; const void *p; size_t n; };
@@ -95,7 +98,7 @@ void check(const char *what, const DSys *d, int nsys, const int *cs, const int *
 
 extern "C" {
 const char *mock_report(void) { return g_report.c_str(); }
-void mock_reset(void) { g_report.clear(); g_init = g_run = g_diag = 0; g_handoff = -1; g_last_targets.clear(); }
+void mock_reset(void) { g_report.clear(); g_init = g_run = g_diag = 0; g_handoff = -1; g_outgrown = -1; g_last_targets.clear(); }
 void mock_set_handoff(int system) { g_handoff = system; }
 long long mock_last_target_of(int system) {
     return system >= 0 && system < (int)g_last_targets.size() ? g_last_targets[system] : -2;
@@ -115,9 +118,16 @@ cudaError_t dmd_launch_init(DSys *d, int nsys, int, cudaStream_t) {
  * per event, and its collision count advances by as much; positions do not
  * move.  The system set by mock_set_handoff stops halfway at its next compact
  * launch with need_full set, as a system whose lists outgrew the compact
- * variant at a rebuild does. */
-cudaError_t dmd_launch_run(DSys *d, int nsys, int, int C, int compact, long long target, const long long *targets,
-                           int, const int *cs, const int *cl, const int *co, dmd_diag *, cudaStream_t) {
+ * variant at a rebuild does, and leaves every later compact launch at once
+ * with need_full set again.  A rebuild-cycle launch (cycles != 0) runs
+ * system r for at most 1000 + 500 r events (its mock rebuild interval) and
+ * writes the rest of its target back.  A launch made during a capture is
+ * recorded and runs when the graph is launched. */
+cudaError_t dmd_launch_run(DSys *d, int nsys, int mb, int C, int compact, long long target, long long *targets,
+                           int hb, const int *cs, const int *cl, const int *co, dmd_diag *out, cudaStream_t st,
+                           int cycles) {
+    if (mock_capture_push([=]() { dmd_launch_run(d, nsys, mb, C, compact, target, targets, hb, cs, cl, co, out, st, cycles); }))
+        return cudaSuccess;
     ++g_run;
     g_last_target = target; g_last_C = C; g_last_compact = compact;
     check("run", d, nsys, cs, cl, co);
@@ -125,13 +135,21 @@ cudaError_t dmd_launch_run(DSys *d, int nsys, int, int C, int compact, long long
     for (int r = 0; r < nsys; ++r) {
         DScal &sc = *d[r].sc;
         long long t = targets ? targets[r] : target;
+        const long long want = t;
         g_last_targets[r] = t;
         sc.need_full = 0;
+        if (cycles) t = std::min(t, 1000LL + 500LL * r);
         if (compact > 0 && r == g_handoff) {
             t = t / 2;
             sc.need_full = 1;
             g_handoff = -1;
+            g_outgrown = r;
+            sc.max_dn = DMD_COMPACT_DN + 1;
+        } else if (compact > 0 && r == g_outgrown) {   /* its lists stay too long: it leaves at once */
+            t = 0;
+            sc.need_full = 1;
         }
+        if (cycles && targets) targets[r] = want - t;
         sc.done = t;
         sc.done_all += t;
         sc.coll += t;

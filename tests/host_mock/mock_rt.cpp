@@ -11,9 +11,20 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <vector>
 
 struct MockAlloc { size_t n; bool dev; };
+struct MockGraph { std::vector<std::function<void()>> ops; };
+static MockGraph *g_capture = nullptr;
+static int g_graph_launches = 0;
+/* a launch made while a capture is open is recorded, not run */
+bool mock_capture_push(std::function<void()> f) {
+    if (!g_capture) return false;
+    g_capture->ops.push_back(std::move(f));
+    return true;
+}
 static std::map<uintptr_t, MockAlloc> g_allocs;
 
 /* the allocation holding p: its base and size */
@@ -67,15 +78,45 @@ cudaError_t cudaEventSynchronize(cudaEvent_t) { return cudaSuccess; }
 cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t, cudaEvent_t) { *ms = 1.0f; return cudaSuccess; }
 cudaError_t cudaGetLastError(void) { return cudaSuccess; }
 const char *cudaGetErrorString(cudaError_t) { return "mock runtime error"; }
+cudaError_t cudaGetDevice(int *d) { *d = 0; return cudaSuccess; }
+/* a GB300: compute capability 10.3, 152 SMs */
+cudaError_t cudaDeviceGetAttribute(int *v, cudaDeviceAttr a, int) {
+    *v = a == cudaDevAttrComputeCapabilityMajor ? 10 : a == cudaDevAttrComputeCapabilityMinor ? 3
+       : a == cudaDevAttrMultiProcessorCount ? 152 : 0;
+    return cudaSuccess;
+}
 cudaError_t cudaMemGetInfo(size_t *f, size_t *t) { *f = (size_t)100 << 30; *t = (size_t)200 << 30; return cudaSuccess; }
 cudaError_t cudaGetSymbolAddress(void **, const void *) { return cudaErrorInvalidSymbol; }
-cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus *s) { *s = cudaStreamCaptureStatusNone; return cudaSuccess; }
-cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) { return cudaErrorNotSupported; }
-cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t *) { return cudaErrorNotSupported; }
-cudaError_t cudaGraphInstantiate(cudaGraphExec_t *, cudaGraph_t, unsigned long long) { return cudaErrorNotSupported; }
-cudaError_t cudaGraphLaunch(cudaGraphExec_t, cudaStream_t) { return cudaErrorNotSupported; }
-cudaError_t cudaGraphDestroy(cudaGraph_t) { return cudaSuccess; }
-cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
+/* graphs: a capture records the launches made on the stream (the stand-in
+ * launches push themselves through mock_capture_push) and a graph launch
+ * runs them in order */
+cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus *s) {
+    *s = g_capture ? cudaStreamCaptureStatusActive : cudaStreamCaptureStatusNone;
+    return cudaSuccess;
+}
+cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) {
+    if (g_capture) return cudaErrorIllegalState;
+    g_capture = new MockGraph;
+    return cudaSuccess;
+}
+cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t *g) {
+    if (!g_capture) return cudaErrorIllegalState;
+    *g = (cudaGraph_t)g_capture;
+    g_capture = nullptr;
+    return cudaSuccess;
+}
+cudaError_t cudaGraphInstantiate(cudaGraphExec_t *e, cudaGraph_t g, unsigned long long) {
+    *e = (cudaGraphExec_t) new MockGraph(*(MockGraph *)g);
+    return cudaSuccess;
+}
+cudaError_t cudaGraphLaunch(cudaGraphExec_t e, cudaStream_t) {
+    ++g_graph_launches;
+    for (auto &f : ((MockGraph *)e)->ops) f();
+    return cudaSuccess;
+}
+cudaError_t cudaGraphDestroy(cudaGraph_t g) { delete (MockGraph *)g; return cudaSuccess; }
+cudaError_t cudaGraphExecDestroy(cudaGraphExec_t e) { delete (MockGraph *)e; return cudaSuccess; }
+int mock_graph_launches(void) { return g_graph_launches; }
 void **__cudaRegisterFatBinary(void *) { static void *h = nullptr; return &h; }
 void __cudaRegisterFatBinaryEnd(void **) {}
 void __cudaUnregisterFatBinary(void **) {}

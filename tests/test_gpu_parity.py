@@ -235,6 +235,51 @@ def test_graph_replay_and_grid(built):
     g.close()
 
 
+def test_autotune_cache(built, tmp_path):
+    """The autotuner's choice kept in a JSON file is taken by a second batch
+    of the same replicas without trials."""
+    specs = systems.config_c3(32, seed=4)[:4]
+    for s in specs:
+        systems.generate(s)
+    path = str(tmp_path / "tune.json")
+    with Batch(specs) as b:
+        first = b.autotune(3000, cache=path)
+    with Batch(specs) as b:
+        again = b.autotune(3000, cache=path)
+        b.run(2000)
+        assert b.lib.dmd_batch_cluster(b.h) == first["cluster"]
+    assert not first["cached"] and again["cached"]
+    assert (again["cluster"], again["cell_div"]) == (first["cluster"], first["cell_div"])
+
+
+def test_rebuild_cycle_graph(built):
+    """Rebuild cycles replayed from a captured CUDA graph (each launch ends
+    every system at its next neighbour-list rebuild) commit the same events
+    as one plain run, and take at least one launch per rebuild."""
+    specs = systems.config_c3(32, seed=3)[:3]
+    for s in specs:
+        systems.generate(s)
+    ref = Batch(specs)
+    ref.run(30000)
+    want = [ref.state(r) for r in range(3)]
+    ref.close()
+    g = Batch(specs)
+    u0 = [g.diagnostics(r)["n_updates"] for r in range(3)]
+    k1 = g.run_cycles(15000, 2)
+    u1 = [g.diagnostics(r)["n_updates"] for r in range(3)]
+    k2 = g.run_cycles(15000, 2)   # the second call replays the same graph
+    u2 = [g.diagnostics(r)["n_updates"] for r in range(3)]
+    for r in range(3):
+        st = g.state(r)
+        for key in ("x", "y", "z", "vx", "vy", "vz", "bptnr", "identity"):
+            assert np.array_equal(st[key], want[r][key]), (r, key)
+        assert st["coll"] == want[r]["coll"]
+    assert max(b - a for a, b in zip(u0, u1)) >= 1
+    assert k1 >= max(b - a for a, b in zip(u0, u1)) and k1 % 2 == 0
+    assert k2 >= max(b - a for a, b in zip(u1, u2)) and k2 % 2 == 0
+    g.close()
+
+
 def test_autotune_keeps_state(built):
     specs = systems.config_c3(32, seed=4)[:4]
     for s in specs:
@@ -299,8 +344,8 @@ def test_compact_variant_hands_over(built):
 
 def test_compact_variant_batch_and_graph(built):
     """Replicas that cross the compact limit at different times, in a batch
-    run and in graph replay: the follow-up full launches give every replica
-    the events of one plain run."""
+    run, in graph replay and in rebuild-cycle replay: the follow-up full
+    launches give every replica the events of one plain run."""
     specs = systems.config_c3(32, seed=5)[:4]
     for s in specs:
         systems.generate(s)
@@ -312,10 +357,12 @@ def test_compact_variant_batch_and_graph(built):
     b0 = Batch(specs)
     limit = min(32, max(b0.diagnostics(r)["max_down"] for r in range(4)))
     b0.close()
-    for graph in (False, True):
+    for graph in (False, True, "cycles"):
         b = Batch(specs)
         b.set_compact_limit(limit)
-        if graph:
+        if graph == "cycles":
+            b.run_cycles(16000, 3)
+        elif graph:
             b.run_graph(4000, 4)
         else:
             b.run(16000)

@@ -312,6 +312,90 @@ def test_compact_variant_hands_over_to_the_full_one(mock):
     mock.dmd_batch_destroy(h)
 
 
+def test_rebuild_cycle_graph_replays_until_every_target(mock):
+    """dmd_batch_run_cycles captures its launches once and replays the graph
+    until every system has run its events; each launch takes the remaining
+    counts the previous one wrote back.  In the stand-in, system r runs at
+    most 1000 + 500 r events per launch (its rebuild interval), so 5000
+    events take 5, 4, 3 and 3 launches; system 2 hands over to the full
+    variant halfway through its first launch and makes no progress in the
+    second (compact) one: three replays of two launches, the last two on
+    the full variant."""
+    mock.mock_set_handoff.argtypes = [C.c_int]
+    specs = [systems.generate(systems.klvffae_system(3, 5.0, 0.2 + 0.02 * r, seed=40 + r)) for r in range(4)]
+    n = len(specs)
+    tabs = abi.tables_struct(default_tables())
+    cfgs = (abi.RunCfg * n)(*[s.run_cfg(0, 0) for s in specs])
+    syss = (abi.System * n)(*[s.c_system() for s in specs])
+    mock.mock_reset()
+    h = C.c_void_p()
+    assert mock.dmd_batch_create(n, cfgs, C.byref(tabs), syss, C.byref(h)) == 0
+    g0 = mock.mock_graph_launches()
+    mock.mock_set_handoff(2)
+    k = C.c_int64()
+    assert mock.dmd_batch_run_cycles(h, 5000, 2, C.byref(k)) == 0, mock.dmd_batch_last_error(h)
+    init, run, diag, target, C_, compact = counts(mock)
+    assert k.value == 6 and run == 6 and mock.mock_graph_launches() - g0 == 3
+    assert compact == 0                                         # recaptured on the full variant
+    for r, s in enumerate(specs):
+        assert state_of(mock, h, r, s.n_beads)[3] == 5000
+    # a second call reuses the full-variant graph: every system starts again
+    assert mock.dmd_batch_run_cycles(h, 1000, 2, C.byref(k)) == 0
+    assert k.value == 2
+    for r, s in enumerate(specs):
+        assert state_of(mock, h, r, s.n_beads)[3] == 6000
+    assert mock.dmd_batch_run_cycles(h, 10, 0, None) == -1     # no launches per graph
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    mock.dmd_batch_destroy(h)
+
+
+def test_autotune_cache_file(mock, tmp_path):
+    """The autotuner's choice is kept in a JSON file: the first batch of a
+    shape runs the trials and stores its choice, a second batch of the same
+    shapes takes it without a launch, another shape adds an entry, and a
+    file that is not a cache is refused and left as it was."""
+    import json
+
+    def make(k, seed):
+        specs = [systems.generate(systems.klvffae_system(k, 5.0, 0.2, seed=seed + r)) for r in range(3)]
+        tabs = abi.tables_struct(default_tables())
+        cfgs = (abi.RunCfg * 3)(*[s.run_cfg(0, 0) for s in specs])
+        syss = (abi.System * 3)(*[s.c_system() for s in specs])
+        h = C.c_void_p()
+        assert mock.dmd_batch_create(3, cfgs, C.byref(tabs), syss, C.byref(h)) == 0
+        return h
+
+    path = str(tmp_path / "tune.json")
+    c, d, ms, hit = C.c_int32(), C.c_int32(), C.c_double(), C.c_int32()
+    mock.mock_reset()
+    h = make(3, 50)
+    assert mock.dmd_batch_autotune_cached(h, 2000, path.encode(), C.byref(c), C.byref(d), C.byref(ms), C.byref(hit)) == 0
+    runs = counts(mock)[1]
+    assert hit.value == 0 and runs > 0
+    doc = json.load(open(path))
+    assert doc["format"] == "dmd-autotune-1" and len(doc["entries"]) == 1
+    (key, e), = doc["entries"].items()
+    assert key.startswith("cc10.3/sm152/") and e["cluster"] == c.value and e["cell_div"] == d.value
+    assert e["systems"] == 3 and e["trial_events"] == 2000
+    mock.dmd_batch_destroy(h)
+    h = make(3, 50)
+    assert mock.dmd_batch_autotune_cached(h, 2000, path.encode(), C.byref(c), C.byref(d), C.byref(ms), C.byref(hit)) == 0
+    assert hit.value == 1 and counts(mock)[1] == runs          # no trial launch
+    assert c.value == e["cluster"] and d.value == e["cell_div"]
+    assert mock.dmd_batch_run(h, 100, None) == 0 and mock.dmd_batch_cluster(h) == e["cluster"]
+    mock.dmd_batch_destroy(h)
+    h = make(4, 60)
+    assert mock.dmd_batch_autotune_cached(h, 2000, path.encode(), None, None, None, C.byref(hit)) == 0
+    assert hit.value == 0 and len(json.load(open(path))["entries"]) == 2
+    bad = tmp_path / "other.json"
+    bad.write_text('{"format": "something else", "entries": {}}')
+    assert mock.dmd_batch_autotune_cached(h, 2000, str(bad).encode(), None, None, None, None) == -1
+    assert b"not a dmd-autotune-1 file" in mock.dmd_batch_last_error(h)
+    assert bad.read_text() == '{"format": "something else", "entries": {}}'
+    mock.dmd_batch_destroy(h)
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+
+
 def test_server_step_books_a_failed_read_back(mock):
     """A result read-back that fails while a finished request is retired
     fails that request alone: its pool is freed and it leaves the active
