@@ -55,7 +55,16 @@ def build(verbose: bool = False, extra: list | None = None) -> str:
     srcs = CU_SOURCES + CPP_SOURCES
     newest = max(os.path.getmtime(os.path.join(CSRC, f)) for f in os.listdir(CSRC))
     newest = max(newest, os.path.getmtime(os.path.join(REPO, "include", "dmd.h")), os.path.getmtime(__file__))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= newest and not extra:
+    # the extra flags the library was built with: a library built with
+    # other flags (a debug build with timers, say) is rebuilt, not reused
+    flags_file = os.path.join(OUT, "build.flags")
+    want_flags = " ".join(extra or [])
+    try:
+        with open(flags_file) as fh:
+            have_flags = fh.read()
+    except OSError:
+        have_flags = None
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= newest and not extra and have_flags == want_flags:
         return LIB
     objs, cmds = [], []
     for s in srcs:
@@ -74,6 +83,8 @@ def build(verbose: bool = False, extra: list | None = None) -> str:
     tmp = LIB + ".tmp"
     _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
     os.replace(tmp, LIB)
+    with open(flags_file, "w") as fh:
+        fh.write(want_flags)
     if CHECKED:
         open(os.path.join(OUT, "checked.stamp"), "w").close()
     return LIB

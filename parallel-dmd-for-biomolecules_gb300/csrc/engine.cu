@@ -117,6 +117,16 @@ __device__ long long g_lsub_last;
             g_lsub_last = now_;                                                            \
         }                                                                                  \
     } while (0)
+/* steps of a light collision on warp 0 of CTA g_sub_cta (row DMD_PHASE_CTAS - 7) */
+__device__ long long g_csub_last;
+#define DMD_CSUB(k)                                                                        \
+    do {                                                                                   \
+        if (blockIdx.x == g_sub_cta && threadIdx.x == 0) {                                 \
+            long long now_ = clock64();                                                    \
+            if ((k) >= 0) g_phase_cycles[DMD_PHASE_CTAS - 7][(k)] += now_ - g_csub_last;   \
+            g_csub_last = now_;                                                            \
+        }                                                                                  \
+    } while (0)
 /* sub-phases of the candidate gather, per CTA (rows 512 + block index) */
 #define DMD_GSUB_START() long long gs_t_ = clock64()
 #define DMD_GSUB(k)                                                                        \
@@ -130,6 +140,7 @@ __device__ long long g_lsub_last;
 #else
 #define DMD_GSUB_START() do { } while (0)
 #define DMD_LSUB(k) do { } while (0)
+#define DMD_CSUB(k) do { } while (0)
 #define DMD_GSUB(k) do { } while (0)
 #define DMD_PHASE_START(row) do { (void)(row); } while (0)
 #define DMD_PHASE(k) do { (void)(k); } while (0)
@@ -398,18 +409,30 @@ __device__ __forceinline__ int cell_coord(double p, int nc) {
 struct ListStage {
     const float *xf, *yf, *zf;
     int *cell_of, *cell_count, *cell_start, *cell_beads;
+    BeadInfo *info;     /* the bead records, or null: the system's array */
+    uint8_t *ovf;       /* 1 where a bead has an override slot in use (null with info) */
 };
+/* Staging order, each part only if it and the ones before it fit: positions,
+ * cells and sorted beads (20 B per bead); bead records and override flags
+ * (sizeof(BeadInfo) + 1 B per bead); cell counts and starts. */
 __device__ ListStage list_stage(const DSys &S, char *scr, int scr_bytes) {
     const int N = S.N, nc = S.ncell;
     const size_t nc3 = (size_t)nc * nc * nc;
-    ListStage L{S.xf, S.yf, S.zf, nullptr, S.cell_count, S.cell_start, S.cell_beads};
+    ListStage L{S.xf, S.yf, S.zf, nullptr, S.cell_count, S.cell_start, S.cell_beads, nullptr, nullptr};
     if (scr == nullptr || (size_t)20 * N > (size_t)scr_bytes) return L;
     float *f = reinterpret_cast<float *>(scr);
     L.xf = f; L.yf = f + N; L.zf = f + 2 * N;
     L.cell_of = reinterpret_cast<int *>(f + 3 * N);
     L.cell_beads = L.cell_of + N;
-    if ((size_t)20 * N + 4 * (2 * nc3 + 1) <= (size_t)scr_bytes) {
-        L.cell_count = L.cell_beads + N;
+    size_t used = (size_t)20 * N;
+    const size_t info_bytes = ((sizeof(BeadInfo) * (size_t)N + (size_t)N) + 15) & ~(size_t)15;
+    if (used + info_bytes <= (size_t)scr_bytes) {
+        L.info = reinterpret_cast<BeadInfo *>(scr + used);
+        L.ovf = reinterpret_cast<uint8_t *>(scr + used + sizeof(BeadInfo) * (size_t)N);
+        used += info_bytes;
+    }
+    if (used + 4 * (2 * nc3 + 1) <= (size_t)scr_bytes) {
+        L.cell_count = reinterpret_cast<int *>(scr + used);
         L.cell_start = L.cell_count + nc3;
     }
     return L;
@@ -468,7 +491,7 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, cons
         int nu = 0, nd = 0;
         int *up = S.up + (size_t)b * S.cap, *dn = S.dn + (size_t)b * S.cap;
         int8_t *upc = S.upc + (size_t)b * S.cap;
-        const BeadInfo ib = S.info[b];
+        const BeadInfo ib = L.info ? L.info[b] : S.info[b];
         const float xbf = L.xf[b], ybf = L.yf[b], zbf = L.zf[b];
         auto consider = [&](int c) {
             if (c == b) return;
@@ -480,18 +503,21 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, cons
             float fx = xbf - L.xf[c], fy = ybf - L.yf[c], fz = zbf - L.zf[c];
             fx = fx - rintf(fx); fy = fy - rintf(fy); fz = fz - rintf(fz);
             const float r2f = fx * fx + fy * fy + fz * fz;
-            const BeadInfo ic = S.info[c];
+            const BeadInfo ic = L.info ? L.info[c] : S.info[c];
+            /* a bead without any override: its pair codes are the rule's */
+            const bool no_ov = L.ovf && !L.ovf[c];
             /* Beyond every pair type's cutoff: listed only as a bond pair
              * (same chain, residues at most 2 apart) or through an override */
             if (r2f > far_f) {
                 const int dres = ic.res - ib.res;
                 if (ic.chain != ib.chain || dres < -2 || dres > 2) {
+                    if (no_ov) return;
                     const int *op = S.ovp + 4 * c;
                     if (op[0] != b && op[1] != b && op[2] != b && op[3] != b) return;
                 }
             }
             int st = static_code(ic, ib, hbonds);
-            int code = pair_code_st(S, c, b, st);
+            int code = no_ov ? st : pair_code_st(S, c, b, st);
             bool take;
             if ((code >= 4 && code <= 12) || (code >= 17 && code < 27)) take = true;
             else {
@@ -762,6 +788,11 @@ __device__ void cta_rebuild(const DSys &S, SharedState &sh, ScratchRef fr, int h
             float *sx = const_cast<float *>(L.xf);
             sx[b] = fx; sx[b + S.N] = fy; sx[b + 2 * S.N] = fz;
             if (nc >= 3) L.cell_of[b] = (cell_coord(pz, nc) * nc + cell_coord(py, nc)) * nc + cell_coord(px, nc);
+        }
+        if (L.info) {
+            L.info[b] = S.info[b];
+            const int *op = S.ovp + 4 * b;
+            L.ovf[b] = (op[0] >= 0) | (op[1] >= 0) | (op[2] >= 0) | (op[3] >= 0);
         }
     }
     __syncthreads();

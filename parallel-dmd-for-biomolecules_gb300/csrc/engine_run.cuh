@@ -488,21 +488,69 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
     const int lane = threadIdx.x & 31, hl = lane & 15;
     const unsigned hbase = lane & 16;          /* first lane of this half */
     const DTab &T = *S.tab;
-    /* every load that needs only i and j, issued together: lanes 0..11 of
-     * the half hold the positions and velocities of i (0..5) and j (6..11),
-     * which are also the snapshot of what the collision writes */
+    /* Two rounds of loads.  The first holds every load that needs only i
+     * and j: lanes 0..11 of the half the positions and velocities of i
+     * (0..5) and j (6..11), which are also the snapshot of what the
+     * collision writes; lane 0 the coltype, identities, masses, bond
+     * windows and everything the pair code is made of (the overrides of i
+     * and both bead records, taken whether or not an override applies).
+     * The second, on lane 0, the tables indexed by the identities and the
+     * pair code. */
+    DMD_CSUB(-1);
     const int fb = hl < 6 ? i : j, ff = hl % 6;
     const double *A = ff == 0 ? S.x : ff == 1 ? S.y : ff == 2 ? S.z : ff == 3 ? S.vx : ff == 4 ? S.vy : S.vz;
     const double mine = hl < 12 ? A[fb] : 0.0;
-    const int ct = S.colt[i];
-    const int a = S.ident[i], b = S.ident[j];
-    const int evcode = pair_code(S, i, j, hbonds);
+    int ct = 0, evcode = 0;
+    double rm = 0.0, R = 1.0, rR = 1.0, bmi = 0.0, bmj = 0.0, rbmi = 0.0, rbmj = 0.0;
+    if (hl == 0) {
+        ct = S.colt[i];
+        const int a = S.ident[i], b = S.ident[j];
+        const int o0 = S.ovp[4 * i], o1 = S.ovp[4 * i + 1], o2 = S.ovp[4 * i + 2], o3 = S.ovp[4 * i + 3];
+        const int c0 = S.ovc[4 * i], c1 = S.ovc[4 * i + 1], c2 = S.ovc[4 * i + 2], c3 = S.ovc[4 * i + 3];
+        const BeadInfo ia = S.info[i], ib = S.info[j];
+        bmi = S.bm[i]; bmj = S.bm[j];
+        const double lo_s = S.blmin_sq[i], rlo_s = S.rblmin_sq[i], hi_s = S.blmax_sq[i], rhi_s = S.rblmax_sq[i];
+        const int bp = S.bptnr[i];
+        /* pair_code(): the first override slot holding j, else the rule */
+        evcode = o0 == j ? c0 : o1 == j ? c1 : o2 == j ? c2 : o3 == j ? c3 : static_code(ia, ib, hbonds);
+        /* second round: the reduced mass, the reciprocal masses and the
+         * squared diameter of the wall met (warp_eventdyn, coltypes 1-3) */
+        rm = T.rmass[a][b];
+        rbmi = T.rbm[a]; rbmj = T.rbm[b];   /* bm(b) = mass(identity(b)) */
+        const bool side = evcode >= 10 && evcode <= 12;
+        if (ct == 2) {
+            R = side ? lo_s : T.evp2_sq[evcode];
+            rR = side ? rlo_s : T.revp2_sq[evcode];
+        } else if (ct == 3) {
+            R = side ? hi_s : T.evp3_sq[evcode];
+            rR = side ? rhi_s : T.revp3_sq[evcode];
+        } else if (ct == 1) {
+            if (evcode == 15) {
+                const bool hb = bp == j;
+                R = hb ? T.core15_sq[a][b] : T.sigma_sq[a][b];
+                rR = hb ? T.rcore15_sq[a][b] : T.rsigma_sq[a][b];
+            } else if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {
+                const int sl = core_slot_d(evcode);
+                R = T.core_sq[sl][a][b];
+                rR = T.rcore_sq[sl][a][b];
+            } else {
+                /* the other codes with a core (16: inside a hydrophobic well;
+                 * 40/50: under a shoulder): eventdyn.f's sigma_sq *
+                 * ev_param(1,code)**2 with ev_param(1,code) = 1, which is
+                 * sigma_sq */
+                R = T.sigma_sq[a][b];
+                rR = T.rsigma_sq[a][b];
+            }
+        }
+    }
     if (has && hl < 12) W.sij[hl] = mine;
     if (has && hl == 0) { W.nmeta = 0; W.colt_i = (int8_t)ct; }
+    DMD_CSUB(4);
     /* relative position and velocity (warp_rel), lanes 0..2 of the half */
     const int d = hl % 3;
     const double xi = __shfl_sync(FULL, mine, hbase + d), vi = __shfl_sync(FULL, mine, hbase + 3 + d);
     const double xj = __shfl_sync(FULL, mine, hbase + 6 + d), vj = __shfl_sync(FULL, mine, hbase + 9 + d);
+    DMD_CSUB(0);
     const double v = vi - vj;
     double r = xi - xj + v * tf;
     r = d_wrap(r);
@@ -516,37 +564,16 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
     const double s2 = hl == 0 ? b2 : (hl == 1 ? r2 : v2);
     const double sum = s0 + s1 + s2;
     const double bij = __shfl_sync(FULL, sum, 0, 16);
+    DMD_CSUB(1);
     /* the impulse ratio (warp_eventdyn, coltypes 1-3) on lane 0 of the half */
     double ratio = 0.0;
-    if (hl == 0) {
-        const double rmass = T.rmass[a][b];
-        const bool side = evcode >= 10 && evcode <= 12;
-        if (ct == 2) {
-            const double lo = side ? S.blmin_sq[i] : T.evp2_sq[evcode];
-            const double rlo = side ? S.rblmin_sq[i] : T.revp2_sq[evcode];
-            ratio = div_by(rmass * bij, lo, rlo);
-        } else if (ct == 3) {
-            const double hi = side ? S.blmax_sq[i] : T.evp3_sq[evcode];
-            const double rhi = side ? S.rblmax_sq[i] : T.revp3_sq[evcode];
-            ratio = div_by(rmass * bij, hi, rhi);
-        } else if (ct == 1) {
-            if (evcode == 15) {
-                const bool hb = S.bptnr[i] == j;
-                ratio = div_by(rmass * bij, hb ? T.core15_sq[a][b] : T.sigma_sq[a][b],
-                               hb ? T.rcore15_sq[a][b] : T.rsigma_sq[a][b]);
-            } else if (evcode <= 3 || (evcode >= 17 && evcode <= 26)) {
-                const int sl = core_slot_d(evcode);
-                ratio = div_by(rmass * bij, T.core_sq[sl][a][b], T.rcore_sq[sl][a][b]);
-            } else {
-                /* the other codes with a core (16: inside a hydrophobic well;
-                 * 40/50: under a shoulder): eventdyn.f's sigma_sq *
-                 * ev_param(1,code)**2 with ev_param(1,code) = 1, which is
-                 * sigma_sq */
-                ratio = div_by(rmass * bij, T.sigma_sq[a][b], T.rsigma_sq[a][b]);
-            }
-        }
-    }
+    if (hl == 0 && ct >= 1 && ct <= 3) ratio = div_by(rm * bij, R, rR);
     ratio = __shfl_sync(FULL, ratio, 0, 16);
+    const double bm_i = __shfl_sync(FULL, bmi, 0, 16), bm_j = __shfl_sync(FULL, bmj, 0, 16);
+    const double rbm_i = __shfl_sync(FULL, rbmi, 0, 16), rbm_j = __shfl_sync(FULL, rbmj, 0, 16);
+    ct = __shfl_sync(FULL, ct, 0, 16);
+    evcode = __shfl_sync(FULL, evcode, 0, 16);
+    DMD_CSUB(2);
     /* the impulse (warp_impulse without a bump), lanes 0..5 of the half;
      * the position and velocity are the values held above (lanes 0..5:
      * position of component dd, lanes 3..5 of i hold velocities, so the
@@ -561,7 +588,7 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
         double *PP = dd == 0 ? S.x : (dd == 1 ? S.y : S.z);
         double *VV = dd == 0 ? S.vx : (dd == 1 ? S.vy : S.vz);
         const double rr = dd == 0 ? rx : (dd == 1 ? ry : rz);
-        const double bmb = S.bm[bb], rbmb = T.rbm[isj ? b : a];   /* bm(b) = mass(identity(b)) */
+        const double bmb = isj ? bm_j : bm_i, rbmb = isj ? rbm_j : rbm_i;
         const double delv = ratio * rr;
         const double dv = div_by(delv, bmb, rbmb);
         const double dp = div_by(delv * tf, bmb, rbmb);
@@ -573,6 +600,7 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
         W.ct = ct; W.evcode = evcode; W.xpulse = 0;
     }
     __syncwarp();
+    DMD_CSUB(3);
 }
 
 /* The ghost collision of lane_ghost() on a warp, with the same draws and
