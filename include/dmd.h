@@ -153,6 +153,9 @@ typedef struct dmd_diag {
      * repuls_check, and unbonded NH-CO pairs inside their well whose
      * geometry passes it (0 and 0 in a consistent state) */
     int64_t nc_boundbad, nc_unboundbad;
+    /* SM clock cycles the system's (leader) CTA spent in its last event-loop
+     * launch (0 before any, and in the CPU restatement) */
+    int64_t run_cycles;
 } dmd_diag;
 
 typedef struct dmd_handle dmd_handle;

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -816,12 +817,12 @@ int batch_run(dmd_batch &B, int64_t n_events, dmd_event_log *logs) {
     }
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
     CK(cudaEventRecord(B.ev0, B.st));
-    int max_beads = 0;
-    for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
+    int max_beads = 0, min_beads = INT_MAX;
+    for (const HostSys &H : B.hs) { max_beads = std::max(max_beads, H.N); min_beads = std::min(min_beads, H.N); }
     int C = B.cluster > 0 ? B.cluster : auto_cluster(n);
     B.last_cluster = C;
     CK(dmd_launch_run(B.d_sys, n, max_beads, C, compact, (long long)n_events, nullptr, B.hbonds, B.d_cstart, B.d_clen,
-                      B.d_coff, nullptr, B.st));
+                      B.d_coff, nullptr, B.st, 0, min_beads));
     CK(cudaEventRecord(B.ev1, B.st));
     int rc = sync_check(B);
     if (rc == DMD_OK && compact) {
@@ -946,8 +947,8 @@ int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
         done0[r] = sc.done_all;
         if (sc.max_dn > B.compact_dn) compact = 0;
     }
-    int max_beads = 0;
-    for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
+    int max_beads = 0, min_beads = INT_MAX;
+    for (const HostSys &H : B.hs) { max_beads = std::max(max_beads, H.N); min_beads = std::min(min_beads, H.N); }
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
     if (!B.graph || B.graph_events != n_events || B.graph_launches != n_launches || B.graph_cluster != C ||
         B.graph_compact != compact) {
@@ -958,7 +959,7 @@ int batch_run_graph(dmd_batch &B, int64_t n_events, int n_launches) {
         cudaError_t ce = cudaSuccess;
         for (int k = 0; k < n_launches && ce == cudaSuccess; ++k)
             ce = dmd_launch_run(B.d_sys, n, max_beads, C, compact, (long long)n_events, nullptr, B.hbonds, B.d_cstart,
-                                B.d_clen, B.d_coff, nullptr, B.st);
+                                B.d_clen, B.d_coff, nullptr, B.st, 0, min_beads);
         cudaError_t ce2 = cudaStreamEndCapture(B.st, &g);
         if (ce != cudaSuccess) { err = cudaGetErrorString(ce); if (ce2 == cudaSuccess) cudaGraphDestroy(g); return DMD_E_CUDA; }
         CK(ce2);
@@ -1023,8 +1024,8 @@ int batch_run_cycles(dmd_batch &B, int64_t n_events, int per_graph, int64_t *lau
         CK(cudaMemcpy(&sc, B.ds[r].d.sc, sizeof sc, cudaMemcpyDeviceToHost));
         if (sc.max_dn > B.compact_dn) compact = 0;
     }
-    int max_beads = 0;
-    for (const HostSys &H : B.hs) max_beads = std::max(max_beads, H.N);
+    int max_beads = 0, min_beads = INT_MAX;
+    for (const HostSys &H : B.hs) { max_beads = std::max(max_beads, H.N); min_beads = std::min(min_beads, H.N); }
     CK(cudaMemcpy(B.d_sys, hd.data(), n * sizeof(DSys), cudaMemcpyHostToDevice));
     if (!B.d_targets) CK(cudaMalloc(&B.d_targets, (size_t)n * sizeof(long long)));
     std::vector<long long> rem(n, (long long)n_events);
@@ -1042,7 +1043,7 @@ int batch_run_cycles(dmd_batch &B, int64_t n_events, int per_graph, int64_t *lau
             cudaError_t ce = cudaSuccess;
             for (int k = 0; k < per_graph && ce == cudaSuccess; ++k)
                 ce = dmd_launch_run(B.d_sys, n, max_beads, C, compact, 0, B.d_targets, B.hbonds, B.d_cstart, B.d_clen,
-                                    B.d_coff, nullptr, B.st, 1);
+                                    B.d_coff, nullptr, B.st, 1, min_beads);
             cudaError_t ce2 = cudaStreamEndCapture(B.st, &g);
             if (ce != cudaSuccess) { err = cudaGetErrorString(ce); if (ce2 == cudaSuccess) cudaGraphDestroy(g); return DMD_E_CUDA; }
             CK(ce2);
@@ -1479,7 +1480,7 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
         std::vector<DSys> hd(n);
         std::vector<long long> tg(n);
         std::vector<int> cstart, clen, coff;
-        int max_beads = 0;
+        int max_beads = 0, min_beads = INT_MAX;
         /* Balance the round: every request gets about the SM time that
          * the typical one needs for chunk events (from each request's
          * measured cycles per event), so that no CTA idles while the
@@ -1501,6 +1502,7 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
             coff.push_back((int)cstart.size());
             for (int c = 0; c < R.H.nchains; ++c) { cstart.push_back(R.H.chain_start[c]); clen.push_back(R.H.chain_len[c]); }
             max_beads = std::max(max_beads, R.H.N);
+            min_beads = std::min(min_beads, R.H.N);
         }
         int rc = server_grow(V, n, cstart.size());
         if (rc != DMD_OK) return rc;
@@ -1516,7 +1518,7 @@ int server_step(dmd_server &V, int32_t *n_active, int32_t *n_finished) {
         int compact = DMD_COMPACT_DN;
         for (ServerReq *R : act) if (R->H.sc.max_dn > DMD_COMPACT_DN) compact = 0;
         CK(dmd_launch_run(V.d_sys, n, max_beads, 1, compact, 0, V.d_targets, V.hbonds, V.d_cstart, V.d_clen, V.d_coff,
-                          nullptr, V.run_st));
+                          nullptr, V.run_st, 0, min_beads));
         CK(cudaEventRecord(V.e1, V.run_st));
         CK(dmd_launch_diag(V.d_sys, n, V.d_cstart, V.d_clen, V.d_coff, V.d_diag, V.run_st));
         /* From here on requests change state (admitted, retired, failed):

@@ -1131,6 +1131,7 @@ __device__ void cta_diag(const DSys &S, SharedState &sh, const int *chain_start,
         out->max_down = sh.sc.max_dn;
         out->nc_boundbad = boundbad;
         out->nc_unboundbad = unboundbad;
+        out->run_cycles = sh.sc.run_cycles;
     }
     __syncthreads();
 }
@@ -1350,6 +1351,59 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
 }
 
 /* ------------------------------------------------------------------ */
+/* hot per-bead arrays of a small system in shared memory (k_run)      */
+/* ------------------------------------------------------------------ */
+struct HotArrays {
+    double *x, *y, *z, *vx, *vy, *vz, *tim;
+    long long *key, *l1k;
+    int *nptnr, *l1i;
+    int8_t *colt;
+    uint8_t *queued;
+};
+/* bytes of the hot arrays of a system of N beads and nl1 level-1 groups */
+__host__ __device__ constexpr size_t hot_bytes(int N, int nl1) {
+    const size_t n = (size_t)N, n3 = n + 3, g = (size_t)nl1;
+    return ((48 * n + 16 * n3 + 8 * g + 4 * n3 + 4 * g + 2 * n3) + 15) & ~(size_t)15;
+}
+/* where they start: after the event areas and task pool (base bytes) and
+ * the claim tables of own_cap beads, on a 16-byte boundary */
+__host__ __device__ constexpr size_t hot_offset(size_t base, int own_cap) {
+    return (base + (size_t)own_cap * 3 * sizeof(unsigned) + 15) & ~(size_t)15;
+}
+__device__ __forceinline__ HotArrays hot_layout(char *p, int N, int nl1) {
+    HotArrays H;
+    const size_t n = (size_t)N, n3 = n + 3;
+    H.x = (double *)p; H.y = H.x + n; H.z = H.y + n; H.vx = H.z + n; H.vy = H.vx + n; H.vz = H.vy + n;
+    H.tim = H.vz + n;
+    H.key = (long long *)(H.tim + n3);
+    H.l1k = H.key + n3;
+    H.nptnr = (int *)(H.l1k + nl1);
+    H.l1i = H.nptnr + n3;
+    H.colt = (int8_t *)(H.l1i + nl1);
+    H.queued = (uint8_t *)(H.colt + n3);
+    return H;
+}
+/* the CTA copies the system's arrays G into H (in) or H back into G */
+__device__ void hot_copy(const HotArrays &H, const DSys &G, bool in) {
+    const int n = G.N, n3 = n + 3, nl1 = G.nl1;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        if (in) {
+            H.x[k] = G.x[k]; H.y[k] = G.y[k]; H.z[k] = G.z[k]; H.vx[k] = G.vx[k]; H.vy[k] = G.vy[k]; H.vz[k] = G.vz[k];
+        } else {
+            G.x[k] = H.x[k]; G.y[k] = H.y[k]; G.z[k] = H.z[k]; G.vx[k] = H.vx[k]; G.vy[k] = H.vy[k]; G.vz[k] = H.vz[k];
+        }
+    }
+    for (int k = threadIdx.x; k < n3; k += blockDim.x) {
+        if (in) { H.tim[k] = G.tim[k]; H.key[k] = G.key[k]; H.nptnr[k] = G.nptnr[k]; H.colt[k] = G.colt[k]; H.queued[k] = G.queued[k]; }
+        else { G.tim[k] = H.tim[k]; G.key[k] = H.key[k]; G.nptnr[k] = H.nptnr[k]; G.colt[k] = H.colt[k]; G.queued[k] = H.queued[k]; }
+    }
+    for (int k = threadIdx.x; k < nl1; k += blockDim.x) {
+        if (in) { H.l1k[k] = G.l1k[k]; H.l1i[k] = G.l1i[k]; }
+        else { G.l1k[k] = H.l1k[k]; G.l1i[k] = H.l1i[k]; }
+    }
+}
+
+/* ------------------------------------------------------------------ */
 /* kernels                                                             */
 /* ------------------------------------------------------------------ */
 __device__ void log_event(const DSys &S, long long slot, long long coll, double t, double tfalse, int i, int j,
@@ -1456,7 +1510,15 @@ static_assert(run_smem_of<run_full::WarpArea>(OWN_SMEM_FULL, RUN_NT_FULL / 32) +
 static_assert(run_smem_of<run_compact::WarpArea>(OWN_SMEM_COMPACT, RUN_NT_COMPACT / 32) + sizeof(SharedState) +
                       sizeof(DSys) + 1024 <= RUN_CARVEOUT_COMPACT_KB * 1024,
               "compact k_run (with the 1 KB the system reserves per block) must fit its shared-memory carve-out");
-static size_t run_smem(int compact, int own_cap) {
+/* the compact variant's shared-memory room for the hot arrays of small
+ * single-CTA systems (hot_bytes: 70 B per bead, so up to ~930 beads) */
+#define HOT_SMEM_COMPACT (64 * 1024)
+constexpr size_t run_compact_base = sizeof(run_compact::WarpArea) * (RUN_NT_COMPACT / 32) + sizeof(TaskPool);
+static_assert(hot_offset(run_compact_base, OWN_SMEM_COMPACT) + HOT_SMEM_COMPACT + sizeof(SharedState) +
+                      sizeof(DSys) <= 227 * 1024,
+              "compact k_run with its hot arrays above the 227 KB a block may use");
+static size_t run_smem(int compact, int own_cap, int hot_cap = 0) {
+    if (compact && hot_cap > 0) return hot_offset(run_compact_base, own_cap) + (size_t)hot_cap;
     return compact ? run_smem_of<run_compact::WarpArea>(own_cap, RUN_NT_COMPACT / 32)
                    : run_smem_of<run_full::WarpArea>(own_cap, RUN_NT_FULL / 32);
 }
@@ -1493,7 +1555,7 @@ static cudaError_t k_run_attributes() {
                                  (int)run_smem(0, OWN_SMEM_FULL));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(run_compact::k_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)run_smem(1, OWN_SMEM_COMPACT));
+                                     (int)run_smem(1, OWN_SMEM_COMPACT, HOT_SMEM_COMPACT));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(run_full::k_run, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxL1);
@@ -1524,20 +1586,26 @@ static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, i
 /* k_run with one cluster of C CTAs per system (C = 1, 2, 4 or 8) */
 cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int compact, long long target,
                            long long *targets, int hbonds, const int *chain_start, const int *chain_len,
-                           const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles) {
+                           const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles, int min_beads) {
     if (C != 1 && C != 2 && C != 4 && C != 8) return cudaErrorInvalidValue;
     cudaError_t e = k_run_attributes();
     if (e != cudaSuccess) return e;
     /* claim tables in shared memory for the systems up to own_cap beads */
     int own_cap = C == 1 ? std::min(max_beads, own_smem_max(compact)) : 0;
+    /* room for the hot arrays of small systems (compact, one CTA each),
+     * when the smallest system fits it: the room comes out of L1 */
+    const int hot_cap = (compact && C == 1 && min_beads > 0 &&
+                         hot_bytes(min_beads, (min_beads + 3 + 31) / 32) <= (size_t)HOT_SMEM_COMPACT)
+                            ? HOT_SMEM_COMPACT : 0;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    cluster_config(cfg, attr, nsys, C, run_smem(compact, own_cap), st, compact ? RUN_NT_COMPACT : RUN_NT_FULL);
+    cluster_config(cfg, attr, nsys, C, run_smem(compact, own_cap, hot_cap), st, compact ? RUN_NT_COMPACT : RUN_NT_FULL);
     if (compact)
         return cudaLaunchKernelEx(&cfg, run_compact::k_run, d_systems, nsys, target, targets, hbonds, chain_start,
-                                  chain_len, chain_off, outputs, own_cap, C, std::min(compact, (int)DMD_COMPACT_DN), cycles);
+                                  chain_len, chain_off, outputs, own_cap, C, std::min(compact, (int)DMD_COMPACT_DN), cycles,
+                                  hot_cap);
     return cudaLaunchKernelEx(&cfg, run_full::k_run, d_systems, nsys, target, targets, hbonds, chain_start, chain_len,
-                              chain_off, outputs, own_cap, C, INT_MAX, cycles);
+                              chain_off, outputs, own_cap, C, INT_MAX, cycles, 0);
 }
 
 /* how many clusters of C CTAs of k_run can be resident at once */

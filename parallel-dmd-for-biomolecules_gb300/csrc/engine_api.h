@@ -17,10 +17,14 @@ cudaError_t dmd_launch_init(DSys *d_systems, int nsys, int hbonds, cudaStream_t 
 #define DMD_COMPACT_DN 32
 /* targets: per-system event counts (device array), or NULL for target.
  * cycles != 0: each system also stops after its next list rebuild and
- * writes the events it still has to run back into targets[r]. */
+ * writes the events it still has to run back into targets[r].
+ * min_beads: the smallest system of the launch (0: unknown); when it is
+ * small enough, a compact one-CTA launch gets shared memory for the hot
+ * per-bead arrays of the systems that fit. */
 cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int compact, long long target,
                            long long *targets, int hbonds, const int *chain_start, const int *chain_len,
-                           const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles = 0);
+                           const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles = 0,
+                           int min_beads = 0);
 cudaError_t dmd_max_active_clusters(int C, int *n);
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st);

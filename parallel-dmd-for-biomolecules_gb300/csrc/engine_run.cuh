@@ -1412,7 +1412,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                                                      long long *targets, int hbonds_mask,
                                                      const int *chain_start, const int *chain_len,
                                                      const int *chain_off, dmd_diag *outputs, int own_cap, int C,
-                                                     int dn_limit, int cycles) {
+                                                     int dn_limit, int cycles, int hot_cap) {
     extern __shared__ __align__(16) unsigned char dsmem[];
     WarpArea *warea = reinterpret_cast<WarpArea *>(dsmem);
     __shared__ SharedState sh;
@@ -1424,6 +1424,25 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
     const bool leader = rank == 0;
     if (threadIdx.x == 0) S_sh = systems[r];
     __syncthreads();
+    /* A single-CTA system whose hot per-bead arrays fit hot_cap bytes of
+     * shared memory (after the claim tables) keeps them there for the
+     * launch: positions, velocities, queue times, keys, partners, coltypes,
+     * queue flags and the level-1 tournament.  Every access goes through
+     * S_sh's pointers, which now point there; the arrays go back to the
+     * system's pool at the end of the launch. */
+    char *const hot = (char *)dsmem + hot_offset(sizeof(WarpArea) * RUN_NW + sizeof(TaskPool), own_cap);
+    const bool use_hot = C == 1 && hot_cap > 0 && hot_bytes(S_sh.N, S_sh.nl1) <= (size_t)hot_cap;
+    if (use_hot) {
+        HotArrays H = hot_layout(hot, S_sh.N, S_sh.nl1);
+        hot_copy(H, S_sh, true);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            S_sh.x = H.x; S_sh.y = H.y; S_sh.z = H.z; S_sh.vx = H.vx; S_sh.vy = H.vy; S_sh.vz = H.vz;
+            S_sh.tim = H.tim; S_sh.key = H.key; S_sh.l1k = H.l1k; S_sh.nptnr = H.nptnr; S_sh.l1i = H.l1i;
+            S_sh.colt = H.colt; S_sh.queued = H.queued;
+        }
+        __syncthreads();
+    }
     const DSys &S = S_sh;
     const int N = S.N;
     const int hbonds = hbonds_mask & 1;
@@ -2042,6 +2061,10 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
         if (threadIdx.x == 0) sh.ncand = 0;   /* the next gather may start without a barrier */
         csync(C);
         DMD_PHASE(ph_kind);
+    }
+    if (use_hot) {   /* the hot arrays back to the system's pool */
+        __syncthreads();
+        hot_copy(hot_layout(hot, N, S.nl1), systems[r], false);
     }
     if (leader) {
         __syncthreads();

@@ -91,7 +91,7 @@ class Diag(C.Structure):
         ("n_output", C.c_int64), ("n_updates", C.c_int64), ("n_forced_updates", C.c_int64),
         ("t", C.c_double), ("tfalse", C.c_double), ("nbr_mean", C.c_double),
         ("n_batches", C.c_int64), ("n_rolled_back", C.c_int64), ("n_candidates", C.c_int64),
-        ("nc_boundbad", C.c_int64), ("nc_unboundbad", C.c_int64),
+        ("nc_boundbad", C.c_int64), ("nc_unboundbad", C.c_int64), ("run_cycles", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -125,8 +125,8 @@ cudaError_t dmd_launch_init(DSys *d, int nsys, int, cudaStream_t) {
  * recorded and runs when the graph is launched. */
 cudaError_t dmd_launch_run(DSys *d, int nsys, int mb, int C, int compact, long long target, long long *targets,
                            int hb, const int *cs, const int *cl, const int *co, dmd_diag *out, cudaStream_t st,
-                           int cycles) {
-    if (mock_capture_push([=]() { dmd_launch_run(d, nsys, mb, C, compact, target, targets, hb, cs, cl, co, out, st, cycles); }))
+                           int cycles, int min_beads) {
+    if (mock_capture_push([=]() { dmd_launch_run(d, nsys, mb, C, compact, target, targets, hb, cs, cl, co, out, st, cycles, min_beads); }))
         return cudaSuccess;
     ++g_run;
     g_last_target = target; g_last_C = C; g_last_compact = compact;
