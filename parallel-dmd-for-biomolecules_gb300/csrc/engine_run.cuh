@@ -2000,12 +2000,15 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
             ph_kind = 6;
             /* ---- ghost collision: leader warp 0 ---- */
             if (leader && warp == 0) {
+                DMD_CSUB(-1);
                 double tf = sh.tf_iv;
                 const int i = warp_ghost(S, sh, tf);
                 if (lane == 0) { W.i = i; W.tf = tf; }
                 __syncwarp();
                 DMD_SUB(-1);
+                DMD_CSUB(8);
                 warp_repredict(S, cta_err(sh), W, i, -1, tf, sh.sc.interval_max, hbonds, Ver{nullptr, warea, 0u, 0, 0});
+                DMD_CSUB(9);
                 warp_commit_preds(S, W);
                 if (lane == 0) {
                     W.pb[W.npred] = N;   /* the ghost entry itself */
@@ -2016,7 +2019,9 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                     sh.sc.done += 1;
                 }
                 __syncwarp();
+                DMD_CSUB(10);
                 warp_l1_refresh(S, W.pb, W.npred + 1);
+                DMD_CSUB(11);
             }
         } else if (e == N + 1) {
             ph_kind = 7;
