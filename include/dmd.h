@@ -199,6 +199,18 @@ int dmd_set_state(dmd_handle *h, const double *x, const double *y, const double 
 
 /* Replaces code/energy.f, code/radgyr.f, code/end2end.f at the current time. */
 int dmd_diagnostics(dmd_handle *h, dmd_diag *out);
+/* The backbone dihedral histogram of code/phipsi.f (-Dwrite_phipsi, the
+ * reference's in-run analysis): dmd_phipsi_sample adds the current (phi,
+ * psi) of every residue 2..L-1 of every chain, each as its whole-degree bin
+ * res(phi + 180, psi + 180) of a 361 x 361 histogram kept on the device
+ * (code/phipsi.f:25-290; the reference samples at the output events of a
+ * run's second half and at its end, code/main.F90:1227-1231,1315-1317).
+ * dmd_phipsi_histogram copies it out (hist: 361 * 361 counts, index
+ * (phi + 180) * 361 + (psi + 180); may be NULL) with the number of samples
+ * (may be NULL) and clears both when reset != 0.  A residue whose frame is
+ * degenerate (collinear beads) is not counted. */
+int dmd_phipsi_sample(dmd_handle *h);
+int dmd_phipsi_histogram(dmd_handle *h, int64_t *hist, int64_t *nsamples, int32_t reset);
 
 /* Dense pair-type table ev_code (n_beads x n_beads, row-major, 1-based
  * rows/cols mapped to 0-based), reconstructed from the rule function and
@@ -283,6 +295,9 @@ int dmd_batch_get_state(dmd_batch *b, int32_t r, double *x, double *y, double *z
                         int32_t *identity, int32_t *extra_repuls,
                         double *t, double *tfalse, int64_t *coll);
 int dmd_batch_diagnostics(dmd_batch *b, int32_t r, dmd_diag *out);
+/* dmd_phipsi_* for system r of a batch (sample: r < 0 samples every system) */
+int dmd_batch_phipsi_sample(dmd_batch *b, int32_t r);
+int dmd_batch_phipsi_histogram(dmd_batch *b, int32_t r, int64_t *hist, int64_t *nsamples, int32_t reset);
 double dmd_batch_last_run_ms(dmd_batch *b);
 /* CTAs (one thread-block cluster) that advance each system: 1, 2, 4 or 8,
  * or 0 (default) to let the library choose from the number of systems and

@@ -1374,6 +1374,82 @@ struct Oracle {
     }
 
     /* ------------------------------------------------------------------ */
+    /* backbone dihedral histogram: code/phipsi.f:25-290 (-Dwrite_phipsi)  */
+    /* ------------------------------------------------------------------ */
+    /* Adds the (phi, psi) bin of residues 2..L-1 of every chain to hist
+     * (361 x 361, [phi + 180][psi + 180] in whole degrees, res(0:360,0:360)).
+     * Each step in phipsi.f's order: positions advanced by tfalse
+     * (:30-53), the N->Ca axis and the C-Ca perpendicular (:58-126), C(i-1)
+     * in that frame and its angle from the second axis (:128-168); psi the
+     * same from the C->Ca axis with N(i+1) (:170-285). */
+    void phipsi_sample(int64_t *hist) const {
+        const double pi = 4.0 * std::atan(1.0);   /* main.F90:125 */
+        auto pos = [&](int k, double &x, double &y, double &z) {   /* k 1-based */
+            x = sx[k] + vx[k] * tfalse; y = sy[k] + vy[k] * tfalse; z = sz[k] + vz[k] * tfalse;
+        };
+        /* the angle of (0, y, z) from the second axis, as a bin 0..360 */
+        auto bin_of = [&](double ynew, double znew) {
+            const double d = std::sqrt(ynew * ynew + znew * znew);
+            const double yy = ynew / d, zz = znew / d;
+            double c = yy;
+            if (c > 1.0) c = 1.0;
+            if (c < -1.0) c = -1.0;
+            const double angle = std::acos(c);
+            double degs = 180.0 * angle / pi;
+            if (zz > 0.0) degs = degs * -1.0;
+            if (degs < -180.0) degs = -180.0;
+            if (degs > 180.0) degs = 180.0;
+            degs = degs + 180.0;
+            /* a degenerate frame (collinear beads: a NaN angle) is not counted */
+            return degs >= 0.0 && degs <= 360.0 ? (int)std::trunc(degs) : -1;
+        };
+        /* one dihedral: axis a->b (unit x), third point c (its component
+         * perpendicular to the axis gives y), fourth point e in that frame */
+        auto dihedral_bin = [&](double xa, double ya, double za, double xb, double yb, double zb, double xc, double yc,
+                                double zc, double xe, double ye, double ze) {
+            double x1 = xb - xa, y1 = yb - ya, z1 = zb - za;
+            x1 = x1 - dnint(x1); y1 = y1 - dnint(y1); z1 = z1 - dnint(z1);
+            const double d1 = std::sqrt(x1 * x1 + y1 * y1 + z1 * z1);
+            x1 = x1 / d1; y1 = y1 / d1; z1 = z1 / d1;
+            double xu = xc - xb, yu = yc - yb, zu = zc - zb;
+            xu = xu - dnint(xu); yu = yu - dnint(yu); zu = zu - dnint(zu);
+            const double du = std::sqrt(xu * xu + yu * yu + zu * zu);
+            xu = xu / du; yu = yu / du; zu = zu / du;
+            double c = x1 * xu + y1 * yu + z1 * zu;
+            if (c > 1.0) c = 1.0;
+            if (c < -1.0) c = -1.0;
+            const double dq = c * du;                          /* distance from b to q */
+            /* phipsi.f also forms q = b + x1 dq and the unit vector q -> c,
+             * of which only the length dcq is used */
+            const double dcq = std::sqrt(du * du - dq * dq);
+            const double xr = xc - x1 * (d1 + dq), yr = yc - y1 * (d1 + dq), zr = zc - z1 * (d1 + dq);
+            double x2 = xr - xa, y2 = yr - ya, z2 = zr - za;
+            x2 = x2 - dnint(x2); y2 = y2 - dnint(y2); z2 = z2 - dnint(z2);
+            x2 = x2 / dcq; y2 = y2 / dcq; z2 = z2 / dcq;
+            const double x3 = y1 * z2 - z1 * y2, y3 = z1 * x2 - x1 * z2, z3 = x1 * y2 - y1 * x2;
+            double xd = xe - xa, yd = ye - ya, zd = ze - za;
+            xd = xd - dnint(xd); yd = yd - dnint(yd); zd = zd - dnint(zd);
+            const double ynew = x2 * xd + y2 * yd + z2 * zd;
+            const double znew = x3 * xd + y3 * yd + z3 * zd;
+            return bin_of(ynew, znew);
+        };
+        for (int c = 0; c < nchains; ++c) {
+            const int L = chain_L[c], s = chain_start[c];
+            for (int r = 2; r <= L - 1; ++r) {
+                const int ca = s + r, nh = s + L + r, co = s + 2 * L + r;   /* 1-based beads */
+                double xn, yn, zn, xca, yca, zca, xc, yc, zc, xn1, yn1, zn1, xcm, ycm, zcm;
+                pos(nh, xn, yn, zn); pos(ca, xca, yca, zca); pos(co, xc, yc, zc);
+                pos(nh + 1, xn1, yn1, zn1); pos(co - 1, xcm, ycm, zcm);
+                /* phi: axis N(i) -> Ca(i), plane with C(i), point C(i-1) */
+                const int bphi = dihedral_bin(xn, yn, zn, xca, yca, zca, xc, yc, zc, xcm, ycm, zcm);
+                /* psi: axis C(i) -> Ca(i), plane with N(i), point N(i+1) */
+                const int bpsi = dihedral_bin(xc, yc, zc, xca, yca, zca, xn, yn, zn, xn1, yn1, zn1);
+                if (bphi >= 0 && bpsi >= 0) hist[(size_t)bphi * 361 + bpsi] += 1;
+            }
+        }
+    }
+
+    /* ------------------------------------------------------------------ */
     /* diagnostics: code/energy.f, code/radgyr.f, code/end2end.f           */
     /* ------------------------------------------------------------------ */
     void diagnostics(dmd_diag *d) {
@@ -1508,6 +1584,7 @@ int ora_get_state(ora_handle *h, double *x, double *y, double *z, double *vx, do
 }
 
 int ora_diagnostics(ora_handle *h, dmd_diag *d) { h->o.diagnostics(d); return 0; }
+int ora_phipsi_sample(ora_handle *h, int64_t *hist) { h->o.phipsi_sample(hist); return 0; }
 
 int ora_get_evcode(ora_handle *h, int8_t *out) {
     std::memcpy(out, h->o.ev.data(), h->o.ev.size());

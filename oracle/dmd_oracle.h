@@ -17,6 +17,9 @@ int ora_predict_all(ora_handle *h, double *tim, int32_t *nptnr, int32_t *coltype
 int ora_get_state(ora_handle *h, double *x, double *y, double *z, double *vx, double *vy, double *vz,
                   int32_t *bptnr, int32_t *identity, int32_t *er, double *t, double *tfalse, int64_t *coll);
 int ora_diagnostics(ora_handle *h, dmd_diag *d);
+/* adds the current state's backbone (phi, psi) bins (code/phipsi.f) to
+ * hist[361 * 361] */
+int ora_phipsi_sample(ora_handle *h, int64_t *hist);
 int ora_get_evcode(ora_handle *h, int8_t *out);
 int ora_get_lists(ora_handle *h, int32_t *up_count, int32_t *up, int32_t *dn_count, int32_t *dn, int32_t cap);
 int ora_get_scalars(ora_handle *h, double *out, int n);

@@ -40,6 +40,7 @@ def lib():
         L.ora_predict_all.argtypes = [C.c_void_p, abi.dbl_p, abi.i32_p, abi.i32_p]
         L.ora_get_state.argtypes = [C.c_void_p] + [abi.dbl_p] * 6 + [abi.i32_p] * 3 + [abi.dbl_p, abi.dbl_p, abi.i64_p]
         L.ora_diagnostics.argtypes = [C.c_void_p, C.POINTER(abi.Diag)]
+        L.ora_phipsi_sample.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_get_evcode.argtypes = [C.c_void_p, abi.i8_p]
         L.ora_get_lists.argtypes = [C.c_void_p, abi.i32_p, abi.i32_p, abi.i32_p, abi.i32_p, C.c_int32]
         L.ora_get_scalars.argtypes = [C.c_void_p, abi.dbl_p, C.c_int]
@@ -127,6 +128,11 @@ class Oracle:
         d = abi.Diag()
         self.L.ora_diagnostics(self.h, C.byref(d))
         return d.as_dict()
+
+    def phipsi_sample(self, hist: np.ndarray):
+        """Adds the current backbone (phi, psi) bins (code/phipsi.f) to hist (361 x 361 int64)."""
+        assert hist.dtype == np.int64 and hist.size == 361 * 361 and hist.flags.c_contiguous
+        self.L.ora_phipsi_sample(self.h, hist.ctypes.data)
 
     def evcode(self) -> np.ndarray:
         out = np.zeros((self.n, self.n), np.int8)

@@ -524,6 +524,8 @@ struct dmd_batch {
     int graph_launches = 0, graph_cluster = 0, graph_compact = -1;
     long long *d_targets = nullptr;    /* per-system event targets of a follow-up launch */
     cudaGraphExec_t cyc_graph = nullptr;   /* captured rebuild-cycle launches of dmd_batch_run_cycles */
+    unsigned long long *d_phipsi = nullptr;  /* per system: 361 x 361 (phi, psi) histogram (dmd_*phipsi*) */
+    std::vector<long long> phipsi_n;         /* samples in each system's histogram */
     int cyc_launches = 0, cyc_cluster = 0, cyc_compact = -1;
     long long upload_bytes = 0;        /* host-to-device bytes of the creation */
     int compact_dn = DMD_COMPACT_DN;   /* down-list limit of the compact variant, 0: never */
@@ -903,6 +905,52 @@ int get_state(dmd_batch &B, int r, double *x, double *y, double *z, double *vx, 
     if (t) *t = sc.t;
     if (tfalse) *tfalse = sc.tfalse;
     if (coll) *coll = sc.coll;
+    return DMD_OK;
+}
+
+/* The backbone dihedral histogram of code/phipsi.f (-Dwrite_phipsi): each
+ * sample adds the current (phi, psi) bins of every residue 2..L-1 of every
+ * chain of system r (r < 0: of every system) to the system's histogram on
+ * the device.  The reference samples at the output events of a run's second
+ * half and at its end (code/main.F90:1227-1231,1315-1317). */
+constexpr size_t PHIPSI_BINS = 361 * 361;
+int phipsi_sample(dmd_batch &B, int r) {
+    std::string &err = B.err;
+    const int n = (int)B.hs.size();
+    if (!B.ready) { err = "batch not ready"; return DMD_E_STATE; }
+    if (r >= n) { err = "replica index out of range"; return DMD_E_INPUT; }
+    if (!B.d_phipsi) {
+        CK(cudaMalloc(&B.d_phipsi, (size_t)n * PHIPSI_BINS * sizeof(unsigned long long)));
+        CK(cudaMemsetAsync(B.d_phipsi, 0, (size_t)n * PHIPSI_BINS * sizeof(unsigned long long), B.st));
+        B.phipsi_n.assign(n, 0);
+    }
+    CK(dmd_launch_phipsi(B.d_sys, n, r < 0 ? -1 : r, B.d_cstart, B.d_clen, B.d_coff, B.d_phipsi, B.st));
+    for (int q = 0; q < n; ++q) if (r < 0 || q == r) B.phipsi_n[q] += 1;
+    return DMD_OK;
+}
+/* system r's histogram ([phi + 180][psi + 180], whole degrees) and its
+ * number of samples; reset != 0 then clears both */
+int phipsi_histogram(dmd_batch &B, int r, int64_t *hist, int64_t *nsamples, int reset) {
+    std::string &err = B.err;
+    const int n = (int)B.hs.size();
+    if (r < 0 || r >= n) { err = "replica index out of range"; return DMD_E_INPUT; }
+    if (!B.d_phipsi) {
+        if (hist) std::memset(hist, 0, PHIPSI_BINS * sizeof(int64_t));
+        if (nsamples) *nsamples = 0;
+        return DMD_OK;
+    }
+    unsigned long long *blk = B.d_phipsi + (size_t)r * PHIPSI_BINS;
+    if (hist) {
+        std::vector<unsigned long long> h(PHIPSI_BINS);
+        CK(cudaStreamSynchronize(B.st));
+        CK(cudaMemcpy(h.data(), blk, PHIPSI_BINS * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < PHIPSI_BINS; ++k) hist[k] = (int64_t)h[k];
+    }
+    if (nsamples) *nsamples = B.phipsi_n[r];
+    if (reset) {
+        CK(cudaMemsetAsync(blk, 0, PHIPSI_BINS * sizeof(unsigned long long), B.st));
+        B.phipsi_n[r] = 0;
+    }
     return DMD_OK;
 }
 
@@ -1294,6 +1342,8 @@ void batch_free(dmd_batch &B) {
     B.graph = nullptr;
     if (B.cyc_graph) cudaGraphExecDestroy(B.cyc_graph);
     B.cyc_graph = nullptr;
+    if (B.d_phipsi) cudaFree(B.d_phipsi);
+    B.d_phipsi = nullptr;
     for (auto &D : B.ds) if (D.pool) cudaFree(D.pool);
     if (B.pool_all) cudaFree(B.pool_all);
     B.pool_all = nullptr;
@@ -1628,6 +1678,14 @@ int dmd_batch_diagnostics(dmd_batch *b, int32_t r, dmd_diag *out) {
     if (!b) return DMD_E_INPUT;
     return diagnostics(*b, r, out);
 }
+int dmd_batch_phipsi_sample(dmd_batch *b, int32_t r) {
+    if (!b) return DMD_E_INPUT;
+    return phipsi_sample(*b, r);
+}
+int dmd_batch_phipsi_histogram(dmd_batch *b, int32_t r, int64_t *hist, int64_t *nsamples, int32_t reset) {
+    if (!b) return DMD_E_INPUT;
+    return phipsi_histogram(*b, r, hist, nsamples, reset);
+}
 void dmd_batch_destroy(dmd_batch *b) {
     if (!b) return;
     batch_free(*b);
@@ -1771,6 +1829,14 @@ int dmd_get_state(dmd_handle *h, double *x, double *y, double *z, double *vx, do
 int dmd_diagnostics(dmd_handle *h, dmd_diag *out) {
     if (!h) return DMD_E_INPUT;
     return diagnostics(h->b, 0, out);
+}
+int dmd_phipsi_sample(dmd_handle *h) {
+    if (!h) return DMD_E_INPUT;
+    return phipsi_sample(h->b, 0);
+}
+int dmd_phipsi_histogram(dmd_handle *h, int64_t *hist, int64_t *nsamples, int32_t reset) {
+    if (!h) return DMD_E_INPUT;
+    return phipsi_histogram(h->b, 0, hist, nsamples, reset);
 }
 int dmd_get_evcode(dmd_handle *h, int8_t *out) {
     if (!h || !out || !h->b.ready) return DMD_E_INPUT;

@@ -1482,6 +1482,83 @@ namespace run_compact {
 #undef DMD_RUN_DN_LIMIT
 #undef DMD_RUN_NT
 
+/* ------------------------------------------------------------------ */
+/* backbone dihedral histogram: code/phipsi.f:25-290 (-Dwrite_phipsi)  */
+/* ------------------------------------------------------------------ */
+/* The angle of (0, y, z) from the frame's second axis as a whole-degree bin
+ * 0..360 (phipsi.f:150-168, 268-285); -1 for a degenerate frame (NaN). */
+__device__ int phipsi_bin(double ynew, double znew) {
+    const double pi = 3.141592653589793;   /* 4 atan(1) of main.F90:125, rounded to nearest */
+    const double d = sqrt(ynew * ynew + znew * znew);
+    const double yy = ynew / d, zz = znew / d;
+    double c = yy;
+    if (c > 1.0) c = 1.0;
+    if (c < -1.0) c = -1.0;
+    const double angle = acos(c);
+    double degs = 180.0 * angle / pi;
+    if (zz > 0.0) degs = degs * -1.0;
+    if (degs < -180.0) degs = -180.0;
+    if (degs > 180.0) degs = 180.0;
+    degs = degs + 180.0;
+    return degs >= 0.0 && degs <= 360.0 ? (int)trunc(degs) : -1;
+}
+/* one dihedral in phipsi.f's construction: unit axis a -> b, the
+ * perpendicular from the axis to c as the second axis, their cross product
+ * as the third, and the fourth point e in that frame (phipsi.f:58-168 for
+ * phi with a = N(i), b = Ca(i), c = C(i), e = C(i-1); :170-285 for psi with
+ * a = C(i), b = Ca(i), c = N(i), e = N(i+1)) */
+__device__ int phipsi_dihedral(const double *a, const double *b, const double *c, const double *e) {
+    double x1 = b[0] - a[0], y1 = b[1] - a[1], z1 = b[2] - a[2];
+    x1 = x1 - d_nint(x1); y1 = y1 - d_nint(y1); z1 = z1 - d_nint(z1);
+    const double d1 = sqrt(x1 * x1 + y1 * y1 + z1 * z1);
+    x1 = x1 / d1; y1 = y1 / d1; z1 = z1 / d1;
+    double xu = c[0] - b[0], yu = c[1] - b[1], zu = c[2] - b[2];
+    xu = xu - d_nint(xu); yu = yu - d_nint(yu); zu = zu - d_nint(zu);
+    const double du = sqrt(xu * xu + yu * yu + zu * zu);
+    xu = xu / du; yu = yu / du; zu = zu / du;
+    double cs = x1 * xu + y1 * yu + z1 * zu;
+    if (cs > 1.0) cs = 1.0;
+    if (cs < -1.0) cs = -1.0;
+    const double dq = cs * du;
+    const double dcq = sqrt(du * du - dq * dq);
+    const double xr = c[0] - x1 * (d1 + dq), yr = c[1] - y1 * (d1 + dq), zr = c[2] - z1 * (d1 + dq);
+    double x2 = xr - a[0], y2 = yr - a[1], z2 = zr - a[2];
+    x2 = x2 - d_nint(x2); y2 = y2 - d_nint(y2); z2 = z2 - d_nint(z2);
+    x2 = x2 / dcq; y2 = y2 / dcq; z2 = z2 / dcq;
+    const double x3 = y1 * z2 - z1 * y2, y3 = z1 * x2 - x1 * z2, z3 = x1 * y2 - y1 * x2;
+    double xd = e[0] - a[0], yd = e[1] - a[1], zd = e[2] - a[2];
+    xd = xd - d_nint(xd); yd = yd - d_nint(yd); zd = zd - d_nint(zd);
+    return phipsi_bin(x2 * xd + y2 * yd + z2 * zd, x3 * xd + y3 * yd + z3 * zd);
+}
+/* one CTA per system (only: that system alone, or -1): residues 2..L-1 of
+ * every chain at the current positions (advanced by tfalse) into the
+ * system's 361 x 361 histogram hist + r * 361 * 361 */
+__global__ void __launch_bounds__(NTHREADS) k_phipsi(DSys *systems, int nsys, int only, const int *chain_start,
+                                                     const int *chain_len, const int *chain_off,
+                                                     unsigned long long *hist) {
+    const int r = blockIdx.x;
+    if (r >= nsys || (only >= 0 && r != only)) return;
+    const DSys &S = systems[r];
+    const double tf = S.sc->tfalse;
+    const int *cs = chain_start + chain_off[r], *cl = chain_len + chain_off[r];
+    unsigned long long *h = hist + (size_t)r * 361 * 361;
+    for (int c = 0; c < S.nchains; ++c) {
+        const int L = cl[c], s0 = cs[c];
+        for (int ir = 2 + (int)threadIdx.x; ir <= L - 1; ir += blockDim.x) {
+            const int ca = s0 + ir - 1, nh = s0 + L + ir - 1, co = s0 + 2 * L + ir - 1;   /* 0-based */
+            double p[5][3];
+            const int bead[5] = {nh, ca, co, nh + 1, co - 1};
+            for (int k = 0; k < 5; ++k) {
+                const int b = bead[k];
+                p[k][0] = S.x[b] + S.vx[b] * tf; p[k][1] = S.y[b] + S.vy[b] * tf; p[k][2] = S.z[b] + S.vz[b] * tf;
+            }
+            const int bphi = phipsi_dihedral(p[0], p[1], p[2], p[4]);
+            const int bpsi = phipsi_dihedral(p[2], p[1], p[0], p[3]);
+            if (bphi >= 0 && bpsi >= 0) atomicAdd(&h[(size_t)bphi * 361 + bpsi], 1ull);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(NTHREADS) k_diag(DSys *systems, int nsys, const int *chain_start, const int *chain_len,
                                                    const int *chain_off, dmd_diag *out) {
     __shared__ SharedState sh;
@@ -1620,6 +1697,12 @@ cudaError_t dmd_max_active_clusters(int C, int *n) {
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st) {
     k_diag<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, chain_start, chain_len, chain_off, out);
+    return cudaGetLastError();
+}
+
+cudaError_t dmd_launch_phipsi(DSys *d_systems, int nsys, int only, const int *chain_start, const int *chain_len,
+                              const int *chain_off, unsigned long long *hist, cudaStream_t st) {
+    k_phipsi<<<nsys, NTHREADS, 0, st>>>(d_systems, nsys, only, chain_start, chain_len, chain_off, hist);
     return cudaGetLastError();
 }
 

@@ -26,6 +26,10 @@ cudaError_t dmd_launch_run(DSys *d_systems, int nsys, int max_beads, int C, int 
                            const int *chain_off, dmd_diag *outputs, cudaStream_t st, int cycles = 0,
                            int min_beads = 0);
 cudaError_t dmd_max_active_clusters(int C, int *n);
+/* backbone (phi, psi) bins of every system (only < 0) or system only, added
+ * to its 361 x 361 histogram at hist + r * 361 * 361 (code/phipsi.f) */
+cudaError_t dmd_launch_phipsi(DSys *d_systems, int nsys, int only, const int *chain_start, const int *chain_len,
+                              const int *chain_off, unsigned long long *hist, cudaStream_t st);
 cudaError_t dmd_launch_diag(DSys *d_systems, int nsys, const int *chain_start, const int *chain_len,
                             const int *chain_off, dmd_diag *out, cudaStream_t st);
 

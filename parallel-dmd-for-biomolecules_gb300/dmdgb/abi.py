@@ -117,6 +117,7 @@ ENGINE_SYMBOLS = [
     "dmd_server_create", "dmd_server_submit", "dmd_server_step", "dmd_server_status", "dmd_server_result",
     "dmd_server_release", "dmd_server_stats", "dmd_server_last_error", "dmd_server_destroy",
     "dmd_sidechain_search", "dmd_sidechain_grid",
+    "dmd_phipsi_sample", "dmd_phipsi_histogram", "dmd_batch_phipsi_sample", "dmd_batch_phipsi_histogram",
 ]
 
 REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -202,6 +203,14 @@ def _declare(lib) -> None:
     lib.dmd_batch_run_graph.restype = C.c_int
     lib.dmd_batch_run_cycles.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_int64)]
     lib.dmd_batch_run_cycles.restype = C.c_int
+    lib.dmd_phipsi_sample.argtypes = [C.c_void_p]
+    lib.dmd_phipsi_sample.restype = C.c_int
+    lib.dmd_phipsi_histogram.argtypes = [C.c_void_p, i64_p, i64_p, C.c_int32]
+    lib.dmd_phipsi_histogram.restype = C.c_int
+    lib.dmd_batch_phipsi_sample.argtypes = [C.c_void_p, C.c_int32]
+    lib.dmd_batch_phipsi_sample.restype = C.c_int
+    lib.dmd_batch_phipsi_histogram.argtypes = [C.c_void_p, C.c_int32, i64_p, i64_p, C.c_int32]
+    lib.dmd_batch_phipsi_histogram.restype = C.c_int
     lib.dmd_batch_autotune.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dbl_p]
     lib.dmd_batch_autotune.restype = C.c_int
     lib.dmd_batch_autotune_cached.argtypes = [C.c_void_p, C.c_int64, C.c_char_p, C.POINTER(C.c_int32),

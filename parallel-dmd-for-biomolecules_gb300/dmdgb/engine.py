@@ -155,6 +155,18 @@ class Engine:
         _check(self.lib.dmd_diagnostics(self.h, C.byref(d)), self.lib, self.h)
         return d.as_dict()
 
+    def phipsi_sample(self):
+        """Adds the current backbone (phi, psi) bins to the histogram (code/phipsi.f)."""
+        _check(self.lib.dmd_phipsi_sample(self.h), self.lib, self.h)
+
+    def phipsi_histogram(self, reset: bool = False):
+        """(361 x 361 counts [phi + 180, psi + 180] in whole degrees, samples)."""
+        hist = np.zeros((361, 361), np.int64)
+        n = C.c_int64()
+        _check(self.lib.dmd_phipsi_histogram(self.h, hist.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(n),
+                                             int(bool(reset))), self.lib, self.h)
+        return hist, n.value
+
     def evcode(self) -> np.ndarray:
         out = np.zeros((self.n, self.n), np.int8)
         _check(self.lib.dmd_get_evcode(self.h, out.ctypes.data_as(abi.i8_p)), self.lib, self.h)
@@ -268,3 +280,16 @@ class Batch:
         d = abi.Diag()
         _check(self.lib.dmd_batch_diagnostics(self.h, r, C.byref(d)), self.lib, self.h, "dmd_batch_last_error")
         return d.as_dict()
+
+    def phipsi_sample(self, r: int = -1):
+        """Adds the backbone (phi, psi) bins of system r (-1: every system)."""
+        _check(self.lib.dmd_batch_phipsi_sample(self.h, int(r)), self.lib, self.h, "dmd_batch_last_error")
+
+    def phipsi_histogram(self, r: int, reset: bool = False):
+        """System r's (361 x 361 counts [phi + 180, psi + 180], samples)."""
+        hist = np.zeros((361, 361), np.int64)
+        n = C.c_int64()
+        _check(self.lib.dmd_batch_phipsi_histogram(self.h, int(r), hist.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                   C.byref(n), int(bool(reset))), self.lib, self.h,
+               "dmd_batch_last_error")
+        return hist, n.value

@@ -164,6 +164,11 @@ cudaError_t dmd_launch_diag(DSys *d, int nsys, const int *cs, const int *cl, con
     check("diag", d, nsys, cs, cl, co);
     return cudaSuccess;
 }
+cudaError_t dmd_launch_phipsi(DSys *d, int nsys, int, const int *cs, const int *cl, const int *co,
+                              unsigned long long *, cudaStream_t) {
+    check("phipsi", d, nsys, cs, cl, co);
+    return cudaSuccess;
+}
 cudaError_t dmd_noalloc_scratch(void **) { return cudaErrorNotSupported; }
 cudaError_t dmd_launch_predict_noalloc(const DSys &, int, double *, int *, int *, cudaStream_t) {
     return cudaErrorNotSupported;

@@ -68,6 +68,7 @@ cudaError_t cudaMemcpy(void *d, const void *s, size_t n, cudaMemcpyKind k) {
     return cudaSuccess;
 }
 cudaError_t cudaMemcpyAsync(void *d, const void *s, size_t n, cudaMemcpyKind k, cudaStream_t) { return cudaMemcpy(d, s, n, k); }
+cudaError_t cudaMemsetAsync(void *d, int v, size_t n, cudaStream_t) { std::memset(d, v, n); return cudaSuccess; }
 cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
 cudaError_t cudaStreamCreateWithFlags(cudaStream_t *s, unsigned int) { *s = (cudaStream_t)take(8, false); return cudaSuccess; }
 cudaError_t cudaStreamDestroy(cudaStream_t s) { give(s); return cudaSuccess; }

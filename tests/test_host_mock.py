@@ -396,6 +396,35 @@ def test_autotune_cache_file(mock, tmp_path):
     assert mock.mock_report() == b"", mock.mock_report().decode()
 
 
+def test_phipsi_sample_counts_and_reset(mock):
+    """The (phi, psi) histogram's host side: samples of every system or of
+    one, the count per system, reset, and a replica index out of range."""
+    specs = [systems.generate(systems.klvffae_system(3, 5.0, 0.2, seed=70 + r)) for r in range(3)]
+    tabs = abi.tables_struct(default_tables())
+    cfgs = (abi.RunCfg * 3)(*[s.run_cfg(0, 0) for s in specs])
+    syss = (abi.System * 3)(*[s.c_system() for s in specs])
+    mock.mock_reset()
+    h = C.c_void_p()
+    assert mock.dmd_batch_create(3, cfgs, C.byref(tabs), syss, C.byref(h)) == 0
+    n = C.c_int64()
+    hist = np.ones(361 * 361, np.int64)
+    assert mock.dmd_batch_phipsi_histogram(h, 0, hist.ctypes.data_as(abi.i64_p), C.byref(n), 0) == 0
+    assert n.value == 0 and hist.sum() == 0                      # nothing sampled yet
+    assert mock.dmd_batch_phipsi_sample(h, -1) == 0
+    assert mock.dmd_batch_phipsi_sample(h, 2) == 0
+    counts = []
+    for r in range(3):
+        assert mock.dmd_batch_phipsi_histogram(h, r, None, C.byref(n), 0) == 0
+        counts.append(n.value)
+    assert counts == [1, 1, 2]
+    assert mock.dmd_batch_phipsi_histogram(h, 2, None, C.byref(n), 1) == 0 and n.value == 2
+    assert mock.dmd_batch_phipsi_histogram(h, 2, None, C.byref(n), 0) == 0 and n.value == 0
+    assert mock.dmd_batch_phipsi_sample(h, 3) == -1
+    assert mock.dmd_batch_phipsi_histogram(h, -1, None, None, 0) == -1
+    assert mock.mock_report() == b"", mock.mock_report().decode()
+    mock.dmd_batch_destroy(h)
+
+
 def test_server_step_books_a_failed_read_back(mock):
     """A result read-back that fails while a finished request is retired
     fails that request alone: its pool is freed and it leaves the active
