@@ -487,6 +487,10 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, cons
     }
     int mdn = 0;
     const float far_f = T.rlsq_max_f + (4e-7f + 4e-7f * T.rlsq_max_f);   /* above every cut + margin */
+#ifdef DMD_PHASE_TIMERS
+    const long long walk_t0 = clock64();
+    long long walk_n = 0;
+#endif
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
         int nu = 0, nd = 0;
         int *up = S.up + (size_t)b * S.cap, *dn = S.dn + (size_t)b * S.cap;
@@ -554,27 +558,41 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, cons
              * all of them as one sequence, so that the lanes of a warp (one
              * bead each) stay together for as many steps as their longest
              * sequence instead of their longest cell of every one of 27. */
-            int rlo[18], rhi[18];
             const int xl = cx == 0 ? nc - 1 : cx - 1, xh = cx == nc - 1 ? 0 : cx + 1;
             const bool wrapx = xl > xh;
-#pragma unroll
-            for (int row = 0; row < 9; ++row) {
+            /* range sr (0..17) of the 27 cells: rows of three cells along x,
+             * two ranges where a row wraps around the box; its bounds come
+             * from the cell starts when the walk reaches it (a dynamically
+             * indexed array of them would live in local memory) */
+            auto range = [&](int sr, int &lo, int &hi) {
+                const int row = sr >> 1;
                 int gy = cy + row % 3 - 1, gz = cz + row / 3 - 1;
                 gy = gy < 0 ? gy + nc : (gy >= nc ? gy - nc : gy);
                 gz = gz < 0 ? gz + nc : (gz >= nc ? gz - nc : gz);
                 const int base = (gz * nc + gy) * nc;
-                rlo[2 * row] = cell_start[base + xl];
-                rhi[2 * row] = cell_start[base + (wrapx ? nc : xh + 1)];
-                rlo[2 * row + 1] = wrapx ? cell_start[base] : 0;
-                rhi[2 * row + 1] = wrapx ? cell_start[base + xh + 1] : 0;
-            }
-            int sr = 0, q = rlo[0], e = rhi[0];
-            while (q >= e && ++sr < 18) { q = rlo[sr]; e = rhi[sr]; }
+                if ((sr & 1) == 0) { lo = cell_start[base + xl]; hi = cell_start[base + (wrapx ? nc : xh + 1)]; }
+                else if (wrapx) { lo = cell_start[base]; hi = cell_start[base + xh + 1]; }
+                else { lo = 0; hi = 0; }
+            };
+            int sr = 0, q = 0, e = 0;
+            range(0, q, e);
+            while (q >= e && ++sr < 18) range(sr, q, e);
             int c = sr < 18 ? cell_beads[q] : -1;
+#ifdef DMD_PHASE_TIMERS
+            {   /* candidates this bead walks: the total, and the grid size */
+                int cnt = 0;
+                for (int k = 0; k < 18; ++k) { int lo, hi; range(k, lo, hi); cnt += hi > lo ? hi - lo : 0; }
+                walk_n += cnt;
+                if (blockIdx.x == g_sub_cta) {
+                    atomicAdd((unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 7][13], (unsigned long long)cnt);
+                    if (b == 0) g_phase_cycles[DMD_PHASE_CTAS - 7][14] = nc;
+                }
+            }
+#endif
             while (sr < 18) {
                 /* the next candidate's index is loaded before this one is tested */
                 ++q;
-                while (q >= e && ++sr < 18) { q = rlo[sr]; e = rhi[sr]; }
+                while (q >= e && ++sr < 18) range(sr, q, e);
                 const int cn = sr < 18 ? cell_beads[q] : -1;
                 consider(c);
                 c = cn;
@@ -587,6 +605,13 @@ __device__ void cta_build_lists(const DSys &S, SharedState &sh, int hbonds, cons
         S.dnn[b] = min(nd, S.cap);
         mdn = max(mdn, min(nd, S.cap));
     }
+#ifdef DMD_PHASE_TIMERS
+    if (blockIdx.x == g_sub_cta) {   /* the slowest thread's walk: cycles, and its candidates */
+        const unsigned long long wt = (unsigned long long)(clock64() - walk_t0);
+        const unsigned long long old = atomicMax((unsigned long long *)&g_phase_cycles[DMD_PHASE_CTAS - 7][12], wt);
+        if (wt > old) g_phase_cycles[DMD_PHASE_CTAS - 7][15] = walk_n;
+    }
+#endif
     /* the longest down list, which selects the k_run variant */
     mdn = __reduce_max_sync(FULL, mdn);
     __syncthreads();
@@ -1246,10 +1271,15 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
                     const int o = warp + u * nw;
                     gsel[u] = -1;
                     if (o < ng) {
-                        int q = 0;
+                        /* the register word holding ordinal o, picked with
+                         * constant indices (a computed index would put gm
+                         * and pre in local memory) */
+                        int q = 0, pq = 0;
+                        unsigned gq = gm[0];
 #pragma unroll
-                        for (int qq = 1; qq < FEW_GROUPS / 32; ++qq) q += o >= pre[qq];
-                        gsel[u] = 32 * q + (int)__fns(gm[q], 0, o - pre[q] + 1);
+                        for (int qq = 1; qq < FEW_GROUPS / 32; ++qq)
+                            if (o >= pre[qq]) { q = qq; pq = pre[qq]; gq = gm[qq]; }
+                        gsel[u] = 32 * q + (int)__fns(gq, 0, o - pq + 1);
                         ns = u + 1;
                     }
                 }
