@@ -56,10 +56,12 @@
 #define OWN_SMEM_FULL 2048
 #define OWN_SMEM_COMPACT 1024
 /* threads of k_run per CTA: one candidate event per warp, so the warps of a
- * CTA bound a batch; the compact variant's smaller event areas leave room
- * for twice the warps */
+ * CTA bound a batch.  The compact variant's smaller event areas leave room
+ * for more warps; 12 keep 168 registers per thread (16 would cap them at 128
+ * and spill) and measured fastest on the 32-replica workload (16, 10 and 8
+ * warps: 5 %, 3 % and 9 % slower) */
 #define RUN_NT_FULL 256
-#define RUN_NT_COMPACT 512
+#define RUN_NT_COMPACT 384
 #define RUN_CARVEOUT_COMPACT_KB 164
 #define DMD_TICKET_SEQ_MAX ((1 << 25) - 2)
 #define FULL 0xffffffffu
