@@ -292,7 +292,7 @@ def run_ours(args):
     E = args.events
     batch = Batch(specs)
     lib = batch.lib
-    tuned = batch.autotune(max(2000, E // 4), cache=args.tune_cache) if not args.no_tune else None
+    tuned = batch.autotune(min(25000, max(2000, E // 4)), cache=args.tune_cache) if not args.no_tune else None
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -563,8 +563,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c3")
-    ap.add_argument("--events", type=int, default=100000,
-                    help="events per replica per step (both arms, and the CPU baseline's sample)")
+    ap.add_argument("--events", type=int, default=300000,
+                    help="events per replica per step (both arms, and the CPU baseline's sample); "
+                         "the workload asks 10^7 per replica")
     ap.add_argument("--plain-replicas", type=int, default=32)
     ap.add_argument("--plain-events", type=int, default=20000, help="events per system on the plain path")
     ap.add_argument("--single-events", type=int, default=100000, help="events of the single-system runs")
