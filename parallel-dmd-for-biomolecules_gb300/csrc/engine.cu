@@ -1219,7 +1219,7 @@ __device__ __forceinline__ double key_time(long long k) {
 /* The batch candidates: every bead entry whose key lies below a cut (and
  * below every pseudo event), sorted in (key, index) order into
  * sh.sort_key/sort_idx; the first is the root.  The cut is the root's time
- * plus a window sh.delta that adapts to aim at one to four candidates per
+ * plus a window sh.delta that adapts to aim at one to two candidates per
  * warp slot.  Every warp scans the level-1 minima against the cut and takes
  * every nw-th group below it; warp 0 sorts.  Each step issues all of its
  * global loads before it uses the first (they take hundreds of cycles
@@ -1373,9 +1373,9 @@ __device__ int cta_gather_candidates(const DSys &S, SharedState &sh, int root, l
             if (lane + 32 * h < nc) { sh.sort_key[rk[h]] = kk[h]; sh.sort_idx[rk[h]] = ee[h]; }
     } else if (threadIdx.x == 32) {
         /* the window for the next batch (beside the sort): aim at one to
-         * four candidates per slot */
+         * two candidates per slot */
         if (nc < slots) sh.delta = sh.delta * 2.0;
-        else if (nc > 4 * slots) sh.delta = sh.delta * 0.5;
+        else if (nc > 2 * slots) sh.delta = sh.delta * 0.5;
         if (!(sh.delta > sh.sc.interval * 1e-9)) sh.delta = sh.sc.interval * 1e-9;
     }
     DMD_GSUB(3);
