@@ -3,8 +3,8 @@
  *
  * A plain C++ restatement, on the CPU and one event at a time, of the serial
  * semantics of the reference PRIME20 DMD program (parallel-dmd-PRIME20/code,
- * Fortran 90 + MPI).  It is the checker for the GB300 engine and the timed
- * CPU baseline; the engine never calls it.  Each routine cites the reference
+ * Fortran 90 + MPI).  It is the oracle the GB300 engine is tested against and
+ * the timed CPU baseline; the engine never calls it.  Each routine cites the reference
  * file:line it restates.  Expressions keep the reference's evaluation order
  * so that, compiled without FMA contraction, they give the same IEEE bits as
  * the CUDA engine.

@@ -2,7 +2,7 @@
  * dmd_oracle.h -- TEST INFRASTRUCTURE ONLY: C ABI of the CPU restatement of
  * the reference PRIME20 DMD engine (see dmd_oracle.cpp).  Used by tests/,
  * __graft_entry__.smoke() and the cpu_baseline leg of bench.py as the
- * checker; the GB300 engine never links it.
+ * oracle; the GB300 engine never links it.
  */
 #ifndef DMD_ORACLE_H
 #define DMD_ORACLE_H

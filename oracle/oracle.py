@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY: ctypes binding of the CPU restatement of the
-reference engine (dmd_oracle.cpp).  It is the checker of the GB300 engine
-and the timed CPU baseline; the product never imports it."""
+reference engine (dmd_oracle.cpp).  It is the oracle the GB300 engine is
+tested against and the timed CPU baseline; the product never imports it."""
 from __future__ import annotations
 
 import ctypes as C

@@ -1,7 +1,7 @@
 /*
  * sidechain_oracle.cpp -- TEST INFRASTRUCTURE ONLY: CPU restatement of the
  * side-chain placement search of the reference's initial-configuration
- * generator (genconfig/gen_config_random-SQZ.f90:250-348), the checker of
+ * generator (genconfig/gen_config_random-SQZ.f90:250-348), the oracle of
  * dmd_sidechain_search.
  *
  * For every residue k the side-chain bead is moved over a cubic grid of

@@ -174,7 +174,7 @@ cudaError_t dmd_launch_predict_noalloc(const DSys &, int, double *, int *, int *
     return cudaErrorNotSupported;
 }
 
-/* the checker flags a pool whose arrays overlap (its own test) */
+/* the layout check flags a pool whose arrays overlap (its own test) */
 extern "C" int mock_selftest(void) {
     const std::string saved = g_report;
     g_report.clear();

@@ -92,7 +92,7 @@ def state_of(lib, h, r, n, batch=True):
     return f, i, t.value, coll.value
 
 
-def test_layout_checker_flags_an_overlap(mock):
+def test_layout_check_flags_an_overlap(mock):
     assert mock.mock_selftest() == 1
 
 

@@ -16,7 +16,7 @@ its constants (code/def.h, code/scale_down.f:32-35, code/make_code.f).
          capture +eps, escape -eps, shoulder entry -eps, exit +eps), and a
          pair without the energy to climb the step bounces.
 
-The CPU test pins the oracle (the CPU restatement used as the checker) to
+The CPU test pins the oracle (the CPU restatement the engine is tested against) to
 these answers; the GPU test runs the same cases through the engine's own
 device predictor and impulse (tests/gpu_src/known_answers.cu), and the
 core and bond cases also through the light batches' half-warp collision,

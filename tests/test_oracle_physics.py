@@ -1,4 +1,4 @@
-"""Physics checks of the CPU restatement itself (it is the checker, so it is
+"""Physics checks of the CPU restatement itself (it is the oracle, so it is
 pinned independently): conservation laws and analytic two-bead answers.
 The reference ships no tests or golden trajectories (its only run-time
 checks are the energy-drift and overlap tests of code/main.F90:928-942 and
