@@ -175,8 +175,20 @@ struct TaskPool {
     int16_t live[PTASK_MAX];      /* the tasks left for double precision */
 };
 
+/* the draws of one ghost collision that do not depend on the state
+ * (code/main.F90:998-1041): the bead (1-based, before the clamp), the two
+ * accepted (v1, v2) pairs, the next ghost time's uniform, and the logarithms
+ * of r1, r2 and that uniform; g: the ghost index they belong to (-1: none) */
+struct GhostDraws {
+    long long g;
+    int ok, i;
+    double v1a, v2a, v1b, ra, rb, tg;
+    double L[3];
+};
+
 struct SharedState {
     DScal sc;
+    GhostDraws gdraw[2];   /* ghost g's draws at [g & 1], drawn ahead by a free warp */
     int ev;
     long long cand_key[CAND_MAX];
     int cand_idx[CAND_MAX];

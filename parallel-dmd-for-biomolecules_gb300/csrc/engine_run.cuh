@@ -603,18 +603,17 @@ __device__ void hw_collision_light(const DSys &S, WarpArea &W, bool has, int i, 
     DMD_CSUB(3);
 }
 
-/* The ghost collision of lane_ghost() on a warp, with the same draws and
- * arithmetic: the lanes draw the counter-based uniforms of the bead choice,
- * of the two accept/reject pairs and of the next ghost time in parallel
- * and ballots find the first accepted of each; the two square roots and
- * the three logarithms run on three lanes, the three velocity components
- * on three lanes.  If 32 draws do not settle a choice (never in practice),
- * lane 0 runs lane_ghost() itself. */
-__device__ int warp_ghost(const DSys &S, SharedState &sh, double &tfalse) {
+/* The draws of ghost g that do not depend on the state, on a warp: the
+ * bead, the two accepted (v1, v2) pairs, the next ghost time's uniform and
+ * the logarithms of r1, r2 and that uniform (lanes 0..2).  The lanes draw
+ * the counter-based uniforms of each choice in parallel and ballots find the
+ * first accepted one, so they equal lane_ghost()'s draws.  D.ok = 0 when 32
+ * draws do not settle a choice (never in practice: lane_ghost() then draws
+ * one at a time).  D.g is written last. */
+__device__ void warp_ghost_draws(const DSys &S, long long gl, GhostDraws &D) {
     const int lane = threadIdx.x & 31;
-    const DTab &T = *S.tab;
     const int N = S.N;
-    const uint64_t g = (uint64_t)sh.sc.ghost_index;
+    const uint64_t g = (uint64_t)gl;
     /* the bead: the first draw k with (int)(u * N) + 1 != N + 1 */
     const int iv = (int)(dmd_uniform(S.seed, DMD_STREAM_GHOST, g, (uint32_t)lane) * N) + 1;
     const unsigned mi = __ballot_sync(FULL, iv != N + 1);
@@ -642,7 +641,30 @@ __device__ int warp_ghost(const DSys &S, SharedState &sh, double &tfalse) {
         if (mt == 0) fallback = true;
         else tg = __shfl_sync(FULL, u, __ffs(mt) - 1);
     }
-    if (fallback) {
+    /* lanes 0, 1: the logarithms of the two factors; lane 2: of the next
+     * ghost time's uniform */
+    if (!fallback && lane < 3) D.L[lane] = dmd_log(lane == 0 ? ra : (lane == 1 ? rb : tg));
+    if (lane == 0) {
+        D.ok = !fallback; D.i = i;
+        D.v1a = v1a; D.v2a = v2a; D.v1b = v1b; D.ra = ra; D.rb = rb; D.tg = tg;
+    }
+    __syncwarp();
+    if (lane == 0) D.g = gl;
+    __syncwarp();
+}
+
+/* The ghost collision of lane_ghost() on a warp, with the same draws and
+ * arithmetic (code/main.F90:997-1121).  D holds the draws of the current
+ * ghost when another warp drew them ahead (D.g == the ghost index), else
+ * they are drawn here; the two square roots and the next time run on three
+ * lanes, the three velocity components on three lanes.  When the draws did
+ * not settle (D.ok == 0), lane 0 runs lane_ghost() itself. */
+__device__ int warp_ghost(const DSys &S, SharedState &sh, double &tfalse, GhostDraws &D) {
+    const int lane = threadIdx.x & 31;
+    const DTab &T = *S.tab;
+    const int N = S.N;
+    if (D.g != sh.sc.ghost_index) warp_ghost_draws(S, sh.sc.ghost_index, D);
+    if (!D.ok) {
         int ii = 0;
         double tf = tfalse;
         if (lane == 0) ii = lane_ghost(S, sh, tf);
@@ -650,12 +672,13 @@ __device__ int warp_ghost(const DSys &S, SharedState &sh, double &tfalse) {
         tfalse = __shfl_sync(FULL, tf, 0);
         return __shfl_sync(FULL, ii, 0);
     }
+    int i = D.i;
     if (i > N) i = N;
     i -= 1;
     const double bmi = S.bm[i], rbmi = T.rbm[S.ident[i]];   /* bm(i) = mass(identity(i)) */
     /* lanes 0, 1: the two factors; lane 2: the next ghost time */
-    const double lx = lane == 0 ? ra : (lane == 1 ? rb : tg);
-    const double L = dmd_log(lx);
+    const double lx = lane == 0 ? D.ra : (lane == 1 ? D.rb : D.tg);
+    const double L = lane < 3 ? D.L[lane] : 0.0;
     double fact = 0.0, tn = 0.0;
     if (lane < 2) fact = sqrt(-2.0 * T.setemp * bmi * L / lx);
     else if (lane == 2) tn = -1.0 * L * T.avegtime + tfalse;
@@ -666,7 +689,7 @@ __device__ int warp_ghost(const DSys &S, SharedState &sh, double &tfalse) {
         double *P = lane == 0 ? S.x : (lane == 1 ? S.y : S.z);
         double *V = lane == 0 ? S.vx : (lane == 1 ? S.vy : S.vz);
         double x = P[i] + V[i] * tfalse;
-        const double num = lane == 0 ? v1a * fa : (lane == 1 ? v2a * fa : v1b * fb);
+        const double num = lane == 0 ? D.v1a * fa : (lane == 1 ? D.v2a * fa : D.v1b * fb);
         const double v = div_by(num, bmi, rbmi);
         V[i] = v;
         P[i] = x - v * tfalse;
@@ -1463,6 +1486,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
         sh.delta = sh.sc.interval * 0.05;
         sh.bseq = 0;
         sh.exitf = 0;
+        sh.gdraw[0].g = -1; sh.gdraw[1].g = -1;
     }
     /* footprint claim table: shared memory when one CTA holds the system and
      * it fits, else the system's global array; cleared at every launch */
@@ -1479,6 +1503,9 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
     while (true) {
         /* ---- the leader selects the next event (and a batch) ---- */
         ++iter;   /* on every thread, so that each can take the test below */
+        /* the ghost index before this iteration (only a ghost event moves
+         * it, after the barrier below) */
+        const long long gidx = sh.sc.ghost_index;
         /* One CTA with at most 256 level-1 groups: every warp finds the root
          * itself from the level-1 minima and, when it is a bead's event of a
          * batch, goes straight into the candidate gather without a barrier;
@@ -2002,7 +2029,7 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
             if (leader && warp == 0) {
                 DMD_CSUB(-1);
                 double tf = sh.tf_iv;
-                const int i = warp_ghost(S, sh, tf);
+                const int i = warp_ghost(S, sh, tf, sh.gdraw[gidx & 1]);
                 if (lane == 0) { W.i = i; W.tf = tf; }
                 __syncwarp();
                 DMD_SUB(-1);
@@ -2022,6 +2049,10 @@ __global__ void __launch_bounds__(RUN_NT, 1) k_run(DSys *systems, int nsys, long
                 DMD_CSUB(10);
                 warp_l1_refresh(S, W.pb, W.npred + 1);
                 DMD_CSUB(11);
+            } else if (leader && warp == 1) {
+                /* the next ghost's draws (they depend on the seed and the
+                 * ghost index only), while warp 0 handles this one */
+                warp_ghost_draws(S, gidx + 1, sh.gdraw[(gidx + 1) & 1]);
             }
         } else if (e == N + 1) {
             ph_kind = 7;
