@@ -181,20 +181,28 @@ __device__ __forceinline__ bool key_less(long long ka, int pa, long long kb, int
 }
 
 /* static pair code: code/make_code.f:6-573 applied per chain, as a rule */
+/* codes for residue offsets d = -2..2, 5 bits each */
+#define DMD_BOND_ROW(m2, m1, z, p1, p2) \
+    ((uint32_t)(m2) | ((uint32_t)(m1) << 5) | ((uint32_t)(z) << 10) | ((uint32_t)(p1) << 15) | ((uint32_t)(p2) << 20))
 __host__ __device__ __forceinline__ int bond_code_dir(int ka, int kb, int ra, int rb) {
-    int d = rb - ra;
-    switch (ka * 4 + kb) {
-        case BK_CA * 4 + BK_NH: return d == 0 ? 4 : d == 1 ? 7 : d == -1 ? 18 : 0;
-        case BK_CA * 4 + BK_CO: return d == 0 ? 5 : d == -1 ? 8 : d == 1 ? 17 : 0;
-        case BK_NH * 4 + BK_CO: return d == -1 ? 6 : d == 0 ? 8 : d == -2 ? 19 : 0;
-        case BK_CA * 4 + BK_CA: return d == 1 ? 9 : 0;
-        case BK_CA * 4 + BK_R: return d == 0 ? 10 : d == 1 ? 24 : d == -1 ? 25 : 0;
-        case BK_NH * 4 + BK_R: return d == 0 ? 11 : d == -1 ? 23 : 0;
-        case BK_CO * 4 + BK_R: return d == 0 ? 12 : d == 1 ? 22 : d == 2 ? 26 : 0;
-        case BK_NH * 4 + BK_NH: return d == 1 ? 20 : 0;
-        case BK_CO * 4 + BK_CO: return d == 1 ? 21 : 0;
-        default: return 0;
-    }
+    /* the bonded and squeezed pair codes of make_code.f by bead kinds and
+     * residue offset d = rb - ra: one packed word per pair of kinds, picked
+     * by selects rather than a switch (a switch whose lanes take different
+     * cases runs them one after another) */
+    const int d = rb - ra;
+    const int pk = ka * 4 + kb;
+    uint32_t w = 0;
+    w = pk == BK_CA * 4 + BK_NH ? DMD_BOND_ROW(0, 18, 4, 7, 0) : w;
+    w = pk == BK_CA * 4 + BK_CO ? DMD_BOND_ROW(0, 8, 5, 17, 0) : w;
+    w = pk == BK_NH * 4 + BK_CO ? DMD_BOND_ROW(19, 6, 8, 0, 0) : w;
+    w = pk == BK_CA * 4 + BK_CA ? DMD_BOND_ROW(0, 0, 0, 9, 0) : w;
+    w = pk == BK_CA * 4 + BK_R ? DMD_BOND_ROW(0, 25, 10, 24, 0) : w;
+    w = pk == BK_NH * 4 + BK_R ? DMD_BOND_ROW(0, 23, 11, 0, 0) : w;
+    w = pk == BK_CO * 4 + BK_R ? DMD_BOND_ROW(0, 0, 12, 22, 26) : w;
+    w = pk == BK_NH * 4 + BK_NH ? DMD_BOND_ROW(0, 0, 0, 20, 0) : w;
+    w = pk == BK_CO * 4 + BK_CO ? DMD_BOND_ROW(0, 0, 0, 21, 0) : w;
+    const unsigned sh = (unsigned)(d + 2);
+    return sh <= 4u ? (int)((w >> (5u * sh)) & 31u) : 0;
 }
 
 __host__ __device__ __forceinline__ int static_code(const BeadInfo &A, const BeadInfo &B, int hbonds) {
