@@ -206,42 +206,51 @@ __host__ __device__ __forceinline__ int bond_code_dir(int ka, int kb, int ra, in
 }
 
 __host__ __device__ __forceinline__ int static_code(const BeadInfo &A, const BeadInfo &B, int hbonds) {
-    if (A.chain == B.chain) {
-        int c = bond_code_dir(A.kind, B.kind, A.res, B.res);
-        if (!c) c = bond_code_dir(B.kind, A.kind, B.res, A.res);
-        if (c) return c;
-        int dr = A.res - B.res;
-        if (dr < 0) dr = -dr;
-        if (A.kind == BK_R && B.kind == BK_R) return (dr >= 4 && A.hp == 1 && B.hp == 1) ? 16 : 1;
-        if (hbonds && ((A.kind == BK_NH && B.kind == BK_CO) || (A.kind == BK_CO && B.kind == BK_NH)))
-            return dr >= 4 ? 15 : 1;
-        return 1;
-    }
-    /* side chains of two chains; two species-2 chains meet as hard cores
+    /* every case evaluated and the result picked by selects: the lanes of a
+     * warp hold pairs of all kinds, and branches on the kinds would run one
+     * after another */
+    const bool same = A.chain == B.chain;
+    const int c1 = bond_code_dir(A.kind, B.kind, A.res, B.res);
+    const int c2 = bond_code_dir(B.kind, A.kind, B.res, A.res);
+    const int cb = c1 ? c1 : c2;                       /* bonded or squeezed pair of one chain */
+    int dr = A.res - B.res;
+    dr = dr < 0 ? -dr : dr;
+    const bool rr = A.kind == BK_R && B.kind == BK_R;
+    const bool hp = A.hp == 1 && B.hp == 1;
+    const bool nc = A.kind == BK_NH && B.kind == BK_CO;
+    const bool cn = A.kind == BK_CO && B.kind == BK_NH;
+    /* one chain (make_code.f's intra-chain blocks) */
+    const int rr_intra = (dr >= 4 && hp) ? 16 : 1;
+    const int hb_intra = (hbonds && (nc || cn)) ? (dr >= 4 ? 15 : 1) : 1;
+    const int intra = cb ? cb : (rr ? rr_intra : hb_intra);
+    /* two chains; two species-2 chains' side chains meet as hard cores
      * (code/make_code.f:515-541) */
-    if (A.kind == BK_R && B.kind == BK_R) return (A.hp == 1 && B.hp == 1 && !(A.sp2 && B.sp2)) ? 16 : 1;
-    if (hbonds) {
-        if (A.kind == BK_NH && B.kind == BK_CO) return (A.pro_nh && B.chain > A.chain) ? 1 : 15;
-        if (A.kind == BK_CO && B.kind == BK_NH) return (B.pro_nh && A.chain > B.chain) ? 1 : 15;
-    }
-    return 1;
+    const int rr_inter = (hp && !(A.sp2 && B.sp2)) ? 16 : 1;
+    const int nc_inter = (A.pro_nh && B.chain > A.chain) ? 1 : 15;
+    const int cn_inter = (B.pro_nh && A.chain > B.chain) ? 1 : 15;
+    const int hb_inter = hbonds ? (nc ? nc_inter : (cn ? cn_inter : 1)) : 1;
+    const int inter = rr ? rr_inter : hb_inter;
+    return same ? intra : inter;
 }
 
 /* ev_code(a,b) when the static code of the pair is already known */
 __device__ __forceinline__ int pair_code_st(const DSys &S, int a, int b, int st) {
+    /* the first override slot holding b, picked by selects (all loads issued
+     * together, no early exit) */
     const int *op = S.ovp + 4 * a;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-        if (op[s] == b) return S.ovc[4 * a + s];
-    return st;
+    const int8_t *oc = S.ovc + 4 * a;
+    const int o0 = op[0], o1 = op[1], o2 = op[2], o3 = op[3];
+    const int c0 = oc[0], c1 = oc[1], c2 = oc[2], c3 = oc[3];
+    int r = st;
+    r = o3 == b ? c3 : r;
+    r = o2 == b ? c2 : r;
+    r = o1 == b ? c1 : r;
+    r = o0 == b ? c0 : r;
+    return r;
 }
 /* ev_code(a,b): the rule plus the H-bond shoulder overrides of repuls_add */
 __device__ __forceinline__ int pair_code(const DSys &S, int a, int b, int hbonds) {
-    const int *op = S.ovp + 4 * a;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-        if (op[s] == b) return S.ovc[4 * a + s];
-    return static_code(S.info[a], S.info[b], hbonds);
+    return pair_code_st(S, a, b, static_code(S.info[a], S.info[b], hbonds));
 }
 
 /* ------------------------------------------------------------------ */
